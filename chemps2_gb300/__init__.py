@@ -1,0 +1,372 @@
+"""GB300 implementation of CheMPS2's two-site DMRG sweep.
+
+Python mirror of the reference's Python interface (PyCheMPS2/PyCheMPS2.pyx:47-188):
+Hamiltonian, Problem, ConvergenceScheme and DMRG with the same method names, bound with
+ctypes to the C-ABI of libchemps2_gb300.so (include/chemps2_gb300.h). The library is built
+in-tree by chemps2_gb300.build; the DMRG object runs only on a CUDA device and raises
+NoDeviceError when there is none.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+_LIB = None
+
+C2G_OK = 0
+C2G_ERR_INVALID = -1
+C2G_ERR_CUDA = -2
+C2G_ERR_NO_DEVICE = -3
+C2G_ERR_INTERNAL = -4
+C2G_ERR_OTHER = -5
+NUM_STATS = 11
+STAT_NAMES = ("n_matvec", "n_davidson", "t_join", "t_solve", "t_split", "t_update", "t_matvec", "t_compile",
+              "matvec_flops", "matvec_bytes", "last_energy")
+
+
+class Chemps2Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class NoDeviceError(Chemps2Error):
+    pass
+
+
+def library_path() -> Path:
+    return _PKG / "_lib" / "libchemps2_gb300.so"
+
+
+def load(build_if_missing: bool = True):
+    """Loads the native library (building it first when it is missing)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        if not build_if_missing:
+            raise FileNotFoundError(f"{path} is missing; run chemps2_gb300.build.build()")
+        from . import build as _build
+
+        _build.build()
+    lib = C.CDLL(str(path))
+    lib.c2g_last_error.restype = C.c_char_p
+    _LIB = lib
+    return lib
+
+
+def _check(rc):
+    if rc != C2G_OK:
+        msg = load().c2g_last_error().decode(errors="replace")
+        if rc == C2G_ERR_NO_DEVICE:
+            raise NoDeviceError(rc, msg)
+        raise Chemps2Error(rc, msg)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def srand(seed: int) -> None:
+    """Seeds the generator of the random initial MPS, Davidson fallback guess and noise."""
+    _check(load().c2g_srand(C.c_uint(seed)))
+
+
+def kernel_launches() -> int:
+    n = C.c_longlong()
+    _check(load().c2g_kernel_launches(C.byref(n)))
+    return n.value
+
+
+def wigner6j(a, b, c, d, e, f) -> float:
+    v = C.c_double()
+    _check(load().c2g_wigner6j(a, b, c, d, e, f, C.byref(v)))
+    return v.value
+
+
+def wigner9j(a, b, c, d, e, f, g, h, i) -> float:
+    v = C.c_double()
+    _check(load().c2g_wigner9j(a, b, c, d, e, f, g, h, i, C.byref(v)))
+    return v.value
+
+
+class Hamiltonian:
+    """CheMPS2::Hamiltonian (PyHamiltonian): Hamiltonian(L, group, irreps) or
+    Hamiltonian(L, group, irreps, filename=fcidump)."""
+
+    def __init__(self, Norbitals, nGroup, OrbIrreps, filename="none"):
+        self._h = C.c_void_p()
+        lib = load()
+        if filename and filename != "none":
+            _check(lib.c2g_hamiltonian_create_fcidump(str(filename).encode(), int(nGroup), C.byref(self._h)))
+        else:
+            irr = np.ascontiguousarray(OrbIrreps, dtype=np.int32)
+            if irr.size != Norbitals:
+                raise ValueError("one irrep per orbital is required")
+            _check(lib.c2g_hamiltonian_create(int(Norbitals), int(nGroup), irr.ctypes.data_as(C.POINTER(C.c_int)),
+                                              C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _LIB is not None:
+            _LIB.c2g_hamiltonian_destroy(self._h)
+            self._h = None
+
+    def getL(self):
+        v = C.c_int()
+        _check(load().c2g_hamiltonian_get_L(self._h, C.byref(v)))
+        return v.value
+
+    def getNGroup(self):
+        v = C.c_int()
+        _check(load().c2g_hamiltonian_get_group(self._h, C.byref(v)))
+        return v.value
+
+    def getOrbitalIrrep(self, orb):
+        v = C.c_int()
+        _check(load().c2g_hamiltonian_get_irrep(self._h, int(orb), C.byref(v)))
+        return v.value
+
+    def setEconst(self, value):
+        _check(load().c2g_hamiltonian_set_econst(self._h, C.c_double(value)))
+
+    def getEconst(self):
+        v = C.c_double()
+        _check(load().c2g_hamiltonian_get_econst(self._h, C.byref(v)))
+        return v.value
+
+    def setTmat(self, i, j, value):
+        _check(load().c2g_hamiltonian_set_tmat(self._h, int(i), int(j), C.c_double(value)))
+
+    def getTmat(self, i, j):
+        v = C.c_double()
+        _check(load().c2g_hamiltonian_get_tmat(self._h, int(i), int(j), C.byref(v)))
+        return v.value
+
+    def setVmat(self, i, j, k, l, value):
+        _check(load().c2g_hamiltonian_set_vmat(self._h, int(i), int(j), int(k), int(l), C.c_double(value)))
+
+    def getVmat(self, i, j, k, l):
+        v = C.c_double()
+        _check(load().c2g_hamiltonian_get_vmat(self._h, int(i), int(j), int(k), int(l), C.byref(v)))
+        return v.value
+
+
+class Problem:
+    """CheMPS2::Problem (PyProblem)."""
+
+    def __init__(self, Hami: Hamiltonian, TwoS, N, Irrep):
+        self._ham = Hami  # the Hamiltonian must outlive the Problem
+        self._p = C.c_void_p()
+        _check(load().c2g_problem_create(Hami._h, int(TwoS), int(N), int(Irrep), C.byref(self._p)))
+        self._TwoS, self._N, self._Irrep = int(TwoS), int(N), int(Irrep)
+
+    def __del__(self):
+        if getattr(self, "_p", None) and _LIB is not None:
+            _LIB.c2g_problem_destroy(self._p)
+            self._p = None
+
+    def gL(self):
+        return self._ham.getL()
+
+    def gSy(self):
+        return self._ham.getNGroup()
+
+    def gTwoS(self):
+        return self._TwoS
+
+    def gN(self):
+        return self._N
+
+    def gIrrep(self, orb=None):
+        return self._Irrep if orb is None else self._ham.getOrbitalIrrep(orb)
+
+    def gEconst(self):
+        return self._ham.getEconst()
+
+    def construct_mxelem(self):
+        _check(load().c2g_problem_construct_mxelem(self._p))
+
+    def gMxElement(self, a, b, c, d):
+        v = C.c_double()
+        _check(load().c2g_problem_get_mx_element(self._p, a, b, c, d, C.byref(v)))
+        return v.value
+
+    def setMxElement(self, a, b, c, d, value):
+        _check(load().c2g_problem_set_mx_element(self._p, a, b, c, d, C.c_double(value)))
+
+    def SetupReorderD2h(self):
+        _check(load().c2g_problem_setup_reorder_d2h(self._p))
+
+    def SetupReorderC2v(self):
+        _check(load().c2g_problem_setup_reorder_c2v(self._p))
+
+    def setup_reorder_custom(self, dmrg2ham):
+        a = np.ascontiguousarray(dmrg2ham, dtype=np.int32)
+        _check(load().c2g_problem_setup_reorder_custom(self._p, a.ctypes.data_as(C.POINTER(C.c_int))))
+
+    def checkConsistency(self):
+        v = C.c_int()
+        _check(load().c2g_problem_check_consistency(self._p, C.byref(v)))
+        return bool(v.value)
+
+    def bookkeeper_sectors(self, D, boundary):
+        """(N, 2S, I, FCI dim, current dim) of every sector at `boundary` (no GPU needed)."""
+        n = C.c_int()
+        _check(load().c2g_bookkeeper_sectors(self._p, int(D), int(boundary), None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 5), dtype=np.int32)
+        _check(load().c2g_bookkeeper_sectors(self._p, int(D), int(boundary), out.ctypes.data_as(C.POINTER(C.c_int)),
+                                             n.value, C.byref(n)))
+        return out[: n.value]
+
+    def sobject_layout(self, D, index):
+        """Block labels (nkappa x 9), kappa2index and the visiting order of the two-site
+        object at sites (index, index + 1) (no GPU needed)."""
+        n = C.c_int()
+        _check(load().c2g_sobject_layout(self._p, int(D), int(index), None, None, None, 0, C.byref(n)))
+        k = n.value
+        labels = np.zeros((max(k, 1), 9), dtype=np.int32)
+        k2i = np.zeros(k + 1, dtype=np.int64)
+        order = np.zeros(max(k, 1), dtype=np.int32)
+        _check(load().c2g_sobject_layout(self._p, int(D), int(index), labels.ctypes.data_as(C.POINTER(C.c_int)),
+                                         k2i.ctypes.data_as(C.POINTER(C.c_int64)),
+                                         order.ctypes.data_as(C.POINTER(C.c_int)), k, C.byref(n)))
+        return labels[:k], k2i, order[:k]
+
+
+class ConvergenceScheme:
+    """CheMPS2::ConvergenceScheme (PyConvergenceScheme)."""
+
+    def __init__(self, nInstructions):
+        self._s = C.c_void_p()
+        _check(load().c2g_scheme_create(int(nInstructions), C.byref(self._s)))
+        self._instr = {}
+
+    def __del__(self):
+        if getattr(self, "_s", None) and _LIB is not None:
+            _LIB.c2g_scheme_destroy(self._s)
+            self._s = None
+
+    def set_instruction(self, instruction, D, Econv, nMax, noisePrefactor, dvdson_rtol):
+        _check(load().c2g_scheme_set_instruction(self._s, int(instruction), int(D), C.c_double(Econv), int(nMax),
+                                                 C.c_double(noisePrefactor), C.c_double(dvdson_rtol)))
+        self._instr[instruction] = (D, Econv, nMax, noisePrefactor, dvdson_rtol)
+
+    def setInstruction(self, instruction, D, Econv, nMax, noisePrefactor):
+        self.set_instruction(instruction, D, Econv, nMax, noisePrefactor, 1e-5)
+
+    def getD(self, i):
+        return self._instr[i][0]
+
+    def getEconv(self, i):
+        return self._instr[i][1]
+
+    def getMaxSweeps(self, i):
+        return self._instr[i][2]
+
+    def getNoisePrefactor(self, i):
+        return self._instr[i][3]
+
+    def getDavidsonRTOL(self, i):
+        return self._instr[i][4]
+
+
+class DMRG:
+    """CheMPS2::DMRG (PyDMRG): the sweep runs on the GPU."""
+
+    def __init__(self, Probl: Problem, OptScheme: ConvergenceScheme, makechkpt=False, tmpfolder="/tmp",
+                 occupancies=None):
+        self._prob, self._scheme = Probl, OptScheme
+        self._d = C.c_void_p()
+        occ = None
+        if occupancies is not None:
+            occ = np.ascontiguousarray(occupancies, dtype=np.int32)
+        _check(load().c2g_dmrg_create(Probl._p, OptScheme._s,
+                                      occ.ctypes.data_as(C.POINTER(C.c_int)) if occ is not None else None,
+                                      C.byref(self._d)))
+
+    def close(self):
+        if getattr(self, "_d", None) and _LIB is not None:
+            _check(_LIB.c2g_dmrg_destroy(self._d))
+            self._d = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def Solve(self):
+        e = C.c_double()
+        _check(load().c2g_dmrg_solve(self._d, C.byref(e)))
+        return e.value
+
+    def PreSolve(self):
+        _check(load().c2g_dmrg_presolve(self._d))
+
+    def set_verbose(self, v=True):
+        _check(load().c2g_dmrg_set_verbose(self._d, int(bool(v))))
+
+    def get_num_mps_var(self):
+        n = C.c_int()
+        _check(load().c2g_dmrg_num_mps_var(self._d, C.byref(n)))
+        return n.value
+
+    def get_max_discarded_weight(self):
+        w = C.c_double()
+        _check(load().c2g_dmrg_max_discarded_weight(self._d, C.byref(w)))
+        return w.value
+
+    def solve_site(self, index, dvdson_rtol, noise_level, D, moving_right, change):
+        e = C.c_double()
+        _check(load().c2g_dmrg_solve_site(self._d, int(index), C.c_double(dvdson_rtol), C.c_double(noise_level),
+                                          int(D), int(bool(moving_right)), int(bool(change)), C.byref(e)))
+        return e.value
+
+    def update(self, index, moving_right):
+        _check(load().c2g_dmrg_update(self._d, int(index), int(bool(moving_right))))
+
+    def stats(self):
+        out = np.zeros(NUM_STATS)
+        _check(load().c2g_dmrg_stats(self._d, _dp(out), NUM_STATS))
+        return dict(zip(STAT_NAMES, out.tolist()))
+
+    def reset_stats(self):
+        _check(load().c2g_dmrg_reset_stats(self._d))
+
+    def sobject_size(self, index):
+        n = C.c_int64()
+        _check(load().c2g_dmrg_sobject_size(self._d, int(index), C.byref(n)))
+        return n.value
+
+    def heff_apply(self, index, x=None, want_diag=False):
+        """y = Heff x at sites (index, index + 1); x None: the joined current state."""
+        n = self.sobject_size(index)
+        join = x is None
+        xx = np.zeros(n) if join else np.ascontiguousarray(x, dtype=np.float64).copy()
+        y = np.zeros(n)
+        d = np.zeros(n) if want_diag else None
+        _check(load().c2g_dmrg_heff_apply(self._d, int(index), int(join), _dp(xx), _dp(y),
+                                          _dp(d) if d is not None else None, C.c_int64(n)))
+        return xx, y, d
+
+    def bench_heff(self, index, warmup, steps):
+        ms, fl, by = C.c_double(), C.c_double(), C.c_double()
+        nl = C.c_longlong()
+        _check(load().c2g_dmrg_bench_heff(self._d, int(index), int(warmup), int(steps), C.byref(ms), C.byref(fl),
+                                          C.byref(by), C.byref(nl)))
+        return {"ms_per_matvec": ms.value, "flops": fl.value, "bytes": by.value, "launches": nl.value}
+
+
+# Names of the reference's Cython module.
+PyHamiltonian = Hamiltonian
+PyProblem = Problem
+PyConvergenceScheme = ConvergenceScheme
+PyDMRG = DMRG
+
+__all__ = ["Hamiltonian", "Problem", "ConvergenceScheme", "DMRG", "PyHamiltonian", "PyProblem",
+           "PyConvergenceScheme", "PyDMRG", "srand", "wigner6j", "wigner9j", "kernel_launches", "load",
+           "Chemps2Error", "NoDeviceError"]

@@ -1,0 +1,438 @@
+// extern "C" boundary: wraps the drop-in C++ classes into opaque handles with status codes.
+#include "../../include/chemps2_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "dmrg/runtime.hpp"
+#include "host/chemps2/ConvergenceScheme.h"
+#include "host/chemps2/DMRG.h"
+#include "host/chemps2/Hamiltonian.h"
+#include "host/chemps2/Problem.h"
+#include "host/chemps2/SyBookkeeper.h"
+#include "host/layout.hpp"
+#include "host/symm.hpp"
+
+struct c2g_hamiltonian {
+  std::unique_ptr<CheMPS2::Hamiltonian> h;
+};
+struct c2g_problem {
+  std::unique_ptr<CheMPS2::Problem> p;
+};
+struct c2g_scheme {
+  std::unique_ptr<CheMPS2::ConvergenceScheme> s;
+};
+struct c2g_dmrg {
+  std::unique_ptr<CheMPS2::DMRG> d;
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+  g_error = msg;
+  return code;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    g_error.clear();
+    return C2G_OK;
+  } catch (const c2g::CudaError& e) {
+    if (e.code == cudaErrorNoDevice || e.code == cudaErrorInsufficientDriver) return fail(C2G_ERR_NO_DEVICE, e.what());
+    return fail(C2G_ERR_CUDA, e.what());
+  } catch (const std::invalid_argument& e) {
+    return fail(C2G_ERR_INVALID, e.what());
+  } catch (const std::out_of_range& e) {
+    return fail(C2G_ERR_INVALID, e.what());
+  } catch (const std::logic_error& e) {
+    return fail(C2G_ERR_INTERNAL, e.what());
+  } catch (const std::runtime_error& e) {
+    const std::string w = e.what();
+    if (w.find("no CUDA device") != std::string::npos) return fail(C2G_ERR_NO_DEVICE, w);
+    return fail(C2G_ERR_OTHER, w);
+  } catch (const std::exception& e) {
+    return fail(C2G_ERR_OTHER, e.what());
+  } catch (...) {
+    return fail(C2G_ERR_OTHER, "unknown exception");
+  }
+}
+
+#define NEED(x)                                                        \
+  do {                                                                 \
+    if (!(x)) throw std::invalid_argument("null argument: " #x);       \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+const char* c2g_last_error(void) { return g_error.c_str(); }
+int c2g_version(void) { return 100; }
+int c2g_srand(unsigned int seed) {
+  std::srand(seed);
+  return C2G_OK;
+}
+int c2g_kernel_launches(long long* count) {
+  return guarded([&] {
+    NEED(count);
+    *count = c2g::kernel_launches();
+  });
+}
+
+// ---- Hamiltonian
+int c2g_hamiltonian_create(int L, int group, const int* irreps, c2g_hamiltonian** out) {
+  return guarded([&] {
+    NEED(irreps);
+    NEED(out);
+    auto h = std::make_unique<c2g_hamiltonian>();
+    h->h = std::make_unique<CheMPS2::Hamiltonian>(L, group, irreps);
+    *out = h.release();
+  });
+}
+int c2g_hamiltonian_create_fcidump(const char* path, int group, c2g_hamiltonian** out) {
+  return guarded([&] {
+    NEED(path);
+    NEED(out);
+    auto h = std::make_unique<c2g_hamiltonian>();
+    h->h = std::make_unique<CheMPS2::Hamiltonian>(std::string(path), group);
+    *out = h.release();
+  });
+}
+int c2g_hamiltonian_destroy(c2g_hamiltonian* h) {
+  delete h;
+  return C2G_OK;
+}
+int c2g_hamiltonian_get_L(const c2g_hamiltonian* h, int* L) {
+  return guarded([&] {
+    NEED(h);
+    NEED(L);
+    *L = h->h->getL();
+  });
+}
+int c2g_hamiltonian_get_group(const c2g_hamiltonian* h, int* group) {
+  return guarded([&] {
+    NEED(h);
+    NEED(group);
+    *group = h->h->getNGroup();
+  });
+}
+int c2g_hamiltonian_get_irrep(const c2g_hamiltonian* h, int orb, int* irrep) {
+  return guarded([&] {
+    NEED(h);
+    NEED(irrep);
+    if (orb < 0 || orb >= h->h->getL()) throw std::invalid_argument("orbital index");
+    *irrep = h->h->getOrbitalIrrep(orb);
+  });
+}
+int c2g_hamiltonian_set_econst(c2g_hamiltonian* h, double v) {
+  return guarded([&] {
+    NEED(h);
+    h->h->setEconst(v);
+  });
+}
+int c2g_hamiltonian_get_econst(const c2g_hamiltonian* h, double* v) {
+  return guarded([&] {
+    NEED(h);
+    NEED(v);
+    *v = h->h->getEconst();
+  });
+}
+static void check_orb(const CheMPS2::Hamiltonian& h, int i) {
+  if (i < 0 || i >= h.getL()) throw std::invalid_argument("orbital index out of range");
+}
+int c2g_hamiltonian_set_tmat(c2g_hamiltonian* h, int i, int j, double v) {
+  return guarded([&] {
+    NEED(h);
+    check_orb(*h->h, i);
+    check_orb(*h->h, j);
+    h->h->setTmat(i, j, v);
+  });
+}
+int c2g_hamiltonian_get_tmat(const c2g_hamiltonian* h, int i, int j, double* v) {
+  return guarded([&] {
+    NEED(h);
+    NEED(v);
+    check_orb(*h->h, i);
+    check_orb(*h->h, j);
+    *v = h->h->getTmat(i, j);
+  });
+}
+int c2g_hamiltonian_set_vmat(c2g_hamiltonian* h, int i, int j, int k, int l, double v) {
+  return guarded([&] {
+    NEED(h);
+    for (int o : {i, j, k, l}) check_orb(*h->h, o);
+    h->h->setVmat(i, j, k, l, v);
+  });
+}
+int c2g_hamiltonian_get_vmat(const c2g_hamiltonian* h, int i, int j, int k, int l, double* v) {
+  return guarded([&] {
+    NEED(h);
+    NEED(v);
+    for (int o : {i, j, k, l}) check_orb(*h->h, o);
+    *v = h->h->getVmat(i, j, k, l);
+  });
+}
+
+// ---- Problem
+int c2g_problem_create(const c2g_hamiltonian* h, int two_s, int n, int irrep, c2g_problem** out) {
+  return guarded([&] {
+    NEED(h);
+    NEED(out);
+    auto p = std::make_unique<c2g_problem>();
+    p->p = std::make_unique<CheMPS2::Problem>(h->h.get(), two_s, n, irrep);
+    *out = p.release();
+  });
+}
+int c2g_problem_destroy(c2g_problem* p) {
+  delete p;
+  return C2G_OK;
+}
+int c2g_problem_setup_reorder_d2h(c2g_problem* p) {
+  return guarded([&] {
+    NEED(p);
+    p->p->SetupReorderD2h();
+  });
+}
+int c2g_problem_setup_reorder_c2v(c2g_problem* p) {
+  return guarded([&] {
+    NEED(p);
+    p->p->SetupReorderC2v();
+  });
+}
+int c2g_problem_setup_reorder_custom(c2g_problem* p, const int* dmrg2ham) {
+  return guarded([&] {
+    NEED(p);
+    NEED(dmrg2ham);
+    p->p->setup_reorder_custom(const_cast<int*>(dmrg2ham));
+  });
+}
+int c2g_problem_construct_mxelem(c2g_problem* p) {
+  return guarded([&] {
+    NEED(p);
+    p->p->construct_mxelem();
+  });
+}
+static void check_mx(const CheMPS2::Problem& p, int a, int b, int c, int d) {
+  for (int o : {a, b, c, d})
+    if (o < 0 || o >= p.gL()) throw std::invalid_argument("orbital index out of range");
+  if (!p.has_mxelem()) throw std::invalid_argument("matrix elements not constructed (construct_mxelem)");
+}
+int c2g_problem_set_mx_element(c2g_problem* p, int a, int b, int c, int d, double v) {
+  return guarded([&] {
+    NEED(p);
+    check_mx(*p->p, a, b, c, d);
+    p->p->setMxElement(a, b, c, d, v);
+  });
+}
+int c2g_problem_get_mx_element(const c2g_problem* p, int a, int b, int c, int d, double* v) {
+  return guarded([&] {
+    NEED(p);
+    NEED(v);
+    check_mx(*p->p, a, b, c, d);
+    *v = p->p->gMxElement(a, b, c, d);
+  });
+}
+int c2g_problem_check_consistency(const c2g_problem* p, int* ok) {
+  return guarded([&] {
+    NEED(p);
+    NEED(ok);
+    *ok = p->p->checkConsistency() ? 1 : 0;
+  });
+}
+
+// ---- ConvergenceScheme
+int c2g_scheme_create(int n, c2g_scheme** out) {
+  return guarded([&] {
+    NEED(out);
+    if (n < 1) throw std::invalid_argument("number of instructions must be positive");
+    auto s = std::make_unique<c2g_scheme>();
+    s->s = std::make_unique<CheMPS2::ConvergenceScheme>(n);
+    *out = s.release();
+  });
+}
+int c2g_scheme_destroy(c2g_scheme* s) {
+  delete s;
+  return C2G_OK;
+}
+int c2g_scheme_set_instruction(c2g_scheme* s, int i, int D, double econv, int max_sweeps, double noise,
+                               double rtol) {
+  return guarded([&] {
+    NEED(s);
+    s->s->set_instruction(i, D, econv, max_sweeps, noise, rtol);
+  });
+}
+
+// ---- bookkeeping (no GPU)
+int c2g_bookkeeper_sectors(const c2g_problem* p, int D, int boundary, int* out, int cap, int* count) {
+  return guarded([&] {
+    NEED(p);
+    NEED(count);
+    CheMPS2::SyBookkeeper bk(p->p.get(), D);
+    if (boundary < 0 || boundary > bk.gL()) throw std::invalid_argument("boundary out of range");
+    const int ns = bk.num_sectors(boundary);
+    *count = ns;
+    if (cap <= 0) return;
+    NEED(out);
+    for (int id = 0; id < ns && id < cap; id++) {
+      int n, s, i;
+      bk.sector_labels(boundary, id, &n, &s, &i);
+      out[5 * id + 0] = n;
+      out[5 * id + 1] = s;
+      out[5 * id + 2] = i;
+      out[5 * id + 3] = bk.fci_dim_by_id(boundary, id);
+      out[5 * id + 4] = bk.cur_dim_by_id(boundary, id);
+    }
+  });
+}
+
+int c2g_sobject_layout(const c2g_problem* p, int D, int index, int* labels, int64_t* k2i, int* reorder, int cap,
+                       int* nkappa) {
+  return guarded([&] {
+    NEED(p);
+    NEED(nkappa);
+    CheMPS2::SyBookkeeper bk(p->p.get(), D);
+    if (index < 0 || index > bk.gL() - 2) throw std::invalid_argument("index out of range");
+    c2g::TwoSiteLayout S;
+    S.build(bk, index);
+    *nkappa = S.nkappa;
+    if (cap <= 0) return;
+    if (cap < S.nkappa) throw std::invalid_argument("capacity too small");
+    NEED(labels);
+    NEED(k2i);
+    NEED(reorder);
+    for (int k = 0; k < S.nkappa; k++) {
+      const int v[9] = {S.NL[k], S.TwoSL[k], S.IL[k], S.N1[k], S.N2[k], S.TwoJ[k], S.NR[k], S.TwoSR[k], S.IR[k]};
+      for (int j = 0; j < 9; j++) labels[9 * k + j] = v[j];
+      k2i[k] = S.k2i[k];
+      reorder[k] = S.reorder[k];
+    }
+    k2i[S.nkappa] = S.k2i[S.nkappa];
+  });
+}
+
+int c2g_wigner6j(int a, int b, int c, int d, int e, int f, double* v) {
+  return guarded([&] {
+    NEED(v);
+    *v = c2g::wigner6j(a, b, c, d, e, f);
+  });
+}
+int c2g_wigner9j(int a, int b, int c, int d, int e, int f, int g, int h, int i, double* v) {
+  return guarded([&] {
+    NEED(v);
+    *v = c2g::wigner9j(a, b, c, d, e, f, g, h, i);
+  });
+}
+
+// ---- DMRG
+int c2g_dmrg_create(c2g_problem* p, c2g_scheme* s, const int* occupancies, c2g_dmrg** out) {
+  return guarded([&] {
+    NEED(p);
+    NEED(s);
+    NEED(out);
+    auto d = std::make_unique<c2g_dmrg>();
+    d->d = std::make_unique<CheMPS2::DMRG>(p->p.get(), s->s.get(), false, "/tmp", const_cast<int*>(occupancies));
+    *out = d.release();
+  });
+}
+int c2g_dmrg_destroy(c2g_dmrg* d) {
+  return guarded([&] { delete d; });
+}
+int c2g_dmrg_solve(c2g_dmrg* d, double* energy) {
+  return guarded([&] {
+    NEED(d);
+    NEED(energy);
+    *energy = d->d->Solve();
+  });
+}
+int c2g_dmrg_presolve(c2g_dmrg* d) {
+  return guarded([&] {
+    NEED(d);
+    d->d->PreSolve();
+  });
+}
+int c2g_dmrg_set_verbose(c2g_dmrg* d, int v) {
+  return guarded([&] {
+    NEED(d);
+    d->d->set_verbose(v != 0);
+  });
+}
+int c2g_dmrg_num_mps_var(const c2g_dmrg* d, int* n) {
+  return guarded([&] {
+    NEED(d);
+    NEED(n);
+    *n = d->d->get_num_mps_var();
+  });
+}
+int c2g_dmrg_max_discarded_weight(const c2g_dmrg* d, double* w) {
+  return guarded([&] {
+    NEED(d);
+    NEED(w);
+    *w = d->d->get_MaxDiscardedWeightLastSweep();
+  });
+}
+int c2g_dmrg_solve_site(c2g_dmrg* d, int index, double rtol, double noise, int D, int moving_right, int change,
+                        double* energy) {
+  return guarded([&] {
+    NEED(d);
+    NEED(energy);
+    *energy = d->d->solve_site(index, rtol, noise, D, moving_right != 0, change != 0);
+  });
+}
+int c2g_dmrg_update(c2g_dmrg* d, int index, int moving_right) {
+  return guarded([&] {
+    NEED(d);
+    if (moving_right)
+      d->d->update_moving_right(index);
+    else
+      d->d->update_moving_left(index);
+  });
+}
+int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n) {
+  return guarded([&] {
+    NEED(d);
+    NEED(out);
+    const CheMPS2::DMRGStats& s = d->d->stats();
+    const double v[C2G_NUM_STATS] = {static_cast<double>(s.n_matvec), static_cast<double>(s.n_davidson),
+                                     s.t_join, s.t_solve, s.t_split, s.t_update, s.t_matvec, s.t_compile,
+                                     s.matvec_flops, s.matvec_bytes, s.last_energy};
+    for (int i = 0; i < n && i < C2G_NUM_STATS; i++) out[i] = v[i];
+  });
+}
+int c2g_dmrg_reset_stats(c2g_dmrg* d) {
+  return guarded([&] {
+    NEED(d);
+    d->d->reset_stats();
+  });
+}
+int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, double* ms, double* flops, double* bytes,
+                        long long* launches) {
+  return guarded([&] {
+    NEED(d);
+    NEED(ms);
+    *ms = d->d->bench_heff(index, warmup, steps, flops, bytes, launches);
+  });
+}
+
+int c2g_dmrg_sobject_size(const c2g_dmrg* d, int index, int64_t* n) {
+  return guarded([&] {
+    NEED(d);
+    NEED(n);
+    *n = d->d->sobject_size(index);
+  });
+}
+int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, double* y, double* diag, int64_t n) {
+  return guarded([&] {
+    NEED(d);
+    d->d->heff_apply_host(index, join_into_x != 0, x, y, diag, n);
+  });
+}
+
+}  // extern "C"

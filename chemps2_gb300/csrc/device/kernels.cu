@@ -1,0 +1,567 @@
+// Device kernels: the grouped FP64 block GEMM that executes task-program stages, and the
+// vector / small dense kernels of the Davidson eigensolver.
+#include "kernels.cuh"
+
+#include <cmath>
+
+namespace c2g {
+
+namespace {
+
+__device__ __forceinline__ const double* resolve(const SlotPtrs& sp, Ref r) {
+  const int s = static_cast<int>(r >> kRefShift);
+  const int64_t off = static_cast<int64_t>(r & kRefMask);
+  const double* base;
+  switch (s) {
+    case kSlotX: base = sp.x; break;
+    case kSlotY: base = sp.y; break;
+    case kSlotP1: base = sp.p1; break;
+    case kSlotCombo: base = sp.combo; break;
+    case kSlotOnes: base = sp.ones; break;
+    default: base = sp.table[s]; break;
+  }
+  return base + off;
+}
+
+// One CTA = one 32 x 32 tile of one output block. 256 threads as a 16 x 16 grid; thread
+// (tx, ty) owns rows ty, ty + 16 and columns tx, tx + 16 of the tile. The terms of the
+// group are accumulated in order, so the result does not depend on the launch order.
+__global__ void __launch_bounds__(256) grouped_gemm_kernel(const Group* __restrict__ groups,
+                                                           const Term* __restrict__ terms,
+                                                           const int2* __restrict__ tiles, SlotPtrs sp) {
+  __shared__ double As[kTileK][kTile + 1];  // alpha * op(U)(row0 + i, k0 + kk)
+  __shared__ double Bs[kTileK][kTile + 1];  // op(V)(k0 + kk, col0 + j)
+  const int2 td = tiles[blockIdx.x];
+  const Group G = groups[td.x];
+  const int row0 = (td.y >> 16) * kTile;
+  const int col0 = (td.y & 0xffff) * kTile;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  double acc00 = 0.0, acc01 = 0.0, acc10 = 0.0, acc11 = 0.0;
+  for (int t = G.t0; t < G.t1; t++) {
+    const Term T = terms[t];
+    const double* U = resolve(sp, T.u);
+    const bool tu = (T.flags & kTransU) != 0;
+    const int64_t ldu = T.ldu;
+    if (T.flags & kScalar) {
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+          const int r = row0 + ty + 16 * i, c = col0 + tx + 16 * j;
+          if (r < G.m && c < G.n) {
+            const double v = T.alpha * (tu ? U[c + ldu * r] : U[r + ldu * c]);
+            if (i == 0 && j == 0) acc00 += v;
+            if (i == 0 && j == 1) acc01 += v;
+            if (i == 1 && j == 0) acc10 += v;
+            if (i == 1 && j == 1) acc11 += v;
+          }
+        }
+      continue;
+    }
+    const double* V = resolve(sp, T.v);
+    const bool tv = (T.flags & kTransV) != 0;
+    const int64_t ldv = T.ldv;
+    for (int k0 = 0; k0 < T.k; k0 += kTileK) {
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const int e = tid + 256 * s;
+        int i, kk;
+        if (!tu) { i = e & 31; kk = e >> 5; } else { kk = e & 15; i = e >> 4; }
+        const int r = row0 + i, k = k0 + kk;
+        As[kk][i] = (r < G.m && k < T.k) ? T.alpha * (tu ? U[k + ldu * r] : U[r + ldu * k]) : 0.0;
+      }
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const int e = tid + 256 * s;
+        int j, kk;
+        if (!tv) { kk = e & 15; j = e >> 4; } else { j = e & 31; kk = e >> 5; }
+        const int c = col0 + j, k = k0 + kk;
+        Bs[kk][j] = (c < G.n && k < T.k) ? (tv ? V[c + ldv * k] : V[k + ldv * c]) : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < kTileK; kk++) {
+        const double a0 = As[kk][ty], a1 = As[kk][ty + 16];
+        const double b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
+        acc00 = fma(a0, b0, acc00);
+        acc01 = fma(a0, b1, acc01);
+        acc10 = fma(a1, b0, acc10);
+        acc11 = fma(a1, b1, acc11);
+      }
+      __syncthreads();
+    }
+  }
+  double* O = const_cast<double*>(resolve(sp, G.out));
+  const int64_t ldo = G.ldo;
+  const bool accum = (G.flags & kAccumulate) != 0;
+  const double accs[2][2] = {{acc00, acc01}, {acc10, acc11}};
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int r = row0 + ty + 16 * i, c = col0 + tx + 16 * j;
+      if (r < G.m && c < G.n) {
+        const int64_t idx = r + ldo * c;
+        O[idx] = accum ? O[idx] + accs[i][j] : accs[i][j];
+      }
+    }
+}
+
+// ---------------------------------------------------------------- vector kernels
+
+template <int MAXC>
+__global__ void __launch_bounds__(kDotThreads) multi_dot_kernel(const double* __restrict__ A, int64_t lda, int ncol,
+                                                                const double* __restrict__ x, int64_t n,
+                                                                double* __restrict__ partial) {
+  double acc[MAXC];
+#pragma unroll
+  for (int j = 0; j < MAXC; j++) acc[j] = 0.0;
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t start = chunk * blockIdx.x;
+  const int64_t end = (start + chunk < n) ? start + chunk : n;
+  for (int64_t i = start + threadIdx.x; i < end; i += blockDim.x) {
+    const double xi = x[i];
+#pragma unroll
+    for (int j = 0; j < MAXC; j++)
+      if (j < ncol) acc[j] = fma(A[i + lda * j], xi, acc[j]);
+  }
+  __shared__ double red[kDotThreads / 32][MAXC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < MAXC; j++) {
+    if (j >= ncol) break;
+    double v = acc[j];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < ncol) {
+    double v = 0.0;
+    for (int w = 0; w < kDotThreads / 32; w++) v += red[w][threadIdx.x];
+    partial[static_cast<int64_t>(blockIdx.x) * ncol + threadIdx.x] = v;
+  }
+}
+
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int nblk, int ncol, double* __restrict__ out) {
+  const int j = threadIdx.x;
+  if (j >= ncol) return;
+  double v = 0.0;
+  for (int b = 0; b < nblk; b++) v += partial[static_cast<int64_t>(b) * ncol + j];
+  out[j] = v;
+}
+
+__global__ void combine_kernel(double* __restrict__ out, double beta, const double* __restrict__ A, int64_t lda,
+                               const double* __restrict__ coef, int ncol, int64_t n) {
+  __shared__ double c[64];
+  if (threadIdx.x < ncol) c[threadIdx.x] = coef[threadIdx.x];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double v = (beta == 0.0) ? 0.0 : beta * out[i];
+    for (int j = 0; j < ncol; j++) v = fma(c[j], A[i + lda * j], v);
+    out[i] = v;
+  }
+}
+
+__global__ void scale_kernel(double* x, double s, int64_t n) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    x[i] *= s;
+}
+
+__global__ void axpy_kernel(double* y, double a, const double* x, int64_t n) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    y[i] = fma(a, x[i], y[i]);
+}
+
+__global__ void fill_kernel(double* x, double v, int64_t n) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    x[i] = v;
+}
+
+// dst[:, j] = sign_j * src[:, cols - 1 - j], one CTA per column. sign_j makes the entry of
+// largest magnitude (the first one on ties) positive, which fixes the gauge of each
+// eigenvector so that every executor produces the same singular vectors.
+__global__ void reverse_columns_kernel(double* __restrict__ dst, const double* __restrict__ src, int rows, int cols) {
+  const int j = blockIdx.x;
+  if (j >= cols) return;
+  const double* col = src + static_cast<int64_t>(rows) * (cols - 1 - j);
+  double best = -1.0;
+  int bi = 0;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+    const double a = fabs(col[i]);
+    if (a > best) {
+      best = a;
+      bi = i;
+    }
+  }
+  __shared__ double sb[256];
+  __shared__ int si[256];
+  sb[threadIdx.x] = best;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      const double b2 = sb[threadIdx.x + o];
+      const int i2 = si[threadIdx.x + o];
+      if (b2 > sb[threadIdx.x] || (b2 == sb[threadIdx.x] && i2 < si[threadIdx.x])) {
+        sb[threadIdx.x] = b2;
+        si[threadIdx.x] = i2;
+      }
+    }
+    __syncthreads();
+  }
+  const double sgn = (col[si[0]] < 0.0) ? -1.0 : 1.0;
+  double* out = dst + static_cast<int64_t>(rows) * j;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) out[i] = sgn * col[i];
+}
+
+// t -= evals[0] * u   (CheMPS2/Davidson.cpp:280-283)
+__global__ void residual_kernel(double* t, const double* u, const double* evals, int64_t n) {
+  const double lam = evals[0];
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    t[i] = fma(-lam, u[i], t[i]);
+}
+
+__device__ __forceinline__ double precond_den(double d, double cutoff) {
+  return (fabs(d) > cutoff) ? d : cutoff;
+}
+
+// w = K^-1 u   (CheMPS2/Davidson.cpp:294-305)
+__global__ void precond_w_kernel(double* w, const double* u, const double* diag, const double* evals, double cutoff,
+                                 int64_t n) {
+  const double shift = evals[0];
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    w[i] = u[i] / precond_den(diag[i] - shift, cutoff);
+}
+
+// t = -K^-1 (t + alpha u), alpha = -(w.t)/(w.u)   (CheMPS2/Davidson.cpp:306-316)
+__global__ void precond_t_kernel(double* t, const double* u, const double* diag, const double* evals,
+                                 const double* dots2, double cutoff, int64_t n) {
+  const double shift = evals[0];
+  const double alpha = -dots2[0] / dots2[1];
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double v = fma(alpha, u[i], t[i]);
+    t[i] = -v / precond_den(diag[i] - shift, cutoff);
+  }
+}
+
+__global__ void neg_kernel(double* c, int n) {
+  if (threadIdx.x < n) c[threadIdx.x] = -c[threadIdx.x];
+}
+
+__global__ void inv_sqrt_scale_kernel(double* x, const double* sumsq, int64_t n) {
+  const double s = 1.0 / sqrt(sumsq[0]);
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    x[i] *= s;
+}
+
+__global__ void mxm_row_kernel(double* mxm, int ld, int row, const double* dots, int ncol) {
+  const int c = threadIdx.x;
+  if (c < ncol) {
+    mxm[c + ld * row] = dots[c];
+    mxm[row + ld * c] = dots[c];
+  }
+}
+
+// ---------------------------------------------------------------- small eigenproblems
+
+// Cyclic Jacobi for a symmetric n x n matrix (n <= 32) held in shared memory; one CTA.
+// Parallel (round-robin) ordering: every round rotates n/2 disjoint planes at once.
+// Eigenvalues ascending in evals[0..n), eigenvectors in the columns of evecs (ld).
+constexpr int kEigMax = 32;
+__global__ void __launch_bounds__(256) small_eig_kernel(const double* __restrict__ mat, int n, int ld,
+                                                        double* __restrict__ evals, double* __restrict__ evecs) {
+  __shared__ double A[kEigMax][kEigMax + 1];
+  __shared__ double B[kEigMax][kEigMax + 1];
+  __shared__ double Vm[kEigMax][kEigMax + 1];
+  __shared__ double W[kEigMax][kEigMax + 1];
+  __shared__ double cs[kEigMax / 2], sn[kEigMax / 2];
+  __shared__ int pp[kEigMax / 2], qq[kEigMax / 2];
+  __shared__ int role[kEigMax];  // pair index * 2 + (0: p, 1: q), or -1
+  __shared__ int pos[kEigMax];
+  __shared__ double offn, totn;
+  __shared__ int order[kEigMax];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int i = e % n, j = e / n;
+    A[i][j] = mat[i + ld * j];
+    Vm[i][j] = (i == j) ? 1.0 : 0.0;
+  }
+  const int m = (n % 2 == 0) ? n : n + 1;  // padded size; index n is a dummy when odd
+  const int npair = m / 2;
+  if (tid < m) pos[tid] = tid;
+  __syncthreads();
+  for (int sweep = 0; sweep < 30; sweep++) {
+    if (tid == 0) {
+      double off = 0.0, tot = 0.0;
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          const double v = A[i][j] * A[i][j];
+          tot += v;
+          if (i != j) off += v;
+        }
+      offn = off;
+      totn = tot;
+    }
+    __syncthreads();
+    if (!(offn > 1e-28 * totn) || n < 2) break;
+    for (int round = 0; round < m - 1; round++) {
+      if (tid < m) role[tid] = -1;
+      __syncthreads();
+      if (tid < npair) {
+        int p = pos[tid], q = pos[m - 1 - tid];
+        if (p > q) { const int t = p; p = q; q = t; }
+        double c = 1.0, s = 0.0;
+        if (q < n) {
+          const double apq = A[p][q];
+          if (apq != 0.0) {
+            const double tau = (A[q][q] - A[p][p]) / (2.0 * apq);
+            const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+          role[p] = 2 * tid;
+          role[q] = 2 * tid + 1;
+        }
+        cs[tid] = c;
+        sn[tid] = s;
+        pp[tid] = p;
+        qq[tid] = q;
+      }
+      __syncthreads();
+      // rows: B = J^T A
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        const int r = role[i];
+        double v = A[i][j];
+        if (r >= 0) {
+          const int k = r >> 1;
+          const double c = cs[k], s = sn[k];
+          v = (r & 1) ? s * A[pp[k]][j] + c * A[qq[k]][j] : c * A[pp[k]][j] - s * A[qq[k]][j];
+        }
+        B[i][j] = v;
+      }
+      __syncthreads();
+      // columns: A = B J, V = V J
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        const int r = role[j];
+        double v = B[i][j], w = Vm[i][j];
+        if (r >= 0) {
+          const int k = r >> 1;
+          const double c = cs[k], s = sn[k];
+          if (r & 1) {
+            v = s * B[i][pp[k]] + c * B[i][qq[k]];
+            w = s * Vm[i][pp[k]] + c * Vm[i][qq[k]];
+          } else {
+            v = c * B[i][pp[k]] - s * B[i][qq[k]];
+            w = c * Vm[i][pp[k]] - s * Vm[i][qq[k]];
+          }
+        }
+        A[i][j] = v;
+        W[i][j] = w;
+      }
+      __syncthreads();
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        Vm[i][j] = W[i][j];
+      }
+      // next pairing: position 0 fixed, the others rotate
+      if (tid == 0) {
+        const int last = pos[m - 1];
+        for (int k = m - 1; k > 1; k--) pos[k] = pos[k - 1];
+        pos[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  if (tid == 0) {
+    for (int i = 0; i < n; i++) order[i] = i;
+    for (int i = 0; i < n; i++) {  // selection sort, ascending
+      int best = i;
+      for (int j = i + 1; j < n; j++)
+        if (A[order[j]][order[j]] < A[order[best]][order[best]]) best = j;
+      const int t = order[i];
+      order[i] = order[best];
+      order[best] = t;
+    }
+  }
+  __syncthreads();
+  if (tid < n) evals[tid] = A[order[tid]][order[tid]];
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int i = e % n, j = e / n;
+    evecs[i + ld * j] = Vm[i][order[j]];
+  }
+}
+
+// Loewdin orthonormaliser of k <= 4 vectors: L = S^-1/2 from the k x k overlap S
+// (CheMPS2/Davidson.cpp:367-381). Serial Jacobi, one thread.
+__global__ void lowdin_kernel(const double* __restrict__ overlap, int k, double* __restrict__ lowdin) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a[4][4], v[4][4];
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < k; j++) {
+      a[i][j] = overlap[i + k * j];
+      v[i][j] = (i == j) ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 50; sweep++) {
+    double off = 0.0;
+    for (int i = 0; i < k; i++)
+      for (int j = 0; j < k; j++)
+        if (i != j) off += a[i][j] * a[i][j];
+    if (off < 1e-60) break;
+    for (int p = 0; p < k; p++)
+      for (int q = p + 1; q < k; q++) {
+        if (a[p][q] == 0.0) continue;
+        const double tau = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+        const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+        for (int j = 0; j < k; j++) {
+          const double x = a[p][j], y = a[q][j];
+          a[p][j] = c * x - s * y;
+          a[q][j] = s * x + c * y;
+        }
+        for (int i = 0; i < k; i++) {
+          const double x = a[i][p], y = a[i][q];
+          a[i][p] = c * x - s * y;
+          a[i][q] = s * x + c * y;
+          const double vx = v[i][p], vy = v[i][q];
+          v[i][p] = c * vx - s * vy;
+          v[i][q] = s * vx + c * vy;
+        }
+      }
+  }
+  double f[4];
+  for (int j = 0; j < k; j++) f[j] = pow(a[j][j], -0.5);
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < k; j++) {
+      double s = 0.0;
+      for (int l = 0; l < k; l++) s += v[i][l] * f[l] * v[j][l];
+      lowdin[i + k * j] = s;
+    }
+}
+
+inline int grid_for(int64_t n, int threads = 256) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b > 152 * 8) b = 152 * 8;
+  if (b < 1) b = 1;
+  return static_cast<int>(b);
+}
+
+}  // namespace
+
+cudaError_t launch_grouped_gemm(const Group* groups, const Term* terms, const int2* tiles, int ntiles,
+                                const SlotPtrs& sp, cudaStream_t stream) {
+  if (ntiles <= 0) return cudaSuccess;
+  grouped_gemm_kernel<<<ntiles, 256, 0, stream>>>(groups, terms, tiles, sp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_multi_dot(const double* A, int64_t lda, int ncol, const double* x, int64_t n, double* partial,
+                             double* out, cudaStream_t stream) {
+  if (ncol <= 0) return cudaSuccess;
+  if (ncol > 32) return cudaErrorInvalidValue;
+  if (ncol <= 4)
+    multi_dot_kernel<4><<<kDotBlocks, kDotThreads, 0, stream>>>(A, lda, ncol, x, n, partial);
+  else if (ncol <= 8)
+    multi_dot_kernel<8><<<kDotBlocks, kDotThreads, 0, stream>>>(A, lda, ncol, x, n, partial);
+  else
+    multi_dot_kernel<32><<<kDotBlocks, kDotThreads, 0, stream>>>(A, lda, ncol, x, n, partial);
+  reduce_partials_kernel<<<1, 32, 0, stream>>>(partial, kDotBlocks, ncol, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_combine(double* out, double beta, const double* A, int64_t lda, const double* coef, int ncol,
+                           int64_t n, cudaStream_t stream) {
+  if (ncol > 64) return cudaErrorInvalidValue;
+  if (n <= 0) return cudaSuccess;
+  combine_kernel<<<grid_for(n), 256, 0, stream>>>(out, beta, A, lda, coef, ncol, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norm2(const double* x, int64_t n, double* partial, double* out, cudaStream_t stream) {
+  return launch_multi_dot(x, n, 1, x, n, partial, out, stream);
+}
+
+cudaError_t launch_scale(double* x, double s, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  scale_kernel<<<grid_for(n), 256, 0, stream>>>(x, s, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpy(double* y, double a, const double* x, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  axpy_kernel<<<grid_for(n), 256, 0, stream>>>(y, a, x, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill(double* x, double v, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  fill_kernel<<<grid_for(n), 256, 0, stream>>>(x, v, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reverse_columns(double* dst, const double* src, int rows, int cols, cudaStream_t stream) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  reverse_columns_kernel<<<cols, 256, 0, stream>>>(dst, src, rows, cols);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream) {
+  if (n < 1 || n > kEigMax || ld < n) return cudaErrorInvalidValue;
+  small_eig_kernel<<<1, 256, 0, stream>>>(mat, n, ld, evals, evecs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_residual(double* t, const double* u, const double* evals, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  residual_kernel<<<grid_for(n), 256, 0, stream>>>(t, u, evals, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_precond_w(double* w, const double* u, const double* diag, const double* evals, double cutoff,
+                             int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  precond_w_kernel<<<grid_for(n), 256, 0, stream>>>(w, u, diag, evals, cutoff, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_precond_t(double* t, const double* u, const double* diag, const double* evals,
+                             const double* dots2, double cutoff, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  precond_t_kernel<<<grid_for(n), 256, 0, stream>>>(t, u, diag, evals, dots2, cutoff, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_neg(double* c, int n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  neg_kernel<<<1, 64, 0, stream>>>(c, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inv_sqrt_scale(double* x, const double* sumsq, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  inv_sqrt_scale_kernel<<<grid_for(n), 256, 0, stream>>>(x, sumsq, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mxm_row(double* mxm, int ld, int row, const double* dots, int ncol, cudaStream_t stream) {
+  mxm_row_kernel<<<1, 64, 0, stream>>>(mxm, ld, row, dots, ncol);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lowdin(const double* overlap, int k, double* lowdin, cudaStream_t stream) {
+  if (k < 1 || k > 4) return cudaErrorInvalidValue;
+  lowdin_kernel<<<1, 32, 0, stream>>>(overlap, k, lowdin);
+  return cudaGetLastError();
+}
+
+}  // namespace c2g

@@ -1,0 +1,71 @@
+// Device kernels of the DMRG hot path and their host launchers.
+//
+//   grouped block GEMM  one launch per task-program stage: every output block (group) is
+//                       cut into 32 x 32 tiles, one CTA per tile, and the CTA sums its
+//                       group's terms alpha * op(U) * op(V) (or alpha * op(U)) in order.
+//   vector kernels      the Davidson eigensolver's dots, linear combinations and
+//                       preconditioner, with deterministic two-pass reductions.
+//   small_eig           Jacobi diagonalisation of the <= 32 x 32 Rayleigh-Ritz matrix in
+//                       one CTA (FP64).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../host/tasks.hpp"
+
+namespace c2g {
+
+constexpr int kTile = 32;      // output tile edge of the grouped GEMM
+constexpr int kTileK = 16;     // inner-dimension chunk staged in shared memory
+constexpr int kMaxSlots = 512; // slot table size on the device
+
+// Device pointers the kernels resolve references against. X, Y, P1, Combo and Ones are
+// per launch; everything else comes from the slot table.
+struct SlotPtrs {
+  const double* const* table;  // device array [kMaxSlots]
+  double* x;
+  double* y;
+  double* p1;
+  double* combo;
+  const double* ones;
+};
+
+// Launch one stage: `tiles` holds (group, tile row << 16 | tile col) pairs.
+cudaError_t launch_grouped_gemm(const Group* groups, const Term* terms, const int2* tiles, int ntiles,
+                                const SlotPtrs& sp, cudaStream_t stream);
+
+// out[j] = sum_i A[i + lda * j] * x[i] for j < ncol (A has n rows). Uses `partial`
+// (at least ncol * kDotBlocks doubles) as scratch.
+constexpr int kDotBlocks = 152;
+constexpr int kDotThreads = 256;
+cudaError_t launch_multi_dot(const double* A, int64_t lda, int ncol, const double* x, int64_t n, double* partial,
+                             double* out, cudaStream_t stream);
+// out[i] = beta * out[i] + sum_j coef[j] * A[i + lda * j]   (coef on the device)
+cudaError_t launch_combine(double* out, double beta, const double* A, int64_t lda, const double* coef, int ncol,
+                           int64_t n, cudaStream_t stream);
+// Sum of squares of x, written to out[0]
+cudaError_t launch_norm2(const double* x, int64_t n, double* partial, double* out, cudaStream_t stream);
+// x *= s (scalar on the host)
+cudaError_t launch_scale(double* x, double s, int64_t n, cudaStream_t stream);
+// y += a * x
+cudaError_t launch_axpy(double* y, double a, const double* x, int64_t n, cudaStream_t stream);
+cudaError_t launch_fill(double* x, double v, int64_t n, cudaStream_t stream);
+// dst[:, j] = +-src[:, cols - 1 - j] for a rows x cols column-major matrix (ld = rows), the
+// sign making the largest-magnitude entry of each column positive
+cudaError_t launch_reverse_columns(double* dst, const double* src, int rows, int cols, cudaStream_t stream);
+
+// Davidson device steps (CheMPS2/Davidson.cpp). `sc` is a small device scratch of
+// scalars; layout documented in kernels.cu.
+cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream);
+cudaError_t launch_residual(double* t, const double* u, const double* evals, int64_t n, cudaStream_t stream);
+cudaError_t launch_precond_w(double* w, const double* u, const double* diag, const double* evals, double cutoff,
+                             int64_t n, cudaStream_t stream);
+cudaError_t launch_precond_t(double* t, const double* u, const double* diag, const double* evals,
+                             const double* dots2, double cutoff, int64_t n, cudaStream_t stream);
+cudaError_t launch_neg(double* c, int n, cudaStream_t stream);
+cudaError_t launch_inv_sqrt_scale(double* x, const double* sumsq, int64_t n, cudaStream_t stream);
+cudaError_t launch_mxm_row(double* mxm, int ld, int row, const double* dots, int ncol, cudaStream_t stream);
+cudaError_t launch_lowdin(const double* overlap, int k, double* lowdin, cudaStream_t stream);
+
+}  // namespace c2g

@@ -1,0 +1,144 @@
+#include "davidson.hpp"
+
+#include <cmath>
+#include <cstdlib>
+#include <vector>
+
+namespace c2g {
+
+namespace {
+// Offsets in the small device scratch sm_.
+constexpr int kMxM = 0;         // 32 x 32 Rayleigh-Ritz matrix (ld 32)
+constexpr int kEvecs = 1024;    // its eigenvectors (ld 32)
+constexpr int kEvals = 2048;    // eigenvalues, ascending
+constexpr int kDots = 2112;     // up to 64 dot products
+constexpr int kDots2 = 2176;    // w.t, w.u
+constexpr int kOverlap = 2184;  // keep x keep overlap
+constexpr int kLowdin = 2200;   // keep x keep Loewdin matrix
+constexpr int kSumSq = 2216;    // one sum of squares
+constexpr int kSmall = 2304;
+constexpr int kLd = 32;
+}  // namespace
+
+DeviceDavidson::DeviceDavidson(Runtime& rt, int64_t n, int max_vec, int keep, double rtol, double cutoff)
+    : rt_(rt), n_(n), max_vec_(max_vec), keep_(keep), rtol_(rtol), cutoff_(cutoff) {
+  if (max_vec > kLd || keep < 1 || keep > 4 || keep >= max_vec)
+    throw std::invalid_argument("Davidson: unsupported number of vectors");
+  V_ = rt_.alloc(n_ * max_vec_);
+  HV_ = rt_.alloc(n_ * max_vec_);
+  W_ = rt_.alloc(n_ * (3 + keep_));
+  sm_ = rt_.alloc(kSmall);
+  rt_.zero(sm_, kSmall);
+  C2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&host_), sizeof(double) * 8));
+}
+
+DeviceDavidson::~DeviceDavidson() {
+  rt_.release(V_);
+  rt_.release(HV_);
+  rt_.release(W_);
+  rt_.release(sm_);
+  if (host_) cudaFreeHost(host_);
+}
+
+void DeviceDavidson::multi_dot(const double* A, int ncol, const double* x, double* out) {
+  C2G_CUDA(launch_multi_dot(A, n_, ncol, x, n_, rt_.partial(), out, rt_.stream()));
+  count_launches(2);
+}
+
+double DeviceDavidson::norm2(const double* x) {
+  multi_dot(x, 1, x, sm_ + kSumSq);
+  C2G_CUDA(cudaMemcpyAsync(host_, sm_ + kSumSq, sizeof(double), cudaMemcpyDeviceToHost, rt_.stream()));
+  rt_.sync();
+  return host_[0];
+}
+
+// CheMPS2/Davidson.cpp:216-236 (AddNewVec): t <- t - V V^T t (twice), t <- t / |t|, V[nv] <- t.
+void DeviceDavidson::add_new_vec(double* t, int nv) {
+  cudaStream_t s = rt_.stream();
+  for (int pass = 0; pass < 2 && nv > 0; pass++) {
+    multi_dot(V_, nv, t, sm_ + kDots);
+    C2G_CUDA(launch_neg(sm_ + kDots, nv, s));
+    C2G_CUDA(launch_combine(t, 1.0, V_, n_, sm_ + kDots, nv, n_, s));
+    count_launches(2);
+  }
+  multi_dot(t, 1, t, sm_ + kSumSq);
+  C2G_CUDA(launch_inv_sqrt_scale(t, sm_ + kSumSq, n_, s));
+  count_launches(1);
+  C2G_CUDA(cudaMemcpyAsync(V(nv), t, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+}
+
+DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const MatVec& matvec) {
+  cudaStream_t s = rt_.stream();
+  DavidsonStats st;
+  double* t = W(0);
+  double* u = W(1);
+  double* w = W(2);
+  C2G_CUDA(cudaMemcpyAsync(t, guess, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+  // SafetyCheckGuess (CheMPS2/Davidson.cpp:204-214)
+  if (norm2(t) == 0.0) {
+    std::vector<double> r(n_);
+    for (int64_t i = 0; i < n_; i++) r[i] = static_cast<double>(std::rand()) / RAND_MAX;
+    C2G_CUDA(cudaMemcpyAsync(t, r.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
+    rt_.sync();
+  }
+  int nv = 0;
+  add_new_vec(t, nv);
+  matvec(V(nv), HV(nv));
+  st.n_matvec++;
+  for (;;) {
+    // DiagonalizeSmallMatrixAndCalcResidual (CheMPS2/Davidson.cpp:238-289)
+    multi_dot(HV_, nv + 1, V(nv), sm_ + kDots);
+    C2G_CUDA(launch_mxm_row(sm_ + kMxM, kLd, nv, sm_ + kDots, nv + 1, s));
+    nv++;
+    C2G_CUDA(launch_small_eig(sm_ + kMxM, nv, kLd, sm_ + kEvals, sm_ + kEvecs, s));
+    C2G_CUDA(launch_combine(t, 0.0, HV_, n_, sm_ + kEvecs, nv, n_, s));
+    C2G_CUDA(launch_combine(u, 0.0, V_, n_, sm_ + kEvecs, nv, n_, s));
+    C2G_CUDA(launch_residual(t, u, sm_ + kEvals, n_, s));
+    count_launches(5);
+    const double rnorm = std::sqrt(norm2(t));
+    st.n_iter++;
+    st.rnorm = rnorm;
+    if (!(rnorm > rtol_)) break;
+    // CalculateNewVec (CheMPS2/Davidson.cpp:291-317)
+    C2G_CUDA(launch_precond_w(w, u, diag, sm_ + kEvals, cutoff_, n_, s));
+    multi_dot(W(0), 2, w, sm_ + kDots2);  // w.t, w.u
+    C2G_CUDA(launch_precond_t(t, u, diag, sm_ + kEvals, sm_ + kDots2, cutoff_, n_, s));
+    count_launches(2);
+    if (nv == max_vec_) {
+      // Deflation (CheMPS2/Davidson.cpp:319-384): keep the lowest keep_ Ritz vectors
+      C2G_CUDA(cudaMemcpyAsync(W(3), u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+      for (int c = 1; c < keep_; c++) {
+        C2G_CUDA(launch_combine(W(3 + c), 0.0, V_, n_, sm_ + kEvecs + kLd * c, nv, n_, s));
+        count_launches(1);
+      }
+      for (int c = 0; c < keep_; c++) multi_dot(W(3), keep_, W(3 + c), sm_ + kOverlap + keep_ * c);
+      C2G_CUDA(launch_lowdin(sm_ + kOverlap, keep_, sm_ + kLowdin, s));
+      count_launches(1);
+      for (int c = 0; c < keep_; c++) {
+        C2G_CUDA(launch_combine(V(c), 0.0, W(3), n_, sm_ + kLowdin + keep_ * c, keep_, n_, s));
+        count_launches(1);
+      }
+      for (int c = 0; c < keep_; c++) {
+        matvec(V(c), HV(c));
+        st.n_matvec++;
+      }
+      // MxMafterDeflation (CheMPS2/Davidson.cpp:510-536)
+      for (int j = 0; j < keep_; j++) {
+        multi_dot(V_, j + 1, HV(j), sm_ + kDots);
+        C2G_CUDA(launch_mxm_row(sm_ + kMxM, kLd, j, sm_ + kDots, j + 1, s));
+        count_launches(1);
+      }
+      nv = keep_;
+    }
+    add_new_vec(t, nv);
+    matvec(V(nv), HV(nv));
+    st.n_matvec++;
+  }
+  C2G_CUDA(cudaMemcpyAsync(guess, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+  C2G_CUDA(cudaMemcpyAsync(host_, sm_ + kEvals, sizeof(double), cudaMemcpyDeviceToHost, s));
+  rt_.sync();
+  st.energy = host_[0];
+  return st;
+}
+
+}  // namespace c2g

@@ -1,0 +1,693 @@
+// CheMPS2::DMRG on the GPU: sweep control on the host (CheMPS2/DMRG.cpp:268-452), every
+// numerical step as device task programs or device kernels.
+#include "chemps2/DMRG.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cusolverDn.h>
+
+#include "davidson.hpp"
+#include "heff.hpp"
+#include "layout.hpp"
+#include "operators.hpp"
+#include "runtime.hpp"
+#include "sobject.hpp"
+#include "symm.hpp"
+
+namespace CheMPS2 {
+
+using c2g::Blk;
+using c2g::BoundaryOps;
+using c2g::DevProgram;
+using c2g::MpsLayout;
+using c2g::MpsT;
+using c2g::Program;
+using c2g::TaskBuilder;
+using c2g::TwoSiteLayout;
+
+namespace {
+
+// Davidson parameters of CheMPS2/include/chemps2/Options.h:70-72.
+constexpr int kDavidsonNumVec = 32;
+constexpr int kDavidsonNumVecKeep = 3;
+constexpr double kDavidsonPrecondCutoff = 1e-12;
+
+double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+MpsT mps_tensor(const MpsLayout* lay, int site) {
+  MpsT t;
+  t.lay = lay;
+  t.base = c2g::make_ref(c2g::kSlotMpsBase + site, 0);
+  return t;
+}
+
+void check_solver(cusolverStatus_t s, const char* what) {
+  if (s != CUSOLVER_STATUS_SUCCESS)
+    throw std::runtime_error(std::string("cuSOLVER error ") + std::to_string(static_cast<int>(s)) + " in " + what);
+}
+
+}  // namespace
+
+DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool, const std::string, int* occupancies)
+    : Prob(ProbIn), OptScheme(OptSchemeIn) {
+  if (!Prob->checkConsistency()) throw std::invalid_argument("DMRG: inconsistent Problem");
+  if (OptScheme->get_number() < 1) throw std::invalid_argument("DMRG: empty ConvergenceScheme");
+  L = Prob->gL();
+  if (L < 2) throw std::invalid_argument("DMRG: at least two orbitals are required");
+  Prob->construct_mxelem();
+  rt = std::make_unique<c2g::Runtime>(L);
+  mps_lay.resize(L);
+  mps_dev.assign(L, nullptr);
+  ops.resize(L - 1);
+  ops_dev.assign(L - 1, nullptr);
+  isAllocated.assign(L - 1, 0);
+  setup_mps(occupancies);
+  PreSolve();
+}
+
+DMRG::~DMRG() {
+  if (rt) {
+    try {
+      rt->sync();
+    } catch (...) {
+    }
+    for (double* p : mps_dev) rt->release(p);
+    for (double* p : ops_dev) rt->release(p);
+    try {
+      rt->sync();
+    } catch (...) {
+    }
+  }
+}
+
+// CheMPS2/DMRG.cpp:100-256 (setupBookkeeperAndMPS) with CheMPS2/TensorT.cpp:167-173.
+void DMRG::setup_mps(int* occupancies) {
+  denBK = std::make_unique<SyBookkeeper>(Prob, OptScheme->get_D(0));
+  if (!denBK->IsPossible()) throw std::invalid_argument("DMRG: the targeted symmetry sector is impossible");
+  std::vector<int> occ;
+  if (occupancies) {
+    occ.assign(occupancies, occupancies + L);
+    if (Prob->gReorder()) {
+      std::vector<int> tmp(occ);
+      for (int c = 0; c < L; c++) occ[c] = tmp[Prob->gf2(c)];
+      for (int c = 0; c < L; c++) occupancies[c] = occ[c];
+    }
+  }
+  int left_n = 0, left_i = 0, left_2s = 0;
+  for (int site = 0; site < L; site++) {
+    mps_lay[site] = std::make_unique<MpsLayout>();
+    mps_lay[site]->build(*denBK, site);
+    const MpsLayout& lay = *mps_lay[site];
+    std::vector<double> data(lay.size());
+    for (auto& v : data) v = (2 * static_cast<double>(std::rand()) / RAND_MAX) - 1.0;
+    if (occupancies) {
+      const int right_n = left_n + occ[site];
+      const int right_i = (occ[site] == 1) ? c2g::irrep_prod(left_i, Prob->gIrrep(site)) : left_i;
+      const int right_2s = (occ[site] == 1) ? left_2s + 1 : left_2s;
+      for (int NL = right_n - 2; NL <= right_n; NL++) {
+        const int DS = (right_n == NL + 1) ? 1 : 0;
+        const int IL = (right_n == NL + 1) ? c2g::irrep_prod(right_i, Prob->gIrrep(site)) : right_i;
+        for (int TwoSL = right_2s - DS; TwoSL <= right_2s + DS; TwoSL += 2) {
+          const int k = lay.kappa(NL, TwoSL, IL, right_n, right_2s, right_i);
+          if (k < 0) continue;
+          const int dimL2 = lay.rows[k];
+          double* space = data.data() + lay.k2i[k];
+          for (int row = 0; row < dimL2; row++) space[row] = 0.0;
+          if (NL == left_n && TwoSL == left_2s && IL == left_i) space[0] = 42;
+        }
+      }
+      left_n = right_n;
+      left_i = right_i;
+      left_2s = right_2s;
+    }
+    left_normalize_host(site, data);
+    upload_mps(site, data);
+  }
+}
+
+// CheMPS2/TensorT.cpp:188-289 (QR per right sector, Householder, Q kept) as used by
+// DMRG::left_normalize(site, NULL). Initialisation only.
+void DMRG::left_normalize_host(int site, std::vector<double>& data) {
+  const MpsLayout& lay = *mps_lay[site];
+  const SyBookkeeper& bk = *denBK;
+  for (int NR = bk.gNmin(site + 1); NR <= bk.gNmax(site + 1); NR++)
+    for (int TwoSR = bk.gTwoSmin(site + 1, NR); TwoSR <= bk.gTwoSmax(site + 1, NR); TwoSR += 2)
+      for (int IR = 0; IR < bk.getNumberOfIrreps(); IR++) {
+        const int dimR = bk.gCurrentDim(site + 1, NR, TwoSR, IR);
+        if (dimR <= 0) continue;
+        std::vector<int> blocks;
+        int m = 0;
+        for (int k = 0; k < lay.nkappa; k++)
+          if (lay.NR[k] == NR && lay.TwoSR[k] == TwoSR && lay.IR[k] == IR && lay.rows[k] > 0) {
+            blocks.push_back(k);
+            m += lay.rows[k];
+          }
+        if (m == 0) continue;
+        const int n = dimR;
+        std::vector<double> a(static_cast<size_t>(m) * n);
+        int r0 = 0;
+        for (int k : blocks) {
+          for (int l = 0; l < lay.rows[k]; l++)
+            for (int r = 0; r < n; r++) a[r0 + l + static_cast<size_t>(m) * r] = data[lay.k2i[k] + l + lay.rows[k] * r];
+          r0 += lay.rows[k];
+        }
+        // Householder QR (dgeqr2 conventions), then Q = H_1 ... H_kk applied to I (dorg2r).
+        const int kk = std::min(m, n);
+        std::vector<double> tau(kk, 0.0);
+        for (int j = 0; j < kk; j++) {
+          double* x = &a[j + static_cast<size_t>(m) * j];
+          const int len = m - j;
+          double xnorm = 0.0;
+          for (int i = 1; i < len; i++) xnorm += x[i] * x[i];
+          xnorm = std::sqrt(xnorm);
+          if (xnorm == 0.0) {
+            tau[j] = 0.0;
+            continue;
+          }
+          const double alpha = x[0];
+          const double beta = -std::copysign(std::hypot(alpha, xnorm), alpha);
+          tau[j] = (beta - alpha) / beta;
+          const double scal = 1.0 / (alpha - beta);
+          for (int i = 1; i < len; i++) x[i] *= scal;
+          x[0] = beta;
+          for (int c = j + 1; c < n; c++) {  // apply H_j to the trailing columns
+            double* y = &a[j + static_cast<size_t>(m) * c];
+            double s = y[0];
+            for (int i = 1; i < len; i++) s += x[i] * y[i];
+            s *= tau[j];
+            y[0] -= s;
+            for (int i = 1; i < len; i++) y[i] -= s * x[i];
+          }
+        }
+        std::vector<double> q(static_cast<size_t>(m) * n, 0.0);
+        for (int c = 0; c < kk; c++) q[c + static_cast<size_t>(m) * c] = 1.0;
+        for (int j = kk - 1; j >= 0; j--) {
+          const double* v = &a[j + static_cast<size_t>(m) * j];
+          const int len = m - j;
+          for (int c = j; c < kk; c++) {
+            double* y = &q[j + static_cast<size_t>(m) * c];
+            double s = y[0];
+            for (int i = 1; i < len; i++) s += v[i] * y[i];
+            s *= tau[j];
+            y[0] -= s;
+            for (int i = 1; i < len; i++) y[i] -= s * v[i];
+          }
+        }
+        r0 = 0;
+        for (int k : blocks) {
+          for (int l = 0; l < lay.rows[k]; l++)
+            for (int r = 0; r < n; r++) data[lay.k2i[k] + l + lay.rows[k] * r] = q[r0 + l + static_cast<size_t>(m) * r];
+          r0 += lay.rows[k];
+        }
+      }
+}
+
+void DMRG::upload_mps(int site, const std::vector<double>& data) {
+  if (mps_dev[site]) rt->release(mps_dev[site]);
+  mps_dev[site] = rt->alloc(static_cast<int64_t>(data.size()));
+  C2G_CUDA(cudaMemcpyAsync(mps_dev[site], data.data(), sizeof(double) * data.size(), cudaMemcpyHostToDevice,
+                           rt->stream()));
+  rt->sync();
+  rt->set_slot(c2g::kSlotMpsBase + site, mps_dev[site]);
+}
+
+int DMRG::get_num_mps_var() const {
+  int n = 0;
+  for (int s = 0; s < L; s++) n += static_cast<int>(mps_lay[s]->size());
+  return n;
+}
+
+void DMRG::delete_all_ops() {
+  for (int b = 0; b < L - 1; b++) {
+    if (ops_dev[b]) rt->release(ops_dev[b]);
+    ops_dev[b] = nullptr;
+    ops[b].reset();
+    rt->set_slot(c2g::slot_ops(L, b), nullptr);
+    isAllocated[b] = 0;
+  }
+}
+
+void DMRG::PreSolve() {
+  delete_all_ops();
+  for (int cnt = 0; cnt < L - 2; cnt++) update_moving_right(cnt);
+  TotalMinEnergy = 1e8;
+  MaxDiscWeightLastSweep = 0.0;
+}
+
+// CheMPS2/DMRGoperators.cpp:243-575 via the task compiler: all operators of boundary
+// index + 1, moving right, from those of boundary index and MPS[index].
+void DMRG::update_moving_right(const int index) {
+  const double t0 = now();
+  if (ops_dev[index]) rt->release(ops_dev[index]);
+  ops[index] = std::make_unique<BoundaryOps>();
+  c2g::allocate_ops(*ops[index], *denBK, L, index, true, c2g::slot_ops(L, index));
+  ops_dev[index] = rt->alloc(ops[index]->size);
+  rt->set_slot(c2g::slot_ops(L, index), ops_dev[index]);
+  isAllocated[index] = 1;
+  c2g::UpdateContext ctx;
+  ctx.bk = denBK.get();
+  ctx.prob = Prob;
+  ctx.L = L;
+  ctx.index = index;
+  ctx.moving_right = true;
+  ctx.prev = (index > 0) ? ops[index - 1].get() : nullptr;
+  if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("update_moving_right: left operators missing");
+  ctx.next = ops[index].get();
+  ctx.mps = mps_tensor(mps_lay[index].get(), index);
+  const double tc = now();
+  TaskBuilder tb;
+  c2g::compile_update(tb, ctx);
+  Program p = tb.finalize();
+  stats_.t_compile += now() - tc;
+  auto dp = rt->upload(p);
+  rt->zero(ops_dev[index], ops[index]->size);
+  rt->run(*dp, nullptr, nullptr);
+  rt->sync();
+  stats_.t_update += now() - t0;
+}
+
+// CheMPS2/DMRGoperators.cpp:577-908, mirrored.
+void DMRG::update_moving_left(const int index) {
+  const double t0 = now();
+  if (ops_dev[index]) rt->release(ops_dev[index]);
+  ops[index] = std::make_unique<BoundaryOps>();
+  c2g::allocate_ops(*ops[index], *denBK, L, index, false, c2g::slot_ops(L, index));
+  ops_dev[index] = rt->alloc(ops[index]->size);
+  rt->set_slot(c2g::slot_ops(L, index), ops_dev[index]);
+  isAllocated[index] = 2;
+  c2g::UpdateContext ctx;
+  ctx.bk = denBK.get();
+  ctx.prob = Prob;
+  ctx.L = L;
+  ctx.index = index;
+  ctx.moving_right = false;
+  ctx.prev = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
+  if (index + 1 < L - 1 && isAllocated[index + 1] != 2)
+    throw std::logic_error("update_moving_left: right operators missing");
+  ctx.next = ops[index].get();
+  ctx.mps = mps_tensor(mps_lay[index + 1].get(), index + 1);
+  const double tc = now();
+  TaskBuilder tb;
+  c2g::compile_update(tb, ctx);
+  Program p = tb.finalize();
+  stats_.t_compile += now() - tc;
+  auto dp = rt->upload(p);
+  rt->zero(ops_dev[index], ops[index]->size);
+  rt->run(*dp, nullptr, nullptr);
+  rt->sync();
+  stats_.t_update += now() - t0;
+}
+
+double DMRG::Solve() {
+  bool change = (TotalMinEnergy < 1e8);
+  double Energy = 0.0;
+  for (int instruction = 0; instruction < OptScheme->get_number(); instruction++) {
+    int nIterations = 0;
+    double EnergyPrevious = Energy + 10 * OptScheme->get_energy_conv(instruction);
+    while (std::fabs(Energy - EnergyPrevious) > OptScheme->get_energy_conv(instruction) &&
+           nIterations < OptScheme->get_max_sweeps(instruction)) {
+      EnergyPrevious = Energy;
+      Energy = sweep(false, change, instruction);
+      change = true;
+      Energy = sweep(true, change, instruction);
+      if (verbose)
+        std::printf("instruction %d sweep %d: E = %.15f  max discarded weight = %.3e\n", instruction, nIterations,
+                    Energy, MaxDiscWeightLastSweep);
+      nIterations++;
+    }
+  }
+  return TotalMinEnergy;
+}
+
+// CheMPS2/DMRG.cpp:335-402 (sweepleft / sweepright).
+double DMRG::sweep(const bool moving_right, const bool change, const int instruction) {
+  double Energy = 0.0;
+  const double noise_level = std::fabs(OptScheme->get_noise_prefactor(instruction)) * MaxDiscWeightLastSweep;
+  const double rtol = OptScheme->get_dvdson_rtol(instruction);
+  const int D = OptScheme->get_D(instruction);
+  MaxDiscWeightLastSweep = 0.0;
+  LastMinEnergy = 1e8;
+  if (moving_right) {
+    for (int index = 0; index < L - 2; index++) {
+      Energy = solve_site(index, rtol, noise_level, D, true, change);
+      TotalMinEnergy = std::min(TotalMinEnergy, Energy);
+      LastMinEnergy = std::min(LastMinEnergy, Energy);
+      update_moving_right(index);
+    }
+  } else {
+    for (int index = L - 2; index > 0; index--) {
+      Energy = solve_site(index, rtol, noise_level, D, false, change);
+      TotalMinEnergy = std::min(TotalMinEnergy, Energy);
+      LastMinEnergy = std::min(LastMinEnergy, Energy);
+      update_moving_left(index);
+    }
+  }
+  return Energy;
+}
+
+// CheMPS2/DMRG.cpp:404-452 (solve_site) with Sobject::Join / Split and Heff::SolveDAVIDSON.
+double DMRG::solve_site(const int index, const double dvdson_rtol, const double noise_level,
+                        const int virtual_dimension, const bool moving_right, const bool change) {
+  cudaStream_t s = rt->stream();
+  // ---- Join
+  double t0 = now();
+  TwoSiteLayout S;
+  S.build(*denBK, index);
+  const int64_t veclen = S.size();
+  double* svec = rt->alloc(veclen);
+  {
+    TaskBuilder tb;
+    c2g::compile_join(tb, *denBK, S, mps_tensor(mps_lay[index].get(), index),
+                      mps_tensor(mps_lay[index + 1].get(), index + 1));
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, nullptr, svec);
+    rt->sync();
+  }
+  stats_.t_join += now() - t0;
+
+  // ---- Davidson
+  t0 = now();
+  c2g::HeffContext ctx;
+  ctx.bk = denBK.get();
+  ctx.prob = Prob;
+  ctx.S = &S;
+  ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
+  ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
+  if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("solve_site: left operators missing");
+  if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("solve_site: right operators missing");
+  double tc = now();
+  TaskBuilder tbd;
+  c2g::compile_heff_diag(tbd, ctx);
+  Program pd = tbd.finalize();
+  TaskBuilder tbh;
+  c2g::compile_heff(tbh, ctx);
+  Program ph = tbh.finalize();
+  stats_.t_compile += now() - tc;
+  int maxdim = 1;
+  for (int k = 0; k < S.nkappa; k++) maxdim = std::max(maxdim, std::max(S.rows[k], S.cols[k]));
+  rt->ones(maxdim);
+  double* diag = rt->alloc(veclen);
+  auto dpd = rt->upload(pd);
+  rt->run(*dpd, nullptr, diag);
+  auto dph = rt->upload(ph);
+  rt->prepare(*dph);
+  c2g::DeviceDavidson dav(*rt, veclen, kDavidsonNumVec, kDavidsonNumVecKeep, dvdson_rtol, kDavidsonPrecondCutoff);
+  cudaEvent_t e0, e1;
+  C2G_CUDA(cudaEventCreate(&e0));
+  C2G_CUDA(cudaEventCreate(&e1));
+  float mv_ms = 0.f;
+  auto matvec = [&](const double* x, double* y) {
+    C2G_CUDA(cudaEventRecord(e0, s));
+    rt->run(*dph, const_cast<double*>(x), y);
+    C2G_CUDA(cudaEventRecord(e1, s));
+    C2G_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    mv_ms += ms;
+  };
+  const c2g::DavidsonStats ds = dav.solve(svec, diag, matvec);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  rt->release(diag);
+  stats_.n_matvec += ds.n_matvec;
+  stats_.n_davidson++;
+  stats_.t_matvec += 1e-3 * mv_ms;
+  stats_.matvec_flops += static_cast<double>(dph->flops_repeat) * ds.n_matvec;
+  const double Energy = ds.energy + Prob->gEconst();
+  stats_.last_energy = Energy;
+  stats_.t_solve += now() - t0;
+  if (verbose) std::printf("Energy at sites (%d, %d) is %.15f  [%d matvecs]\n", index, index + 1, Energy, ds.n_matvec);
+
+  // ---- Split
+  t0 = now();
+  if (noise_level > 0.0) {
+    // CheMPS2/Sobject.cpp:652-661: noise in program convention, i.e. scaled by
+    // sqrt(2S_R + 1) in the symmetric convention kept here.
+    std::vector<double> noise(veclen);
+    for (int k = 0; k < S.nkappa; k++) {
+      const double f = std::sqrt(S.TwoSR[k] + 1.0);
+      for (int64_t c = S.k2i[k]; c < S.k2i[k + 1]; c++)
+        noise[c] = f * noise_level * (static_cast<double>(std::rand()) / RAND_MAX - 0.5);
+    }
+    double* dn = rt->alloc(veclen);
+    C2G_CUDA(cudaMemcpyAsync(dn, noise.data(), sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
+    C2G_CUDA(c2g::launch_axpy(svec, 1.0, dn, veclen, s));
+    c2g::count_launches(1);
+    rt->sync();
+    rt->release(dn);
+  }
+  const c2g::SplitPlan plan = c2g::plan_split(*denBK, index, moving_right);
+  double* work = rt->alloc(std::max<int64_t>(plan.work_size, 1));
+  rt->zero(work, plan.work_size);
+  rt->set_slot(c2g::kSlotWork, work);
+  {
+    TaskBuilder tb;
+    c2g::compile_split_assemble(tb, *denBK, S, plan);
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, svec, nullptr);
+  }
+  // Eigendecomposition of every Gram matrix (FP64, cuSOLVER syevd).
+  cusolverDnHandle_t sh;
+  check_solver(cusolverDnCreate(&sh), "create");
+  check_solver(cusolverDnSetStream(sh, s), "stream");
+  int gmax = 0;
+  for (const auto& c : plan.centers) gmax = std::max(gmax, c.cd > 0 ? c.g : 0);
+  int lwork = 0;
+  double* dwork = nullptr;
+  int* dinfo = nullptr;
+  C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dinfo), sizeof(int) * std::max<size_t>(plan.centers.size(), 1), s));
+  C2G_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * std::max<size_t>(plan.centers.size(), 1), s));
+  if (gmax > 0) {
+    check_solver(cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, gmax, work, gmax,
+                                             work, &lwork),
+                 "bufferSize");
+    dwork = rt->alloc(std::max(lwork, 1));
+  }
+  for (size_t ic = 0; ic < plan.centers.size(); ic++) {
+    const auto& c = plan.centers[ic];
+    if (c.cd <= 0) continue;
+    int lw = 0;
+    check_solver(cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, c.g, work + c.offG,
+                                             c.g, work + c.offE, &lw),
+                 "bufferSize");
+    if (lw > lwork) {
+      rt->release(dwork);
+      lwork = lw;
+      dwork = rt->alloc(lwork);
+    }
+    check_solver(cusolverDnDsyevd(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, c.g, work + c.offG, c.g,
+                                  work + c.offE, dwork, lwork, dinfo + ic),
+                 "syevd");
+    // eigenvectors in descending order of the eigenvalue
+    C2G_CUDA(c2g::launch_reverse_columns(work + c.offU, work + c.offG, c.g, c.g, s));
+    c2g::count_launches(1);
+  }
+  std::vector<double> evals(plan.work_size > 0 ? plan.work_size : 1);
+  std::vector<int> info(std::max<size_t>(plan.centers.size(), 1));
+  // only the eigenvalue segments are needed; copy each
+  for (const auto& c : plan.centers)
+    if (c.cd > 0)
+      C2G_CUDA(cudaMemcpyAsync(evals.data() + c.offE, work + c.offE, sizeof(double) * c.g, cudaMemcpyDeviceToHost, s));
+  C2G_CUDA(cudaMemcpyAsync(info.data(), dinfo, sizeof(int) * info.size(), cudaMemcpyDeviceToHost, s));
+  rt->sync();
+  for (size_t ic = 0; ic < plan.centers.size(); ic++)
+    if (info[ic] != 0) throw std::runtime_error("Split: eigensolver failed for a center sector");
+  cusolverDnDestroy(sh);
+  if (dwork) rt->release(dwork);
+  C2G_CUDA(cudaFreeAsync(dinfo, s));
+
+  // Singular values per center sector, descending (CheMPS2/Sobject.cpp:418-420).
+  const int nC = static_cast<int>(plan.centers.size());
+  std::vector<std::vector<double>> lambdas(nC);
+  for (int ic = 0; ic < nC; ic++) {
+    const auto& c = plan.centers[ic];
+    lambdas[ic].resize(c.cd);
+    for (int i = 0; i < c.cd; i++) lambdas[ic][i] = std::sqrt(std::max(evals[c.offE + c.g - 1 - i], 0.0));
+  }
+  // CheMPS2/Sobject.cpp:431-519: new virtual dimensions and discarded weight.
+  double discardedWeight = 0.0;
+  bool updateSectors = false;
+  std::vector<int> NewDims(nC);
+  if (change) {
+    int totalDimSVD = 0;
+    for (int ic = 0; ic < nC; ic++) {
+      NewDims[ic] = plan.centers[ic].cd;
+      totalDimSVD += NewDims[ic];
+    }
+    if (totalDimSVD > virtual_dimension) {
+      std::vector<double> values;
+      values.reserve(totalDimSVD);
+      for (int ic = 0; ic < nC; ic++)
+        for (int i = 0; i < NewDims[ic]; i++) values.push_back(lambdas[ic][i]);
+      std::sort(values.begin(), values.end(), std::greater<double>());
+      const double lowerBound = values[virtual_dimension];
+      for (int ic = 0; ic < nC; ic++)
+        for (int cnt = 0; cnt < NewDims[ic]; cnt++)
+          if (lambdas[ic][cnt] <= lowerBound) NewDims[ic] = cnt;
+      double totalSum = 0.0, discardedSum = 0.0;
+      for (int ic = 0; ic < nC; ic++)
+        for (int i = 0; i < plan.centers[ic].cd; i++) {
+          const double temp = (plan.centers[ic].TwoSM + 1) * lambdas[ic][i] * lambdas[ic][i];
+          totalSum += temp;
+          if (lambdas[ic][i] <= lowerBound) discardedSum += temp;
+        }
+      discardedWeight = discardedSum / totalSum;
+    }
+    for (int ic = 0; ic < nC; ic++) {
+      const auto& c = plan.centers[ic];
+      if (NewDims[ic] != denBK->gCurrentDim(index + 1, c.NM, c.TwoSM, c.IM)) updateSectors = true;
+    }
+  }
+  if (updateSectors)
+    for (int ic = 0; ic < nC; ic++) {
+      const auto& c = plan.centers[ic];
+      denBK->SetDim(index + 1, c.NM, c.TwoSM, c.IM, NewDims[ic]);
+    }
+  std::vector<int> dims_m(nC);
+  for (int ic = 0; ic < nC; ic++) {
+    const auto& c = plan.centers[ic];
+    dims_m[ic] = denBK->gCurrentDim(index + 1, c.NM, c.TwoSM, c.IM);
+  }
+  // New MPS tensors for sites index and index + 1 (CheMPS2/Sobject.cpp:521-590).
+  for (int site = index; site <= index + 1; site++) {
+    mps_lay[site] = std::make_unique<MpsLayout>();
+    mps_lay[site]->build(*denBK, site);
+    double* old = mps_dev[site];
+    mps_dev[site] = rt->alloc(mps_lay[site]->size());
+    rt->zero(mps_dev[site], mps_lay[site]->size());
+    rt->set_slot(c2g::kSlotMpsBase + site, mps_dev[site]);
+    rt->release(old);
+  }
+  {
+    TaskBuilder tb;
+    c2g::compile_split_copy(tb, plan, dims_m, mps_tensor(mps_lay[index].get(), index),
+                            mps_tensor(mps_lay[index + 1].get(), index + 1));
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, nullptr, nullptr);
+  }
+  rt->sync();
+  rt->set_slot(c2g::kSlotWork, nullptr);
+  rt->release(work);
+  rt->release(svec);
+  MaxDiscWeightLastSweep = std::max(MaxDiscWeightLastSweep, discardedWeight);
+  stats_.t_split += now() - t0;
+  return Energy;
+}
+
+double DMRG::bench_heff(const int index, const int warmup, const int steps, double* flops, double* bytes,
+                        long long* launches) {
+  if (index < 0 || index > L - 2) throw std::out_of_range("bench_heff: index");
+  cudaStream_t s = rt->stream();
+  TwoSiteLayout S;
+  S.build(*denBK, index);
+  const int64_t veclen = S.size();
+  double* x = rt->alloc(veclen);
+  double* y = rt->alloc(veclen);
+  {
+    TaskBuilder tb;
+    c2g::compile_join(tb, *denBK, S, mps_tensor(mps_lay[index].get(), index),
+                      mps_tensor(mps_lay[index + 1].get(), index + 1));
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, nullptr, x);
+  }
+  c2g::HeffContext ctx;
+  ctx.bk = denBK.get();
+  ctx.prob = Prob;
+  ctx.S = &S;
+  ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
+  ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
+  if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("bench_heff: left operators missing");
+  if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("bench_heff: right operators missing");
+  TaskBuilder tbh;
+  c2g::compile_heff(tbh, ctx);
+  Program ph = tbh.finalize();
+  auto dph = rt->upload(ph);
+  rt->prepare(*dph);
+  for (int i = 0; i < warmup; i++) rt->run(*dph, x, y);
+  rt->sync();
+  const long long l0 = c2g::kernel_launches();
+  cudaEvent_t e0, e1;
+  C2G_CUDA(cudaEventCreate(&e0));
+  C2G_CUDA(cudaEventCreate(&e1));
+  C2G_CUDA(cudaEventRecord(e0, s));
+  for (int i = 0; i < steps; i++) rt->run(*dph, x, y);
+  C2G_CUDA(cudaEventRecord(e1, s));
+  C2G_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (launches) *launches = c2g::kernel_launches() - l0;
+  if (flops) *flops = static_cast<double>(dph->flops_repeat);
+  if (bytes) *bytes = static_cast<double>(tbh.operand_bytes()) + 16.0 * veclen;
+  rt->release(x);
+  rt->release(y);
+  rt->sync();
+  return steps > 0 ? ms / steps : 0.0;
+}
+
+long long DMRG::sobject_size(const int index) const {
+  if (index < 0 || index > L - 2) throw std::out_of_range("sobject_size: index");
+  TwoSiteLayout S;
+  S.build(*denBK, index);
+  return S.size();
+}
+
+void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, double* y, double* diag,
+                           const long long n) {
+  if (index < 0 || index > L - 2) throw std::out_of_range("heff_apply: index");
+  if (!x || !y) throw std::invalid_argument("heff_apply: null buffer");
+  cudaStream_t s = rt->stream();
+  TwoSiteLayout S;
+  S.build(*denBK, index);
+  const int64_t veclen = S.size();
+  if (n != veclen) throw std::invalid_argument("heff_apply: vector length differs from the two-site object size");
+  double* dx = rt->alloc(veclen);
+  double* dy = rt->alloc(veclen);
+  if (join_into_x) {
+    TaskBuilder tb;
+    c2g::compile_join(tb, *denBK, S, mps_tensor(mps_lay[index].get(), index),
+                      mps_tensor(mps_lay[index + 1].get(), index + 1));
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, nullptr, dx);
+    C2G_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
+  } else {
+    C2G_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
+  }
+  c2g::HeffContext ctx;
+  ctx.bk = denBK.get();
+  ctx.prob = Prob;
+  ctx.S = &S;
+  ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
+  ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
+  if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("heff_apply: left operators missing");
+  if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("heff_apply: right operators missing");
+  {
+    TaskBuilder tb;
+    c2g::compile_heff(tb, ctx);
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, dx, dy);
+    C2G_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
+  }
+  if (diag) {
+    int maxdim = 1;
+    for (int k = 0; k < S.nkappa; k++) maxdim = std::max(maxdim, std::max(S.rows[k], S.cols[k]));
+    rt->ones(maxdim);
+    TaskBuilder tb;
+    c2g::compile_heff_diag(tb, ctx);
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, nullptr, dy);
+    C2G_CUDA(cudaMemcpyAsync(diag, dy, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
+  }
+  rt->sync();
+  rt->release(dx);
+  rt->release(dy);
+  rt->sync();
+}
+
+}  // namespace CheMPS2

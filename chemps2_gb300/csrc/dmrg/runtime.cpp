@@ -1,0 +1,210 @@
+#include "runtime.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <numeric>
+#include <sstream>
+
+namespace c2g {
+
+namespace {
+std::atomic<int64_t> g_launches{0};
+inline int64_t align64(int64_t x) { return (x + 63) & ~int64_t(63); }
+}  // namespace
+
+int64_t kernel_launches() { return g_launches.load(); }
+void count_launches(int64_t n) { g_launches += n; }
+
+void cuda_check(cudaError_t e, const char* expr, const char* file, int line) {
+  if (e == cudaSuccess) return;
+  std::ostringstream os;
+  os << "CUDA error " << cudaGetErrorName(e) << " (" << cudaGetErrorString(e) << ") at " << file << ":" << line
+     << " in " << expr;
+  throw CudaError(e, os.str());
+}
+
+DevProgram::~DevProgram() {
+  if (rt) {
+    if (blob) rt->release(blob);
+    if (combo) rt->release(combo);
+  }
+}
+
+Runtime::Runtime(int L, int device) : L_(L) {
+  if (num_slots(L) > kMaxSlots) throw std::invalid_argument("chain too long for the device slot table");
+  int count = 0;
+  C2G_CUDA(cudaGetDeviceCount(&count));
+  if (count <= 0) throw std::runtime_error("no CUDA device available: the DMRG hot path runs only on the GPU");
+  C2G_CUDA(cudaSetDevice(device));
+  C2G_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  // Keep freed blocks in the stream-ordered pool instead of returning them to the driver.
+  cudaMemPool_t pool;
+  C2G_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t threshold = UINT64_MAX;
+  C2G_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+  host_slots_.assign(kMaxSlots, nullptr);
+  C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots_), sizeof(double*) * kMaxSlots));
+  C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&partial_), sizeof(double) * (kDotBlocks * 64 + 4096)));
+}
+
+Runtime::~Runtime() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  if (p1_) cudaFreeAsync(p1_, stream_);
+  if (ones_) cudaFreeAsync(ones_, stream_);
+  if (stream_) cudaStreamSynchronize(stream_);
+  cudaFree(dev_slots_);
+  cudaFree(partial_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+double* Runtime::alloc(int64_t n) {
+  void* p = nullptr;
+  const size_t bytes = sizeof(double) * static_cast<size_t>(std::max<int64_t>(n, 1));
+  C2G_CUDA(cudaMallocAsync(&p, bytes, stream_));
+  return static_cast<double*>(p);
+}
+
+void Runtime::release(void* p) {
+  if (p) C2G_CUDA(cudaFreeAsync(p, stream_));
+}
+
+void Runtime::zero(double* p, int64_t n) {
+  if (n > 0) C2G_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, stream_));
+}
+
+void Runtime::set_slot(int slot, double* p) {
+  if (slot < 0 || slot >= kMaxSlots) throw std::out_of_range("slot");
+  if (host_slots_[slot] != p) {
+    host_slots_[slot] = p;
+    slots_dirty_ = true;
+  }
+}
+
+void Runtime::flush_slots() {
+  if (!slots_dirty_) return;
+  C2G_CUDA(cudaMemcpyAsync(dev_slots_, host_slots_.data(), sizeof(double*) * kMaxSlots, cudaMemcpyHostToDevice,
+                           stream_));
+  // The host vector may change before the copy runs: wait for it.
+  C2G_CUDA(cudaStreamSynchronize(stream_));
+  slots_dirty_ = false;
+}
+
+void Runtime::ensure_p1(int64_t n) {
+  if (n <= p1_cap_) return;
+  if (p1_) release(p1_);
+  p1_cap_ = std::max<int64_t>(n, p1_cap_ * 3 / 2);
+  p1_ = alloc(p1_cap_);
+}
+
+const double* Runtime::ones(int64_t n) {
+  if (n > ones_cap_) {
+    if (ones_) release(ones_);
+    ones_cap_ = std::max<int64_t>(n, 1024);
+    ones_ = alloc(ones_cap_);
+    C2G_CUDA(launch_fill(ones_, 1.0, ones_cap_, stream_));
+    count_launches(1);
+  }
+  return ones_;
+}
+
+SlotPtrs Runtime::ptrs(double* x, double* y, double* combo) {
+  flush_slots();
+  SlotPtrs sp;
+  sp.table = dev_slots_;
+  sp.x = x;
+  sp.y = y;
+  sp.p1 = p1_;
+  sp.combo = combo;
+  sp.ones = ones_;
+  return sp;
+}
+
+std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
+  auto dp = std::make_unique<DevProgram>();
+  dp->rt = this;
+  dp->first_repeat = p.first_repeat_stage;
+  dp->p1_size = p.p1_size;
+  dp->combo_size = p.combo_size;
+  // Tile lists: every group cut into 32 x 32 tiles, groups with the most work first.
+  std::vector<std::vector<int2>> tiles(p.stages.size());
+  int64_t bytes = 0;
+  for (size_t s = 0; s < p.stages.size(); s++) {
+    const Stage& st = p.stages[s];
+    std::vector<int> order(st.groups.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return st.groups[a].work > st.groups[b].work; });
+    for (int g : order) {
+      const Group& G = st.groups[g];
+      if (G.m <= 0 || G.n <= 0) continue;
+      const int tm = (G.m + kTile - 1) / kTile, tn = (G.n + kTile - 1) / kTile;
+      if (tm >= 32768 || tn >= 65536) throw std::invalid_argument("output block too large for the tile index");
+      for (int i = 0; i < tm; i++)
+        for (int j = 0; j < tn; j++) tiles[s].push_back(make_int2(g, (i << 16) | j));
+    }
+    bytes += align64(sizeof(Group) * st.groups.size()) + align64(sizeof(Term) * st.terms.size()) +
+             align64(sizeof(int2) * tiles[s].size());
+  }
+  std::vector<char> host(static_cast<size_t>(std::max<int64_t>(bytes, 64)));
+  if (bytes > 0) {
+    C2G_CUDA(cudaMallocAsync(&dp->blob, bytes, stream_));
+  }
+  char* dbase = static_cast<char*>(dp->blob);
+  int64_t off = 0;
+  for (size_t s = 0; s < p.stages.size(); s++) {
+    const Stage& st = p.stages[s];
+    DevStage ds;
+    ds.name = st.name;
+    ds.ngroups = static_cast<int>(st.groups.size());
+    ds.nterms = static_cast<int>(st.terms.size());
+    ds.ntiles = static_cast<int>(tiles[s].size());
+    ds.flops = st.flops;
+    auto put = [&](const void* src, size_t n) -> const void* {
+      if (n) std::memcpy(host.data() + off, src, n);
+      const void* d = dbase + off;
+      off += align64(static_cast<int64_t>(n));
+      return d;
+    };
+    ds.groups = static_cast<const Group*>(put(st.groups.data(), sizeof(Group) * st.groups.size()));
+    ds.terms = static_cast<const Term*>(put(st.terms.data(), sizeof(Term) * st.terms.size()));
+    ds.tiles = static_cast<const int2*>(put(tiles[s].data(), sizeof(int2) * tiles[s].size()));
+    dp->nterms += ds.nterms;
+    if (static_cast<int>(s) < dp->first_repeat) dp->flops_once += ds.flops;
+    else dp->flops_repeat += ds.flops;
+    dp->stages.push_back(ds);
+  }
+  if (bytes > 0) {
+    C2G_CUDA(cudaMemcpyAsync(dp->blob, host.data(), bytes, cudaMemcpyHostToDevice, stream_));
+    C2G_CUDA(cudaStreamSynchronize(stream_));  // `host` goes out of scope
+  }
+  if (dp->combo_size > 0) dp->combo = alloc(dp->combo_size);
+  return dp;
+}
+
+void Runtime::prepare(DevProgram& p) {
+  if (p.prepared) return;
+  ensure_p1(p.p1_size);
+  const SlotPtrs sp = ptrs(nullptr, nullptr, p.combo);
+  for (int s = 0; s < p.first_repeat; s++) {
+    const DevStage& ds = p.stages[s];
+    C2G_CUDA(launch_grouped_gemm(ds.groups, ds.terms, ds.tiles, ds.ntiles, sp, stream_));
+    if (ds.ntiles) count_launches(1);
+  }
+  p.prepared = true;
+}
+
+void Runtime::run(DevProgram& p, double* x, double* y) {
+  prepare(p);
+  ensure_p1(p.p1_size);
+  const SlotPtrs sp = ptrs(x, y, p.combo);
+  for (size_t s = p.first_repeat; s < p.stages.size(); s++) {
+    const DevStage& ds = p.stages[s];
+    C2G_CUDA(launch_grouped_gemm(ds.groups, ds.terms, ds.tiles, ds.ntiles, sp, stream_));
+    if (ds.ntiles) count_launches(1);
+  }
+}
+
+void Runtime::sync() { C2G_CUDA(cudaStreamSynchronize(stream_)); }
+
+}  // namespace c2g

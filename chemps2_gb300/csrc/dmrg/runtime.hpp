@@ -1,0 +1,109 @@
+// Device runtime of one DMRG object: its CUDA stream, the slot table that turns task
+// references into device pointers, uploaded task programs and their scratch buffers.
+//
+// A task Program (host/tasks.hpp) is uploaded once into one device allocation (groups,
+// terms and the tile list of every stage) and can then be run any number of times with
+// different X / Y vectors, e.g. once per Davidson matvec. Stages that only combine
+// operator blocks (the "once" stages) run when the program is prepared.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../device/kernels.cuh"
+#include "../host/tasks.hpp"
+
+namespace c2g {
+
+struct CudaError : std::runtime_error {
+  cudaError_t code;
+  CudaError(cudaError_t c, const std::string& what) : std::runtime_error(what), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* expr, const char* file, int line);
+#define C2G_CUDA(x) ::c2g::cuda_check((x), #x, __FILE__, __LINE__)
+
+class Runtime;
+
+struct DevStage {
+  const Group* groups = nullptr;
+  const Term* terms = nullptr;
+  const int2* tiles = nullptr;
+  int ngroups = 0, nterms = 0, ntiles = 0;
+  int64_t flops = 0;
+  std::string name;
+};
+
+struct DevProgram {
+  Runtime* rt = nullptr;
+  std::vector<DevStage> stages;
+  int first_repeat = 0;
+  int64_t p1_size = 0, combo_size = 0;
+  int64_t flops_once = 0, flops_repeat = 0;
+  int64_t nterms = 0;
+  void* blob = nullptr;
+  double* combo = nullptr;
+  bool prepared = false;
+  DevProgram() = default;
+  DevProgram(const DevProgram&) = delete;
+  DevProgram& operator=(const DevProgram&) = delete;
+  ~DevProgram();
+};
+
+class Runtime {
+ public:
+  explicit Runtime(int L, int device = 0);
+  ~Runtime();
+  Runtime(const Runtime&) = delete;
+  Runtime& operator=(const Runtime&) = delete;
+
+  cudaStream_t stream() const { return stream_; }
+  int L() const { return L_; }
+
+  // Device memory, stream ordered on this runtime's stream.
+  double* alloc(int64_t n_doubles);
+  void release(void* p);
+  void zero(double* p, int64_t n);
+
+  // Slot table (slots other than X, Y, P1, Combo and Ones).
+  void set_slot(int slot, double* p);
+  double* slot(int s) const { return host_slots_[s]; }
+
+  std::unique_ptr<DevProgram> upload(const Program& p);
+  void prepare(DevProgram& p);
+  void run(DevProgram& p, double* x, double* y);
+
+  const double* ones(int64_t n);
+  void sync();
+
+  // Scratch for reductions and small Davidson quantities.
+  double* partial() { return partial_; }
+
+ private:
+  friend struct DevProgram;
+  void flush_slots();
+  void ensure_p1(int64_t n);
+  SlotPtrs ptrs(double* x, double* y, double* combo);
+
+  int L_;
+  cudaStream_t stream_ = nullptr;
+  std::vector<double*> host_slots_;
+  const double** dev_slots_ = nullptr;
+  bool slots_dirty_ = true;
+  double* p1_ = nullptr;
+  int64_t p1_cap_ = 0;
+  double* ones_ = nullptr;
+  int64_t ones_cap_ = 0;
+  double* partial_ = nullptr;
+};
+
+// Number of kernels this library has launched in this process (all runtimes).
+int64_t kernel_launches();
+void count_launches(int64_t n);
+
+}  // namespace c2g

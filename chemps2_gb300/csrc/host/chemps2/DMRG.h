@@ -1,0 +1,104 @@
+// Drop-in replacement for CheMPS2::DMRG (CheMPS2/include/chemps2/DMRG.h:93-162), for the
+// two-site ground-state sweep: DMRG(Problem*, ConvergenceScheme*, ...), Solve() and
+// PreSolve(). The MPS, the renormalized operators of every boundary and the Davidson
+// vectors live in GPU memory; the Heff matvec, its diagonal, Join, Split and the operator
+// updates run as device task programs (the task compiler is in the host sources, the
+// kernels in the device sources). There is no CPU execution path: without a CUDA device
+// the constructor throws.
+#pragma once
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ConvergenceScheme.h"
+#include "Problem.h"
+#include "SyBookkeeper.h"
+
+namespace c2g {
+class Runtime;
+struct BoundaryOps;
+struct MpsLayout;
+}  // namespace c2g
+
+namespace CheMPS2 {
+
+struct DMRGStats {
+  long long n_matvec = 0;         // Heff applications
+  long long n_davidson = 0;       // Davidson solves
+  double t_join = 0, t_solve = 0, t_split = 0, t_update = 0;  // seconds, host wall clock
+  double t_matvec = 0;            // seconds inside Heff applications (device time)
+  double t_compile = 0;           // seconds in the host task compiler
+  double matvec_flops = 0;        // ledger flops of all Heff applications
+  double matvec_bytes = 0;        // ledger bytes of all Heff applications
+  double last_energy = 0;
+};
+
+class DMRG {
+ public:
+  DMRG(Problem* Prob, ConvergenceScheme* OptScheme, const bool makechkpt = false,
+       const std::string tmpfolder = "/tmp", int* occupancies = nullptr);
+  ~DMRG();
+  DMRG(const DMRG&) = delete;
+  DMRG& operator=(const DMRG&) = delete;
+
+  // Sweeps according to the convergence scheme; returns the lowest energy encountered
+  // (including the constant part of the Hamiltonian), as CheMPS2/DMRG.cpp:268-333.
+  double Solve();
+  // Rebuilds every renormalized operator from the current MPS (CheMPS2/DMRG.cpp:258-266);
+  // required after Problem::setMxElement.
+  void PreSolve();
+
+  int get_num_mps_var() const;
+  double get_MaxDiscardedWeightLastSweep() const { return MaxDiscWeightLastSweep; }
+  double get_TotalMinEnergy() const { return TotalMinEnergy; }
+  const SyBookkeeper* get_bookkeeper() const { return denBK.get(); }
+  const DMRGStats& stats() const { return stats_; }
+  void reset_stats() { stats_ = DMRGStats(); }
+  void set_verbose(bool v) { verbose = v; }
+
+  // One two-site step at sites (index, index + 1): Join, Davidson, Split. Returns the
+  // energy (with the constant part). Exposed for the benchmark and tests.
+  double solve_site(const int index, const double dvdson_rtol, const double noise_level,
+                    const int virtual_dimension, const bool moving_right, const bool change);
+  void update_moving_right(const int index);
+  void update_moving_left(const int index);
+
+  // Benchmark support: build the two-site object at `index`, then time `steps` Heff
+  // applications after `warmup` untimed ones. Returns milliseconds per application and
+  // the ledger work of one application.
+  double bench_heff(const int index, const int warmup, const int steps, double* flops, double* bytes,
+                    long long* launches);
+
+  // Host-buffer access to the effective Hamiltonian at sites (index, index + 1), in the
+  // symmetric convention: y = Heff x (and its diagonal when diag is non-null). With
+  // join_into_x, x is first overwritten by the joined current two-site object.
+  long long sobject_size(const int index) const;
+  void heff_apply_host(const int index, const bool join_into_x, double* x, double* y, double* diag,
+                       const long long n);
+
+ private:
+  void setup_mps(int* occupancies);
+  void left_normalize_host(int site, std::vector<double>& data);
+  void upload_mps(int site, const std::vector<double>& data);
+  void delete_all_ops();
+  double sweep(const bool moving_right, const bool change, const int instruction);
+
+  Problem* Prob;
+  ConvergenceScheme* OptScheme;
+  int L;
+  bool verbose = false;
+  std::unique_ptr<SyBookkeeper> denBK;
+  std::unique_ptr<c2g::Runtime> rt;
+  std::vector<std::unique_ptr<c2g::MpsLayout>> mps_lay;
+  std::vector<double*> mps_dev;
+  std::vector<std::unique_ptr<c2g::BoundaryOps>> ops;
+  std::vector<double*> ops_dev;
+  std::vector<int> isAllocated;  // 0 none, 1 moving right, 2 moving left
+  double TotalMinEnergy = 1e8;
+  double LastMinEnergy = 1e8;
+  double MaxDiscWeightLastSweep = 0.0;
+  DMRGStats stats_;
+};
+
+}  // namespace CheMPS2

@@ -19,8 +19,6 @@
 
 namespace c2g {
 
-constexpr int kSlotOnes = 5;  // a vector of 1.0, at least as long as the largest sector dim
-
 struct HeffContext {
   const CheMPS2::SyBookkeeper* bk = nullptr;
   const CheMPS2::Problem* prob = nullptr;

@@ -365,6 +365,7 @@ struct Emit {
           case 2: nx = n - 2; sxu = su; ixu = i; sxd = su - 1; ixd = irrep_prod(i, Li); break;
           default: nx = n - 2; sxu = su; ixu = i; sxd = su + 1; ixd = irrep_prod(i, Li); break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         alpha = (g <= 1) ? std::sqrt(0.5) : ph(su + 1 - sxd) * std::sqrt(0.5 * (sxd + 1.0) / (su + 1.0));
       } else {
         const int irr = irrep_prod(i, bk.gIrrep(index));
@@ -374,6 +375,7 @@ struct Emit {
           case 2: nx = n + 1; sxu = su - 1; ixu = irr; sxd = su; ixd = idn; break;
           default: nx = n + 1; sxu = su + 1; ixu = irr; sxd = su; ixd = idn; break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         alpha = (g <= 1) ? std::sqrt(0.5) * (sxd + 1.0) / (su + 1.0)
                          : ph(su - sxu + 1) * std::sqrt(0.5 * (sxu + 1.0) / (su + 1.0));
       }
@@ -397,6 +399,7 @@ struct Emit {
           case 2: nx = n - 2; sxu = su; ixu = i; sxd = sd - 1; ixd = irrep_prod(i, Li); break;
           default: nx = n - 2; sxu = su; ixu = i; sxd = sd + 1; ixd = irrep_prod(i, Li); break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         if (g <= 1) alpha = ph(sxu + sd + 3) * std::sqrt(3.0 * (su + 1)) * wigner6j(1, 1, 2, su, sd, sxu);
         else alpha = ph(su + sd + 2) * std::sqrt(3.0 * (sxd + 1)) * wigner6j(1, 1, 2, su, sd, sxd);
       } else {
@@ -407,6 +410,7 @@ struct Emit {
           case 2: nx = n + 1; sxu = su - 1; ixu = irr; sxd = sd; ixd = idn; break;
           default: nx = n + 1; sxu = su + 1; ixu = irr; sxd = sd; ixd = idn; break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         if (g <= 1)
           alpha = ph(sd + sxd + 1) * std::sqrt(3.0 / (su + 1.0)) * (sxd + 1) * wigner6j(1, 1, 2, su, sd, sxd);
         else
@@ -434,6 +438,7 @@ struct Emit {
           case 2: nx = n - 1; sxu = su - 1; ixu = il; sxd = su; ixd = idn; break;
           default: nx = n - 1; sxu = su + 1; ixu = il; sxd = su; ixd = idn; break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         alpha = (g <= 1) ? ph(su - sxd + 1) * std::sqrt(0.5 * (sxd + 1.0) / (su + 1.0)) : -std::sqrt(0.5);
       } else {
         const int irr = irrep_prod(i, bk.gIrrep(index));
@@ -443,6 +448,7 @@ struct Emit {
           case 2: nx = n + 2; sxu = su; ixu = i; sxd = su - 1; ixd = irrep_prod(i, Li); break;
           default: nx = n + 2; sxu = su; ixu = i; sxd = su + 1; ixd = irrep_prod(i, Li); break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         alpha = (g <= 1) ? ph(su - sxu + 1) * std::sqrt(0.5 * (sxu + 1.0) / (su + 1.0))
                          : -std::sqrt(0.5) * (sxd + 1.0) / (su + 1.0);
       }
@@ -466,6 +472,7 @@ struct Emit {
           case 2: nx = n - 1; sxu = su - 1; ixu = il; sxd = sd; ixd = idn; break;
           default: nx = n - 1; sxu = su + 1; ixu = il; sxd = sd; ixd = idn; break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         if (g <= 1) alpha = ph(su + sd + 2) * std::sqrt(3.0 * (sxd + 1)) * wigner6j(1, 1, 2, su, sd, sxd);
         else alpha = ph(sxu + sd + 1) * std::sqrt(3.0 * (su + 1)) * wigner6j(1, 1, 2, su, sd, sxu);
       } else {
@@ -476,6 +483,7 @@ struct Emit {
           case 2: nx = n + 2; sxu = su; ixu = i; sxd = sd - 1; ixd = irrep_prod(i, Li); break;
           default: nx = n + 2; sxu = su; ixu = i; sxd = sd + 1; ixd = irrep_prod(i, Li); break;
         }
+        if (sxu < 0 || sxd < 0) return false;
         if (g <= 1) alpha = ph(su + sd + 2) * std::sqrt(3.0 * (sxu + 1)) * wigner6j(1, 1, 2, su, sd, sxu);
         else
           alpha = ph(su + sxd + 1) * std::sqrt(3.0 / (sd + 1.0)) * (sxd + 1) * wigner6j(1, 1, 2, su, sd, sxd);

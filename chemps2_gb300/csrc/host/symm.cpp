@@ -5,7 +5,8 @@
 #include "symm.hpp"
 
 #include <algorithm>
-#include <cassert>
+#include <stdexcept>
+#include <string>
 #include <cstdlib>
 
 namespace c2g {
@@ -28,9 +29,11 @@ double sqrt_delta(int a, int b, int c) {
 }  // namespace
 
 double wigner6j(int ja, int jb, int jc, int jd, int je, int jf) {
-  assert(ja >= 0 && jb >= 0 && jc >= 0 && jd >= 0 && je >= 0 && jf >= 0);
-  assert(ja <= kWignerMax2j && jb <= kWignerMax2j && jc <= kWignerMax2j &&
-         jd <= kWignerMax2j && je <= kWignerMax2j && jf <= kWignerMax2j);
+  if (ja < 0 || jb < 0 || jc < 0 || jd < 0 || je < 0 || jf < 0 || ja > kWignerMax2j || jb > kWignerMax2j ||
+      jc > kWignerMax2j || jd > kWignerMax2j || je > kWignerMax2j || jf > kWignerMax2j)
+    throw std::logic_error("wigner6j: argument out of range (" + std::to_string(ja) + "," + std::to_string(jb) + "," +
+                           std::to_string(jc) + "," + std::to_string(jd) + "," + std::to_string(je) + "," +
+                           std::to_string(jf) + ")");
   if (triangle_fails(ja, jb, jc) || triangle_fails(jd, je, jc) ||
       triangle_fails(ja, je, jf) || triangle_fails(jd, jb, jf))
     return 0.0;

@@ -73,6 +73,19 @@ void TaskBuilder::add_term(StageBuf& sb, const Blk& out, double alpha, const Blk
   gr.work += V ? int64_t(2) * gr.m * gr.n * t.k : int64_t(gr.m) * gr.n;
 }
 
+void TaskBuilder::note_operand(const Blk& b) {
+  if (!b.valid || ref_slot(b.ref) < kSlotMpsBase) return;
+  const int64_t n = int64_t(b.rows) * b.cols;
+  int64_t& cur = operands_[b.ref];
+  if (n > cur) cur = n;
+}
+
+int64_t TaskBuilder::operand_bytes() const {
+  int64_t s = 0;
+  for (const auto& kv : operands_) s += kv.second;
+  return 8 * s;
+}
+
 Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int rows, int cols,
                          const std::vector<bool>* transposed) {
   if (parts.empty()) return Blk();
@@ -90,6 +103,7 @@ Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int r
   append_bytes(key, &cols, sizeof(int));
   auto it = combo_cache_.find(key);
   if (it != combo_cache_.end()) return it->second;
+  for (const auto& pr : parts) note_operand(pr.second);
   const Blk out = Blk::make(make_ref(kSlotCombo, combo_size_), rows, cols);
   combo_size_ = align4(combo_size_ + int64_t(rows) * cols);
   for (size_t i = 0; i < parts.size(); i++) {
@@ -144,6 +158,9 @@ void TaskBuilder::contract(const Blk& out, double alpha, const Blk& A, bool ta, 
     n = sb.c;
   }
   if (m != out.rows || n != out.cols) shape_error("contract (out)");
+  note_operand(A);
+  note_operand(B);
+  note_operand(C);
   const bool acc = written_.count(out.ref) > 0;
   StageBuf& sb2 = p2_stages_.back();
   // Zero-sized or zero-weight contractions add nothing; the output still exists.

@@ -44,6 +44,7 @@ enum Slot : int {
   kSlotP1 = 2,      // phase-1 products of the program being run
   kSlotCombo = 3,   // combined blocks of the program being run
   kSlotWork = 4,    // truncation workspace (assembled sector matrices, Gram, eigvecs)
+  kSlotOnes = 5,    // a vector of 1.0, at least as long as the largest sector dimension
   kSlotMpsBase = 8, // + site: MPS tensors
 };
 inline int slot_ops(int L, int boundary) { return kSlotMpsBase + L + boundary; }
@@ -143,6 +144,10 @@ class TaskBuilder {
 
   int64_t num_terms() const { return static_cast<int64_t>(p2_terms_.size()); }
 
+  // Bytes of the distinct MPS / operator blocks the recorded contractions read (each
+  // block counted once, FP64), the operand traffic of one execution of the program.
+  int64_t operand_bytes() const;
+
  private:
   struct PendingTerm { int group; Term t; };
   struct StageBuf {
@@ -161,6 +166,8 @@ class TaskBuilder {
   int64_t p1_size_ = 0;
   std::vector<Term> p2_terms_;  // only for counting
   std::unordered_map<Ref, bool> written_;  // outputs written by closed stages
+  std::unordered_map<Ref, int64_t> operands_;  // footprint of MPS / operator operands
+  void note_operand(const Blk& b);
 
   int group_for(StageBuf& sb, const Blk& out, bool accumulate);
   Blk product(const Blk& U, bool tu, const Blk& V, bool tv);

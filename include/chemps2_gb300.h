@@ -1,0 +1,132 @@
+/* C-ABI of the GB300 implementation of CheMPS2's two-site DMRG sweep.
+ *
+ * Every entry point returns an int status: C2G_OK (0) or a negative error code; the
+ * message of the last error on the calling thread is returned by c2g_last_error(). No
+ * C++ exception crosses this boundary. Objects are opaque handles owned by the caller,
+ * with the reference's ownership rules: a Hamiltonian must outlive the Problems built on
+ * it, and a Problem and a ConvergenceScheme must outlive the DMRG built on them
+ * (CheMPS2/include/chemps2/DMRG.h, private-member comments).
+ *
+ * Each function names the reference interface it replaces (path:line inside the CheMPS2
+ * project). The bindings a caller of the reference would switch to are shown in
+ * INTEGRATION.md.
+ */
+#ifndef CHEMPS2_GB300_H
+#define CHEMPS2_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  C2G_OK = 0,
+  C2G_ERR_INVALID = -1,   /* invalid argument (the reference asserts)            */
+  C2G_ERR_CUDA = -2,      /* a CUDA call failed                                   */
+  C2G_ERR_NO_DEVICE = -3, /* no CUDA device: there is no CPU execution path       */
+  C2G_ERR_INTERNAL = -4,  /* internal consistency check failed                    */
+  C2G_ERR_OTHER = -5
+};
+
+typedef struct c2g_hamiltonian c2g_hamiltonian;
+typedef struct c2g_problem c2g_problem;
+typedef struct c2g_scheme c2g_scheme;
+typedef struct c2g_dmrg c2g_dmrg;
+
+/* Library */
+const char* c2g_last_error(void);
+int c2g_version(void);
+/* Seeds the C library generator used for the random initial MPS, the Davidson fallback
+ * guess and the noise, as the reference's callers do with srand (CheMPS2/Initialize.cpp:29). */
+int c2g_srand(unsigned int seed);
+/* Number of kernels this library launched in this process. */
+int c2g_kernel_launches(long long* count);
+
+/* CheMPS2::Hamiltonian (CheMPS2/Hamiltonian.cpp:33-64, :66-102 FCIDUMP, :104-145 setters) */
+int c2g_hamiltonian_create(int L, int group, const int* irreps, c2g_hamiltonian** out);
+int c2g_hamiltonian_create_fcidump(const char* path, int group, c2g_hamiltonian** out);
+int c2g_hamiltonian_destroy(c2g_hamiltonian* h);
+int c2g_hamiltonian_get_L(const c2g_hamiltonian* h, int* L);
+int c2g_hamiltonian_get_group(const c2g_hamiltonian* h, int* group);
+int c2g_hamiltonian_get_irrep(const c2g_hamiltonian* h, int orb, int* irrep);
+int c2g_hamiltonian_set_econst(c2g_hamiltonian* h, double value);
+int c2g_hamiltonian_get_econst(const c2g_hamiltonian* h, double* value);
+int c2g_hamiltonian_set_tmat(c2g_hamiltonian* h, int i, int j, double value);
+int c2g_hamiltonian_get_tmat(const c2g_hamiltonian* h, int i, int j, double* value);
+int c2g_hamiltonian_set_vmat(c2g_hamiltonian* h, int i, int j, int k, int l, double value);
+int c2g_hamiltonian_get_vmat(const c2g_hamiltonian* h, int i, int j, int k, int l, double* value);
+
+/* CheMPS2::Problem (CheMPS2/Problem.cpp:33-56 ctor, :57-335 reorderings, :351-384 matrix elements) */
+int c2g_problem_create(const c2g_hamiltonian* h, int two_s, int n, int irrep, c2g_problem** out);
+int c2g_problem_destroy(c2g_problem* p);
+int c2g_problem_setup_reorder_d2h(c2g_problem* p);
+int c2g_problem_setup_reorder_c2v(c2g_problem* p);
+int c2g_problem_setup_reorder_custom(c2g_problem* p, const int* dmrg2ham);
+int c2g_problem_construct_mxelem(c2g_problem* p);
+int c2g_problem_set_mx_element(c2g_problem* p, int a, int b, int c, int d, double value);
+int c2g_problem_get_mx_element(const c2g_problem* p, int a, int b, int c, int d, double* value);
+int c2g_problem_check_consistency(const c2g_problem* p, int* ok);
+
+/* CheMPS2::ConvergenceScheme (CheMPS2/ConvergenceScheme.cpp:29-76) */
+int c2g_scheme_create(int n_instructions, c2g_scheme** out);
+int c2g_scheme_destroy(c2g_scheme* s);
+int c2g_scheme_set_instruction(c2g_scheme* s, int instruction, int D, double energy_conv, int max_sweeps,
+                               double noise_prefactor, double dvdson_rtol);
+
+/* CheMPS2::SyBookkeeper (CheMPS2/SyBookkeeper.cpp:29-323): sector dimensions at boundary b
+ * for a bookkeeper built with virtual dimension D. Writes up to `cap` rows of
+ * (N, 2S, I, FCI dim, current dim) into `out` (5 ints per row) and their count into
+ * `count`; call with cap = 0 to query the count. Needs no GPU. */
+int c2g_bookkeeper_sectors(const c2g_problem* p, int D, int boundary, int* out, int cap, int* count);
+
+/* CheMPS2::Sobject block table (CheMPS2/Sobject.cpp:36-145) of sites (index, index + 1)
+ * for a bookkeeper with virtual dimension D: per block the 9 labels
+ * (NL, 2SL, IL, N1, N2, 2J, NR, 2SR, IR), kappa2index (nkappa + 1 entries) and the
+ * size-sorted visiting order. Query sizes with cap = 0. Needs no GPU. */
+int c2g_sobject_layout(const c2g_problem* p, int D, int index, int* labels, int64_t* kappa2index, int* reorder,
+                       int cap, int* nkappa);
+
+/* Wigner symbols (CheMPS2/Wigner.cpp:294-370), arguments are twice the spins. */
+int c2g_wigner6j(int a, int b, int c, int d, int e, int f, double* value);
+int c2g_wigner9j(int a, int b, int c, int d, int e, int f, int g, int h, int i, double* value);
+
+/* CheMPS2::DMRG (CheMPS2/include/chemps2/DMRG.h:93-162, CheMPS2/DMRG.cpp:36-452). The
+ * constructor builds the random initial MPS and all renormalized operators on the GPU. */
+int c2g_dmrg_create(c2g_problem* p, c2g_scheme* s, const int* occupancies, c2g_dmrg** out);
+int c2g_dmrg_destroy(c2g_dmrg* d);
+int c2g_dmrg_solve(c2g_dmrg* d, double* energy);            /* DMRG::Solve    */
+int c2g_dmrg_presolve(c2g_dmrg* d);                         /* DMRG::PreSolve */
+int c2g_dmrg_set_verbose(c2g_dmrg* d, int verbose);
+int c2g_dmrg_num_mps_var(const c2g_dmrg* d, int* n);        /* DMRG::get_num_mps_var */
+int c2g_dmrg_max_discarded_weight(const c2g_dmrg* d, double* w);
+/* One two-site step (DMRG::solve_site, CheMPS2/DMRG.cpp:404-452) and one operator update
+ * (DMRG::updateMovingRight / updateMovingLeft, CheMPS2/DMRGoperators.cpp:243-908). */
+int c2g_dmrg_solve_site(c2g_dmrg* d, int index, double dvdson_rtol, double noise_level, int D, int moving_right,
+                        int change, double* energy);
+int c2g_dmrg_update(c2g_dmrg* d, int index, int moving_right);
+/* Statistics, in this order: n_matvec, n_davidson, t_join, t_solve, t_split, t_update,
+ * t_matvec, t_compile, matvec_flops, matvec_bytes, last_energy (seconds, flops, bytes). */
+#define C2G_NUM_STATS 11
+int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n);
+int c2g_dmrg_reset_stats(c2g_dmrg* d);
+/* Heff applications at sites (index, index + 1) on the current MPS (CheMPS2/Heff.cpp:43-248):
+ * `steps` timed applications after `warmup` untimed ones, CUDA-event timed on the DMRG's
+ * stream. Returns milliseconds per application, the ledger flops and bytes of one
+ * application and the number of kernels launched in the timed region. */
+int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, double* ms_per_matvec, double* flops,
+                        double* bytes, long long* launches);
+
+/* Effective Hamiltonian on host buffers (the path of CheMPS2/Heff.cpp:43-315 with the
+ * copies in and out included): n must equal the size of the two-site object at sites
+ * (index, index + 1) (c2g_dmrg_sobject_size). y = Heff x in the symmetric convention
+ * (CheMPS2/Sobject.cpp:624-650); diag (nullable) receives the diagonal of Heff. With
+ * join_into_x != 0, x is first overwritten by the joined current two-site object. */
+int c2g_dmrg_sobject_size(const c2g_dmrg* d, int index, int64_t* n);
+int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, double* y, double* diag, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHEMPS2_GB300_H */

@@ -1,0 +1,286 @@
+// ORACLE (test infrastructure, not product code): full configuration interaction in the
+// determinant basis, for small systems, as an independent check of DMRG energies.
+//
+// Plays the role of CheMPS2::FCI (CheMPS2/include/chemps2/FCI.h:43,100,110) in the
+// reference's DMRG-versus-FCI tests (tests/test1-4.cpp.in): the Hamiltonian
+//   H = sum_ij T_ij E_ij + 1/2 sum_ijkl V_ijkl sum_st a+_is a+_jt a_lt a_ks
+// (V in physics notation, V_ijkl = (ik|jl)) is applied in the space of determinants with
+// N_up = (N + 2S)/2 up and N_down = (N - 2S)/2 down electrons whose irrep product equals
+// the target, and its lowest eigenvalue is found by Davidson iteration. This space holds
+// every spin >= S; the tests use systems whose lowest state in it has spin S.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_fci_err;
+
+int popcount(uint64_t x) { return __builtin_popcountll(x); }
+
+struct Strings {
+  std::vector<uint64_t> str;
+  std::vector<int> irrep;
+  std::vector<int> index_of;  // dense over 2^L, -1 when absent (L <= 24)
+};
+
+Strings make_strings(int L, int ne, const int* orb_irrep) {
+  Strings s;
+  s.index_of.assign(size_t(1) << L, -1);
+  for (uint64_t m = 0; m < (uint64_t(1) << L); m++) {
+    if (popcount(m) != ne) continue;
+    int ir = 0;
+    for (int i = 0; i < L; i++)
+      if (m >> i & 1) ir ^= orb_irrep[i];
+    s.index_of[m] = static_cast<int>(s.str.size());
+    s.str.push_back(m);
+    s.irrep.push_back(ir);
+  }
+  return s;
+}
+
+// a+_i a_j |m>: returns the sign (0 if the result vanishes) and the new string.
+inline int excite(uint64_t m, int i, int j, uint64_t& out) {
+  if (!(m >> j & 1)) return 0;
+  uint64_t t = m & ~(uint64_t(1) << j);
+  if (t >> i & 1) return 0;
+  int sgn = (popcount(m & ((uint64_t(1) << j) - 1)) & 1) ? -1 : 1;
+  sgn *= (popcount(t & ((uint64_t(1) << i) - 1)) & 1) ? -1 : 1;
+  out = t | (uint64_t(1) << i);
+  return sgn;
+}
+
+struct FCI {
+  int L;
+  std::vector<double> T, V;  // V physics notation
+  Strings A, B;
+  std::vector<int64_t> det_of;  // [ia * nb + ib] -> det index or -1
+  std::vector<std::pair<int, int>> dets;
+  struct Exc {
+    int to;
+    int sign;
+  };
+  std::vector<std::vector<std::vector<Exc>>> exA, exB;  // [string][ij] (ij = i + L j)
+
+  void build_exc(const Strings& S, std::vector<std::vector<std::vector<Exc>>>& ex) {
+    ex.assign(S.str.size(), std::vector<std::vector<Exc>>(size_t(L) * L));
+    for (size_t k = 0; k < S.str.size(); k++)
+      for (int i = 0; i < L; i++)
+        for (int j = 0; j < L; j++) {
+          uint64_t o;
+          const int sg = excite(S.str[k], i, j, o);
+          if (sg) ex[k][i + size_t(L) * j].push_back({S.index_of[o], sg});
+        }
+  }
+
+  // D[ij][det] = <det| E_ij |c>
+  void apply_E(int i, int j, const std::vector<double>& c, std::vector<double>& out) {
+    const size_t nb = B.str.size();
+    std::fill(out.begin(), out.end(), 0.0);
+    for (size_t d = 0; d < dets.size(); d++) {
+      const double cd = c[d];
+      if (cd == 0.0) continue;
+      const int ia = dets[d].first, ib = dets[d].second;
+      for (const Exc& e : exA[ia][i + size_t(L) * j]) {
+        const int64_t t = det_of[size_t(e.to) * nb + ib];
+        if (t >= 0) out[t] += e.sign * cd;
+      }
+      for (const Exc& e : exB[ib][i + size_t(L) * j]) {
+        const int64_t t = det_of[size_t(ia) * nb + e.to];
+        if (t >= 0) out[t] += e.sign * cd;
+      }
+    }
+  }
+
+  // sigma = H c, with H = sum_ij k_ij E_ij + 1/2 sum_ijkl (ij|kl) E_ij E_kl,
+  // k_ij = T_ij - 1/2 sum_k (ik|kj), (ij|kl) = V_ikjl.
+  void sigma(const std::vector<double>& c, std::vector<double>& s) {
+    const size_t n = dets.size();
+    const size_t L2 = size_t(L) * L;
+    std::vector<std::vector<double>> D(L2, std::vector<double>(n));
+    for (int k = 0; k < L; k++)
+      for (int l = 0; l < L; l++) apply_E(k, l, c, D[k + size_t(L) * l]);
+    auto chem = [&](int i, int j, int k, int l) { return V[i + size_t(L) * (k + size_t(L) * (j + size_t(L) * l))]; };
+    std::fill(s.begin(), s.end(), 0.0);
+    std::vector<double> G(n), tmp(n);
+    for (int i = 0; i < L; i++)
+      for (int j = 0; j < L; j++) {
+        double kij = T[i + size_t(L) * j];
+        for (int k = 0; k < L; k++) kij -= 0.5 * chem(i, k, k, j);
+        for (size_t d = 0; d < n; d++) G[d] = kij * c[d];
+        for (int k = 0; k < L; k++)
+          for (int l = 0; l < L; l++) {
+            const double v = 0.5 * chem(i, j, k, l);
+            if (v == 0.0) continue;
+            const std::vector<double>& Dkl = D[k + size_t(L) * l];
+            for (size_t d = 0; d < n; d++) G[d] += v * Dkl[d];
+          }
+        apply_E(i, j, G, tmp);
+        for (size_t d = 0; d < n; d++) s[d] += tmp[d];
+      }
+  }
+
+  double diag_element(size_t d) {
+    const uint64_t a = A.str[dets[d].first], b = B.str[dets[d].second];
+    double e = 0.0;
+    auto occ = [&](uint64_t m, int i) { return int(m >> i & 1); };
+    for (int i = 0; i < L; i++) e += (occ(a, i) + occ(b, i)) * T[i + size_t(L) * i];
+    auto Vp = [&](int i, int j, int k, int l) { return V[i + size_t(L) * (j + size_t(L) * (k + size_t(L) * l))]; };
+    for (int i = 0; i < L; i++)
+      for (int j = 0; j < L; j++) {
+        const int ni = occ(a, i) + occ(b, i);
+        const int nj = occ(a, j) + occ(b, j);
+        double coul = 0.5 * Vp(i, j, i, j) * ni * nj;
+        if (i == j) coul -= 0.5 * Vp(i, i, i, i) * (occ(a, i) + occ(b, i));  // remove self pairs
+        const int same = occ(a, i) * occ(a, j) + occ(b, i) * occ(b, j);
+        const double exch = (i == j) ? 0.0 : 0.5 * Vp(i, j, j, i) * same;
+        e += coul - exch;
+      }
+    return e;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* oracle_fci_last_error() { return g_fci_err.c_str(); }
+
+// Lowest eigenvalue of H (plus econst) in the (N_up, N_down, irrep) determinant space.
+// tmat: L x L; vmat: L^4 physics notation, (i,j,k,l) at i + L*(j + L*(k + L*l)).
+int oracle_fci_ground_state(int L, const int* orb_irrep, const double* tmat, const double* vmat, double econst,
+                            int n_up, int n_down, int irrep, double tol, int max_iter, double* energy, int64_t* dim) {
+  try {
+    if (L > 24) throw std::invalid_argument("FCI oracle: at most 24 orbitals");
+    FCI f;
+    f.L = L;
+    f.T.assign(tmat, tmat + size_t(L) * L);
+    f.V.assign(vmat, vmat + size_t(L) * L * L * L);
+    f.A = make_strings(L, n_up, orb_irrep);
+    f.B = make_strings(L, n_down, orb_irrep);
+    const size_t na = f.A.str.size(), nb = f.B.str.size();
+    f.det_of.assign(na * nb, -1);
+    // All (N_up, N_down) determinants: the intermediate vectors E_kl |c> of the sigma
+    // build leave the target irrep. The iterates are kept in the target irrep by masking.
+    std::vector<char> target;
+    for (size_t ia = 0; ia < na; ia++)
+      for (size_t ib = 0; ib < nb; ib++) {
+        f.det_of[ia * nb + ib] = static_cast<int64_t>(f.dets.size());
+        f.dets.push_back({static_cast<int>(ia), static_cast<int>(ib)});
+        target.push_back((f.A.irrep[ia] ^ f.B.irrep[ib]) == irrep);
+      }
+    const size_t n = f.dets.size();
+    size_t ntarget = 0;
+    for (char c : target) ntarget += c;
+    *dim = static_cast<int64_t>(ntarget);
+    if (ntarget == 0) throw std::invalid_argument("FCI oracle: empty determinant space");
+    f.build_exc(f.A, f.exA);
+    f.build_exc(f.B, f.exB);
+    std::vector<double> hd(n);
+    for (size_t d = 0; d < n; d++) hd[d] = f.diag_element(d);
+    // Davidson with diagonal preconditioner, restart at 24 vectors.
+    size_t best = n;
+    for (size_t d = 0; d < n; d++)
+      if (target[d] && (best == n || hd[d] < hd[best])) best = d;
+    std::vector<std::vector<double>> vs, hv;
+    std::vector<double> t(n, 0.0);
+    t[best] = 1.0;
+    for (size_t d = 0; d < n; d++)
+      if (target[d]) t[d] += 1e-3 * std::sin(1.0 + d);  // break symmetry ties
+    double theta = 0.0;
+    auto dot = [&](const std::vector<double>& x, const std::vector<double>& y) {
+      double s = 0.0;
+      for (size_t i = 0; i < n; i++) s += x[i] * y[i];
+      return s;
+    };
+    std::vector<double> ritz(n), hritz(n);
+    for (int it = 0; it < max_iter; it++) {
+      for (size_t d = 0; d < n; d++)
+        if (!target[d]) t[d] = 0.0;
+      for (int pass = 0; pass < 2; pass++)
+        for (auto& v : vs) {
+          const double o = dot(v, t);
+          for (size_t i = 0; i < n; i++) t[i] -= o * v[i];
+        }
+      const double nt = std::sqrt(dot(t, t));
+      if (nt < 1e-14) break;
+      for (auto& e : t) e /= nt;
+      vs.push_back(t);
+      hv.emplace_back(n);
+      f.sigma(vs.back(), hv.back());
+      const int m = static_cast<int>(vs.size());
+      std::vector<double> Hm(size_t(m) * m);
+      for (int a = 0; a < m; a++)
+        for (int b = 0; b < m; b++) Hm[a + size_t(m) * b] = dot(vs[a], hv[b]);
+      // Jacobi on the small matrix
+      std::vector<double> Vm(size_t(m) * m, 0.0);
+      for (int a = 0; a < m; a++) Vm[a + size_t(m) * a] = 1.0;
+      for (int sw = 0; sw < 100; sw++) {
+        double off = 0.0;
+        for (int a = 0; a < m; a++)
+          for (int b = 0; b < m; b++)
+            if (a != b) off += Hm[a + size_t(m) * b] * Hm[a + size_t(m) * b];
+        if (off < 1e-28) break;
+        for (int p = 0; p < m; p++)
+          for (int q = p + 1; q < m; q++) {
+            const double apq = Hm[p + size_t(m) * q];
+            if (apq == 0.0) continue;
+            const double tau = (Hm[q + size_t(m) * q] - Hm[p + size_t(m) * p]) / (2 * apq);
+            const double tt = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1 + tau * tau));
+            const double c = 1 / std::sqrt(1 + tt * tt), s = tt * c;
+            for (int j = 0; j < m; j++) {
+              const double x = Hm[p + size_t(m) * j], y = Hm[q + size_t(m) * j];
+              Hm[p + size_t(m) * j] = c * x - s * y;
+              Hm[q + size_t(m) * j] = s * x + c * y;
+            }
+            for (int i = 0; i < m; i++) {
+              const double x = Hm[i + size_t(m) * p], y = Hm[i + size_t(m) * q];
+              Hm[i + size_t(m) * p] = c * x - s * y;
+              Hm[i + size_t(m) * q] = s * x + c * y;
+              const double vx = Vm[i + size_t(m) * p], vy = Vm[i + size_t(m) * q];
+              Vm[i + size_t(m) * p] = c * vx - s * vy;
+              Vm[i + size_t(m) * q] = s * vx + c * vy;
+            }
+          }
+      }
+      int lo = 0;
+      for (int a = 1; a < m; a++)
+        if (Hm[a + size_t(m) * a] < Hm[lo + size_t(m) * lo]) lo = a;
+      theta = Hm[lo + size_t(m) * lo];
+      std::fill(ritz.begin(), ritz.end(), 0.0);
+      std::fill(hritz.begin(), hritz.end(), 0.0);
+      for (int a = 0; a < m; a++) {
+        const double y = Vm[a + size_t(m) * lo];
+        for (size_t i = 0; i < n; i++) {
+          ritz[i] += y * vs[a][i];
+          hritz[i] += y * hv[a][i];
+        }
+      }
+      double rn = 0.0;
+      for (size_t i = 0; i < n; i++) {
+        const double r = hritz[i] - theta * ritz[i];
+        rn += r * r;
+        const double den = hd[i] - theta;
+        t[i] = -r / ((std::fabs(den) > 1e-10) ? den : 1e-10);
+      }
+      if (std::sqrt(rn) < tol) break;
+      if (m >= 24) {  // restart with the Ritz vector
+        vs.clear();
+        hv.clear();
+        vs.push_back(ritz);
+        hv.push_back(hritz);
+      }
+    }
+    *energy = theta + econst;
+    return 0;
+  } catch (const std::exception& e) {
+    g_fci_err = e.what();
+    return -1;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+"""Regenerates the golden fixtures of this directory from the reference's own tests.
+
+Run in a checkout that has the reference at REFERENCE (default /root/reference); the
+outputs are committed so that the tests never read the reference at run time.
+
+  * N2.STO3G.FCIDUMP    copied from tests/matrixelements/N2.STO3G.FCIDUMP (the input of
+                        the reference's tests/test1.cpp.in and tests/test5.cpp.in)
+  * golden.json         energies the reference's tests assert, parsed from their sources:
+                        tests/test5.cpp.in (N2 STO-3G ground state, D = 1000) and
+                        tests/test12.cpp.in (the BCS pairing model, L = 8)
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import shutil
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+
+def main(reference: Path) -> None:
+    tests = reference / "tests"
+    shutil.copyfile(tests / "matrixelements" / "N2.STO3G.FCIDUMP", HERE / "N2.STO3G.FCIDUMP")
+    t5 = (tests / "test5.cpp.in").read_text()
+    t12 = (tests / "test12.cpp.in").read_text()
+    e5 = [float(x) for x in re.findall(r"fabs\(\s*Energy\d\s*\+\s*([0-9.]+)\s*\)", t5)]
+    e12 = [float(x) for x in re.findall(r"fabs\(\s*Energy\s*\+\s*([0-9.]+)\s*\)", t12)]
+    golden = {
+        "n2_sto3g": {
+            "source": "tests/test5.cpp.in",
+            "fcidump": "N2.STO3G.FCIDUMP",
+            "group": 7,
+            "two_s": 0,
+            "n": 14,
+            "irrep": 0,
+            "reorder": "d2h",
+            "schedule": [[1000, 1e-12, 100, 0.0, 1e-5]],
+            "energy": -e5[0],
+            "tolerance": 1e-8,
+        },
+        "bcs_l8": {
+            "source": "tests/test12.cpp.in",
+            "eps": [-3.5, -2.5, -1.5, -0.5, 0.5, 1.5, 2.5, 3.5],
+            "g": -1.0,
+            "power": 0.0,
+            "two_s": 0,
+            "n": 8,
+            "irrep": 0,
+            "schedule": [[100, 1e-10, 10, 0.5, 1e-5], [1000, 1e-10, 10, 0.0, 1e-5]],
+            "energy": -e12[0],
+            "tolerance": 1e-8,
+        },
+    }
+    (HERE / "golden.json").write_text(json.dumps(golden, indent=2) + "\n")
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE", "/root/reference")))

@@ -1,0 +1,136 @@
+"""ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so): CPU DMRG sweep and
+determinant FCI. Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+from models import Model, hubbard  # noqa: F401
+
+ROOT = Path(__file__).resolve().parents[1]
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        sys.path.insert(0, str(ROOT))
+        from oracle import build as ob  # noqa: E402
+
+        path = ob.build()
+        _lib = C.CDLL(str(path), mode=C.RTLD_GLOBAL)
+        _lib.oracle_last_error.restype = C.c_char_p
+        _lib.oracle_fci_last_error.restype = C.c_char_p
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def fci_energy(model: Model, n_up: int, n_down: int, irrep: int, tol=1e-10) -> float:
+    e = C.c_double()
+    dim = C.c_int64()
+    rc = lib().oracle_fci_ground_state(model.L, _ip(model.irreps), _dp(model.tflat()), _dp(model.vflat()),
+                                       C.c_double(model.econst), n_up, n_down, irrep, C.c_double(tol), 400,
+                                       C.byref(e), C.byref(dim))
+    if rc != 0:
+        raise RuntimeError(lib().oracle_fci_last_error().decode())
+    return e.value
+
+
+class OracleDMRG:
+    """CPU DMRG of the oracle. schedule: list of (D, econv, max_sweeps, noise, rtol)."""
+
+    def __init__(self, model: Model | None, two_s, n, irrep, schedule, reorder=0, fcidump=None, group=None,
+                 check=True):
+        L = lib()
+        D = np.array([s[0] for s in schedule], dtype=np.int32)
+        ec = np.array([s[1] for s in schedule], dtype=np.float64)
+        ms = np.array([s[2] for s in schedule], dtype=np.int32)
+        nz = np.array([s[3] for s in schedule], dtype=np.float64)
+        rt = np.array([s[4] for s in schedule], dtype=np.float64)
+        h = C.c_void_p()
+        self._keep = (D, ec, ms, nz, rt)
+        if fcidump is not None:
+            rc = L.oracle_dmrg_create(str(fcidump).encode(), 0, int(group), None, None, None, C.c_double(0.0),
+                                      two_s, n, irrep, reorder, len(schedule), _ip(D), _dp(ec), _ip(ms), _dp(nz),
+                                      _dp(rt), int(check), C.byref(h))
+        else:
+            tf, vf = model.tflat(), model.vflat()
+            self._keep += (tf, vf)
+            rc = L.oracle_dmrg_create(None, model.L, model.group, _ip(model.irreps), _dp(tf), _dp(vf),
+                                      C.c_double(model.econst), two_s, n, irrep, reorder, len(schedule), _ip(D),
+                                      _dp(ec), _ip(ms), _dp(nz), _dp(rt), int(check), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(L.oracle_last_error().decode())
+        self.h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(lib().oracle_last_error().decode())
+
+    def solve(self) -> float:
+        e = C.c_double()
+        self._check(lib().oracle_dmrg_solve(self.h, C.byref(e)))
+        return e.value
+
+    def presolve(self):
+        self._check(lib().oracle_dmrg_presolve(self.h))
+
+    def set_mx_element(self, a, b, c, d, v):
+        self._check(lib().oracle_set_mx_element(self.h, a, b, c, d, C.c_double(v)))
+
+    def step_energies(self):
+        n = C.c_int()
+        self._check(lib().oracle_dmrg_step_energies(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        self._check(lib().oracle_dmrg_step_energies(self.h, _dp(out), n.value, C.byref(n)))
+        return out
+
+    def sobject_size(self, index):
+        n = C.c_int64()
+        self._check(lib().oracle_dmrg_sobject_size(self.h, index, C.byref(n)))
+        return n.value
+
+    def heff_apply(self, index, x=None, want_diag=False):
+        n = self.sobject_size(index)
+        join = x is None
+        xx = np.zeros(n) if join else np.ascontiguousarray(x, dtype=np.float64).copy()
+        y = np.zeros(n)
+        d = np.zeros(n) if want_diag else None
+        self._check(lib().oracle_dmrg_heff_apply(self.h, index, int(join), _dp(xx), C.c_int64(len(xx)), _dp(y),
+                                                 _dp(d) if d is not None else None))
+        return xx, y, d
+
+    def solve_site(self, index, rtol, noise, D, moving_right, change):
+        e = C.c_double()
+        self._check(lib().oracle_dmrg_solve_site(self.h, index, C.c_double(rtol), C.c_double(noise), D,
+                                                 int(moving_right), int(change), C.byref(e)))
+        return e.value
+
+    def update(self, index, moving_right):
+        self._check(lib().oracle_dmrg_update(self.h, index, int(moving_right)))
+
+    def stats(self):
+        out = np.zeros(3)
+        self._check(lib().oracle_dmrg_stats(self.h, _dp(out)))
+        return {"n_matvec": out[0], "t_matvec": out[1], "flops": out[2]}
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().oracle_dmrg_destroy(self.h)
+        except Exception:
+            pass
+
+
+def srand(seed: int):
+    C.CDLL(None).srand(C.c_uint(seed))

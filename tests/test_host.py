@@ -1,0 +1,254 @@
+"""CPU tests of the product library without a GPU: the C-ABI loads and exports every
+symbol of include/chemps2_gb300.h, the host bookkeeping is bit-exact against a direct
+restatement of the reference's loops, and the drop-in API keeps the reference's argument
+checks. No compute kernel is called here."""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import re
+from fractions import Fraction
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import chemps2_gb300 as c2g
+import models
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def header_symbols():
+    text = (ROOT / "include" / "chemps2_gb300.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(c2g_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = c2g.load()
+    syms = header_symbols()
+    assert len(syms) > 40
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_dmrg_without_device_fails_loudly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    ham = c2g.Hamiltonian(4, 0, np.zeros(4, dtype=np.int32))
+    prob = c2g.Problem(ham, 0, 4, 0)
+    sc = c2g.ConvergenceScheme(1)
+    sc.set_instruction(0, 10, 1e-8, 1, 0.0, 1e-6)
+    with pytest.raises(c2g.Chemps2Error):
+        c2g.DMRG(prob, sc)
+
+
+# ---------------------------------------------------------------- bookkeeping parity
+def ref_bookkeeper(L, irreps, nirr, N, two_s, irrep, D):
+    """Restatement of CheMPS2/SyBookkeeper.cpp:29-269 (FCI dims by the left and right
+    recurrences, capped at 262144, then the ceil scaling of the current dims)."""
+    cap = 262144
+    Nmin = [max(0, N - 2 * (L - b)) for b in range(L + 1)]
+    Nmax = [min(2 * b, N) for b in range(L + 1)]
+    # left: dict (b, n, s, i) -> dim
+    left = {(0, 0, 0, 0): 1}
+    for b in range(1, L + 1):
+        for (bb, n, s, i), d in list(left.items()):
+            if bb != b - 1:
+                continue
+            for (dn, ds_list, di) in ((0, [0], 0), (2, [0], 0), (1, [-1, 1], irreps[b - 1])):
+                for ds in ds_list:
+                    key = (b, n + dn, s + ds, i ^ di)
+                    if key[2] < 0:
+                        continue
+                    left[key] = min(cap, left.get(key, 0) + d)
+    right = {(L, N, two_s, irrep): 1}
+    for b in range(L - 1, -1, -1):
+        for (bb, n, s, i), d in list(right.items()):
+            if bb != b + 1:
+                continue
+            for (dn, ds_list, di) in ((0, [0], 0), (2, [0], 0), (1, [-1, 1], irreps[b])):
+                for ds in ds_list:
+                    key = (b, n - dn, s + ds, i ^ di)
+                    if key[2] < 0 or key[1] < 0:
+                        continue
+                    right[key] = min(cap, right.get(key, 0) + d)
+    fci = {}
+    for b in range(L + 1):
+        for n in range(Nmin[b], Nmax[b] + 1):
+            for s in range(0, 2 * L + 2):
+                for i in range(nirr):
+                    v = min(left.get((b, n, s, i), 0), right.get((b, n, s, i), 0))
+                    if v > 0:
+                        fci[(b, n, s, i)] = v
+    cur = {}
+    for b in range(L + 1):
+        tot = sum(v for (bb, *_), v in fci.items() if bb == b)
+        for k, v in fci.items():
+            if k[0] != b:
+                continue
+            cur[k] = v if tot <= D else min(v, math.ceil(D * v / tot))
+    return fci, cur
+
+
+@pytest.mark.parametrize("L,group,N,two_s,irrep,D", [
+    (8, 0, 8, 0, 0, 20), (10, 7, 10, 0, 0, 50), (9, 5, 9, 1, 2, 30), (12, 7, 12, 2, 3, 200), (16, 0, 16, 0, 0, 200),
+])
+def test_bookkeeper_dims_bit_exact(L, group, N, two_s, irrep, D):
+    nirr = models.NIRREPS[group]
+    irreps = [i % nirr for i in range(L)]
+    ham = c2g.Hamiltonian(L, group, np.array(irreps, dtype=np.int32))
+    prob = c2g.Problem(ham, two_s, N, irrep)
+    fci, cur = ref_bookkeeper(L, irreps, nirr, N, two_s, irrep, D)
+    for b in range(L + 1):
+        got = prob.bookkeeper_sectors(D, b)
+        got_f = {(b, int(r[0]), int(r[1]), int(r[2])): int(r[3]) for r in got if r[3] > 0}
+        got_c = {(b, int(r[0]), int(r[1]), int(r[2])): int(r[4]) for r in got if r[3] > 0}
+        exp_f = {k: v for k, v in fci.items() if k[0] == b}
+        exp_c = {k: v for k, v in cur.items() if k[0] == b}
+        assert got_f == exp_f, b
+        assert got_c == exp_c, b
+
+
+def ref_sobject_blocks(prob: c2g.Problem, D, index, L, irreps, nirr):
+    """Restatement of the block enumeration of CheMPS2/Sobject.cpp:36-145: loops NL, 2SL,
+    IL, N1, N2, 2J, NR, 2SR, IR in that order, then the stable size sort of :115-145."""
+    sec = {}
+    for b in (index, index + 2):
+        for r in prob.bookkeeper_sectors(D, b):
+            sec[(b, int(r[0]), int(r[1]), int(r[2]))] = int(r[4])
+    blocks = []
+    I1, I2 = irreps[index], irreps[index + 1]
+    keys_l = sorted(k for k in sec if k[0] == index)
+    for (_, NL, TwoSL, IL) in keys_l:
+        dimL = sec[(index, NL, TwoSL, IL)]
+        if dimL <= 0:
+            continue
+        for N1 in range(3):
+            for N2 in range(3):
+                TwoJmin = (N1 + N2) % 2 if False else (1 if (N1 == 1) != (N2 == 1) else 0)
+                TwoJmax = (1 if N1 == 1 else 0) + (1 if N2 == 1 else 0)
+                for TwoJ in range(TwoJmin, TwoJmax + 1, 2):
+                    NR = NL + N1 + N2
+                    IR = IL ^ (I1 if N1 == 1 else 0) ^ (I2 if N2 == 1 else 0)
+                    for TwoSR in range(TwoSL - TwoJ, TwoSL + TwoJ + 1, 2):
+                        if TwoSR < 0:
+                            continue
+                        dimR = sec.get((index + 2, NR, TwoSR, IR), 0)
+                        if dimR > 0:
+                            blocks.append(((NL, TwoSL, IL, N1, N2, TwoJ, NR, TwoSR, IR), dimL * dimR))
+    return blocks
+
+
+@pytest.mark.parametrize("L,group,N,two_s,irrep,D,index", [
+    (8, 0, 8, 0, 0, 30, 3), (10, 7, 10, 0, 0, 60, 4), (9, 5, 9, 1, 2, 40, 2), (12, 7, 12, 0, 0, 200, 5),
+])
+def test_sobject_layout_bit_exact(L, group, N, two_s, irrep, D, index):
+    nirr = models.NIRREPS[group]
+    irreps = [i % nirr for i in range(L)]
+    ham = c2g.Hamiltonian(L, group, np.array(irreps, dtype=np.int32))
+    prob = c2g.Problem(ham, two_s, N, irrep)
+    labels, k2i, order = prob.sobject_layout(D, index)
+    exp = ref_sobject_blocks(prob, D, index, L, irreps, nirr)
+    assert [tuple(int(v) for v in r) for r in labels] == [b[0] for b in exp]
+    sizes = [b[1] for b in exp]
+    assert list(k2i) == list(np.concatenate([[0], np.cumsum(sizes)]))
+    # visiting order: non-increasing size, stable among equal sizes
+    exp_order = sorted(range(len(sizes)), key=lambda k: -sizes[k])
+    assert list(order) == exp_order
+
+
+# ---------------------------------------------------------------- Wigner symbols
+def racah_6j(a, b, c, d, e, f):
+    """Exact 6j symbol in rationals (arguments twice the spins), Racah's formula."""
+    def tri(x, y, z):
+        return (x + y + z) % 2 == 0 and abs(x - y) <= z <= x + y
+
+    if not (tri(a, b, c) and tri(d, e, c) and tri(a, e, f) and tri(d, b, f)):
+        return 0.0
+    F = math.factorial
+
+    def delta(x, y, z):
+        return Fraction(F((x + y - z) // 2) * F((x - y + z) // 2) * F((-x + y + z) // 2), F((x + y + z) // 2 + 1))
+
+    a1, a2, a3, a4 = (a + b + c) // 2, (d + e + c) // 2, (a + e + f) // 2, (d + b + f) // 2
+    b1, b2, b3 = (a + b + d + e) // 2, (a + c + d + f) // 2, (b + c + e + f) // 2
+    s = Fraction(0)
+    for k in range(max(a1, a2, a3, a4), min(b1, b2, b3) + 1):
+        s += Fraction((-1) ** k * F(k + 1), F(k - a1) * F(k - a2) * F(k - a3) * F(k - a4) * F(b1 - k) * F(b2 - k)
+                      * F(b3 - k))
+    pref2 = delta(a, b, c) * delta(d, e, c) * delta(a, e, f) * delta(d, b, f)
+    return float(s) * math.sqrt(float(pref2))
+
+
+def test_wigner6j_against_exact_racah():
+    rng = np.random.default_rng(0)
+    n = 0
+    for _ in range(3000):
+        a, b, d, e = (int(x) for x in rng.integers(0, 12, size=4))
+        for c in range(abs(a - b), a + b + 1, 2):
+            for f in range(abs(a - e), a + e + 1, 2):
+                ref = racah_6j(a, b, c, d, e, f)
+                got = c2g.wigner6j(a, b, c, d, e, f)
+                assert abs(got - ref) < 1e-13, (a, b, c, d, e, f)
+                n += 1
+    assert n > 1000
+    # large arguments stay accurate (|err| <= 7e-12 at 2j <= 95 in the reference)
+    assert abs(c2g.wigner6j(90, 90, 0, 90, 90, 0) - 1.0 / 91) < 1e-12
+
+
+def test_wigner_argument_errors_are_status_codes():
+    with pytest.raises(c2g.Chemps2Error):
+        c2g.wigner6j(-1, 1, 0, 1, 1, 0)
+
+
+def test_hamiltonian_symmetry_and_checks():
+    L = 4
+    ham = c2g.Hamiltonian(L, 5, np.array([0, 1, 2, 3], dtype=np.int32))  # C2v
+    ham.setVmat(0, 1, 0, 1, 0.3)
+    for perm in [(0, 1, 0, 1), (1, 0, 1, 0), (0, 1, 0, 1)]:
+        assert ham.getVmat(*perm) == 0.3
+    ham.setVmat(0, 1, 2, 3, 0.2)  # I0 x I1 = 1 = I2 x I3
+    for p in [(0, 1, 2, 3), (2, 1, 0, 3), (0, 3, 2, 1), (2, 3, 0, 1), (1, 0, 3, 2), (3, 0, 1, 2), (1, 2, 3, 0),
+              (3, 2, 1, 0)]:
+        assert ham.getVmat(*p) == 0.2
+    with pytest.raises(c2g.Chemps2Error):
+        ham.setTmat(0, 1, 1.0)  # different irreps
+    with pytest.raises(c2g.Chemps2Error):
+        ham.setVmat(0, 0, 0, 1, 1.0)  # irrep product violated
+    with pytest.raises(c2g.Chemps2Error):
+        ham.getTmat(0, L)
+
+
+def test_problem_matrix_elements_and_reorder():
+    L = 4
+    ham = c2g.Hamiltonian(L, 0, np.zeros(L, dtype=np.int32))
+    ham.setTmat(0, 1, -1.0)
+    ham.setVmat(2, 2, 2, 2, 4.0)
+    prob = c2g.Problem(ham, 0, 4, 0)
+    with pytest.raises(c2g.Chemps2Error):
+        prob.gMxElement(0, 0, 0, 0)  # not yet constructed
+    prob.construct_mxelem()
+    # h_abcd = V_abcd + (delta_ac T_bd + delta_bd T_ac) / (N - 1)
+    assert prob.gMxElement(0, 0, 0, 1) == pytest.approx(-1.0 / 3)
+    assert prob.gMxElement(2, 2, 2, 2) == pytest.approx(4.0)
+    prob.setMxElement(0, 1, 2, 3, 0.5)
+    assert prob.gMxElement(0, 1, 2, 3) == 0.5
+    assert prob.checkConsistency()
+    bad = c2g.Problem(ham, 1, 4, 0)  # odd spin with even N
+    assert not bad.checkConsistency()
+
+
+def test_convergence_scheme_checks():
+    sc = c2g.ConvergenceScheme(2)
+    sc.set_instruction(0, 100, 1e-8, 2, 0.1, 1e-5)
+    sc.setInstruction(1, 200, 1e-9, 3, 0.0)
+    assert sc.getDavidsonRTOL(1) == 1e-5
+    for bad in [(0, 0, 1e-8, 2, 0.0, 1e-5), (0, 10, 0.0, 2, 0.0, 1e-5), (0, 10, 1e-8, 0, 0.0, 1e-5),
+                (0, 10, 1e-8, 2, 0.0, 0.0), (5, 10, 1e-8, 2, 0.0, 1e-5)]:
+        with pytest.raises(c2g.Chemps2Error):
+            sc.set_instruction(*bad)
+    with pytest.raises(c2g.Chemps2Error):
+        c2g.ConvergenceScheme(0)

@@ -1,0 +1,138 @@
+"""CPU tests of the oracle: pinned against the reference's golden energies and against
+exact diagonalisation. These make the oracle trustworthy as the checker of the GPU path."""
+from __future__ import annotations
+
+import itertools
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import models
+import oracle_lib as ol
+
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "golden.json").read_text())
+
+
+def exact_lowest(model, n_up, n_down, irrep, two_s):
+    """Lowest eigenvalue with total spin two_s/2 by dense diagonalisation of H in the
+    (n_up, n_down, irrep) determinant space (spin-orbital 2i + s)."""
+    L = model.L
+    up_mask = int("01" * L, 2)
+    states = [b for b in range(1 << (2 * L))
+              if bin(b & up_mask).count("1") == n_up and bin(b & ~up_mask).count("1") == n_down]
+
+    def irr(b):
+        r = 0
+        for i in range(L):
+            if ((b >> (2 * i)) & 1) ^ ((b >> (2 * i + 1)) & 1):
+                r ^= int(model.irreps[i])
+        return r
+
+    states = [b for b in states if irr(b) == irrep]
+    idx = {b: k for k, b in enumerate(states)}
+
+    def apply(b, ops):
+        sg = 1
+        for kind, p in reversed(ops):
+            occ = (b >> p) & 1
+            if (kind == "a" and not occ) or (kind == "c" and occ):
+                return None, 0
+            sg *= -1 if bin(b & ((1 << p) - 1)).count("1") % 2 else 1
+            b ^= 1 << p
+        return b, sg
+
+    n = len(states)
+    H = np.zeros((n, n))
+    S2 = np.zeros((n, n))
+    for k, b in enumerate(states):
+        for i in range(L):
+            for j in range(L):
+                if model.tmat[i, j] != 0.0:
+                    for s in range(2):
+                        b2, sg = apply(b, [("c", 2 * i + s), ("a", 2 * j + s)])
+                        if b2 is not None:
+                            H[idx[b2], k] += model.tmat[i, j] * sg
+                b2, sg = apply(b, [("c", 2 * i), ("a", 2 * i + 1), ("c", 2 * j + 1), ("a", 2 * j)])
+                if b2 is not None and b2 in idx:
+                    S2[idx[b2], k] += sg
+        for i, j, kk, l in itertools.product(range(L), repeat=4):
+            v = model.vmat[i, j, kk, l]
+            if v == 0.0:
+                continue
+            for s in range(2):
+                for t in range(2):
+                    b2, sg = apply(b, [("c", 2 * i + s), ("c", 2 * j + t), ("a", 2 * l + t), ("a", 2 * kk + s)])
+                    if b2 is not None:
+                        H[idx[b2], k] += 0.5 * v * sg
+    sz = (n_up - n_down) / 2
+    S2 += np.eye(n) * (sz * sz - sz)
+    w, vecs = np.linalg.eigh(H)
+    target = two_s / 2 * (two_s / 2 + 1)
+    for k in range(n):
+        if abs(vecs[:, k] @ S2 @ vecs[:, k] - target) < 1e-6:
+            return w[k] + model.econst, w[0] + model.econst
+    raise AssertionError("no state of the requested spin")
+
+
+@pytest.mark.parametrize("L,group,seed,N,two_s,irrep", [
+    (4, 7, 3, 4, 0, 0),
+    (5, 5, 4, 4, 0, 1),
+    (5, 5, 9, 5, 1, 2),
+    (6, 7, 7, 6, 2, 0),
+])
+def test_fci_and_dmrg_oracles_match_exact_diagonalisation(L, group, seed, N, two_s, irrep):
+    m = models.synthetic_ab_initio(L, group, seed)
+    n_up, n_down = (N + two_s) // 2, (N - two_s) // 2
+    e_spin, e_lowest = exact_lowest(m, n_up, n_down, irrep, two_s)
+    assert abs(ol.fci_energy(m, n_up, n_down, irrep) - e_lowest) < 1e-10
+    ol.srand(1)
+    d = ol.OracleDMRG(m, two_s, N, irrep, [(200, 1e-10, 4, 0.0, 1e-9)])
+    assert abs(d.solve() - e_spin) < 1e-9
+
+
+def test_oracle_hubbard_chain_of_reference_test4():
+    """tests/test4.cpp.in: Hubbard L = 10, U = 2, N = 9, 2S = 5, DMRG against FCI to 1e-8."""
+    m = models.hubbard(10, 2.0)
+    e_fci = ol.fci_energy(m, 7, 2, 0)
+    ol.srand(1)
+    d = ol.OracleDMRG(m, 5, 9, 0, [(30, 1e-10, 3, 0.1, 1e-5), (1000, 1e-10, 10, 0.0, 1e-5)])
+    assert abs(d.solve() - e_fci) < 1e-8
+
+
+def test_oracle_bcs_golden_of_reference_test12():
+    g = GOLDEN["bcs_l8"]
+    L = len(g["eps"])
+    m = models.Model(L, 0, np.zeros(L, dtype=np.int32), np.zeros((L, L)), np.zeros((L, L, L, L)))
+    ol.srand(1)
+    d = ol.OracleDMRG(m, g["two_s"], g["n"], g["irrep"], [tuple(x) for x in g["schedule"]])
+    L, elems = models.bcs(g["eps"], g["g"], g["power"])
+    for o1, o2, eri, oei in elems:
+        if o1 == o2:
+            d.set_mx_element(o1, o1, o2, o2, eri + oei)
+        else:
+            d.set_mx_element(o1, o1, o2, o2, eri)
+            d.set_mx_element(o1, o2, o1, o2, oei)
+    d.presolve()
+    assert abs(d.solve() - g["energy"]) < g["tolerance"]
+
+
+def test_oracle_n2_sto3g_golden_of_reference_test5():
+    g = GOLDEN["n2_sto3g"]
+    ol.srand(1)
+    d = ol.OracleDMRG(None, g["two_s"], g["n"], g["irrep"], [tuple(x) for x in g["schedule"]], reorder=1,
+                      fcidump=Path(__file__).parent / "golden" / g["fcidump"], group=g["group"], check=False)
+    assert abs(d.solve() - g["energy"]) < g["tolerance"]
+
+
+def test_executor_rejects_out_of_bounds_programs():
+    """The checker of the task programs: a program planted with a bad offset is refused on
+    the CPU before it could ever reach a GPU (the mistake is planted in the oracle's input,
+    through a truncated slot binding)."""
+    m = models.hubbard(6, 4.0)
+    ol.srand(3)
+    d = ol.OracleDMRG(m, 0, 6, 0, [(50, 1e-10, 1, 0.0, 1e-8)])
+    x, y, _ = d.heff_apply(4)  # in bounds: fine
+    with pytest.raises(RuntimeError, match="outside slot|not bound|check failed"):
+        d.heff_apply(4, x=x[: len(x) // 2])
