@@ -1,12 +1,16 @@
 // Device kernels of the DMRG hot path and their host launchers.
 //
-//   grouped block GEMM  one launch per task-program stage: every output block (group) is
-//                       cut into 32 x 32 tiles, one CTA per tile, and the CTA sums its
-//                       group's terms alpha * op(U) * op(V) (or alpha * op(U)) in order.
-//   vector kernels      the Davidson eigensolver's dots, linear combinations and
-//                       preconditioner, with deterministic two-pass reductions.
-//   small_eig           Jacobi diagonalisation of the <= 32 x 32 Rayleigh-Ritz matrix in
-//                       one CTA (FP64).
+//   block sandwich     one launch per task-program stage executes every term
+//                      out += alpha sum_p ratio_p op(A_p) op(B) op(C_p) of the stage. One
+//                      CTA per output tile (<= 32 x 32); its 128 threads split into S
+//                      register sub-tiles (<= 4 x 4 elements each) times 128 / S item
+//                      lanes, each lane summing a contiguous range of the group's
+//                      (term, entry) items; the lanes' partial tiles are then reduced in a
+//                      fixed order, so the result is deterministic.
+//   vector kernels     the Davidson eigensolver's dots, linear combinations and
+//                      preconditioner, with deterministic two-pass reductions.
+//   small_eig          Jacobi diagonalisation of the <= 32 x 32 Rayleigh-Ritz matrix in
+//                      one CTA (FP64).
 #pragma once
 
 #include <cstdint>
@@ -16,24 +20,38 @@
 
 namespace c2g {
 
-constexpr int kTile = 32;      // output tile edge of the grouped GEMM
-constexpr int kTileK = 16;     // inner-dimension chunk staged in shared memory
-constexpr int kMaxSlots = 512; // slot table size on the device
+constexpr int kTile = 32;          // output tile edge of the block sandwich
+constexpr int kSub = 4;            // register sub-tile edge
+constexpr int kSandwichThreads = 128;
+constexpr int kMaxSlots = 512;     // slot table size on the device
 
-// Device pointers the kernels resolve references against. X, Y, P1, Combo and Ones are
-// per launch; everything else comes from the slot table.
+// Device pointers the kernels resolve references against. X, Y, Combo and Ones are per
+// launch; everything else comes from the slot table.
 struct SlotPtrs {
   const double* const* table;  // device array [kMaxSlots]
   double* x;
   double* y;
-  double* p1;
   double* combo;
   const double* ones;
 };
 
-// Launch one stage: `tiles` holds (group, tile row << 16 | tile col) pairs.
-cudaError_t launch_grouped_gemm(const Group* groups, const Term* terms, const int2* tiles, int ntiles,
-                                const SlotPtrs& sp, cudaStream_t stream);
+// A CTA work unit: group index, tile position (row << 16 | col, in units of kTile) and the
+// sub-tile grid (rows << 8 | cols) of the tile, chosen on the host.
+struct TileDesc {
+  int32_t group;
+  int32_t pos;
+  int32_t grid;
+  int32_t pad;
+};
+
+// Choose the sub-tile grid (sr x sc, sr * sc <= kSandwichThreads) of an m x n tile.
+inline int sandwich_grid(int m, int n) {
+  const int sr = (m + kSub - 1) / kSub, sc = (n + kSub - 1) / kSub;
+  return (sr << 8) | sc;
+}
+
+cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
+                            int ntiles, const SlotPtrs& sp, cudaStream_t stream);
 
 // out[j] = sum_i A[i + lda * j] * x[i] for j < ncol (A has n rows). Uses `partial`
 // (at least ncol * kDotBlocks doubles) as scratch.

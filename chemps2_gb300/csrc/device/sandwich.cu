@@ -1,0 +1,203 @@
+// The block-sandwich kernel: executes one stage of a task program (FP64).
+#include "kernels.cuh"
+
+namespace c2g {
+
+namespace {
+
+__device__ __forceinline__ const double* resolve(const SlotPtrs& sp, Ref r) {
+  const int s = static_cast<int>(r >> kRefShift);
+  const int64_t off = static_cast<int64_t>(r & kRefMask);
+  const double* base;
+  switch (s) {
+    case kSlotX: base = sp.x; break;
+    case kSlotY: base = sp.y; break;
+    case kSlotCombo: base = sp.combo; break;
+    case kSlotOnes: base = sp.ones; break;
+    default: base = sp.table[s]; break;
+  }
+  return base + off;
+}
+
+// acc[ii][jj] (rows i0 + ii, ii < r; columns j0 + jj, jj < c) += one entry of a term.
+__device__ __forceinline__ void sandwich_item(double (&acc)[kSub][kSub], const Term& T, const double* __restrict__ A,
+                                              const double* __restrict__ B, const double* __restrict__ C, double al,
+                                              int i0, int j0, int r, int c) {
+  const bool ha = T.flags & kHasA, hc = T.flags & kHasC;
+  const bool ta = T.flags & kTransA, tb = T.flags & kTransB, tc = T.flags & kTransC;
+  const int64_t lda = T.lda, ldb = T.ldb, ldc = T.ldc;
+  auto opA = [&](int i, int k) { return ta ? A[k + lda * i] : A[i + lda * k]; };
+  auto opB = [&](int k, int l) { return tb ? B[l + ldb * k] : B[k + ldb * l]; };
+  auto opC = [&](int l, int j) { return tc ? C[j + ldc * l] : C[l + ldc * j]; };
+  if (ha && hc) {
+    if (T.flags & kLeftFirst) {
+      for (int l = 0; l < T.k2; l++) {
+        double s[kSub];
+#pragma unroll
+        for (int ii = 0; ii < kSub; ii++) s[ii] = 0.0;
+        for (int k = 0; k < T.k1; k++) {
+          const double b = opB(k, l);
+#pragma unroll
+          for (int ii = 0; ii < kSub; ii++)
+            if (ii < r) s[ii] = fma(opA(i0 + ii, k), b, s[ii]);
+        }
+#pragma unroll
+        for (int jj = 0; jj < kSub; jj++) {
+          if (jj >= c) break;
+          const double cv = al * opC(l, j0 + jj);
+#pragma unroll
+          for (int ii = 0; ii < kSub; ii++)
+            if (ii < r) acc[ii][jj] = fma(s[ii], cv, acc[ii][jj]);
+        }
+      }
+    } else {
+      for (int k = 0; k < T.k1; k++) {
+        double t[kSub];
+#pragma unroll
+        for (int jj = 0; jj < kSub; jj++) t[jj] = 0.0;
+        for (int l = 0; l < T.k2; l++) {
+          const double b = opB(k, l);
+#pragma unroll
+          for (int jj = 0; jj < kSub; jj++)
+            if (jj < c) t[jj] = fma(b, opC(l, j0 + jj), t[jj]);
+        }
+#pragma unroll
+        for (int ii = 0; ii < kSub; ii++) {
+          if (ii >= r) break;
+          const double av = al * opA(i0 + ii, k);
+#pragma unroll
+          for (int jj = 0; jj < kSub; jj++)
+            if (jj < c) acc[ii][jj] = fma(av, t[jj], acc[ii][jj]);
+        }
+      }
+    }
+  } else if (ha) {
+    for (int k = 0; k < T.k1; k++) {
+      double bv[kSub];
+#pragma unroll
+      for (int jj = 0; jj < kSub; jj++) bv[jj] = (jj < c) ? al * opB(k, j0 + jj) : 0.0;
+#pragma unroll
+      for (int ii = 0; ii < kSub; ii++) {
+        if (ii >= r) break;
+        const double av = opA(i0 + ii, k);
+#pragma unroll
+        for (int jj = 0; jj < kSub; jj++)
+          if (jj < c) acc[ii][jj] = fma(av, bv[jj], acc[ii][jj]);
+      }
+    }
+  } else if (hc) {
+    for (int l = 0; l < T.k2; l++) {
+      double cv[kSub];
+#pragma unroll
+      for (int jj = 0; jj < kSub; jj++) cv[jj] = (jj < c) ? al * opC(l, j0 + jj) : 0.0;
+#pragma unroll
+      for (int ii = 0; ii < kSub; ii++) {
+        if (ii >= r) break;
+        const double b = opB(i0 + ii, l);
+#pragma unroll
+        for (int jj = 0; jj < kSub; jj++)
+          if (jj < c) acc[ii][jj] = fma(b, cv[jj], acc[ii][jj]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int ii = 0; ii < kSub; ii++) {
+      if (ii >= r) break;
+#pragma unroll
+      for (int jj = 0; jj < kSub; jj++)
+        if (jj < c) acc[ii][jj] = fma(al, opB(i0 + ii, j0 + jj), acc[ii][jj]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group* __restrict__ groups,
+                                                                    const Term* __restrict__ terms,
+                                                                    const BatchEntry* __restrict__ entries,
+                                                                    const TileDesc* __restrict__ tiles, SlotPtrs sp) {
+  __shared__ double red[kSandwichThreads * kSub * kSub];
+  const TileDesc td = tiles[blockIdx.x];
+  const Group G = groups[td.group];
+  const int row0 = (td.pos >> 16) * kTile, col0 = (td.pos & 0xffff) * kTile;
+  const int tm = min(kTile, G.m - row0), tn = min(kTile, G.n - col0);
+  const int sr = td.grid >> 8, sc = td.grid & 0xff;
+  const int S = sr * sc;
+  const int P = kSandwichThreads / S;
+  const int tid = threadIdx.x;
+  const int s = tid % S, lane = tid / S;
+  const int si = s % sr, sj = s / sr;
+  const int i0 = row0 + si * kSub, j0 = col0 + sj * kSub;
+  const int r = max(0, min(kSub, row0 + tm - i0)), c = max(0, min(kSub, col0 + tn - j0));
+  double acc[kSub][kSub];
+#pragma unroll
+  for (int ii = 0; ii < kSub; ii++)
+#pragma unroll
+    for (int jj = 0; jj < kSub; jj++) acc[ii][jj] = 0.0;
+  if (lane < P && r > 0 && c > 0 && G.t1 > G.t0) {
+    const Term& last = terms[G.t1 - 1];
+    const int total = last.item0 + last.count;
+    const int chunk = (total + P - 1) / P;
+    const int start = lane * chunk;
+    const int stop = min(total, start + chunk);
+    if (start < stop) {
+      int lo = G.t0, hi = G.t1 - 1;  // last term with item0 <= start
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (terms[mid].item0 <= start) lo = mid;
+        else hi = mid - 1;
+      }
+      int t = lo;
+      Term T = terms[t];
+      const double* B = resolve(sp, T.b);
+      const double* A0 = (T.flags & kHasA) ? resolve(sp, T.a) : nullptr;
+      const double* C0 = (T.flags & kHasC) ? resolve(sp, T.c) : nullptr;
+      for (int item = start; item < stop; item++) {
+        int p = item - T.item0;
+        if (p >= T.count) {
+          T = terms[++t];
+          B = resolve(sp, T.b);
+          A0 = (T.flags & kHasA) ? resolve(sp, T.a) : nullptr;
+          C0 = (T.flags & kHasC) ? resolve(sp, T.c) : nullptr;
+          p = 0;
+        }
+        double ratio = 1.0;
+        const double* A = A0;
+        const double* C = C0;
+        if (T.list >= 0) {
+          const BatchEntry e = entries[T.list + p];
+          ratio = e.ratio;
+          if (A) A += e.da;
+          if (C) C += e.dc;
+        }
+        sandwich_item(acc, T, A, B, C, T.alpha * ratio, i0, j0, r, c);
+      }
+    }
+  }
+#pragma unroll
+  for (int ii = 0; ii < kSub; ii++)
+#pragma unroll
+    for (int jj = 0; jj < kSub; jj++) red[tid * kSub * kSub + ii * kSub + jj] = acc[ii][jj];
+  __syncthreads();
+  double* O = const_cast<double*>(resolve(sp, G.out));
+  const int64_t ldo = G.ldo;
+  const bool accum = (G.flags & kAccumulate) != 0;
+  for (int e = tid; e < tm * tn; e += kSandwichThreads) {
+    const int ii = e % tm, jj = e / tm;
+    const int sub = (ii / kSub) + sr * (jj / kSub);
+    const int w = (ii % kSub) * kSub + (jj % kSub);
+    double v = 0.0;
+    for (int l = 0; l < P; l++) v += red[(sub + S * l) * kSub * kSub + w];
+    const int64_t idx = (row0 + ii) + ldo * (col0 + jj);
+    O[idx] = accum ? O[idx] + v : v;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
+                            int ntiles, const SlotPtrs& sp, cudaStream_t stream) {
+  if (ntiles <= 0) return cudaSuccess;
+  sandwich_kernel<<<ntiles, kSandwichThreads, 0, stream>>>(groups, terms, entries, tiles, sp);
+  return cudaGetLastError();
+}
+
+}  // namespace c2g

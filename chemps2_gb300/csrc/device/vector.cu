@@ -1,5 +1,5 @@
-// Device kernels: the grouped FP64 block GEMM that executes task-program stages, and the
-// vector / small dense kernels of the Davidson eigensolver.
+// Vector and small dense kernels of the Davidson eigensolver and the truncation step
+// (FP64, deterministic reductions).
 #include "kernels.cuh"
 
 #include <cmath>
@@ -7,106 +7,6 @@
 namespace c2g {
 
 namespace {
-
-__device__ __forceinline__ const double* resolve(const SlotPtrs& sp, Ref r) {
-  const int s = static_cast<int>(r >> kRefShift);
-  const int64_t off = static_cast<int64_t>(r & kRefMask);
-  const double* base;
-  switch (s) {
-    case kSlotX: base = sp.x; break;
-    case kSlotY: base = sp.y; break;
-    case kSlotP1: base = sp.p1; break;
-    case kSlotCombo: base = sp.combo; break;
-    case kSlotOnes: base = sp.ones; break;
-    default: base = sp.table[s]; break;
-  }
-  return base + off;
-}
-
-// One CTA = one 32 x 32 tile of one output block. 256 threads as a 16 x 16 grid; thread
-// (tx, ty) owns rows ty, ty + 16 and columns tx, tx + 16 of the tile. The terms of the
-// group are accumulated in order, so the result does not depend on the launch order.
-__global__ void __launch_bounds__(256) grouped_gemm_kernel(const Group* __restrict__ groups,
-                                                           const Term* __restrict__ terms,
-                                                           const int2* __restrict__ tiles, SlotPtrs sp) {
-  __shared__ double As[kTileK][kTile + 1];  // alpha * op(U)(row0 + i, k0 + kk)
-  __shared__ double Bs[kTileK][kTile + 1];  // op(V)(k0 + kk, col0 + j)
-  const int2 td = tiles[blockIdx.x];
-  const Group G = groups[td.x];
-  const int row0 = (td.y >> 16) * kTile;
-  const int col0 = (td.y & 0xffff) * kTile;
-  const int tid = threadIdx.x;
-  const int tx = tid & 15, ty = tid >> 4;
-  double acc00 = 0.0, acc01 = 0.0, acc10 = 0.0, acc11 = 0.0;
-  for (int t = G.t0; t < G.t1; t++) {
-    const Term T = terms[t];
-    const double* U = resolve(sp, T.u);
-    const bool tu = (T.flags & kTransU) != 0;
-    const int64_t ldu = T.ldu;
-    if (T.flags & kScalar) {
-#pragma unroll
-      for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 2; j++) {
-          const int r = row0 + ty + 16 * i, c = col0 + tx + 16 * j;
-          if (r < G.m && c < G.n) {
-            const double v = T.alpha * (tu ? U[c + ldu * r] : U[r + ldu * c]);
-            if (i == 0 && j == 0) acc00 += v;
-            if (i == 0 && j == 1) acc01 += v;
-            if (i == 1 && j == 0) acc10 += v;
-            if (i == 1 && j == 1) acc11 += v;
-          }
-        }
-      continue;
-    }
-    const double* V = resolve(sp, T.v);
-    const bool tv = (T.flags & kTransV) != 0;
-    const int64_t ldv = T.ldv;
-    for (int k0 = 0; k0 < T.k; k0 += kTileK) {
-#pragma unroll
-      for (int s = 0; s < 2; s++) {
-        const int e = tid + 256 * s;
-        int i, kk;
-        if (!tu) { i = e & 31; kk = e >> 5; } else { kk = e & 15; i = e >> 4; }
-        const int r = row0 + i, k = k0 + kk;
-        As[kk][i] = (r < G.m && k < T.k) ? T.alpha * (tu ? U[k + ldu * r] : U[r + ldu * k]) : 0.0;
-      }
-#pragma unroll
-      for (int s = 0; s < 2; s++) {
-        const int e = tid + 256 * s;
-        int j, kk;
-        if (!tv) { kk = e & 15; j = e >> 4; } else { j = e & 31; kk = e >> 5; }
-        const int c = col0 + j, k = k0 + kk;
-        Bs[kk][j] = (c < G.n && k < T.k) ? (tv ? V[c + ldv * k] : V[k + ldv * c]) : 0.0;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int kk = 0; kk < kTileK; kk++) {
-        const double a0 = As[kk][ty], a1 = As[kk][ty + 16];
-        const double b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
-        acc00 = fma(a0, b0, acc00);
-        acc01 = fma(a0, b1, acc01);
-        acc10 = fma(a1, b0, acc10);
-        acc11 = fma(a1, b1, acc11);
-      }
-      __syncthreads();
-    }
-  }
-  double* O = const_cast<double*>(resolve(sp, G.out));
-  const int64_t ldo = G.ldo;
-  const bool accum = (G.flags & kAccumulate) != 0;
-  const double accs[2][2] = {{acc00, acc01}, {acc10, acc11}};
-#pragma unroll
-  for (int i = 0; i < 2; i++)
-#pragma unroll
-    for (int j = 0; j < 2; j++) {
-      const int r = row0 + ty + 16 * i, c = col0 + tx + 16 * j;
-      if (r < G.m && c < G.n) {
-        const int64_t idx = r + ldo * c;
-        O[idx] = accum ? O[idx] + accs[i][j] : accs[i][j];
-      }
-    }
-}
 
 // ---------------------------------------------------------------- vector kernels
 
@@ -457,13 +357,6 @@ inline int grid_for(int64_t n, int threads = 256) {
 }
 
 }  // namespace
-
-cudaError_t launch_grouped_gemm(const Group* groups, const Term* terms, const int2* tiles, int ntiles,
-                                const SlotPtrs& sp, cudaStream_t stream) {
-  if (ntiles <= 0) return cudaSuccess;
-  grouped_gemm_kernel<<<ntiles, 256, 0, stream>>>(groups, terms, tiles, sp);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_multi_dot(const double* A, int64_t lda, int ncol, const double* x, int64_t n, double* partial,
                              double* out, cudaStream_t stream) {

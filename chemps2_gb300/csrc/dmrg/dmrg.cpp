@@ -10,6 +10,7 @@
 #include <cusolverDn.h>
 
 #include "davidson.hpp"
+#include "compile.hpp"
 #include "heff.hpp"
 #include "layout.hpp"
 #include "operators.hpp"
@@ -260,9 +261,7 @@ void DMRG::update_moving_right(const int index) {
   ctx.next = ops[index].get();
   ctx.mps = mps_tensor(mps_lay[index].get(), index);
   const double tc = now();
-  TaskBuilder tb;
-  c2g::compile_update(tb, ctx);
-  Program p = tb.finalize();
+  Program p = c2g::compile_update_program(ctx).program;
   stats_.t_compile += now() - tc;
   auto dp = rt->upload(p);
   rt->zero(ops_dev[index], ops[index]->size);
@@ -292,9 +291,7 @@ void DMRG::update_moving_left(const int index) {
   ctx.next = ops[index].get();
   ctx.mps = mps_tensor(mps_lay[index + 1].get(), index + 1);
   const double tc = now();
-  TaskBuilder tb;
-  c2g::compile_update(tb, ctx);
-  Program p = tb.finalize();
+  Program p = c2g::compile_update_program(ctx).program;
   stats_.t_compile += now() - tc;
   auto dp = rt->upload(p);
   rt->zero(ops_dev[index], ops[index]->size);
@@ -381,12 +378,9 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("solve_site: left operators missing");
   if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("solve_site: right operators missing");
   double tc = now();
-  TaskBuilder tbd;
-  c2g::compile_heff_diag(tbd, ctx);
-  Program pd = tbd.finalize();
-  TaskBuilder tbh;
-  c2g::compile_heff(tbh, ctx);
-  Program ph = tbh.finalize();
+  Program pd = c2g::compile_heff_diag_program(ctx).program;
+  c2g::Compiled ch = c2g::compile_heff_program(ctx);
+  Program& ph = ch.program;
   stats_.t_compile += now() - tc;
   int maxdim = 1;
   for (int k = 0; k < S.nkappa; k++) maxdim = std::max(maxdim, std::max(S.rows[k], S.cols[k]));
@@ -418,6 +412,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   stats_.n_davidson++;
   stats_.t_matvec += 1e-3 * mv_ms;
   stats_.matvec_flops += static_cast<double>(dph->flops_repeat) * ds.n_matvec;
+  stats_.matvec_bytes += static_cast<double>(ch.operand_bytes + 16 * veclen) * ds.n_matvec;
   const double Energy = ds.energy + Prob->gEconst();
   stats_.last_energy = Energy;
   stats_.t_solve += now() - t0;
@@ -603,10 +598,8 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
   if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("bench_heff: left operators missing");
   if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("bench_heff: right operators missing");
-  TaskBuilder tbh;
-  c2g::compile_heff(tbh, ctx);
-  Program ph = tbh.finalize();
-  auto dph = rt->upload(ph);
+  c2g::Compiled ch = c2g::compile_heff_program(ctx);
+  auto dph = rt->upload(ch.program);
   rt->prepare(*dph);
   for (int i = 0; i < warmup; i++) rt->run(*dph, x, y);
   rt->sync();
@@ -624,7 +617,7 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   cudaEventDestroy(e1);
   if (launches) *launches = c2g::kernel_launches() - l0;
   if (flops) *flops = static_cast<double>(dph->flops_repeat);
-  if (bytes) *bytes = static_cast<double>(tbh.operand_bytes()) + 16.0 * veclen;
+  if (bytes) *bytes = static_cast<double>(ch.operand_bytes) + 16.0 * veclen;
   rt->release(x);
   rt->release(y);
   rt->sync();
@@ -668,9 +661,7 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
   if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("heff_apply: left operators missing");
   if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("heff_apply: right operators missing");
   {
-    TaskBuilder tb;
-    c2g::compile_heff(tb, ctx);
-    auto dp = rt->upload(tb.finalize());
+    auto dp = rt->upload(c2g::compile_heff_program(ctx).program);
     rt->run(*dp, dx, dy);
     C2G_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   }
@@ -678,9 +669,7 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
     int maxdim = 1;
     for (int k = 0; k < S.nkappa; k++) maxdim = std::max(maxdim, std::max(S.rows[k], S.cols[k]));
     rt->ones(maxdim);
-    TaskBuilder tb;
-    c2g::compile_heff_diag(tb, ctx);
-    auto dp = rt->upload(tb.finalize());
+    auto dp = rt->upload(c2g::compile_heff_diag_program(ctx).program);
     rt->run(*dp, nullptr, dy);
     C2G_CUDA(cudaMemcpyAsync(diag, dy, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   }

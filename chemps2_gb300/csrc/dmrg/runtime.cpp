@@ -10,7 +10,7 @@ namespace c2g {
 
 namespace {
 std::atomic<int64_t> g_launches{0};
-inline int64_t align64(int64_t x) { return (x + 63) & ~int64_t(63); }
+inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
 }  // namespace
 
 int64_t kernel_launches() { return g_launches.load(); }
@@ -50,7 +50,6 @@ Runtime::Runtime(int L, int device) : L_(L) {
 
 Runtime::~Runtime() {
   if (stream_) cudaStreamSynchronize(stream_);
-  if (p1_) cudaFreeAsync(p1_, stream_);
   if (ones_) cudaFreeAsync(ones_, stream_);
   if (stream_) cudaStreamSynchronize(stream_);
   cudaFree(dev_slots_);
@@ -90,13 +89,6 @@ void Runtime::flush_slots() {
   slots_dirty_ = false;
 }
 
-void Runtime::ensure_p1(int64_t n) {
-  if (n <= p1_cap_) return;
-  if (p1_) release(p1_);
-  p1_cap_ = std::max<int64_t>(n, p1_cap_ * 3 / 2);
-  p1_ = alloc(p1_cap_);
-}
-
 const double* Runtime::ones(int64_t n) {
   if (n > ones_cap_) {
     if (ones_) release(ones_);
@@ -114,7 +106,6 @@ SlotPtrs Runtime::ptrs(double* x, double* y, double* combo) {
   sp.table = dev_slots_;
   sp.x = x;
   sp.y = y;
-  sp.p1 = p1_;
   sp.combo = combo;
   sp.ones = ones_;
   return sp;
@@ -124,11 +115,10 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   auto dp = std::make_unique<DevProgram>();
   dp->rt = this;
   dp->first_repeat = p.first_repeat_stage;
-  dp->p1_size = p.p1_size;
   dp->combo_size = p.combo_size;
-  // Tile lists: every group cut into 32 x 32 tiles, groups with the most work first.
-  std::vector<std::vector<int2>> tiles(p.stages.size());
-  int64_t bytes = 0;
+  // Tile lists: every group cut into 32 x 32 tiles, the groups with the most work first.
+  std::vector<std::vector<TileDesc>> tiles(p.stages.size());
+  int64_t bytes = align256(sizeof(BatchEntry) * p.entries.size());
   for (size_t s = 0; s < p.stages.size(); s++) {
     const Stage& st = p.stages[s];
     std::vector<int> order(st.groups.size());
@@ -141,17 +131,26 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
       const int tm = (G.m + kTile - 1) / kTile, tn = (G.n + kTile - 1) / kTile;
       if (tm >= 32768 || tn >= 65536) throw std::invalid_argument("output block too large for the tile index");
       for (int i = 0; i < tm; i++)
-        for (int j = 0; j < tn; j++) tiles[s].push_back(make_int2(g, (i << 16) | j));
+        for (int j = 0; j < tn; j++) {
+          const int rows = std::min(kTile, G.m - i * kTile), cols = std::min(kTile, G.n - j * kTile);
+          tiles[s].push_back(TileDesc{g, (i << 16) | j, sandwich_grid(rows, cols), 0});
+        }
     }
-    bytes += align64(sizeof(Group) * st.groups.size()) + align64(sizeof(Term) * st.terms.size()) +
-             align64(sizeof(int2) * tiles[s].size());
+    bytes += align256(sizeof(Group) * st.groups.size()) + align256(sizeof(Term) * st.terms.size()) +
+             align256(sizeof(TileDesc) * tiles[s].size());
   }
-  std::vector<char> host(static_cast<size_t>(std::max<int64_t>(bytes, 64)));
-  if (bytes > 0) {
-    C2G_CUDA(cudaMallocAsync(&dp->blob, bytes, stream_));
-  }
+  std::vector<char> host(static_cast<size_t>(std::max<int64_t>(bytes, 256)));
+  C2G_CUDA(cudaMallocAsync(&dp->blob, std::max<int64_t>(bytes, 256), stream_));
   char* dbase = static_cast<char*>(dp->blob);
   int64_t off = 0;
+  auto put = [&](const void* src, size_t n) -> const void* {
+    if (n) std::memcpy(host.data() + off, src, n);
+    const void* d = dbase + off;
+    off += align256(static_cast<int64_t>(n));
+    return d;
+  };
+  dp->entries = static_cast<const BatchEntry*>(put(p.entries.data(), sizeof(BatchEntry) * p.entries.size()));
+  dp->nentries = static_cast<int64_t>(p.entries.size());
   for (size_t s = 0; s < p.stages.size(); s++) {
     const Stage& st = p.stages[s];
     DevStage ds;
@@ -160,35 +159,28 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     ds.nterms = static_cast<int>(st.terms.size());
     ds.ntiles = static_cast<int>(tiles[s].size());
     ds.flops = st.flops;
-    auto put = [&](const void* src, size_t n) -> const void* {
-      if (n) std::memcpy(host.data() + off, src, n);
-      const void* d = dbase + off;
-      off += align64(static_cast<int64_t>(n));
-      return d;
-    };
+    ds.items = st.items;
     ds.groups = static_cast<const Group*>(put(st.groups.data(), sizeof(Group) * st.groups.size()));
     ds.terms = static_cast<const Term*>(put(st.terms.data(), sizeof(Term) * st.terms.size()));
-    ds.tiles = static_cast<const int2*>(put(tiles[s].data(), sizeof(int2) * tiles[s].size()));
+    ds.tiles = static_cast<const TileDesc*>(put(tiles[s].data(), sizeof(TileDesc) * tiles[s].size()));
     dp->nterms += ds.nterms;
     if (static_cast<int>(s) < dp->first_repeat) dp->flops_once += ds.flops;
     else dp->flops_repeat += ds.flops;
     dp->stages.push_back(ds);
   }
-  if (bytes > 0) {
-    C2G_CUDA(cudaMemcpyAsync(dp->blob, host.data(), bytes, cudaMemcpyHostToDevice, stream_));
-    C2G_CUDA(cudaStreamSynchronize(stream_));  // `host` goes out of scope
-  }
+  dp->bytes = bytes;
+  C2G_CUDA(cudaMemcpyAsync(dp->blob, host.data(), bytes, cudaMemcpyHostToDevice, stream_));
+  C2G_CUDA(cudaStreamSynchronize(stream_));  // `host` goes out of scope
   if (dp->combo_size > 0) dp->combo = alloc(dp->combo_size);
   return dp;
 }
 
 void Runtime::prepare(DevProgram& p) {
   if (p.prepared) return;
-  ensure_p1(p.p1_size);
   const SlotPtrs sp = ptrs(nullptr, nullptr, p.combo);
   for (int s = 0; s < p.first_repeat; s++) {
     const DevStage& ds = p.stages[s];
-    C2G_CUDA(launch_grouped_gemm(ds.groups, ds.terms, ds.tiles, ds.ntiles, sp, stream_));
+    C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_));
     if (ds.ntiles) count_launches(1);
   }
   p.prepared = true;
@@ -196,11 +188,10 @@ void Runtime::prepare(DevProgram& p) {
 
 void Runtime::run(DevProgram& p, double* x, double* y) {
   prepare(p);
-  ensure_p1(p.p1_size);
   const SlotPtrs sp = ptrs(x, y, p.combo);
   for (size_t s = p.first_repeat; s < p.stages.size(); s++) {
     const DevStage& ds = p.stages[s];
-    C2G_CUDA(launch_grouped_gemm(ds.groups, ds.terms, ds.tiles, ds.ntiles, sp, stream_));
+    C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_));
     if (ds.ntiles) count_launches(1);
   }
 }

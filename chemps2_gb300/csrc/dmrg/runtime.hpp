@@ -2,9 +2,9 @@
 // references into device pointers, uploaded task programs and their scratch buffers.
 //
 // A task Program (host/tasks.hpp) is uploaded once into one device allocation (groups,
-// terms and the tile list of every stage) and can then be run any number of times with
-// different X / Y vectors, e.g. once per Davidson matvec. Stages that only combine
-// operator blocks (the "once" stages) run when the program is prepared.
+// terms, tile list of every stage, batch table) and can then be run any number of times
+// with different X / Y vectors, e.g. once per Davidson matvec. The combination stage
+// (blocks that only depend on operators) runs when the program is prepared.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -33,19 +33,20 @@ class Runtime;
 struct DevStage {
   const Group* groups = nullptr;
   const Term* terms = nullptr;
-  const int2* tiles = nullptr;
+  const TileDesc* tiles = nullptr;
   int ngroups = 0, nterms = 0, ntiles = 0;
-  int64_t flops = 0;
+  int64_t flops = 0, items = 0;
   std::string name;
 };
 
 struct DevProgram {
   Runtime* rt = nullptr;
   std::vector<DevStage> stages;
+  const BatchEntry* entries = nullptr;
   int first_repeat = 0;
-  int64_t p1_size = 0, combo_size = 0;
+  int64_t combo_size = 0;
   int64_t flops_once = 0, flops_repeat = 0;
-  int64_t nterms = 0;
+  int64_t nterms = 0, nentries = 0, bytes = 0;
   void* blob = nullptr;
   double* combo = nullptr;
   bool prepared = false;
@@ -70,7 +71,7 @@ class Runtime {
   void release(void* p);
   void zero(double* p, int64_t n);
 
-  // Slot table (slots other than X, Y, P1, Combo and Ones).
+  // Slot table (slots other than X, Y, Combo and Ones).
   void set_slot(int slot, double* p);
   double* slot(int s) const { return host_slots_[s]; }
 
@@ -87,7 +88,6 @@ class Runtime {
  private:
   friend struct DevProgram;
   void flush_slots();
-  void ensure_p1(int64_t n);
   SlotPtrs ptrs(double* x, double* y, double* combo);
 
   int L_;
@@ -95,8 +95,6 @@ class Runtime {
   std::vector<double*> host_slots_;
   const double** dev_slots_ = nullptr;
   bool slots_dirty_ = true;
-  double* p1_ = nullptr;
-  int64_t p1_cap_ = 0;
   double* ones_ = nullptr;
   int64_t ones_cap_ = 0;
   double* partial_ = nullptr;

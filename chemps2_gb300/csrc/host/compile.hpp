@@ -1,0 +1,21 @@
+// Parallel task compilation: every hot-path compiler emits disjoint outputs per shard, so
+// shards are compiled on host threads and merged (tasks.hpp, merge_programs).
+#pragma once
+
+#include "heff.hpp"
+#include "operators.hpp"
+#include "tasks.hpp"
+
+namespace c2g {
+
+struct Compiled {
+  Program program;
+  int64_t operand_bytes = 0;   // distinct MPS / operator bytes the program reads
+  int64_t contractions = 0;    // block contractions recorded (before batching)
+};
+
+Compiled compile_heff_program(const HeffContext& ctx);
+Compiled compile_heff_diag_program(const HeffContext& ctx);
+Compiled compile_update_program(const UpdateContext& ctx);
+
+}  // namespace c2g

@@ -8,13 +8,14 @@ using std::sqrt;
 
 // CheMPS2/Heff.cpp:43-248. Every block of Y is an output of the single accumulation
 // stage; its terms keep the reference's diagram order.
-void compile_heff(TaskBuilder& tb, const HeffContext& ctx) {
+void compile_heff(TaskBuilder& tb, const HeffContext& ctx, int shard, int nshards) {
   HeffEmitter h(tb, ctx);
   const int L = ctx.bk->gL();
   const bool atLeft = (h.theindex == 0);
   const bool atRight = (h.theindex == L - 2);
   const TwoSiteLayout& S = *ctx.S;
-  for (int k = 0; k < S.nkappa; k++) {
+  for (int r = shard; r < S.nkappa; r += nshards) {
+    const int k = S.reorder[r];
     h.set_block(k, kSlotY);
     tb.declare_output(h.Y);
     h.d1C();
@@ -106,7 +107,7 @@ Blk ones_row(int n) { return Blk::make(make_ref(kSlotOnes, 0), 1, n, 1); }
 
 // CheMPS2/Heff.cpp:250-315 with CheMPS2/HeffDiagonal.cpp:27-642. Each contribution is
 // a rank-1 update of the block: (left diagonal or ones) x (right diagonal or ones).
-void compile_heff_diag(TaskBuilder& tb, const HeffContext& ctx) {
+void compile_heff_diag(TaskBuilder& tb, const HeffContext& ctx, int shard, int nshards) {
   HeffEmitter h(tb, ctx);
   const int L = ctx.bk->gL();
   const int i = h.theindex;
@@ -115,7 +116,8 @@ void compile_heff_diag(TaskBuilder& tb, const HeffContext& ctx) {
   const TwoSiteLayout& S = *ctx.S;
   const BoundaryOps* Lt = ctx.left;
   const BoundaryOps* Rt = ctx.right;
-  for (int k = 0; k < S.nkappa; k++) {
+  for (int r = shard; r < S.nkappa; r += nshards) {
+    const int k = S.reorder[r];
     h.set_block(k, kSlotY);
     tb.declare_output(h.Y);
     const int NL = h.NL, TwoSL = h.TwoSL, IL = h.IL, NR = h.NR, TwoSR = h.TwoSR, IR = h.IR;

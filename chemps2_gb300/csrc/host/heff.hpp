@@ -27,7 +27,9 @@ struct HeffContext {
   const BoundaryOps* right = nullptr;  // operators at boundary index + 2 (built moving left)
 };
 
-void compile_heff(TaskBuilder& tb, const HeffContext& ctx);
-void compile_heff_diag(TaskBuilder& tb, const HeffContext& ctx);
+// Both compilers visit the blocks in the reference's size-sorted order; with nshards > 1
+// only every nshards-th block of that order (starting at shard) is emitted.
+void compile_heff(TaskBuilder& tb, const HeffContext& ctx, int shard = 0, int nshards = 1);
+void compile_heff_diag(TaskBuilder& tb, const HeffContext& ctx, int shard = 0, int nshards = 1);
 
 }  // namespace c2g

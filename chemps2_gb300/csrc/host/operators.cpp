@@ -5,6 +5,8 @@
 //   podd(x)= (-1)^x                (((x)%2)!=0)?-1:1
 #include "operators.hpp"
 
+#include <unordered_map>
+
 #include <cmath>
 #include <cstdlib>
 #include <stdexcept>
@@ -115,6 +117,12 @@ struct Emit {
   const Problem& prob;
   const MpsT& T;
   int L;
+  int shard = 0, nshards = 1;
+  const std::unordered_map<Ref, int>* tensor_id = nullptr;
+  bool mine(const OpT& o) const {
+    if (nshards <= 1) return true;
+    return tensor_id->at(o.base) % nshards == shard;
+  }
 
   int dim(int b, int n, int s, int i) const { return bk.gCurrentDim(b, n, s, i); }
   Blk need(const Blk& x) const {
@@ -126,6 +134,7 @@ struct Emit {
   // ---------------------------------------------------------------------------------
   // CheMPS2/TensorOperator.cpp:163-291 (update_moving_right) and :293-405 (moving_left)
   void generic_update(const OpT& out, const OpT& prev) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     const int tj = lay.two_j;
@@ -197,12 +206,14 @@ struct Emit {
   }
 
   void declare_all(const OpT& out) {
+    if (!mine(out)) return;
     for (int ik = 0; ik < out.lay->nkappa; ik++) tb.declare_output(out.blk_k(ik));
   }
 
   // ---------------------------------------------------------------------------------
   // CheMPS2/TensorL.cpp:57-135 (create_right / create_left without a previous tensor)
   void L_create(const OpT& out) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -234,6 +245,7 @@ struct Emit {
   // ---------------------------------------------------------------------------------
   // CheMPS2/TensorF0.cpp:53-138 (makenewRight/Left from the MPS only)
   void F0_new(const OpT& out) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     const double sqrt2 = std::sqrt(2.0);
@@ -268,6 +280,7 @@ struct Emit {
 
   // CheMPS2/TensorF1.cpp:54-118
   void F1_new(const OpT& out) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -297,6 +310,7 @@ struct Emit {
 
   // CheMPS2/TensorS0.cpp:53-99
   void S0_new(const OpT& out) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -320,6 +334,7 @@ struct Emit {
   // out += alpha * Tup * Lblk * Tdown^T (moving left).
   template <class Cases>
   void makenew_L(const OpT& out, const OpT& Lop, Cases cases) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -350,6 +365,7 @@ struct Emit {
 
   // CheMPS2/TensorF0.cpp:140-211 (right) and :213-285 (left)
   void F0_newL(const OpT& out, const OpT& Lop) {
+    if (!mine(out)) return;
     const int index = out.lay->index;
     const bool mr = out.moving_right;
     const int Li = Lop.irrep();
@@ -385,6 +401,7 @@ struct Emit {
 
   // CheMPS2/TensorF1.cpp:120-192 (right) and :194-269 (left)
   void F1_newL(const OpT& out, const OpT& Lop) {
+    if (!mine(out)) return;
     const int index = out.lay->index;
     const bool mr = out.moving_right;
     const int Li = Lop.irrep();
@@ -423,6 +440,7 @@ struct Emit {
 
   // CheMPS2/TensorS0.cpp:101-172 (right) and :174-246 (left)
   void S0_newL(const OpT& out, const OpT& Lop) {
+    if (!mine(out)) return;
     const int index = out.lay->index;
     const bool mr = out.moving_right;
     const int Li = Lop.irrep();
@@ -458,6 +476,7 @@ struct Emit {
 
   // CheMPS2/TensorS1.cpp:47-119 (right) and :121-195 (left)
   void S1_newL(const OpT& out, const OpT& Lop) {
+    if (!mine(out)) return;
     const int index = out.lay->index;
     const bool mr = out.moving_right;
     const int Li = Lop.irrep();
@@ -495,6 +514,7 @@ struct Emit {
   // ---------------------------------------------------------------------------------
   // CheMPS2/TensorQ.cpp:45-104 (AddTermSimple)
   void Q_simple(const OpT& out, int mps_site) {
+    if (!mine(out)) return;
     if (bk.gIrrep(mps_site) != out.irrep()) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
@@ -522,6 +542,7 @@ struct Emit {
   // the previous boundary.
   template <class LF>
   void Q_L(const OpT& out, LF Lprev) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     const int site = out.site;
@@ -629,6 +650,7 @@ struct Emit {
 
   // CheMPS2/TensorQ.cpp:386-599 (AddTermsAB)
   void Q_AB(const OpT& out, const OpT& A, const OpT& B) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -717,6 +739,7 @@ struct Emit {
 
   // CheMPS2/TensorQ.cpp:601-785 (AddTermsCD)
   void Q_CD(const OpT& out, const OpT& C, const OpT& D) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -781,6 +804,7 @@ struct Emit {
   // ---------------------------------------------------------------------------------
   // CheMPS2/TensorX.cpp:126-165 (makenewRight / makenewLeft)
   void X_new(const OpT& out) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -815,6 +839,7 @@ struct Emit {
   // CheMPS2/TensorX.cpp:167-371 (addTermQLRight / Left)
   template <class LF>
   void X_QL(const OpT& out, LF Lprev, const OpT& Qprev) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -885,6 +910,7 @@ struct Emit {
 
   // CheMPS2/TensorX.cpp:373-449 (addTermARight / Left)
   void X_A(const OpT& out, const OpT& A) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -904,6 +930,7 @@ struct Emit {
 
   // CheMPS2/TensorX.cpp:451-535 (addTermCRight / Left)
   void X_C(const OpT& out, const OpT& C) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -935,6 +962,7 @@ struct Emit {
 
   // CheMPS2/TensorX.cpp:537-645 (addTermDRight / Left)
   void X_D(const OpT& out, const OpT& D) {
+    if (!mine(out)) return;
     const OpLayout& lay = *out.lay;
     const int index = lay.index;
     for (int ik = 0; ik < lay.nkappa; ik++) {
@@ -974,6 +1002,22 @@ void compile_update(TaskBuilder& tb, const UpdateContext& ctx) {
   BoundaryOps& nx = *ctx.next;
   const BoundaryOps* pv = ctx.prev;
   Emit e{tb, bk, prob, ctx.mps, L};
+  std::unordered_map<Ref, int> ids;
+  if (ctx.nshards > 1) {
+    for (size_t t = 0; t < nx.all.size(); t++) ids[nx.all[t]->base] = static_cast<int>(t);
+    // A, B, C and D of one pair receive their complementary sums in stage 2 from the same
+    // loop iteration: keep them in one shard.
+    for (size_t c2 = 0; c2 < nx.A.size(); c2++)
+      for (size_t c3 = 0; c3 < nx.A[c2].size(); c3++) {
+        const int id = ids.at(nx.A[c2][c3].base);
+        if (c2 > 0) ids[nx.B[c2][c3].base] = id;
+        ids[nx.C[c2][c3].base] = id;
+        ids[nx.D[c2][c3].base] = id;
+      }
+    e.shard = ctx.shard;
+    e.nshards = ctx.nshards;
+    e.tensor_id = &ids;
+  }
   const bool edge = mr ? (index == 0) : (index == L - 2);
   auto Lprev = [&](int site) -> const OpT& { return pv->Lop(site); };
 
@@ -1055,6 +1099,7 @@ void compile_update(TaskBuilder& tb, const UpdateContext& ctx) {
       else { s1 = index - c3 - c2; s2 = index - c3; }
       const int iprod = irrep_prod(bk.gIrrep(s1), bk.gIrrep(s2));
       const int nnum = mr ? index + 1 : L - index - 1;
+      if (!e.mine(nx.A[c2][c3])) continue;
       for (int num = 0; num < nnum; num++) {
         const OpT& S0n = nx.S0[num][0];
         if (iprod != S0n.irrep()) continue;

@@ -86,6 +86,9 @@ struct UpdateContext {
   const BoundaryOps* prev = nullptr;  // boundary index (right) / index + 2 (left); null at the edge
   BoundaryOps* next = nullptr;        // boundary index + 1
   MpsT mps;                            // MPS[index] (right) or MPS[index + 1] (left)
+  // Sharded compilation: only the output tensors t with (allocation order of t) % nshards
+  // == shard are emitted. Shards write disjoint outputs and can be compiled in parallel.
+  int shard = 0, nshards = 1;
 };
 
 // Records the whole operator update of one boundary. Stage 1 builds every tensor from

@@ -1,8 +1,11 @@
 #include "tasks.hpp"
 
-#include <cassert>
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
+#include <thread>
 
 namespace c2g {
 
@@ -17,16 +20,52 @@ inline Shape op_shape(const Blk& b, bool t) { return t ? Shape{b.cols, b.rows} :
   throw std::logic_error(std::string("task compiler: inconsistent block shapes in ") + what);
 }
 
-void append_bytes(std::string& s, const void* p, size_t n) {
-  s.append(static_cast<const char*>(p), n);
+void append_bytes(std::string& s, const void* p, size_t n) { s.append(static_cast<const char*>(p), n); }
+
+inline uint64_t mix(uint64_t h, uint64_t v) {
+  h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+  return h;
 }
 
 }  // namespace
 
+int64_t term_flops(const Term& t, int m, int n) {
+  const bool ha = t.flags & kHasA, hc = t.flags & kHasC;
+  if (ha && hc) {
+    const int64_t ab = int64_t(m) * t.k1 * t.k2 + int64_t(m) * t.k2 * n;
+    const int64_t bc = int64_t(t.k1) * t.k2 * n + int64_t(m) * t.k1 * n;
+    return 2 * std::min(ab, bc);
+  }
+  if (ha) return 2 * int64_t(m) * t.k1 * n;
+  if (hc) return 2 * int64_t(m) * t.k2 * n;
+  return int64_t(m) * n;
+}
+
+size_t TaskBuilder::BatchKeyHash::operator()(const BatchKey& k) const {
+  uint64_t h = static_cast<uint64_t>(k.group);
+  h = mix(h, k.b);
+  h = mix(h, (uint64_t(uint32_t(k.flags)) << 32) | uint32_t(k.k1));
+  h = mix(h, (uint64_t(uint32_t(k.k2)) << 32) | uint32_t(k.lda));
+  h = mix(h, (uint64_t(uint32_t(k.ldc)) << 32) | (uint32_t(k.aslot) << 16) | uint32_t(k.cslot & 0xffff));
+  return static_cast<size_t>(h);
+}
+
 TaskBuilder::TaskBuilder() {
-  p1_stages_.emplace_back();
-  p2_stages_.emplace_back();
-  p2_stages_.back().name = "stage0";
+  stages_.emplace_back();
+  stages_.back().name = "stage0";
+}
+
+void TaskBuilder::note_operand(const Blk& b) {
+  if (!b.valid || ref_slot(b.ref) < kSlotMpsBase) return;
+  const int64_t n = int64_t(b.rows) * b.cols;
+  int64_t& cur = operands_[b.ref];
+  if (n > cur) cur = n;
+}
+
+int64_t TaskBuilder::operand_bytes() const {
+  int64_t s = 0;
+  for (const auto& kv : operands_) s += kv.second;
+  return 8 * s;
 }
 
 int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
@@ -44,52 +83,58 @@ int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
   g.flags = accumulate ? kAccumulate : 0;
   g.work = 0;
   sb.groups.push_back(g);
+  sb.terms.emplace_back();
   const int id = static_cast<int>(sb.groups.size()) - 1;
   sb.group_of[out.ref] = id;
   return id;
 }
 
-void TaskBuilder::add_term(StageBuf& sb, const Blk& out, double alpha, const Blk& U, bool tu,
-                           const Blk* V, bool tv, bool accumulate) {
+void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha, const Blk& A, bool ta,
+                      const Blk& B, bool tb, const Blk& C, bool tc, bool accumulate) {
   const int g = group_for(sb, out, accumulate);
   Term t{};
-  t.u = U.ref;
-  t.ldu = U.ld;
+  t.a = A.valid ? A.ref : 0;
+  t.b = B.ref;
+  t.c = C.valid ? C.ref : 0;
   t.alpha = alpha;
-  t.flags = (tu ? kTransU : 0);
-  if (V) {
-    t.v = V->ref;
-    t.ldv = V->ld;
-    t.flags |= (tv ? kTransV : 0);
-    t.k = op_shape(U, tu).c;
-  } else {
-    t.v = 0;
-    t.ldv = 0;
-    t.k = 0;
-    t.flags |= kScalar;
+  const Shape sb_ = op_shape(B, tb);
+  t.k1 = sb_.r;
+  t.k2 = sb_.c;
+  t.lda = A.valid ? A.ld : 0;
+  t.ldb = B.ld;
+  t.ldc = C.valid ? C.ld : 0;
+  t.flags = (A.valid ? kHasA : 0) | (C.valid ? kHasC : 0) | (A.valid && ta ? kTransA : 0) | (tb ? kTransB : 0) |
+            (C.valid && tc ? kTransC : 0);
+  t.list = -1;
+  t.count = 1;
+  t.item0 = 0;
+  auto& gt = sb.terms[g];
+  Group& G = sb.groups[g];
+  if (batchable) {
+    const BatchKey key{g, t.b, t.flags, t.k1, t.k2, t.lda, t.ldc, A.valid ? ref_slot(A.ref) : -1,
+                       C.valid ? ref_slot(C.ref) : -1};
+    auto it = open_.find(key);
+    if (it != open_.end()) {
+      PendingTerm& pt = gt[it->second];
+      BatchEntry e;
+      e.da = A.valid ? static_cast<int64_t>(A.ref - pt.t.a) : 0;
+      e.dc = C.valid ? static_cast<int64_t>(C.ref - pt.t.c) : 0;
+      e.ratio = alpha / pt.t.alpha;
+      pt.entries.push_back(e);
+      G.work += term_flops(pt.t, G.m, G.n);
+      return;
+    }
+    open_.emplace(key, static_cast<int>(gt.size()));
   }
-  sb.terms.push_back({g, t});
-  Group& gr = sb.groups[g];
-  gr.work += V ? int64_t(2) * gr.m * gr.n * t.k : int64_t(gr.m) * gr.n;
-}
-
-void TaskBuilder::note_operand(const Blk& b) {
-  if (!b.valid || ref_slot(b.ref) < kSlotMpsBase) return;
-  const int64_t n = int64_t(b.rows) * b.cols;
-  int64_t& cur = operands_[b.ref];
-  if (n > cur) cur = n;
-}
-
-int64_t TaskBuilder::operand_bytes() const {
-  int64_t s = 0;
-  for (const auto& kv : operands_) s += kv.second;
-  return 8 * s;
+  gt.push_back(PendingTerm{t, {}});
+  G.work += term_flops(t, G.m, G.n);
 }
 
 Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int rows, int cols,
                          const std::vector<bool>* transposed) {
   if (parts.empty()) return Blk();
   std::string key;
+  key.reserve(parts.size() * 24 + 8);
   for (size_t i = 0; i < parts.size(); i++) {
     const bool t = transposed ? (*transposed)[i] : false;
     const Shape s = op_shape(parts[i].second, t);
@@ -108,38 +153,19 @@ Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int r
   combo_size_ = align4(combo_size_ + int64_t(rows) * cols);
   for (size_t i = 0; i < parts.size(); i++) {
     const bool t = transposed ? (*transposed)[i] : false;
-    add_term(combo_, out, parts[i].first, parts[i].second, t, nullptr, false, false);
+    add(combo_, false, out, parts[i].first, Blk(), false, parts[i].second, t, Blk(), false, false);
   }
-  combo_cache_[key] = out;
+  combo_cache_.emplace(std::move(key), out);
   return out;
-}
-
-Blk TaskBuilder::product(const Blk& U, bool tu, const Blk& V, bool tv) {
-  const Shape su = op_shape(U, tu), sv = op_shape(V, tv);
-  if (su.c != sv.r) shape_error("product");
-  std::string key;
-  append_bytes(key, &U.ref, sizeof(Ref));
-  append_bytes(key, &U.ld, sizeof(int));
-  append_bytes(key, &V.ref, sizeof(Ref));
-  append_bytes(key, &V.ld, sizeof(int));
-  const int dims[4] = {su.r, su.c, sv.c, (tu ? 1 : 0) + (tv ? 2 : 0)};
-  append_bytes(key, dims, sizeof(dims));
-  auto it = p1_cache_.find(key);
-  if (it != p1_cache_.end()) return it->second;
-  const Blk P = Blk::make(make_ref(kSlotP1, p1_size_), su.r, sv.c);
-  p1_size_ = align4(p1_size_ + int64_t(su.r) * sv.c);
-  add_term(p1_stages_.back(), P, 1.0, U, tu, &V, tv, false);
-  p1_cache_[key] = P;
-  return P;
 }
 
 void TaskBuilder::declare_output(const Blk& out) {
   if (!out.valid || out.rows == 0 || out.cols == 0) return;
-  group_for(p2_stages_.back(), out, written_.count(out.ref) > 0);
+  group_for(stages_.back(), out, written_.count(out.ref) > 0);
 }
 
-void TaskBuilder::contract(const Blk& out, double alpha, const Blk& A, bool ta, const Blk& B,
-                           bool tb, const Blk& C, bool tc) {
+void TaskBuilder::contract(const Blk& out, double alpha, const Blk& A, bool ta, const Blk& B, bool tb, const Blk& C,
+                           bool tc) {
   if (!out.valid || !B.valid) shape_error("contract (missing block)");
   const Shape sb = op_shape(B, tb);
   int m, n;
@@ -161,76 +187,146 @@ void TaskBuilder::contract(const Blk& out, double alpha, const Blk& A, bool ta, 
   note_operand(A);
   note_operand(B);
   note_operand(C);
+  n_contract_++;
   const bool acc = written_.count(out.ref) > 0;
-  StageBuf& sb2 = p2_stages_.back();
+  StageBuf& st = stages_.back();
   // Zero-sized or zero-weight contractions add nothing; the output still exists.
   if (alpha == 0.0 || m == 0 || n == 0 || sb.r == 0 || sb.c == 0) {
-    if (m > 0 && n > 0) group_for(sb2, out, acc);
+    if (m > 0 && n > 0) group_for(st, out, acc);
     return;
   }
-  if (A.valid && C.valid) {
-    const Shape sa = op_shape(A, ta);
-    const int k1 = sa.c, k2 = sb.c;
-    const int64_t cost_ab = int64_t(m) * k1 * k2 + int64_t(m) * k2 * n;
-    const int64_t cost_bc = int64_t(k1) * k2 * n + int64_t(m) * k1 * n;
-    if (cost_ab <= cost_bc) {
-      const Blk P = product(A, ta, B, tb);
-      add_term(sb2, out, alpha, P, false, &C, tc, acc);
-    } else {
-      const Blk P = product(B, tb, C, tc);
-      add_term(sb2, out, alpha, A, ta, &P, false, acc);
-    }
-  } else if (A.valid) {
-    add_term(sb2, out, alpha, A, ta, &B, tb, acc);
-  } else if (C.valid) {
-    add_term(sb2, out, alpha, B, tb, &C, tc, acc);
-  } else {
-    add_term(sb2, out, alpha, B, tb, nullptr, false, acc);
-  }
-  p2_terms_.emplace_back();
+  add(st, true, out, alpha, A, ta, B, tb, C, tc, acc);
 }
 
 void TaskBuilder::next_stage(const std::string& name) {
-  for (auto& g : p2_stages_.back().groups) written_[g.out] = true;
-  p1_stages_.emplace_back();
-  p2_stages_.emplace_back();
-  p2_stages_.back().name = name;
-  p1_cache_.clear();
+  for (auto& g : stages_.back().groups) written_[g.out] = true;
+  open_.clear();
+  stages_.emplace_back();
+  stages_.back().name = name;
 }
 
-Stage TaskBuilder::lower(StageBuf& sb, const std::string& name) {
+Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<BatchEntry>& table,
+                         std::unordered_map<std::string, int32_t>& lists) {
   Stage st;
   st.name = name;
-  const size_t ng = sb.groups.size();
-  std::vector<int32_t> count(ng + 1, 0);
-  for (auto& pt : sb.terms) count[pt.group + 1]++;
-  for (size_t g = 0; g < ng; g++) count[g + 1] += count[g];
-  st.terms.resize(sb.terms.size());
-  std::vector<int32_t> pos(count.begin(), count.end() - 1);
-  for (auto& pt : sb.terms) st.terms[pos[pt.group]++] = pt.t;  // stable: keeps emission order
   st.groups = sb.groups;
-  for (size_t g = 0; g < ng; g++) {
-    st.groups[g].t0 = count[g];
-    st.groups[g].t1 = count[g + 1];
-    st.flops += st.groups[g].work;
+  std::string key;
+  for (size_t g = 0; g < sb.groups.size(); g++) {
+    Group& G = st.groups[g];
+    G.t0 = static_cast<int32_t>(st.terms.size());
+    int32_t items = 0;
+    for (PendingTerm& pt : sb.terms[g]) {
+      Term t = pt.t;
+      t.item0 = items;
+      if ((t.flags & kHasA) && (t.flags & kHasC)) {
+        const int64_t ab = int64_t(G.m) * t.k1 * t.k2 + int64_t(G.m) * t.k2 * G.n;
+        const int64_t bc = int64_t(t.k1) * t.k2 * G.n + int64_t(G.m) * t.k1 * G.n;
+        if (ab < bc) t.flags |= kLeftFirst;
+      }
+      if (!pt.entries.empty()) {
+        key.clear();
+        const BatchEntry first{0, 0, 1.0};
+        append_bytes(key, &first, sizeof(BatchEntry));
+        append_bytes(key, pt.entries.data(), sizeof(BatchEntry) * pt.entries.size());
+        auto it = lists.find(key);
+        if (it == lists.end()) {
+          const int32_t off = static_cast<int32_t>(table.size());
+          table.push_back(first);
+          table.insert(table.end(), pt.entries.begin(), pt.entries.end());
+          it = lists.emplace(key, off).first;
+        }
+        t.list = it->second;
+        t.count = static_cast<int32_t>(pt.entries.size()) + 1;
+      }
+      items += t.count;
+      st.items += t.count;
+      st.flops += term_flops(t, G.m, G.n) * t.count;
+      st.terms.push_back(t);
+    }
+    G.t1 = static_cast<int32_t>(st.terms.size());
+    std::vector<PendingTerm>().swap(sb.terms[g]);
   }
   return st;
 }
 
-Program TaskBuilder::finalize() {
+Program TaskBuilder::finalize(bool keep_empty) {
   Program p;
-  if (!combo_.groups.empty()) {
-    p.stages.push_back(lower(combo_, "combine"));
+  std::unordered_map<std::string, int32_t> lists;
+  if (!combo_.groups.empty() || keep_empty) {
+    p.stages.push_back(lower(combo_, "combine", p.entries, lists));
     p.first_repeat_stage = 1;
   }
-  for (size_t s = 0; s < p2_stages_.size(); s++) {
-    if (!p1_stages_[s].groups.empty())
-      p.stages.push_back(lower(p1_stages_[s], p2_stages_[s].name + ".products"));
-    if (!p2_stages_[s].groups.empty()) p.stages.push_back(lower(p2_stages_[s], p2_stages_[s].name));
-  }
-  p.p1_size = p1_size_;
+  for (auto& s : stages_)
+    if (!s.groups.empty() || keep_empty) p.stages.push_back(lower(s, s.name, p.entries, lists));
   p.combo_size = combo_size_;
+  if (p.entries.size() > size_t(INT32_MAX)) throw std::length_error("task compiler: batch table too large");
   return p;
+}
+
+Program merge_programs(std::vector<Program>& parts) {
+  Program out;
+  if (parts.empty()) return out;
+  const size_t ns = parts[0].stages.size();
+  for (auto& p : parts)
+    if (p.stages.size() != ns) throw std::logic_error("merge_programs: shards with different stage lists");
+  std::vector<int64_t> combo_base(parts.size()), entry_base(parts.size());
+  int64_t cb = 0, eb = 0;
+  for (size_t i = 0; i < parts.size(); i++) {
+    combo_base[i] = cb;
+    entry_base[i] = eb;
+    cb = align4(cb + parts[i].combo_size);
+    eb += static_cast<int64_t>(parts[i].entries.size());
+  }
+  if (eb > INT32_MAX) throw std::length_error("merge_programs: batch table too large");
+  out.combo_size = cb;
+  out.entries.reserve(eb);
+  for (auto& p : parts) {
+    out.entries.insert(out.entries.end(), p.entries.begin(), p.entries.end());
+    std::vector<BatchEntry>().swap(p.entries);
+  }
+  auto reloc = [&](Ref r, size_t i) -> Ref {
+    if (r != 0 && ref_slot(r) == kSlotCombo) return make_ref(kSlotCombo, ref_off(r) + combo_base[i]);
+    return r;
+  };
+  for (size_t s = 0; s < ns; s++) {
+    Stage st;
+    st.name = parts[0].stages[s].name;
+    for (size_t i = 0; i < parts.size(); i++) {
+      Stage& ps = parts[i].stages[s];
+      const int32_t toff = static_cast<int32_t>(st.terms.size());
+      for (Group g : ps.groups) {
+        g.out = reloc(g.out, i);
+        g.t0 += toff;
+        g.t1 += toff;
+        st.groups.push_back(g);
+      }
+      for (Term t : ps.terms) {
+        if (t.flags & kHasA) t.a = reloc(t.a, i);
+        t.b = reloc(t.b, i);
+        if (t.flags & kHasC) t.c = reloc(t.c, i);
+        if (t.list >= 0) t.list += static_cast<int32_t>(entry_base[i]);
+        st.terms.push_back(t);
+      }
+      st.flops += ps.flops;
+      st.items += ps.items;
+      std::vector<Group>().swap(ps.groups);
+      std::vector<Term>().swap(ps.terms);
+    }
+    const bool once = (s == 0 && parts[0].first_repeat_stage == 1);
+    if (st.groups.empty()) continue;
+    if (once) out.first_repeat_stage = 1;
+    out.stages.push_back(std::move(st));
+  }
+  return out;
+}
+
+int compile_threads() {
+  if (const char* e = std::getenv("C2G_COMPILE_THREADS")) {
+    const int n = std::atoi(e);
+    if (n > 0) return std::min(n, 256);
+  }
+  const unsigned h = std::thread::hardware_concurrency();
+  return static_cast<int>(std::max(1u, std::min(h, 64u)));
 }
 
 }  // namespace c2g

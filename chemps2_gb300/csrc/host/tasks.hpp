@@ -1,23 +1,28 @@
 // Contraction-task representation of the DMRG hot path.
 //
 // The reference performs every hot-path operation (Heff diagrams, operator updates,
-// Join, the complementary-operator sums) as BLAS calls on symmetry blocks:
+// Join, Split, the complementary-operator sums) as BLAS calls on symmetry blocks:
 //     out_block += alpha * op(A) * op(B) * op(C)        (A and/or C optional)
 // where op() is an optional transpose and the operand blocks live in MPS tensors,
 // operator tensors, the two-site vector or temporary "combined" blocks built with
 // daxpy (e.g. CheMPS2/HeffDiagrams4.cpp:2334-2420, CheMPS2/TensorQ.cpp:113-248).
 // The host task compiler walks the same loops and records these contractions here
 // instead of executing them; the GPU runtime (and the CPU executor of the oracle)
-// then run them as grouped launches.
+// execute them as grouped launches.
 //
-// A Program is a list of stages, each one launch:
-//   * a combination stage: combined blocks = sum_i alpha_i * op(block_i);
-//   * product stages: phase-1 products P = op(A) op(B) (or op(B) op(C)) for every
-//     three-operand contraction, written to scratch and de-duplicated;
-//   * accumulation stages: out_block (+)= sum_t alpha_t * op(U_t) * op(V_t).
-// Within an accumulation stage every output block is owned by exactly one group, and
-// the terms of a group are summed in emission order, so the result is deterministic
-// and identical for every executor that honours the term order.
+// A Term is a fused, batched sandwich:
+//     out += alpha * sum_p ratio_p * op(A + da_p) * op(B) * op(C + dc_p)
+// The reference's innermost loops over an operator index (orbital pairs in diagram 2a,
+// orbitals in 3C, 4B, 5A, ...) multiply the same block B of the input vector by blocks of
+// different operator tensors at the same position inside their tensors; those
+// contractions become one term whose batch list holds the tensor offsets (da_p, dc_p).
+// The lists do not depend on the output block, so the compiler stores each distinct
+// list once per program.
+//
+// A Program is a list of stages, one launch each: an optional combination stage
+// (combined blocks = sum_i alpha_i op(block_i), run once per program preparation) and
+// accumulation stages. Within a stage every output block is owned by one group; the terms
+// of a group are summed in a fixed order, so results are deterministic.
 #pragma once
 
 #include <cstdint>
@@ -41,7 +46,6 @@ inline int64_t ref_off(Ref r) { return static_cast<int64_t>(r & kRefMask); }
 enum Slot : int {
   kSlotX = 0,
   kSlotY = 1,
-  kSlotP1 = 2,      // phase-1 products of the program being run
   kSlotCombo = 3,   // combined blocks of the program being run
   kSlotWork = 4,    // truncation workspace (assembled sector matrices, Gram, eigvecs)
   kSlotOnes = 5,    // a vector of 1.0, at least as long as the largest sector dimension
@@ -67,50 +71,67 @@ struct Blk {
 };
 
 enum TermFlags : int32_t {
-  kTransU = 1,   // U stored k x m (used transposed)
-  kTransV = 2,   // V stored n x k (used transposed)
-  kScalar = 4,   // out += alpha * op(U), no V
+  kHasA = 1,
+  kHasC = 2,
+  kTransA = 4,   // A stored k1 x m
+  kTransB = 8,   // B stored k2 x k1
+  kTransC = 16,  // C stored n x k2
+  kLeftFirst = 32,  // with A and C: evaluate (A B) C, otherwise A (B C) (the cheaper order)
 };
 
-struct Term {       // 48 bytes
-  Ref u, v;
+// out (m x n, from the group) += alpha * sum_p ratio_p op(A_p) (m x k1) op(B) (k1 x k2)
+// op(C_p) (k2 x n). Without A, op(A) = I and k1 = m; without C, op(C) = I and k2 = n.
+struct Term {        // 64 bytes
+  Ref a, b, c;       // entry 0 (a / c are 0 when absent)
   double alpha;
-  int32_t k;        // inner dimension (unused for scalar terms)
-  int32_t ldu, ldv;
+  int32_t k1, k2;
+  int32_t lda, ldb, ldc;
   int32_t flags;
-  int32_t pad0, pad1;
+  int32_t list;      // first entry in Program::entries, -1 for a single contraction
+  int32_t count;     // entries (1 for a single contraction)
+  int32_t item0;     // entries of the previous terms of the same group
+};
+
+// Entry p of a batched term: A_p = a + da, C_p = c + dc, coefficient alpha * ratio.
+struct BatchEntry {  // 24 bytes
+  int64_t da, dc;
+  double ratio;
 };
 
 enum GroupFlags : int32_t {
   kAccumulate = 1,  // out += sum; otherwise out = sum
 };
 
-struct Group {      // 40 bytes
+struct Group {       // 40 bytes
   Ref out;
   int32_t m, n, ldo;
   int32_t flags;
-  int32_t t0, t1;   // term range [t0, t1)
-  int64_t work;     // flop estimate, used for scheduling
+  int32_t t0, t1;    // term range [t0, t1)
+  int64_t work;      // flop count, used for scheduling
 };
 
 struct Stage {
   std::vector<Group> groups;
   std::vector<Term> terms;
   std::string name;
-  int64_t flops = 0;  // 2*m*n*k summed over the stage's terms (m*n for scalar terms)
+  int64_t flops = 0;  // sum over terms and entries of the sandwich flops
+  int64_t items = 0;  // sum of term entry counts
 };
 
 struct Program {
   std::vector<Stage> stages;
-  int64_t p1_size = 0;     // doubles of phase-1 scratch (slot kSlotP1)
-  int64_t combo_size = 0;  // doubles of combined blocks (slot kSlotCombo)
-  int first_repeat_stage = 0;  // stages [0, first_repeat_stage) run once (combinations)
+  std::vector<BatchEntry> entries;  // shared batch lists of all stages
+  int64_t combo_size = 0;           // doubles of combined blocks (slot kSlotCombo)
+  int first_repeat_stage = 0;       // stages [0, first_repeat_stage) run once (combinations)
   int64_t flops() const {
     int64_t f = 0;
     for (auto& s : stages) f += s.flops;
     return f;
   }
 };
+
+// Flops of one entry of a term (2 per multiply-add; m * n for a plain scaled copy).
+int64_t term_flops(const Term& t, int m, int n);
 
 // Records contractions and lowers them into a Program.
 class TaskBuilder {
@@ -136,44 +157,68 @@ class TaskBuilder {
   // term reaches it (so an executor writes zeros instead of leaving stale data).
   void declare_output(const Blk& out);
 
-  // Closes the current product/accumulation stage pair; later contractions accumulate
-  // onto what earlier stages wrote.
+  // Closes the current accumulation stage; later contractions accumulate onto what
+  // earlier stages wrote.
   void next_stage(const std::string& name);
 
-  Program finalize();
+  // keep_empty keeps empty stages (and an empty combination stage), so that programs of
+  // disjoint shards have identical stage lists and can be merged position by position.
+  Program finalize(bool keep_empty = false);
 
-  int64_t num_terms() const { return static_cast<int64_t>(p2_terms_.size()); }
+  int64_t num_contractions() const { return n_contract_; }
 
   // Bytes of the distinct MPS / operator blocks the recorded contractions read (each
   // block counted once, FP64), the operand traffic of one execution of the program.
   int64_t operand_bytes() const;
+  const std::unordered_map<Ref, int64_t>& operands() const { return operands_; }
 
  private:
-  struct PendingTerm { int group; Term t; };
+  struct PendingTerm {
+    Term t;
+    std::vector<BatchEntry> entries;  // beyond entry 0
+  };
   struct StageBuf {
     std::vector<Group> groups;
-    std::vector<PendingTerm> terms;
+    std::vector<std::vector<PendingTerm>> terms;  // per group
     std::unordered_map<Ref, int> group_of;
     std::string name;
   };
-  // combination stage
+  struct BatchKey {
+    int group;
+    Ref b;
+    int32_t flags, k1, k2, lda, ldc, aslot, cslot;
+    bool operator==(const BatchKey& o) const {
+      return group == o.group && b == o.b && flags == o.flags && k1 == o.k1 && k2 == o.k2 && lda == o.lda &&
+             ldc == o.ldc && aslot == o.aslot && cslot == o.cslot;
+    }
+  };
+  struct BatchKeyHash {
+    size_t operator()(const BatchKey& k) const;
+  };
+
   StageBuf combo_;
   int64_t combo_size_ = 0;
   std::unordered_map<std::string, Blk> combo_cache_;
-  // product / accumulation stages
-  std::vector<StageBuf> p1_stages_, p2_stages_;
-  std::unordered_map<std::string, Blk> p1_cache_;
-  int64_t p1_size_ = 0;
-  std::vector<Term> p2_terms_;  // only for counting
-  std::unordered_map<Ref, bool> written_;  // outputs written by closed stages
-  std::unordered_map<Ref, int64_t> operands_;  // footprint of MPS / operator operands
-  void note_operand(const Blk& b);
+  std::vector<StageBuf> stages_;
+  std::unordered_map<BatchKey, int, BatchKeyHash> open_;  // term index within its group
+  std::unordered_map<Ref, bool> written_;                  // outputs written by closed stages
+  std::unordered_map<Ref, int64_t> operands_;              // footprint of MPS / operator operands
+  int64_t n_contract_ = 0;
 
+  void note_operand(const Blk& b);
   int group_for(StageBuf& sb, const Blk& out, bool accumulate);
-  Blk product(const Blk& U, bool tu, const Blk& V, bool tv);
-  void add_term(StageBuf& sb, const Blk& out, double alpha, const Blk& U, bool tu, const Blk* V,
-                bool tv, bool accumulate);
-  static Stage lower(StageBuf& sb, const std::string& name);
+  void add(StageBuf& sb, bool batchable, const Blk& out, double alpha, const Blk& A, bool ta, const Blk& B, bool tb,
+           const Blk& C, bool tc, bool accumulate);
+  static Stage lower(StageBuf& sb, const std::string& name, std::vector<BatchEntry>& table,
+                     std::unordered_map<std::string, int32_t>& lists);
 };
+
+// Concatenates programs compiled (with keep_empty) from disjoint output shards into one
+// program with the same stage structure, relocating combination-scratch references and
+// batch lists. Empty stages are dropped.
+Program merge_programs(std::vector<Program>& parts);
+
+// Number of compile threads (C2G_COMPILE_THREADS overrides the hardware count).
+int compile_threads();
 
 }  // namespace c2g

@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 HOST = HERE.parent / "chemps2_gb300" / "csrc" / "host"
 BUILD = HERE / "_build"
 LIB = BUILD / "liboracle.so"
-FLAGS = ["-std=c++17", "-O3", "-fPIC", "-Wall", "-fno-fast-math"]
+FLAGS = ["-std=c++17", "-O3", "-fPIC", "-Wall", "-fno-fast-math", "-pthread"]
 
 
 def _sources() -> list[Path]:
@@ -55,7 +55,7 @@ def build(verbose: bool = False) -> Path:
         list(ex.map(cc, todo))
     if todo or not LIB.exists():
         tmp = BUILD / "liboracle.so.tmp"
-        cmd = ["g++", "-shared", "-o", str(tmp), *map(str, objs)]
+        cmd = ["g++", "-shared", "-pthread", "-o", str(tmp), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle link failed: {r.stderr}")

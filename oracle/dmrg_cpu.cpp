@@ -27,6 +27,7 @@
 #include "chemps2/Hamiltonian.h"
 #include "chemps2/Problem.h"
 #include "chemps2/SyBookkeeper.h"
+#include "compile.hpp"
 #include "exec_cpu.hpp"
 #include "heff.hpp"
 #include "layout.hpp"
@@ -346,9 +347,7 @@ struct OracleDMRG {
       ctx.prev = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
     ctx.next = ops[index].get();
     ctx.mps = mr ? mpsT(index) : mpsT(index + 1);
-    TaskBuilder tb;
-    compile_update(tb, ctx);
-    exec(tb.finalize(), nullptr, 0, nullptr, 0);
+    exec(compile_update_program(ctx).program, nullptr, 0, nullptr, 0);
   }
 
   void presolve() {
@@ -392,14 +391,8 @@ struct OracleDMRG {
     ones.assign(maxdim, 1.0);
     ex.bind(kSlotOnes, ones.data(), maxdim);
     std::vector<double> diag(n, 0.0);
-    {
-      TaskBuilder tb;
-      compile_heff_diag(tb, ctx);
-      exec(tb.finalize(), nullptr, 0, diag.data(), n);
-    }
-    TaskBuilder tbh;
-    compile_heff(tbh, ctx);
-    const Program ph = tbh.finalize();
+    exec(compile_heff_diag_program(ctx).program, nullptr, 0, diag.data(), n);
+    const Program ph = compile_heff_program(ctx).program;
     ex.prepare_scratch(ph);
     if (check) {
       std::vector<double> dx(n, 0.0), dy(n, 0.0);
@@ -683,14 +676,8 @@ int oracle_dmrg_heff_apply(void* h, int index, int join_into_x, double* x, int64
     for (int k = 0; k < S.nkappa; k++) maxdim = std::max(maxdim, std::max(S.rows[k], S.cols[k]));
     d->ones.assign(maxdim, 1.0);
     d->ex.bind(c2g::kSlotOnes, d->ones.data(), maxdim);
-    c2g::TaskBuilder tb;
-    c2g::compile_heff(tb, ctx);
-    d->exec(tb.finalize(), x, join_into_x ? n : nx, y, n);
-    if (diag) {
-      c2g::TaskBuilder tbd;
-      c2g::compile_heff_diag(tbd, ctx);
-      d->exec(tbd.finalize(), nullptr, 0, diag, n);
-    }
+    d->exec(c2g::compile_heff_program(ctx).program, x, join_into_x ? n : nx, y, n);
+    if (diag) d->exec(c2g::compile_heff_diag_program(ctx).program, nullptr, 0, diag, n);
   });
 }
 

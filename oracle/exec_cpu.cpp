@@ -7,6 +7,7 @@
 
 namespace oracle {
 
+using c2g::BatchEntry;
 using c2g::Group;
 using c2g::Ref;
 using c2g::Stage;
@@ -33,29 +34,24 @@ void add_segments(std::vector<Seg>& out, int64_t off, int rows, int cols, int ld
   }
 }
 
+inline BatchEntry entry_of(const Term& t, const std::vector<BatchEntry>& table, int p) {
+  if (t.list < 0) return BatchEntry{0, 0, 1.0};
+  return table[static_cast<size_t>(t.list) + p];
+}
+
 }  // namespace
 
 const double* CpuExecutor::ptr(Ref r) const {
   const int s = c2g::ref_slot(r);
   const int64_t off = c2g::ref_off(r);
-  const double* base;
-  if (s == c2g::kSlotP1)
-    base = p1_.data();
-  else if (s == c2g::kSlotCombo)
-    base = combo_.data();
-  else
-    base = slots_.at(s).data;
+  const double* base = (s == c2g::kSlotCombo) ? combo_.data() : slots_.at(s).data;
   return base + off;
 }
 
-void CpuExecutor::prepare_scratch(const c2g::Program& p) {
-  p1_.assign(std::max<int64_t>(p.p1_size, 1), 0.0);
-  combo_.assign(std::max<int64_t>(p.combo_size, 1), 0.0);
-}
+void CpuExecutor::prepare_scratch(const c2g::Program& p) { combo_.assign(std::max<int64_t>(p.combo_size, 1), 0.0); }
 
-void CpuExecutor::check_stage(const Stage& st) {
+void CpuExecutor::check_stage(const Stage& st, const std::vector<BatchEntry>& table) {
   auto slot_size = [&](int s) -> int64_t {
-    if (s == c2g::kSlotP1) return static_cast<int64_t>(p1_.size());
     if (s == c2g::kSlotCombo) return static_cast<int64_t>(combo_.size());
     if (s < 0 || s >= static_cast<int>(slots_.size())) fail(st.name, "slot index out of range");
     if (!slots_[s].data) fail(st.name, "slot " + std::to_string(s) + " is not bound");
@@ -80,21 +76,37 @@ void CpuExecutor::check_stage(const Stage& st) {
     if (G.t0 < 0 || G.t1 > static_cast<int>(st.terms.size()) || G.t0 > G.t1) fail(st.name, "term range");
     check_access(G.out, G.m, G.n, G.ldo, "output");
     add_segments(outs.at(c2g::ref_slot(G.out)), c2g::ref_off(G.out), G.m, G.n, G.ldo);
+    int32_t items = 0;
     for (int t = G.t0; t < G.t1; t++) {
       const Term& T = st.terms[t];
-      const bool tu = T.flags & c2g::kTransU, tv = T.flags & c2g::kTransV;
-      if (T.flags & c2g::kScalar) {
-        const int r = tu ? G.n : G.m, c = tu ? G.m : G.n;
-        check_access(T.u, r, c, T.ldu, "scalar operand");
-        add_segments(ins.at(c2g::ref_slot(T.u)), c2g::ref_off(T.u), r, c, T.ldu);
-      } else {
-        if (T.k < 0) fail(st.name, "negative inner dimension");
-        const int ur = tu ? T.k : G.m, uc = tu ? G.m : T.k;
-        const int vr = tv ? G.n : T.k, vc = tv ? T.k : G.n;
-        check_access(T.u, ur, uc, T.ldu, "left operand");
-        check_access(T.v, vr, vc, T.ldv, "right operand");
-        add_segments(ins.at(c2g::ref_slot(T.u)), c2g::ref_off(T.u), ur, uc, T.ldu);
-        add_segments(ins.at(c2g::ref_slot(T.v)), c2g::ref_off(T.v), vr, vc, T.ldv);
+      if (T.item0 != items) fail(st.name, "item offsets");
+      items += T.count;
+      if (T.count < 1) fail(st.name, "empty batch");
+      if (T.list >= 0 && static_cast<size_t>(T.list) + T.count > table.size()) fail(st.name, "batch list range");
+      if (T.list < 0 && T.count != 1) fail(st.name, "single term with a count");
+      const bool ha = T.flags & c2g::kHasA, hc = T.flags & c2g::kHasC;
+      const bool ta = T.flags & c2g::kTransA, tb = T.flags & c2g::kTransB, tc = T.flags & c2g::kTransC;
+      if (!ha && T.k1 != G.m) fail(st.name, "k1 differs from m without A");
+      if (!hc && T.k2 != G.n) fail(st.name, "k2 differs from n without C");
+      const int br = tb ? T.k2 : T.k1, bc = tb ? T.k1 : T.k2;
+      check_access(T.b, br, bc, T.ldb, "B operand");
+      add_segments(ins.at(c2g::ref_slot(T.b)), c2g::ref_off(T.b), br, bc, T.ldb);
+      for (int p = 0; p < T.count; p++) {
+        const BatchEntry e = entry_of(T, table, p);
+        if (ha) {
+          const Ref a = T.a + static_cast<uint64_t>(e.da);
+          if (c2g::ref_slot(a) != c2g::ref_slot(T.a)) fail(st.name, "batched A leaves its slot");
+          const int ar = ta ? T.k1 : G.m, ac = ta ? G.m : T.k1;
+          check_access(a, ar, ac, T.lda, "A operand");
+          add_segments(ins.at(c2g::ref_slot(a)), c2g::ref_off(a), ar, ac, T.lda);
+        }
+        if (hc) {
+          const Ref c = T.c + static_cast<uint64_t>(e.dc);
+          if (c2g::ref_slot(c) != c2g::ref_slot(T.c)) fail(st.name, "batched C leaves its slot");
+          const int cr = tc ? G.n : T.k2, cc = tc ? T.k2 : G.n;
+          check_access(c, cr, cc, T.ldc, "C operand");
+          add_segments(ins.at(c2g::ref_slot(c)), c2g::ref_off(c), cr, cc, T.ldc);
+        }
       }
     }
   }
@@ -113,50 +125,74 @@ void CpuExecutor::check_stage(const Stage& st) {
 }
 
 void CpuExecutor::check(const c2g::Program& p) {
-  if (static_cast<int64_t>(p1_.size()) < std::max<int64_t>(p.p1_size, 1) ||
-      static_cast<int64_t>(combo_.size()) < std::max<int64_t>(p.combo_size, 1))
-    prepare_scratch(p);
-  for (const Stage& st : p.stages) check_stage(st);
+  if (static_cast<int64_t>(combo_.size()) < std::max<int64_t>(p.combo_size, 1)) prepare_scratch(p);
+  for (const Stage& st : p.stages) check_stage(st, p.entries);
 }
 
-void CpuExecutor::run_stage(const Stage& st) {
-  std::vector<double> acc;
+void CpuExecutor::run_stage(const Stage& st, const std::vector<BatchEntry>& table) {
+  std::vector<double> acc, tmp;
   for (const Group& G : st.groups) {
     if (G.m <= 0 || G.n <= 0) continue;
-    acc.assign(static_cast<size_t>(G.m) * G.n, 0.0);
+    const int m = G.m, n = G.n;
+    acc.assign(static_cast<size_t>(m) * n, 0.0);
     for (int t = G.t0; t < G.t1; t++) {
       const Term& T = st.terms[t];
-      const bool tu = T.flags & c2g::kTransU, tv = T.flags & c2g::kTransV;
-      const double* U = ptr(T.u);
-      if (T.flags & c2g::kScalar) {
-        for (int c = 0; c < G.n; c++)
-          for (int r = 0; r < G.m; r++)
-            acc[r + size_t(G.m) * c] += T.alpha * (tu ? U[c + int64_t(T.ldu) * r] : U[r + int64_t(T.ldu) * c]);
-        flops_done += int64_t(G.m) * G.n;
-        continue;
-      }
-      const double* V = ptr(T.v);
-      for (int c = 0; c < G.n; c++)
-        for (int kk = 0; kk < T.k; kk++) {
-          const double v = tv ? V[c + int64_t(T.ldv) * kk] : V[kk + int64_t(T.ldv) * c];
-          if (v == 0.0) continue;
-          const double av = T.alpha * v;
-          double* a = &acc[size_t(G.m) * c];
-          if (!tu) {
-            const double* u = U + int64_t(T.ldu) * kk;
-            for (int r = 0; r < G.m; r++) a[r] += u[r] * av;
-          } else {
-            for (int r = 0; r < G.m; r++) a[r] += U[kk + int64_t(T.ldu) * r] * av;
-          }
+      const bool ha = T.flags & c2g::kHasA, hc = T.flags & c2g::kHasC;
+      const bool ta = T.flags & c2g::kTransA, tb = T.flags & c2g::kTransB, tc = T.flags & c2g::kTransC;
+      const double* B = ptr(T.b);
+      auto opB = [&](int k, int l) { return tb ? B[l + int64_t(T.ldb) * k] : B[k + int64_t(T.ldb) * l]; };
+      for (int p = 0; p < T.count; p++) {
+        const BatchEntry e = entry_of(T, table, p);
+        const double al = T.alpha * e.ratio;
+        const double* A = ha ? ptr(T.a + static_cast<uint64_t>(e.da)) : nullptr;
+        const double* C = hc ? ptr(T.c + static_cast<uint64_t>(e.dc)) : nullptr;
+        auto opA = [&](int i, int k) { return ta ? A[k + int64_t(T.lda) * i] : A[i + int64_t(T.lda) * k]; };
+        auto opC = [&](int l, int j) { return tc ? C[j + int64_t(T.ldc) * l] : C[l + int64_t(T.ldc) * j]; };
+        if (ha && hc) {
+          // tmp = op(B) op(C_p): k1 x n
+          tmp.assign(static_cast<size_t>(T.k1) * n, 0.0);
+          for (int j = 0; j < n; j++)
+            for (int l = 0; l < T.k2; l++) {
+              const double c = opC(l, j);
+              if (c == 0.0) continue;
+              for (int k = 0; k < T.k1; k++) tmp[k + size_t(T.k1) * j] += opB(k, l) * c;
+            }
+          for (int j = 0; j < n; j++)
+            for (int k = 0; k < T.k1; k++) {
+              const double v = al * tmp[k + size_t(T.k1) * j];
+              if (v == 0.0) continue;
+              for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opA(i, k) * v;
+            }
+          flops_done += term_flops(T, m, n);
+        } else if (ha) {
+          for (int j = 0; j < n; j++)
+            for (int k = 0; k < T.k1; k++) {
+              const double v = al * opB(k, j);
+              if (v == 0.0) continue;
+              for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opA(i, k) * v;
+            }
+          flops_done += 2 * int64_t(m) * n * T.k1;
+        } else if (hc) {
+          for (int j = 0; j < n; j++)
+            for (int l = 0; l < T.k2; l++) {
+              const double v = al * opC(l, j);
+              if (v == 0.0) continue;
+              for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opB(i, l) * v;
+            }
+          flops_done += 2 * int64_t(m) * n * T.k2;
+        } else {
+          for (int j = 0; j < n; j++)
+            for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += al * opB(i, j);
+          flops_done += int64_t(m) * n;
         }
-      flops_done += 2 * int64_t(G.m) * G.n * T.k;
+      }
     }
     double* O = const_cast<double*>(ptr(G.out));
     const bool accum = G.flags & c2g::kAccumulate;
-    for (int c = 0; c < G.n; c++)
-      for (int r = 0; r < G.m; r++) {
+    for (int c = 0; c < n; c++)
+      for (int r = 0; r < m; r++) {
         double& o = O[r + int64_t(G.ldo) * c];
-        o = accum ? o + acc[r + size_t(G.m) * c] : acc[r + size_t(G.m) * c];
+        o = accum ? o + acc[r + size_t(m) * c] : acc[r + size_t(m) * c];
       }
   }
 }
@@ -164,7 +200,7 @@ void CpuExecutor::run_stage(const Stage& st) {
 void CpuExecutor::run(const c2g::Program& p, bool once_stages, bool repeat_stages) {
   for (size_t s = 0; s < p.stages.size(); s++) {
     const bool once = static_cast<int>(s) < p.first_repeat_stage;
-    if ((once && once_stages) || (!once && repeat_stages)) run_stage(p.stages[s]);
+    if ((once && once_stages) || (!once && repeat_stages)) run_stage(p.stages[s], p.entries);
   }
 }
 

@@ -28,8 +28,8 @@ class CpuExecutor {
   void bind(int slot, double* data, int64_t size) { slots_.at(slot) = Buffer{data, size}; }
   Buffer& slot(int s) { return slots_.at(s); }
 
-  // Checks (always) and executes the stages [from, to) of p. P1 and Combo scratch are
-  // owned by the executor per call of prepare/run.
+  // check() verifies p; run() executes its once stages and / or repeat stages. The
+  // combination scratch is owned by the executor (prepare_scratch).
   void check(const c2g::Program& p);
   void run(const c2g::Program& p, bool once_stages, bool repeat_stages);
   void prepare_scratch(const c2g::Program& p);
@@ -38,9 +38,9 @@ class CpuExecutor {
 
  private:
   std::vector<Buffer> slots_;
-  std::vector<double> p1_, combo_;
-  void check_stage(const c2g::Stage& st);
-  void run_stage(const c2g::Stage& st);
+  std::vector<double> combo_;
+  void check_stage(const c2g::Stage& st, const std::vector<c2g::BatchEntry>& table);
+  void run_stage(const c2g::Stage& st, const std::vector<c2g::BatchEntry>& table);
   const double* ptr(c2g::Ref r) const;
 };
 
