@@ -353,11 +353,11 @@ class DMRG:
                                           _dp(d) if d is not None else None, C.c_int64(n)))
         return xx, y, d
 
-    def bench_heff(self, index, warmup, steps):
+    def bench_heff(self, index, warmup, steps, flush_bytes=0):
         ms, fl, by = C.c_double(), C.c_double(), C.c_double()
         nl = C.c_longlong()
-        _check(load().c2g_dmrg_bench_heff(self._d, int(index), int(warmup), int(steps), C.byref(ms), C.byref(fl),
-                                          C.byref(by), C.byref(nl)))
+        _check(load().c2g_dmrg_bench_heff(self._d, int(index), int(warmup), int(steps), C.c_longlong(flush_bytes),
+                                          C.byref(ms), C.byref(fl), C.byref(by), C.byref(nl)))
         return {"ms_per_matvec": ms.value, "flops": fl.value, "bytes": by.value, "launches": nl.value}
 
 

@@ -412,12 +412,12 @@ int c2g_dmrg_reset_stats(c2g_dmrg* d) {
     d->d->reset_stats();
   });
 }
-int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, double* ms, double* flops, double* bytes,
-                        long long* launches) {
+int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, long long flush_bytes, double* ms,
+                        double* flops, double* bytes, long long* launches) {
   return guarded([&] {
     NEED(d);
     NEED(ms);
-    *ms = d->d->bench_heff(index, warmup, steps, flops, bytes, launches);
+    *ms = d->d->bench_heff(index, warmup, steps, flops, bytes, launches, flush_bytes);
   });
 }
 

@@ -54,8 +54,20 @@ void check_solver(cusolverStatus_t s, const char* what) {
 
 }  // namespace
 
+struct DMRG::HeffCache {
+  int index = -1;
+  unsigned long long version = 0;
+  std::unique_ptr<TwoSiteLayout> S;
+  std::unique_ptr<DevProgram> program, diag;
+  int64_t operand_bytes = 0;
+  double* xbuf = nullptr;
+  double* ybuf = nullptr;
+  int64_t xbuf_len = 0;
+};
+
 DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool, const std::string, int* occupancies)
     : Prob(ProbIn), OptScheme(OptSchemeIn) {
+  heff_cache_ = std::make_unique<HeffCache>();
   if (!Prob->checkConsistency()) throw std::invalid_argument("DMRG: inconsistent Problem");
   if (OptScheme->get_number() < 1) throw std::invalid_argument("DMRG: empty ConvergenceScheme");
   L = Prob->gL();
@@ -76,6 +88,12 @@ DMRG::~DMRG() {
     try {
       rt->sync();
     } catch (...) {
+    }
+    if (heff_cache_) {
+      heff_cache_->program.reset();
+      heff_cache_->diag.reset();
+      rt->release(heff_cache_->xbuf);
+      rt->release(heff_cache_->ybuf);
     }
     for (double* p : mps_dev) rt->release(p);
     for (double* p : ops_dev) rt->release(p);
@@ -224,6 +242,7 @@ int DMRG::get_num_mps_var() const {
 }
 
 void DMRG::delete_all_ops() {
+  version_++;
   for (int b = 0; b < L - 1; b++) {
     if (ops_dev[b]) rt->release(ops_dev[b]);
     ops_dev[b] = nullptr;
@@ -250,6 +269,7 @@ void DMRG::update_moving_right(const int index) {
   ops_dev[index] = rt->alloc(ops[index]->size);
   rt->set_slot(c2g::slot_ops(L, index), ops_dev[index]);
   isAllocated[index] = 1;
+  version_++;
   c2g::UpdateContext ctx;
   ctx.bk = denBK.get();
   ctx.prob = Prob;
@@ -279,6 +299,7 @@ void DMRG::update_moving_left(const int index) {
   ops_dev[index] = rt->alloc(ops[index]->size);
   rt->set_slot(c2g::slot_ops(L, index), ops_dev[index]);
   isAllocated[index] = 2;
+  version_++;
   c2g::UpdateContext ctx;
   ctx.bk = denBK.get();
   ctx.prob = Prob;
@@ -569,59 +590,95 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   rt->set_slot(c2g::kSlotWork, nullptr);
   rt->release(work);
   rt->release(svec);
+  version_++;
   MaxDiscWeightLastSweep = std::max(MaxDiscWeightLastSweep, discardedWeight);
   stats_.t_split += now() - t0;
   return Energy;
 }
 
+// The Heff program of sites (index, index + 1), compiled once per state of the MPS and
+// operators (every update, split and PreSolve advances the state version).
+DMRG::HeffCache& DMRG::heff_program(const int index, const bool with_diag) {
+  if (index < 0 || index > L - 2) throw std::out_of_range("heff: index");
+  if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("heff: left operators missing");
+  if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("heff: right operators missing");
+  HeffCache& c = *heff_cache_;
+  if (!(c.index == index && c.version == version_ && c.program)) {
+    c.program.reset();
+    c.diag.reset();
+    c.S = std::make_unique<TwoSiteLayout>();
+    c.S->build(*denBK, index);
+    c2g::HeffContext ctx;
+    ctx.bk = denBK.get();
+    ctx.prob = Prob;
+    ctx.S = c.S.get();
+    ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
+    ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
+    const double tc = now();
+    c2g::Compiled ch = c2g::compile_heff_program(ctx, true);
+    stats_.t_compile += now() - tc;
+    c.program = rt->upload(ch.program);
+    rt->prepare(*c.program);
+    c.operand_bytes = ch.operand_bytes;
+    c.index = index;
+    c.version = version_;
+  }
+  if (with_diag && !c.diag) {
+    c2g::HeffContext ctx;
+    ctx.bk = denBK.get();
+    ctx.prob = Prob;
+    ctx.S = c.S.get();
+    ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
+    ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
+    c.diag = rt->upload(c2g::compile_heff_diag_program(ctx).program);
+  }
+  return c;
+}
+
 double DMRG::bench_heff(const int index, const int warmup, const int steps, double* flops, double* bytes,
-                        long long* launches) {
-  if (index < 0 || index > L - 2) throw std::out_of_range("bench_heff: index");
+                        long long* launches, const long long flush_bytes) {
   cudaStream_t s = rt->stream();
-  TwoSiteLayout S;
-  S.build(*denBK, index);
-  const int64_t veclen = S.size();
+  HeffCache& c = heff_program(index, false);
+  const int64_t veclen = c.S->size();
   double* x = rt->alloc(veclen);
   double* y = rt->alloc(veclen);
   {
     TaskBuilder tb;
-    c2g::compile_join(tb, *denBK, S, mps_tensor(mps_lay[index].get(), index),
+    c2g::compile_join(tb, *denBK, *c.S, mps_tensor(mps_lay[index].get(), index),
                       mps_tensor(mps_lay[index + 1].get(), index + 1));
     auto dp = rt->upload(tb.finalize());
     rt->run(*dp, nullptr, x);
   }
-  c2g::HeffContext ctx;
-  ctx.bk = denBK.get();
-  ctx.prob = Prob;
-  ctx.S = &S;
-  ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
-  ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
-  if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("bench_heff: left operators missing");
-  if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("bench_heff: right operators missing");
-  c2g::Compiled ch = c2g::compile_heff_program(ctx);
-  auto dph = rt->upload(ch.program);
-  rt->prepare(*dph);
-  for (int i = 0; i < warmup; i++) rt->run(*dph, x, y);
+  double* flush = nullptr;
+  const int64_t nflush = flush_bytes > 0 ? (flush_bytes + 7) / 8 : 0;
+  if (nflush > 0) flush = rt->alloc(nflush);
+  for (int i = 0; i < warmup; i++) rt->run(*c.program, x, y);
   rt->sync();
   const long long l0 = c2g::kernel_launches();
   cudaEvent_t e0, e1;
   C2G_CUDA(cudaEventCreate(&e0));
   C2G_CUDA(cudaEventCreate(&e1));
-  C2G_CUDA(cudaEventRecord(e0, s));
-  for (int i = 0; i < steps; i++) rt->run(*dph, x, y);
-  C2G_CUDA(cudaEventRecord(e1, s));
-  C2G_CUDA(cudaEventSynchronize(e1));
-  float ms = 0.f;
-  C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  double total_ms = 0.0;
+  for (int i = 0; i < steps; i++) {
+    if (flush) C2G_CUDA(cudaMemsetAsync(flush, i & 0xff, sizeof(double) * nflush, s));  // evicts L2
+    C2G_CUDA(cudaEventRecord(e0, s));
+    rt->run(*c.program, x, y);
+    C2G_CUDA(cudaEventRecord(e1, s));
+    C2G_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    total_ms += ms;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (launches) *launches = c2g::kernel_launches() - l0;
-  if (flops) *flops = static_cast<double>(dph->flops_repeat);
-  if (bytes) *bytes = static_cast<double>(ch.operand_bytes) + 16.0 * veclen;
+  if (flops) *flops = static_cast<double>(c.program->flops_repeat);
+  if (bytes) *bytes = static_cast<double>(c.operand_bytes) + 16.0 * veclen;
+  if (flush) rt->release(flush);
   rt->release(x);
   rt->release(y);
   rt->sync();
-  return steps > 0 ? ms / steps : 0.0;
+  return steps > 0 ? total_ms / steps : 0.0;
 }
 
 long long DMRG::sobject_size(const int index) const {
@@ -633,49 +690,37 @@ long long DMRG::sobject_size(const int index) const {
 
 void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, double* y, double* diag,
                            const long long n) {
-  if (index < 0 || index > L - 2) throw std::out_of_range("heff_apply: index");
   if (!x || !y) throw std::invalid_argument("heff_apply: null buffer");
   cudaStream_t s = rt->stream();
-  TwoSiteLayout S;
-  S.build(*denBK, index);
-  const int64_t veclen = S.size();
+  HeffCache& c = heff_program(index, diag != nullptr);
+  const int64_t veclen = c.S->size();
   if (n != veclen) throw std::invalid_argument("heff_apply: vector length differs from the two-site object size");
-  double* dx = rt->alloc(veclen);
-  double* dy = rt->alloc(veclen);
+  if (c.xbuf_len < veclen) {
+    rt->release(c.xbuf);
+    rt->release(c.ybuf);
+    c.xbuf = rt->alloc(veclen);
+    c.ybuf = rt->alloc(veclen);
+    c.xbuf_len = veclen;
+  }
   if (join_into_x) {
     TaskBuilder tb;
-    c2g::compile_join(tb, *denBK, S, mps_tensor(mps_lay[index].get(), index),
+    c2g::compile_join(tb, *denBK, *c.S, mps_tensor(mps_lay[index].get(), index),
                       mps_tensor(mps_lay[index + 1].get(), index + 1));
     auto dp = rt->upload(tb.finalize());
-    rt->run(*dp, nullptr, dx);
-    C2G_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
+    rt->run(*dp, nullptr, c.xbuf);
+    C2G_CUDA(cudaMemcpyAsync(x, c.xbuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   } else {
-    C2G_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
+    C2G_CUDA(cudaMemcpyAsync(c.xbuf, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
   }
-  c2g::HeffContext ctx;
-  ctx.bk = denBK.get();
-  ctx.prob = Prob;
-  ctx.S = &S;
-  ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
-  ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
-  if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("heff_apply: left operators missing");
-  if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("heff_apply: right operators missing");
-  {
-    auto dp = rt->upload(c2g::compile_heff_program(ctx).program);
-    rt->run(*dp, dx, dy);
-    C2G_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
-  }
+  rt->run(*c.program, c.xbuf, c.ybuf);
+  C2G_CUDA(cudaMemcpyAsync(y, c.ybuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   if (diag) {
     int maxdim = 1;
-    for (int k = 0; k < S.nkappa; k++) maxdim = std::max(maxdim, std::max(S.rows[k], S.cols[k]));
+    for (int k = 0; k < c.S->nkappa; k++) maxdim = std::max(maxdim, std::max(c.S->rows[k], c.S->cols[k]));
     rt->ones(maxdim);
-    auto dp = rt->upload(c2g::compile_heff_diag_program(ctx).program);
-    rt->run(*dp, nullptr, dy);
-    C2G_CUDA(cudaMemcpyAsync(diag, dy, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
+    rt->run(*c.diag, nullptr, c.ybuf);
+    C2G_CUDA(cudaMemcpyAsync(diag, c.ybuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   }
-  rt->sync();
-  rt->release(dx);
-  rt->release(dy);
   rt->sync();
 }
 

@@ -58,7 +58,8 @@ struct DevProgram {
 
 class Runtime {
  public:
-  explicit Runtime(int L, int device = 0);
+  // device < 0: the calling thread's current device (cudaGetDevice).
+  explicit Runtime(int L, int device = -1);
   ~Runtime();
   Runtime(const Runtime&) = delete;
   Runtime& operator=(const Runtime&) = delete;

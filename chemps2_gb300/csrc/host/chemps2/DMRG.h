@@ -67,8 +67,10 @@ class DMRG {
   // Benchmark support: build the two-site object at `index`, then time `steps` Heff
   // applications after `warmup` untimed ones. Returns milliseconds per application and
   // the ledger work of one application.
+  // flush_bytes > 0: a buffer of that size is overwritten before every timed application
+  // (outside the timed interval) so that the operators are read from HBM, not L2.
   double bench_heff(const int index, const int warmup, const int steps, double* flops, double* bytes,
-                    long long* launches);
+                    long long* launches, const long long flush_bytes = 0);
 
   // Host-buffer access to the effective Hamiltonian at sites (index, index + 1), in the
   // symmetric convention: y = Heff x (and its diagonal when diag is non-null). With
@@ -78,6 +80,11 @@ class DMRG {
                        const long long n);
 
  private:
+  struct HeffCache;
+  HeffCache& heff_program(const int index, const bool with_diag);
+  std::unique_ptr<HeffCache> heff_cache_;
+  unsigned long long version_ = 0;  // advanced by every change of the MPS or the operators
+
   void setup_mps(int* occupancies);
   void left_normalize_host(int site, std::vector<double>& data);
   void upload_mps(int site, const std::vector<double>& data);

@@ -9,11 +9,11 @@ namespace c2g {
 namespace {
 
 template <class F>
-Compiled run_sharded(F emit) {
+Compiled run_sharded(F emit, bool track = false) {
   const int n = compile_threads();
   Compiled out;
   if (n <= 1) {
-    TaskBuilder tb;
+    TaskBuilder tb(track);
     emit(tb, 0, 1);
     out.program = tb.finalize();
     out.operand_bytes = tb.operand_bytes();
@@ -29,7 +29,7 @@ Compiled run_sharded(F emit) {
   for (int i = 0; i < n; i++)
     threads.emplace_back([&, i] {
       try {
-        TaskBuilder tb;
+        TaskBuilder tb(track);
         emit(tb, i, n);
         parts[i] = tb.finalize(true);
         operands[i] = tb.operands();
@@ -55,8 +55,8 @@ Compiled run_sharded(F emit) {
 
 }  // namespace
 
-Compiled compile_heff_program(const HeffContext& ctx) {
-  return run_sharded([&](TaskBuilder& tb, int shard, int n) { compile_heff(tb, ctx, shard, n); });
+Compiled compile_heff_program(const HeffContext& ctx, bool track_operands) {
+  return run_sharded([&](TaskBuilder& tb, int shard, int n) { compile_heff(tb, ctx, shard, n); }, track_operands);
 }
 
 Compiled compile_heff_diag_program(const HeffContext& ctx) {

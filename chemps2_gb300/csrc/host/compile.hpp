@@ -14,7 +14,8 @@ struct Compiled {
   int64_t contractions = 0;    // block contractions recorded (before batching)
 };
 
-Compiled compile_heff_program(const HeffContext& ctx);
+// track_operands fills Compiled::operand_bytes (costs compile time).
+Compiled compile_heff_program(const HeffContext& ctx, bool track_operands = false);
 Compiled compile_heff_diag_program(const HeffContext& ctx);
 Compiled compile_update_program(const UpdateContext& ctx);
 

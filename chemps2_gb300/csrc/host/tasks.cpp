@@ -22,10 +22,15 @@ inline Shape op_shape(const Blk& b, bool t) { return t ? Shape{b.cols, b.rows} :
 
 void append_bytes(std::string& s, const void* p, size_t n) { s.append(static_cast<const char*>(p), n); }
 
-inline uint64_t mix(uint64_t h, uint64_t v) {
-  h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
-  return h;
+inline uint64_t fmix(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
 }
+inline uint64_t mix(uint64_t h, uint64_t v) { return fmix(h ^ (v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2))); }
 
 }  // namespace
 
@@ -50,13 +55,13 @@ size_t TaskBuilder::BatchKeyHash::operator()(const BatchKey& k) const {
   return static_cast<size_t>(h);
 }
 
-TaskBuilder::TaskBuilder() {
+TaskBuilder::TaskBuilder(bool track_operands) : track_operands_(track_operands) {
   stages_.emplace_back();
   stages_.back().name = "stage0";
 }
 
 void TaskBuilder::note_operand(const Blk& b) {
-  if (!b.valid || ref_slot(b.ref) < kSlotMpsBase) return;
+  if (!track_operands_ || !b.valid || ref_slot(b.ref) < kSlotMpsBase) return;
   const int64_t n = int64_t(b.rows) * b.cols;
   int64_t& cur = operands_[b.ref];
   if (n > cur) cur = n;
@@ -69,10 +74,14 @@ int64_t TaskBuilder::operand_bytes() const {
 }
 
 int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
+  if (&sb == last_sb_ && out.ref == last_out_) return last_group_;
   auto it = sb.group_of.find(out.ref);
   if (it != sb.group_of.end()) {
     const Group& g = sb.groups[it->second];
     if (g.m != out.rows || g.n != out.cols || g.ldo != out.ld) shape_error("output group");
+    last_sb_ = &sb;
+    last_out_ = out.ref;
+    last_group_ = it->second;
     return it->second;
   }
   Group g{};
@@ -86,6 +95,9 @@ int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
   sb.terms.emplace_back();
   const int id = static_cast<int>(sb.groups.size()) - 1;
   sb.group_of[out.ref] = id;
+  last_sb_ = &sb;
+  last_out_ = out.ref;
+  last_group_ = id;
   return id;
 }
 
@@ -111,6 +123,13 @@ void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha
   auto& gt = sb.terms[g];
   Group& G = sb.groups[g];
   if (batchable) {
+    // The compilers emit all contractions of one output block consecutively, so only the
+    // current group's terms are kept open for batching: the map stays small.
+    if (g != open_group_ || &sb != open_sb_) {
+      open_.clear();
+      open_group_ = g;
+      open_sb_ = &sb;
+    }
     const BatchKey key{g, t.b, t.flags, t.k1, t.k2, t.lda, t.ldc, A.valid ? ref_slot(A.ref) : -1,
                        C.valid ? ref_slot(C.ref) : -1};
     auto it = open_.find(key);
@@ -201,6 +220,9 @@ void TaskBuilder::contract(const Blk& out, double alpha, const Blk& A, bool ta, 
 void TaskBuilder::next_stage(const std::string& name) {
   for (auto& g : stages_.back().groups) written_[g.out] = true;
   open_.clear();
+  last_sb_ = nullptr;
+  open_sb_ = nullptr;
+  open_group_ = -1;
   stages_.emplace_back();
   stages_.back().name = name;
 }

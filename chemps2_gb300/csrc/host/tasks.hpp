@@ -136,7 +136,9 @@ int64_t term_flops(const Term& t, int m, int n);
 // Records contractions and lowers them into a Program.
 class TaskBuilder {
  public:
-  TaskBuilder();
+  // track_operands: record the footprint of the MPS / operator blocks read (for the
+  // benchmark ledger; off by default because it costs a hash insert per operand).
+  explicit TaskBuilder(bool track_operands = false);
 
   // A block of the combination scratch holding sum_i alpha_i * op_i(block_i).
   // All parts must have the shape rows x cols after their optional transpose.
@@ -204,6 +206,12 @@ class TaskBuilder {
   std::unordered_map<Ref, bool> written_;                  // outputs written by closed stages
   std::unordered_map<Ref, int64_t> operands_;              // footprint of MPS / operator operands
   int64_t n_contract_ = 0;
+  bool track_operands_ = false;
+  const StageBuf* open_sb_ = nullptr;  // the group whose terms are open for batching
+  int open_group_ = -1;
+  const StageBuf* last_sb_ = nullptr;  // output-group lookup cache
+  Ref last_out_ = 0;
+  int last_group_ = -1;
 
   void note_operand(const Blk& b);
   int group_for(StageBuf& sb, const Blk& out, bool accumulate);

@@ -112,10 +112,12 @@ int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n);
 int c2g_dmrg_reset_stats(c2g_dmrg* d);
 /* Heff applications at sites (index, index + 1) on the current MPS (CheMPS2/Heff.cpp:43-248):
  * `steps` timed applications after `warmup` untimed ones, CUDA-event timed on the DMRG's
- * stream. Returns milliseconds per application, the ledger flops and bytes of one
- * application and the number of kernels launched in the timed region. */
-int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, double* ms_per_matvec, double* flops,
-                        double* bytes, long long* launches);
+ * stream. With flush_bytes > 0 a buffer of that size is overwritten before each timed
+ * application, outside the timed interval, so that the operators come from HBM. Returns
+ * milliseconds per application, the ledger flops and bytes of one application and the
+ * number of kernels launched in the timed region. No counterpart in the reference. */
+int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, long long flush_bytes, double* ms_per_matvec,
+                        double* flops, double* bytes, long long* launches);
 
 /* Effective Hamiltonian on host buffers (the path of CheMPS2/Heff.cpp:43-315 with the
  * copies in and out included): n must equal the size of the two-site object at sites
