@@ -22,9 +22,9 @@ C2G_ERR_CUDA = -2
 C2G_ERR_NO_DEVICE = -3
 C2G_ERR_INTERNAL = -4
 C2G_ERR_OTHER = -5
-NUM_STATS = 11
+NUM_STATS = 12
 STAT_NAMES = ("n_matvec", "n_davidson", "t_join", "t_solve", "t_split", "t_update", "t_matvec", "t_compile",
-              "matvec_flops", "matvec_bytes", "last_energy")
+              "matvec_flops", "matvec_bytes", "last_energy", "n_matvec_fp32")
 
 
 class Chemps2Error(RuntimeError):
@@ -353,11 +353,24 @@ class DMRG:
                                           _dp(d) if d is not None else None, C.c_int64(n)))
         return xx, y, d
 
-    def bench_heff(self, index, warmup, steps, flush_bytes=0):
+    def heff_apply_fp32(self, index, x):
+        """y = Heff x with FP32 arithmetic (FP64 operands and output)."""
+        xx = np.ascontiguousarray(x, dtype=np.float64).copy()
+        y = np.zeros_like(xx)
+        _check(load().c2g_dmrg_heff_apply_fp32(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
+        return y
+
+    def set_precision(self, mode="fp64", mixed_tol=1e-5):
+        """'fp64' (the reference's arithmetic) or 'mixed' (FP32 Davidson expansion, FP64 finish)."""
+        m = {"fp64": 0, "mixed": 1}[mode] if isinstance(mode, str) else int(mode)
+        _check(load().c2g_dmrg_set_precision(self._d, m, C.c_double(mixed_tol)))
+
+    def bench_heff(self, index, warmup, steps, flush_bytes=0, precision="fp64"):
         ms, fl, by = C.c_double(), C.c_double(), C.c_double()
         nl = C.c_longlong()
+        p = {"fp64": 0, "fp32": 1, "mixed": 1}[precision]
         _check(load().c2g_dmrg_bench_heff(self._d, int(index), int(warmup), int(steps), C.c_longlong(flush_bytes),
-                                          C.byref(ms), C.byref(fl), C.byref(by), C.byref(nl)))
+                                          int(p), C.byref(ms), C.byref(fl), C.byref(by), C.byref(nl)))
         return {"ms_per_matvec": ms.value, "flops": fl.value, "bytes": by.value, "launches": nl.value}
 
 

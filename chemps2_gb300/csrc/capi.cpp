@@ -358,6 +358,14 @@ int c2g_dmrg_presolve(c2g_dmrg* d) {
     d->d->PreSolve();
   });
 }
+int c2g_dmrg_set_precision(c2g_dmrg* d, int mode, double mixed_tol) {
+  return guarded([&] {
+    NEED(d);
+    if (mode != 0 && mode != 1) throw std::invalid_argument("precision mode must be 0 (FP64) or 1 (mixed)");
+    if (!(mixed_tol > 0.0)) throw std::invalid_argument("mixed tolerance must be positive");
+    d->d->set_precision(mode, mixed_tol);
+  });
+}
 int c2g_dmrg_set_verbose(c2g_dmrg* d, int v) {
   return guarded([&] {
     NEED(d);
@@ -402,7 +410,8 @@ int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n) {
     const CheMPS2::DMRGStats& s = d->d->stats();
     const double v[C2G_NUM_STATS] = {static_cast<double>(s.n_matvec), static_cast<double>(s.n_davidson),
                                      s.t_join, s.t_solve, s.t_split, s.t_update, s.t_matvec, s.t_compile,
-                                     s.matvec_flops, s.matvec_bytes, s.last_energy};
+                                     s.matvec_flops, s.matvec_bytes, s.last_energy,
+                                     static_cast<double>(s.n_matvec_fp32)};
     for (int i = 0; i < n && i < C2G_NUM_STATS; i++) out[i] = v[i];
   });
 }
@@ -412,12 +421,12 @@ int c2g_dmrg_reset_stats(c2g_dmrg* d) {
     d->d->reset_stats();
   });
 }
-int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, long long flush_bytes, double* ms,
-                        double* flops, double* bytes, long long* launches) {
+int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, long long flush_bytes, int precision,
+                        double* ms, double* flops, double* bytes, long long* launches) {
   return guarded([&] {
     NEED(d);
     NEED(ms);
-    *ms = d->d->bench_heff(index, warmup, steps, flops, bytes, launches, flush_bytes);
+    *ms = d->d->bench_heff(index, warmup, steps, flops, bytes, launches, flush_bytes, precision);
   });
 }
 
@@ -432,6 +441,12 @@ int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, doub
   return guarded([&] {
     NEED(d);
     d->d->heff_apply_host(index, join_into_x != 0, x, y, diag, n);
+  });
+}
+int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64_t n) {
+  return guarded([&] {
+    NEED(d);
+    d->d->heff_apply_host(index, false, x, y, nullptr, n, 1);
   });
 }
 

@@ -50,8 +50,12 @@ inline int sandwich_grid(int m, int n) {
   return (sr << 8) | sc;
 }
 
+// Arithmetic of the block sandwich: FP64 throughout, or FP32 products and per-lane sums
+// (operands converted on load) with the lane reduction and the output update in FP64.
+enum class Precision : int { kFP64 = 0, kFP32 = 1 };
+
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
-                            int ntiles, const SlotPtrs& sp, cudaStream_t stream);
+                            int ntiles, const SlotPtrs& sp, cudaStream_t stream, Precision prec = Precision::kFP64);
 
 // out[j] = sum_i A[i + lda * j] * x[i] for j < ncol (A has n rows). Uses `partial`
 // (at least ncol * kDotBlocks doubles) as scratch.

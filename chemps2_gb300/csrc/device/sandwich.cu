@@ -1,4 +1,8 @@
-// The block-sandwich kernel: executes one stage of a task program (FP64).
+// The block-sandwich kernel: executes one stage of a task program.
+//
+// Operands are FP64 in memory. The FP64 variant computes in FP64; the FP32 variant
+// converts every operand on load and accumulates each lane's items in FP32, while the
+// reduction over lanes and the update of the FP64 output stay in FP64.
 #include "kernels.cuh"
 
 namespace c2g {
@@ -19,84 +23,88 @@ __device__ __forceinline__ const double* resolve(const SlotPtrs& sp, Ref r) {
   return base + off;
 }
 
+__device__ __forceinline__ double fmaR(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
+
 // acc[ii][jj] (rows i0 + ii, ii < r; columns j0 + jj, jj < c) += one entry of a term.
-__device__ __forceinline__ void sandwich_item(double (&acc)[kSub][kSub], const Term& T, const double* __restrict__ A,
-                                              const double* __restrict__ B, const double* __restrict__ C, double al,
+template <typename Real>
+__device__ __forceinline__ void sandwich_item(Real (&acc)[kSub][kSub], const Term& T, const double* __restrict__ A,
+                                              const double* __restrict__ B, const double* __restrict__ C, Real al,
                                               int i0, int j0, int r, int c) {
   const bool ha = T.flags & kHasA, hc = T.flags & kHasC;
   const bool ta = T.flags & kTransA, tb = T.flags & kTransB, tc = T.flags & kTransC;
   const int64_t lda = T.lda, ldb = T.ldb, ldc = T.ldc;
-  auto opA = [&](int i, int k) { return ta ? A[k + lda * i] : A[i + lda * k]; };
-  auto opB = [&](int k, int l) { return tb ? B[l + ldb * k] : B[k + ldb * l]; };
-  auto opC = [&](int l, int j) { return tc ? C[j + ldc * l] : C[l + ldc * j]; };
+  auto opA = [&](int i, int k) { return static_cast<Real>(ta ? A[k + lda * i] : A[i + lda * k]); };
+  auto opB = [&](int k, int l) { return static_cast<Real>(tb ? B[l + ldb * k] : B[k + ldb * l]); };
+  auto opC = [&](int l, int j) { return static_cast<Real>(tc ? C[j + ldc * l] : C[l + ldc * j]); };
   if (ha && hc) {
     if (T.flags & kLeftFirst) {
       for (int l = 0; l < T.k2; l++) {
-        double s[kSub];
+        Real s[kSub];
 #pragma unroll
-        for (int ii = 0; ii < kSub; ii++) s[ii] = 0.0;
+        for (int ii = 0; ii < kSub; ii++) s[ii] = Real(0);
         for (int k = 0; k < T.k1; k++) {
-          const double b = opB(k, l);
+          const Real b = opB(k, l);
 #pragma unroll
           for (int ii = 0; ii < kSub; ii++)
-            if (ii < r) s[ii] = fma(opA(i0 + ii, k), b, s[ii]);
+            if (ii < r) s[ii] = fmaR(opA(i0 + ii, k), b, s[ii]);
         }
 #pragma unroll
         for (int jj = 0; jj < kSub; jj++) {
           if (jj >= c) break;
-          const double cv = al * opC(l, j0 + jj);
+          const Real cv = al * opC(l, j0 + jj);
 #pragma unroll
           for (int ii = 0; ii < kSub; ii++)
-            if (ii < r) acc[ii][jj] = fma(s[ii], cv, acc[ii][jj]);
+            if (ii < r) acc[ii][jj] = fmaR(s[ii], cv, acc[ii][jj]);
         }
       }
     } else {
       for (int k = 0; k < T.k1; k++) {
-        double t[kSub];
+        Real t[kSub];
 #pragma unroll
-        for (int jj = 0; jj < kSub; jj++) t[jj] = 0.0;
+        for (int jj = 0; jj < kSub; jj++) t[jj] = Real(0);
         for (int l = 0; l < T.k2; l++) {
-          const double b = opB(k, l);
+          const Real b = opB(k, l);
 #pragma unroll
           for (int jj = 0; jj < kSub; jj++)
-            if (jj < c) t[jj] = fma(b, opC(l, j0 + jj), t[jj]);
+            if (jj < c) t[jj] = fmaR(b, opC(l, j0 + jj), t[jj]);
         }
 #pragma unroll
         for (int ii = 0; ii < kSub; ii++) {
           if (ii >= r) break;
-          const double av = al * opA(i0 + ii, k);
+          const Real av = al * opA(i0 + ii, k);
 #pragma unroll
           for (int jj = 0; jj < kSub; jj++)
-            if (jj < c) acc[ii][jj] = fma(av, t[jj], acc[ii][jj]);
+            if (jj < c) acc[ii][jj] = fmaR(av, t[jj], acc[ii][jj]);
         }
       }
     }
   } else if (ha) {
     for (int k = 0; k < T.k1; k++) {
-      double bv[kSub];
+      Real bv[kSub];
 #pragma unroll
-      for (int jj = 0; jj < kSub; jj++) bv[jj] = (jj < c) ? al * opB(k, j0 + jj) : 0.0;
+      for (int jj = 0; jj < kSub; jj++) bv[jj] = (jj < c) ? al * opB(k, j0 + jj) : Real(0);
 #pragma unroll
       for (int ii = 0; ii < kSub; ii++) {
         if (ii >= r) break;
-        const double av = opA(i0 + ii, k);
+        const Real av = opA(i0 + ii, k);
 #pragma unroll
         for (int jj = 0; jj < kSub; jj++)
-          if (jj < c) acc[ii][jj] = fma(av, bv[jj], acc[ii][jj]);
+          if (jj < c) acc[ii][jj] = fmaR(av, bv[jj], acc[ii][jj]);
       }
     }
   } else if (hc) {
     for (int l = 0; l < T.k2; l++) {
-      double cv[kSub];
+      Real cv[kSub];
 #pragma unroll
-      for (int jj = 0; jj < kSub; jj++) cv[jj] = (jj < c) ? al * opC(l, j0 + jj) : 0.0;
+      for (int jj = 0; jj < kSub; jj++) cv[jj] = (jj < c) ? al * opC(l, j0 + jj) : Real(0);
 #pragma unroll
       for (int ii = 0; ii < kSub; ii++) {
         if (ii >= r) break;
-        const double b = opB(i0 + ii, l);
+        const Real b = opB(i0 + ii, l);
 #pragma unroll
         for (int jj = 0; jj < kSub; jj++)
-          if (jj < c) acc[ii][jj] = fma(b, cv[jj], acc[ii][jj]);
+          if (jj < c) acc[ii][jj] = fmaR(b, cv[jj], acc[ii][jj]);
       }
     }
   } else {
@@ -105,11 +113,12 @@ __device__ __forceinline__ void sandwich_item(double (&acc)[kSub][kSub], const T
       if (ii >= r) break;
 #pragma unroll
       for (int jj = 0; jj < kSub; jj++)
-        if (jj < c) acc[ii][jj] = fma(al, opB(i0 + ii, j0 + jj), acc[ii][jj]);
+        if (jj < c) acc[ii][jj] = fmaR(al, opB(i0 + ii, j0 + jj), acc[ii][jj]);
     }
   }
 }
 
+template <typename Real>
 __global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group* __restrict__ groups,
                                                                     const Term* __restrict__ terms,
                                                                     const BatchEntry* __restrict__ entries,
@@ -127,11 +136,11 @@ __global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group*
   const int si = s % sr, sj = s / sr;
   const int i0 = row0 + si * kSub, j0 = col0 + sj * kSub;
   const int r = max(0, min(kSub, row0 + tm - i0)), c = max(0, min(kSub, col0 + tn - j0));
-  double acc[kSub][kSub];
+  Real acc[kSub][kSub];
 #pragma unroll
   for (int ii = 0; ii < kSub; ii++)
 #pragma unroll
-    for (int jj = 0; jj < kSub; jj++) acc[ii][jj] = 0.0;
+    for (int jj = 0; jj < kSub; jj++) acc[ii][jj] = Real(0);
   if (lane < P && r > 0 && c > 0 && G.t1 > G.t0) {
     const Term& last = terms[G.t1 - 1];
     const int total = last.item0 + last.count;
@@ -168,14 +177,14 @@ __global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group*
           if (A) A += e.da;
           if (C) C += e.dc;
         }
-        sandwich_item(acc, T, A, B, C, T.alpha * ratio, i0, j0, r, c);
+        sandwich_item<Real>(acc, T, A, B, C, static_cast<Real>(T.alpha * ratio), i0, j0, r, c);
       }
     }
   }
 #pragma unroll
   for (int ii = 0; ii < kSub; ii++)
 #pragma unroll
-    for (int jj = 0; jj < kSub; jj++) red[tid * kSub * kSub + ii * kSub + jj] = acc[ii][jj];
+    for (int jj = 0; jj < kSub; jj++) red[tid * kSub * kSub + ii * kSub + jj] = static_cast<double>(acc[ii][jj]);
   __syncthreads();
   double* O = const_cast<double*>(resolve(sp, G.out));
   const int64_t ldo = G.ldo;
@@ -194,9 +203,12 @@ __global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group*
 }  // namespace
 
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
-                            int ntiles, const SlotPtrs& sp, cudaStream_t stream) {
+                            int ntiles, const SlotPtrs& sp, cudaStream_t stream, Precision prec) {
   if (ntiles <= 0) return cudaSuccess;
-  sandwich_kernel<<<ntiles, kSandwichThreads, 0, stream>>>(groups, terms, entries, tiles, sp);
+  if (prec == Precision::kFP32)
+    sandwich_kernel<float><<<ntiles, kSandwichThreads, 0, stream>>>(groups, terms, entries, tiles, sp);
+  else
+    sandwich_kernel<double><<<ntiles, kSandwichThreads, 0, stream>>>(groups, terms, entries, tiles, sp);
   return cudaGetLastError();
 }
 

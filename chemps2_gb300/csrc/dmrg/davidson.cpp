@@ -1,5 +1,6 @@
 #include "davidson.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <vector>
@@ -67,24 +68,22 @@ void DeviceDavidson::add_new_vec(double* t, int nv) {
   C2G_CUDA(cudaMemcpyAsync(V(nv), t, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
 }
 
-DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const MatVec& matvec) {
+void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision prec, double tol, bool stop_on_stall,
+                         DavidsonStats& st) {
   cudaStream_t s = rt_.stream();
-  DavidsonStats st;
   double* t = W(0);
   double* u = W(1);
   double* w = W(2);
-  C2G_CUDA(cudaMemcpyAsync(t, guess, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
-  // SafetyCheckGuess (CheMPS2/Davidson.cpp:204-214)
-  if (norm2(t) == 0.0) {
-    std::vector<double> r(n_);
-    for (int64_t i = 0; i < n_; i++) r[i] = static_cast<double>(std::rand()) / RAND_MAX;
-    C2G_CUDA(cudaMemcpyAsync(t, r.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
-    rt_.sync();
-  }
+  auto mv = [&](const double* x, double* y) {
+    matvec(x, y, prec);
+    st.n_matvec++;
+    if (prec == Precision::kFP32) st.n_matvec_fp32++;
+  };
   int nv = 0;
   add_new_vec(t, nv);
-  matvec(V(nv), HV(nv));
-  st.n_matvec++;
+  mv(V(nv), HV(nv));
+  double best = 1e300;
+  int since_best = 0;
   for (;;) {
     // DiagonalizeSmallMatrixAndCalcResidual (CheMPS2/Davidson.cpp:238-289)
     multi_dot(HV_, nv + 1, V(nv), sm_ + kDots);
@@ -98,7 +97,15 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
     const double rnorm = std::sqrt(norm2(t));
     st.n_iter++;
     st.rnorm = rnorm;
-    if (!(rnorm > rtol_)) break;
+    if (!(rnorm > tol)) break;
+    if (stop_on_stall) {  // FP32 phase: stop when the residual no longer improves
+      if (rnorm < 0.7 * best) {
+        best = rnorm;
+        since_best = 0;
+      } else if (++since_best >= 6) {
+        break;
+      }
+    }
     // CalculateNewVec (CheMPS2/Davidson.cpp:291-317)
     C2G_CUDA(launch_precond_w(w, u, diag, sm_ + kEvals, cutoff_, n_, s));
     multi_dot(W(0), 2, w, sm_ + kDots2);  // w.t, w.u
@@ -118,10 +125,7 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
         C2G_CUDA(launch_combine(V(c), 0.0, W(3), n_, sm_ + kLowdin + keep_ * c, keep_, n_, s));
         count_launches(1);
       }
-      for (int c = 0; c < keep_; c++) {
-        matvec(V(c), HV(c));
-        st.n_matvec++;
-      }
+      for (int c = 0; c < keep_; c++) mv(V(c), HV(c));
       // MxMafterDeflation (CheMPS2/Davidson.cpp:510-536)
       for (int j = 0; j < keep_; j++) {
         multi_dot(V_, j + 1, HV(j), sm_ + kDots);
@@ -131,9 +135,30 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
       nv = keep_;
     }
     add_new_vec(t, nv);
-    matvec(V(nv), HV(nv));
-    st.n_matvec++;
+    mv(V(nv), HV(nv));
   }
+}
+
+DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const MatVec& matvec, bool mixed,
+                                    double lo_tol) {
+  cudaStream_t s = rt_.stream();
+  DavidsonStats st;
+  double* t = W(0);
+  double* u = W(1);
+  C2G_CUDA(cudaMemcpyAsync(t, guess, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+  // SafetyCheckGuess (CheMPS2/Davidson.cpp:204-214)
+  if (norm2(t) == 0.0) {
+    std::vector<double> r(n_);
+    for (int64_t i = 0; i < n_; i++) r[i] = static_cast<double>(std::rand()) / RAND_MAX;
+    C2G_CUDA(cudaMemcpyAsync(t, r.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
+    rt_.sync();
+  }
+  if (mixed) {
+    run(diag, matvec, Precision::kFP32, std::max(lo_tol, rtol_), true, st);
+    // restart in FP64 from the FP32 Ritz vector
+    C2G_CUDA(cudaMemcpyAsync(t, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+  }
+  run(diag, matvec, Precision::kFP64, rtol_, false, st);
   C2G_CUDA(cudaMemcpyAsync(guess, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
   C2G_CUDA(cudaMemcpyAsync(host_, sm_ + kEvals, sizeof(double), cudaMemcpyDeviceToHost, s));
   rt_.sync();

@@ -8,6 +8,10 @@
 // FP64; only the residual norm travels to the host, once per iteration, to drive the
 // state machine. Orthogonalisation is classical Gram-Schmidt applied twice (the reference
 // applies one modified Gram-Schmidt pass; both are exact in exact arithmetic).
+//
+// Mixed precision: the matvec is requested in FP32 until the residual reaches a looser
+// tolerance (or stops improving), then the solver restarts from that Ritz vector with
+// FP64 matvecs and the caller's tolerance, so the returned eigenpair is an FP64 one.
 #pragma once
 
 #include <functional>
@@ -18,14 +22,15 @@ namespace c2g {
 
 struct DavidsonStats {
   double energy = 0.0;
-  int n_matvec = 0;
+  int n_matvec = 0;       // all matvecs
+  int n_matvec_fp32 = 0;  // of which in FP32
   int n_iter = 0;
   double rnorm = 0.0;
 };
 
 class DeviceDavidson {
  public:
-  using MatVec = std::function<void(const double* x, double* y)>;
+  using MatVec = std::function<void(const double* x, double* y, Precision prec)>;
 
   DeviceDavidson(Runtime& rt, int64_t n, int max_vec, int keep, double rtol, double cutoff);
   ~DeviceDavidson();
@@ -33,8 +38,10 @@ class DeviceDavidson {
   DeviceDavidson& operator=(const DeviceDavidson&) = delete;
 
   // guess: device vector of length n (in: start vector; out: converged eigenvector).
-  // diag: device vector, the diagonal of the operator.
-  DavidsonStats solve(double* guess, const double* diag, const MatVec& matvec);
+  // diag: device vector, the diagonal of the operator. mixed: run the FP32 phase first,
+  // down to residual lo_tol (never below rtol).
+  DavidsonStats solve(double* guess, const double* diag, const MatVec& matvec, bool mixed = false,
+                      double lo_tol = 1e-5);
 
  private:
   double* V(int i) { return V_ + n_ * i; }
@@ -43,6 +50,9 @@ class DeviceDavidson {
   void add_new_vec(double* t, int nv);  // orthonormalise t against V[0..nv) into V[nv]
   double norm2(const double* x);         // synchronising host read of x.x
   void multi_dot(const double* A, int ncol, const double* x, double* out);
+  // One Davidson run from the vector in W(0); the Ritz vector ends in W(1).
+  void run(const double* diag, const MatVec& matvec, Precision prec, double tol, bool stop_on_stall,
+           DavidsonStats& st);
 
   Runtime& rt_;
   int64_t n_;

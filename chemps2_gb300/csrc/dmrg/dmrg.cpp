@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cusolverDn.h>
+#include <unordered_map>
 
 #include "davidson.hpp"
 #include "compile.hpp"
@@ -54,6 +55,73 @@ void check_solver(cusolverStatus_t s, const char* what) {
 
 }  // namespace
 
+struct DMRG::ProgramCache {
+  struct Entry {
+    std::unique_ptr<DevProgram> dp;
+    long long operand_bytes = 0;
+    unsigned long long last_use = 0;
+  };
+  std::unordered_map<std::string, Entry> map;
+  long long bytes = 0;
+  long long limit = 0;
+  unsigned long long clock = 0;
+  long long hits = 0, misses = 0;
+};
+
+std::string DMRG::dims_key(const char* kind, const int index, const int bmin, const int bmax, const int extra) const {
+  std::string key(kind);
+  key.push_back('|');
+  const int hdr[2] = {index, extra};
+  key.append(reinterpret_cast<const char*>(hdr), sizeof(hdr));
+  for (int b = std::max(bmin, 0); b <= std::min(bmax, L); b++) {
+    const int ns = denBK->num_sectors(b);
+    key.push_back('/');
+    for (int id = 0; id < ns; id++) {
+      const int d = denBK->cur_dim_by_id(b, id);
+      key.append(reinterpret_cast<const char*>(&d), sizeof(d));
+    }
+  }
+  return key;
+}
+
+DevProgram& DMRG::program(const std::string& key, const std::function<c2g::Compiled()>& build,
+                          long long* operand_bytes) {
+  ProgramCache& pc = *pcache_;
+  pc.clock++;
+  auto it = pc.map.find(key);
+  if (it != pc.map.end()) {
+    pc.hits++;
+    it->second.last_use = pc.clock;
+    it->second.dp->prepared = false;  // its combination stage reads operator data: rerun
+    if (operand_bytes) *operand_bytes = it->second.operand_bytes;
+    return *it->second.dp;
+  }
+  pc.misses++;
+  const double tc = now();
+  c2g::Compiled c = build();
+  stats_.t_compile += now() - tc;
+  ProgramCache::Entry e;
+  e.dp = rt->upload(c.program);
+  e.operand_bytes = c.operand_bytes;
+  e.last_use = pc.clock;
+  const long long size = e.dp->bytes + 8 * e.dp->combo_size;
+  // Least recently used programs leave first; the programs of the current step (the last
+  // few requests) stay, since callers hold references to them.
+  while (pc.bytes + size > pc.limit && !pc.map.empty()) {
+    auto victim = pc.map.end();
+    for (auto jt = pc.map.begin(); jt != pc.map.end(); ++jt)
+      if (jt->second.last_use + 8 < pc.clock && (victim == pc.map.end() || jt->second.last_use < victim->second.last_use))
+        victim = jt;
+    if (victim == pc.map.end()) break;
+    pc.bytes -= victim->second.dp->bytes + 8 * victim->second.dp->combo_size;
+    pc.map.erase(victim);
+  }
+  pc.bytes += size;
+  if (operand_bytes) *operand_bytes = e.operand_bytes;
+  auto ins = pc.map.emplace(key, std::move(e));
+  return *ins.first->second.dp;
+}
+
 struct DMRG::HeffCache {
   int index = -1;
   unsigned long long version = 0;
@@ -68,6 +136,9 @@ struct DMRG::HeffCache {
 DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool, const std::string, int* occupancies)
     : Prob(ProbIn), OptScheme(OptSchemeIn) {
   heff_cache_ = std::make_unique<HeffCache>();
+  pcache_ = std::make_unique<ProgramCache>();
+  pcache_->limit = 16LL << 30;
+  if (const char* e = std::getenv("C2G_PROGRAM_CACHE_GB")) pcache_->limit = static_cast<long long>(std::atof(e) * (1LL << 30));
   if (!Prob->checkConsistency()) throw std::invalid_argument("DMRG: inconsistent Problem");
   if (OptScheme->get_number() < 1) throw std::invalid_argument("DMRG: empty ConvergenceScheme");
   L = Prob->gL();
@@ -89,6 +160,7 @@ DMRG::~DMRG() {
       rt->sync();
     } catch (...) {
     }
+    pcache_.reset();
     if (heff_cache_) {
       heff_cache_->program.reset();
       heff_cache_->diag.reset();
@@ -280,12 +352,10 @@ void DMRG::update_moving_right(const int index) {
   if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("update_moving_right: left operators missing");
   ctx.next = ops[index].get();
   ctx.mps = mps_tensor(mps_lay[index].get(), index);
-  const double tc = now();
-  Program p = c2g::compile_update_program(ctx).program;
-  stats_.t_compile += now() - tc;
-  auto dp = rt->upload(p);
+  DevProgram& dp = program(dims_key("update", index, index, index + 2, ctx.moving_right ? 1 : 0),
+                           [&] { return c2g::compile_update_program(ctx); });
   rt->zero(ops_dev[index], ops[index]->size);
-  rt->run(*dp, nullptr, nullptr);
+  rt->run(dp, nullptr, nullptr);
   rt->sync();
   stats_.t_update += now() - t0;
 }
@@ -311,12 +381,10 @@ void DMRG::update_moving_left(const int index) {
     throw std::logic_error("update_moving_left: right operators missing");
   ctx.next = ops[index].get();
   ctx.mps = mps_tensor(mps_lay[index + 1].get(), index + 1);
-  const double tc = now();
-  Program p = c2g::compile_update_program(ctx).program;
-  stats_.t_compile += now() - tc;
-  auto dp = rt->upload(p);
+  DevProgram& dp = program(dims_key("update", index, index, index + 2, ctx.moving_right ? 1 : 0),
+                           [&] { return c2g::compile_update_program(ctx); });
   rt->zero(ops_dev[index], ops[index]->size);
-  rt->run(*dp, nullptr, nullptr);
+  rt->run(dp, nullptr, nullptr);
   rt->sync();
   stats_.t_update += now() - t0;
 }
@@ -379,11 +447,15 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   const int64_t veclen = S.size();
   double* svec = rt->alloc(veclen);
   {
-    TaskBuilder tb;
-    c2g::compile_join(tb, *denBK, S, mps_tensor(mps_lay[index].get(), index),
-                      mps_tensor(mps_lay[index + 1].get(), index + 1));
-    auto dp = rt->upload(tb.finalize());
-    rt->run(*dp, nullptr, svec);
+    DevProgram& dp = program(dims_key("join", index, index, index + 2), [&] {
+      c2g::Compiled c;
+      TaskBuilder tb;
+      c2g::compile_join(tb, *denBK, S, mps_tensor(mps_lay[index].get(), index),
+                        mps_tensor(mps_lay[index + 1].get(), index + 1));
+      c.program = tb.finalize();
+      return c;
+    });
+    rt->run(dp, nullptr, svec);
     rt->sync();
   }
   stats_.t_join += now() - t0;
@@ -398,34 +470,34 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
   if (index > 0 && isAllocated[index - 1] != 1) throw std::logic_error("solve_site: left operators missing");
   if (index + 1 < L - 1 && isAllocated[index + 1] != 2) throw std::logic_error("solve_site: right operators missing");
-  double tc = now();
-  Program pd = c2g::compile_heff_diag_program(ctx).program;
-  c2g::Compiled ch = c2g::compile_heff_program(ctx);
-  Program& ph = ch.program;
-  stats_.t_compile += now() - tc;
   int maxdim = 1;
   for (int k = 0; k < S.nkappa; k++) maxdim = std::max(maxdim, std::max(S.rows[k], S.cols[k]));
   rt->ones(maxdim);
   double* diag = rt->alloc(veclen);
-  auto dpd = rt->upload(pd);
-  rt->run(*dpd, nullptr, diag);
-  auto dph = rt->upload(ph);
+  DevProgram& dpd = program(dims_key("diag", index, index, index + 2, 0),
+                            [&] { return c2g::compile_heff_diag_program(ctx); });
+  rt->run(dpd, nullptr, diag);
+  long long heff_operand_bytes = 0;
+  DevProgram& dph_ref = program(dims_key("heff", index, index, index + 2, 0),
+                                [&] { return c2g::compile_heff_program(ctx, true); }, &heff_operand_bytes);
+  DevProgram* dph = &dph_ref;
   rt->prepare(*dph);
   c2g::DeviceDavidson dav(*rt, veclen, kDavidsonNumVec, kDavidsonNumVecKeep, dvdson_rtol, kDavidsonPrecondCutoff);
   cudaEvent_t e0, e1;
   C2G_CUDA(cudaEventCreate(&e0));
   C2G_CUDA(cudaEventCreate(&e1));
   float mv_ms = 0.f;
-  auto matvec = [&](const double* x, double* y) {
+  auto matvec = [&](const double* x, double* y, c2g::Precision prec) {
     C2G_CUDA(cudaEventRecord(e0, s));
-    rt->run(*dph, const_cast<double*>(x), y);
+    rt->run(*dph, const_cast<double*>(x), y, prec);
     C2G_CUDA(cudaEventRecord(e1, s));
     C2G_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
     C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     mv_ms += ms;
   };
-  const c2g::DavidsonStats ds = dav.solve(svec, diag, matvec);
+  const c2g::DavidsonStats ds = dav.solve(svec, diag, matvec, precision_ == 1, mixed_tol_);
+  stats_.n_matvec_fp32 += ds.n_matvec_fp32;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   rt->release(diag);
@@ -433,7 +505,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   stats_.n_davidson++;
   stats_.t_matvec += 1e-3 * mv_ms;
   stats_.matvec_flops += static_cast<double>(dph->flops_repeat) * ds.n_matvec;
-  stats_.matvec_bytes += static_cast<double>(ch.operand_bytes + 16 * veclen) * ds.n_matvec;
+  stats_.matvec_bytes += static_cast<double>(heff_operand_bytes + 16 * veclen) * ds.n_matvec;
   const double Energy = ds.energy + Prob->gEconst();
   stats_.last_energy = Energy;
   stats_.t_solve += now() - t0;
@@ -462,10 +534,14 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   rt->zero(work, plan.work_size);
   rt->set_slot(c2g::kSlotWork, work);
   {
-    TaskBuilder tb;
-    c2g::compile_split_assemble(tb, *denBK, S, plan);
-    auto dp = rt->upload(tb.finalize());
-    rt->run(*dp, svec, nullptr);
+    DevProgram& dp = program(dims_key("split_assemble", index, index, index + 2, moving_right ? 1 : 0), [&] {
+      c2g::Compiled c;
+      TaskBuilder tb;
+      c2g::compile_split_assemble(tb, *denBK, S, plan);
+      c.program = tb.finalize();
+      return c;
+    });
+    rt->run(dp, svec, nullptr);
   }
   // Eigendecomposition of every Gram matrix (FP64, cuSOLVER syevd).
   cusolverDnHandle_t sh;
@@ -580,11 +656,16 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     rt->release(old);
   }
   {
-    TaskBuilder tb;
-    c2g::compile_split_copy(tb, plan, dims_m, mps_tensor(mps_lay[index].get(), index),
-                            mps_tensor(mps_lay[index + 1].get(), index + 1));
-    auto dp = rt->upload(tb.finalize());
-    rt->run(*dp, nullptr, nullptr);
+    // keyed on the new dimensions at index + 1 (and the unchanged ones at index, index + 2)
+    DevProgram& dp = program(dims_key("split_copy", index, index, index + 2, moving_right ? 1 : 0), [&] {
+      c2g::Compiled c;
+      TaskBuilder tb;
+      c2g::compile_split_copy(tb, plan, dims_m, mps_tensor(mps_lay[index].get(), index),
+                              mps_tensor(mps_lay[index + 1].get(), index + 1));
+      c.program = tb.finalize();
+      return c;
+    });
+    rt->run(dp, nullptr, nullptr);
   }
   rt->sync();
   rt->set_slot(c2g::kSlotWork, nullptr);
@@ -636,7 +717,8 @@ DMRG::HeffCache& DMRG::heff_program(const int index, const bool with_diag) {
 }
 
 double DMRG::bench_heff(const int index, const int warmup, const int steps, double* flops, double* bytes,
-                        long long* launches, const long long flush_bytes) {
+                        long long* launches, const long long flush_bytes, const int precision) {
+  const c2g::Precision prec = (precision == 1) ? c2g::Precision::kFP32 : c2g::Precision::kFP64;
   cudaStream_t s = rt->stream();
   HeffCache& c = heff_program(index, false);
   const int64_t veclen = c.S->size();
@@ -652,7 +734,7 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   double* flush = nullptr;
   const int64_t nflush = flush_bytes > 0 ? (flush_bytes + 7) / 8 : 0;
   if (nflush > 0) flush = rt->alloc(nflush);
-  for (int i = 0; i < warmup; i++) rt->run(*c.program, x, y);
+  for (int i = 0; i < warmup; i++) rt->run(*c.program, x, y, prec);
   rt->sync();
   const long long l0 = c2g::kernel_launches();
   cudaEvent_t e0, e1;
@@ -662,7 +744,7 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   for (int i = 0; i < steps; i++) {
     if (flush) C2G_CUDA(cudaMemsetAsync(flush, i & 0xff, sizeof(double) * nflush, s));  // evicts L2
     C2G_CUDA(cudaEventRecord(e0, s));
-    rt->run(*c.program, x, y);
+    rt->run(*c.program, x, y, prec);
     C2G_CUDA(cudaEventRecord(e1, s));
     C2G_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -689,7 +771,7 @@ long long DMRG::sobject_size(const int index) const {
 }
 
 void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, double* y, double* diag,
-                           const long long n) {
+                           const long long n, const int precision) {
   if (!x || !y) throw std::invalid_argument("heff_apply: null buffer");
   cudaStream_t s = rt->stream();
   HeffCache& c = heff_program(index, diag != nullptr);
@@ -712,7 +794,7 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
   } else {
     C2G_CUDA(cudaMemcpyAsync(c.xbuf, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
   }
-  rt->run(*c.program, c.xbuf, c.ybuf);
+  rt->run(*c.program, c.xbuf, c.ybuf, precision == 1 ? c2g::Precision::kFP32 : c2g::Precision::kFP64);
   C2G_CUDA(cudaMemcpyAsync(y, c.ybuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   if (diag) {
     int maxdim = 1;

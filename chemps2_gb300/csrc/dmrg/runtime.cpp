@@ -187,12 +187,12 @@ void Runtime::prepare(DevProgram& p) {
   p.prepared = true;
 }
 
-void Runtime::run(DevProgram& p, double* x, double* y) {
+void Runtime::run(DevProgram& p, double* x, double* y, Precision prec) {
   prepare(p);
   const SlotPtrs sp = ptrs(x, y, p.combo);
   for (size_t s = p.first_repeat; s < p.stages.size(); s++) {
     const DevStage& ds = p.stages[s];
-    C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_));
+    C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
     if (ds.ntiles) count_launches(1);
   }
 }

@@ -78,7 +78,9 @@ class Runtime {
 
   std::unique_ptr<DevProgram> upload(const Program& p);
   void prepare(DevProgram& p);
-  void run(DevProgram& p, double* x, double* y);
+  // Runs the repeat stages (preparing first if needed). The combination stage always runs
+  // in FP64; prec selects the arithmetic of the repeat stages.
+  void run(DevProgram& p, double* x, double* y, Precision prec = Precision::kFP64);
 
   const double* ones(int64_t n);
   void sync();

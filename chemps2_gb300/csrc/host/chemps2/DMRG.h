@@ -7,6 +7,7 @@
 // the constructor throws.
 #pragma once
 
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -19,12 +20,15 @@ namespace c2g {
 class Runtime;
 struct BoundaryOps;
 struct MpsLayout;
+struct DevProgram;
+struct Compiled;
 }  // namespace c2g
 
 namespace CheMPS2 {
 
 struct DMRGStats {
   long long n_matvec = 0;         // Heff applications
+  long long n_matvec_fp32 = 0;    // of which with FP32 arithmetic (mixed precision)
   long long n_davidson = 0;       // Davidson solves
   double t_join = 0, t_solve = 0, t_split = 0, t_update = 0;  // seconds, host wall clock
   double t_matvec = 0;            // seconds inside Heff applications (device time)
@@ -56,6 +60,15 @@ class DMRG {
   const DMRGStats& stats() const { return stats_; }
   void reset_stats() { stats_ = DMRGStats(); }
   void set_verbose(bool v) { verbose = v; }
+  // 0: FP64 Heff matvecs (the reference's arithmetic). 1: mixed, the Davidson solver
+  // expands its subspace with FP32-arithmetic matvecs down to residual `mixed_tol`, then
+  // finishes with FP64 matvecs to the instruction's tolerance, so energies and
+  // eigenvectors are FP64 results.
+  void set_precision(int mode, double mixed_tol = 1e-5) {
+    precision_ = mode;
+    mixed_tol_ = mixed_tol;
+  }
+  int get_precision() const { return precision_; }
 
   // One two-site step at sites (index, index + 1): Join, Davidson, Split. Returns the
   // energy (with the constant part). Exposed for the benchmark and tests.
@@ -70,20 +83,30 @@ class DMRG {
   // flush_bytes > 0: a buffer of that size is overwritten before every timed application
   // (outside the timed interval) so that the operators are read from HBM, not L2.
   double bench_heff(const int index, const int warmup, const int steps, double* flops, double* bytes,
-                    long long* launches, const long long flush_bytes = 0);
+                    long long* launches, const long long flush_bytes = 0, const int precision = 0);
 
   // Host-buffer access to the effective Hamiltonian at sites (index, index + 1), in the
   // symmetric convention: y = Heff x (and its diagonal when diag is non-null). With
   // join_into_x, x is first overwritten by the joined current two-site object.
   long long sobject_size(const int index) const;
+  // precision 1: FP32 arithmetic for the matvec (the diagonal stays FP64).
   void heff_apply_host(const int index, const bool join_into_x, double* x, double* y, double* diag,
-                       const long long n);
+                       const long long n, const int precision = 0);
 
  private:
   struct HeffCache;
   HeffCache& heff_program(const int index, const bool with_diag);
   std::unique_ptr<HeffCache> heff_cache_;
   unsigned long long version_ = 0;  // advanced by every change of the MPS or the operators
+
+  // Compiled device programs, keyed by their kind, site and the sector dimensions they
+  // depend on: once the virtual dimensions settle, later sweeps reuse the programs and
+  // only their combination stages (which read operator data) run again.
+  struct ProgramCache;
+  std::unique_ptr<ProgramCache> pcache_;
+  c2g::DevProgram& program(const std::string& key, const std::function<c2g::Compiled()>& build,
+                           long long* operand_bytes = nullptr);
+  std::string dims_key(const char* kind, const int index, const int bmin, const int bmax, const int extra = 0) const;
 
   void setup_mps(int* occupancies);
   void left_normalize_host(int site, std::vector<double>& data);
@@ -95,6 +118,8 @@ class DMRG {
   ConvergenceScheme* OptScheme;
   int L;
   bool verbose = false;
+  int precision_ = 0;
+  double mixed_tol_ = 1e-5;
   std::unique_ptr<SyBookkeeper> denBK;
   std::unique_ptr<c2g::Runtime> rt;
   std::vector<std::unique_ptr<c2g::MpsLayout>> mps_lay;

@@ -98,6 +98,10 @@ int c2g_dmrg_destroy(c2g_dmrg* d);
 int c2g_dmrg_solve(c2g_dmrg* d, double* energy);            /* DMRG::Solve    */
 int c2g_dmrg_presolve(c2g_dmrg* d);                         /* DMRG::PreSolve */
 int c2g_dmrg_set_verbose(c2g_dmrg* d, int verbose);
+/* Arithmetic of the Heff matvecs: 0 FP64 (default, the reference's); 1 mixed (FP32
+ * matvecs inside Davidson down to residual mixed_tol, then FP64 to the instruction's
+ * tolerance). No counterpart in the reference. */
+int c2g_dmrg_set_precision(c2g_dmrg* d, int mode, double mixed_tol);
 int c2g_dmrg_num_mps_var(const c2g_dmrg* d, int* n);        /* DMRG::get_num_mps_var */
 int c2g_dmrg_max_discarded_weight(const c2g_dmrg* d, double* w);
 /* One two-site step (DMRG::solve_site, CheMPS2/DMRG.cpp:404-452) and one operator update
@@ -106,8 +110,9 @@ int c2g_dmrg_solve_site(c2g_dmrg* d, int index, double dvdson_rtol, double noise
                         int change, double* energy);
 int c2g_dmrg_update(c2g_dmrg* d, int index, int moving_right);
 /* Statistics, in this order: n_matvec, n_davidson, t_join, t_solve, t_split, t_update,
- * t_matvec, t_compile, matvec_flops, matvec_bytes, last_energy (seconds, flops, bytes). */
-#define C2G_NUM_STATS 11
+ * t_matvec, t_compile, matvec_flops, matvec_bytes, last_energy, n_matvec_fp32 (seconds,
+ * flops, bytes). */
+#define C2G_NUM_STATS 12
 int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n);
 int c2g_dmrg_reset_stats(c2g_dmrg* d);
 /* Heff applications at sites (index, index + 1) on the current MPS (CheMPS2/Heff.cpp:43-248):
@@ -116,8 +121,8 @@ int c2g_dmrg_reset_stats(c2g_dmrg* d);
  * application, outside the timed interval, so that the operators come from HBM. Returns
  * milliseconds per application, the ledger flops and bytes of one application and the
  * number of kernels launched in the timed region. No counterpart in the reference. */
-int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, long long flush_bytes, double* ms_per_matvec,
-                        double* flops, double* bytes, long long* launches);
+int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, long long flush_bytes, int precision,
+                        double* ms_per_matvec, double* flops, double* bytes, long long* launches);
 
 /* Effective Hamiltonian on host buffers (the path of CheMPS2/Heff.cpp:43-315 with the
  * copies in and out included): n must equal the size of the two-site object at sites
@@ -126,6 +131,9 @@ int c2g_dmrg_bench_heff(c2g_dmrg* d, int index, int warmup, int steps, long long
  * join_into_x != 0, x is first overwritten by the joined current two-site object. */
 int c2g_dmrg_sobject_size(const c2g_dmrg* d, int index, int64_t* n);
 int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, double* y, double* diag, int64_t n);
+/* As c2g_dmrg_heff_apply with the matvec in FP32 arithmetic (operands converted on load,
+ * lane sums in FP32, the output in FP64). No counterpart in the reference. */
+int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64_t n);
 
 #ifdef __cplusplus
 }

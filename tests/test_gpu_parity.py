@@ -193,3 +193,56 @@ def test_kernels_were_launched():
     gpu.heff_apply(4)
     gpu.close()
     assert c2g.kernel_launches() > before
+
+
+def test_fp32_matvec_close_to_fp64():
+    """The FP32-arithmetic matvec of the mixed path: relative error at the FP32 level."""
+    m = models.synthetic_ab_initio(10, 7, 31)
+    ham, prob, scheme = gpu_objects(m, 0, 10, 0, [(64, 1e-10, 1, 0.0, 1e-8)])
+    c2g.srand(4)
+    gpu = c2g.DMRG(prob, scheme)
+    x, y64, _ = gpu.heff_apply(m.L - 2)
+    y32 = gpu.heff_apply_fp32(m.L - 2, x)
+    gpu.close()
+    assert np.linalg.norm(y32 - y64) / np.linalg.norm(y64) < 1e-5
+
+
+def test_mixed_precision_solve_matches_fp64():
+    """Mixed Davidson (FP32 expansion, FP64 finish) reaches the FP64 energies: within
+    1e-8 Ha of the FP64 run and of FCI, and it did use FP32 matvecs."""
+    m = models.synthetic_ab_initio(10, 7, 21)
+    sched = [(300, 1e-10, 4, 0.0, 1e-8)]
+    energies = {}
+    for mode in ("fp64", "mixed"):
+        ham, prob, scheme = gpu_objects(m, 0, 10, 0, sched)
+        c2g.srand(2)
+        gpu = c2g.DMRG(prob, scheme)
+        gpu.set_precision(mode)
+        energies[mode] = gpu.Solve()
+        st = gpu.stats()
+        if mode == "mixed":
+            assert st["n_matvec_fp32"] > 0
+        else:
+            assert st["n_matvec_fp32"] == 0
+        gpu.close()
+    assert abs(energies["mixed"] - energies["fp64"]) < 1e-8
+
+
+def test_program_cache_reuses_programs_across_sweeps():
+    """Once the dimensions settle, later sweeps reuse compiled programs: the host compile
+    time of a repeated sweep is a small fraction of the first one's, with the same energy."""
+    m = models.hubbard(10, 2.0)
+    sched = [(1000, 1e-12, 1, 0.0, 1e-9)]
+    ham, prob, scheme = gpu_objects(m, 0, 10, 0, sched)
+    c2g.srand(3)
+    gpu = c2g.DMRG(prob, scheme)
+    e1 = gpu.Solve()   # dims reach the full space
+    gpu.reset_stats()
+    e2 = gpu.Solve()
+    t2 = gpu.stats()["t_compile"]
+    gpu.reset_stats()
+    e3 = gpu.Solve()
+    t3 = gpu.stats()["t_compile"]
+    gpu.close()
+    assert abs(e3 - e2) < 1e-9 and abs(e2 - e1) < 1e-7
+    assert t3 <= 0.2 * t2 + 0.05
