@@ -325,6 +325,17 @@ void DMRG::delete_all_ops() {
 }
 
 void DMRG::PreSolve() {
+  // The matrix elements may have changed (Problem::setMxElement): compiled programs carry
+  // them in their coefficients, so none may be reused.
+  if (pcache_) {
+    pcache_->map.clear();
+    pcache_->bytes = 0;
+  }
+  if (heff_cache_) {
+    heff_cache_->program.reset();
+    heff_cache_->diag.reset();
+    heff_cache_->index = -1;
+  }
   delete_all_ops();
   for (int cnt = 0; cnt < L - 2; cnt++) update_moving_right(cnt);
   TotalMinEnergy = 1e8;
