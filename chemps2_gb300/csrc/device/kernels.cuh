@@ -33,7 +33,15 @@ struct SlotPtrs {
   double* y;
   double* combo;
   const double* ones;
+  // FP32 copies read by the FP32 variant of the block sandwich (Y stays FP64)
+  const float* const* table32;
+  const float* x32;
+  const float* combo32;
+  const float* ones32;
 };
+
+// dst[i] = (float)src[i]
+cudaError_t launch_to_f32(float* dst, const double* src, int64_t n, cudaStream_t stream);
 
 // A CTA work unit: group index, tile position (row << 16 | col, in units of kTile) and the
 // sub-tile grid (rows << 8 | cols) of the tile, chosen on the host.
@@ -50,8 +58,9 @@ inline int sandwich_grid(int m, int n) {
   return (sr << 8) | sc;
 }
 
-// Arithmetic of the block sandwich: FP64 throughout, or FP32 products and per-lane sums
-// (operands converted on load) with the lane reduction and the output update in FP64.
+// Arithmetic of the block sandwich: FP64 throughout, or FP32 operands (the FP32 copies of
+// SlotPtrs), products and per-lane sums, with the lane reduction and the FP64 output
+// update in FP64. The FP32 variant issues no FP64 instruction in its item loop.
 enum class Precision : int { kFP64 = 0, kFP32 = 1 };
 
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,

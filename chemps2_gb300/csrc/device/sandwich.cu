@@ -1,26 +1,47 @@
 // The block-sandwich kernel: executes one stage of a task program.
 //
-// Operands are FP64 in memory. The FP64 variant computes in FP64; the FP32 variant
-// converts every operand on load and accumulates each lane's items in FP32, while the
-// reduction over lanes and the update of the FP64 output stay in FP64.
+// FP64 variant: FP64 operands and arithmetic. FP32 variant: reads the FP32 copies of the
+// operands (SlotPtrs::table32, x32, combo32) and multiplies / sums in FP32 inside each
+// lane, so its item loop issues no FP64 instruction (on GB300 the FP64 pipe is the
+// bottleneck of the FP64 variant); the lane reduction and the update of the FP64 output
+// stay in FP64.
 #include "kernels.cuh"
 
 namespace c2g {
 
 namespace {
 
-__device__ __forceinline__ const double* resolve(const SlotPtrs& sp, Ref r) {
+template <typename Real>
+struct Tables;
+template <>
+struct Tables<double> {
+  __device__ static const double* get(const SlotPtrs& sp, int s) {
+    switch (s) {
+      case kSlotX: return sp.x;
+      case kSlotY: return sp.y;
+      case kSlotCombo: return sp.combo;
+      case kSlotOnes: return sp.ones;
+      default: return sp.table[s];
+    }
+  }
+};
+template <>
+struct Tables<float> {
+  __device__ static const float* get(const SlotPtrs& sp, int s) {
+    switch (s) {
+      case kSlotX: return sp.x32;
+      case kSlotCombo: return sp.combo32;
+      case kSlotOnes: return sp.ones32;
+      default: return sp.table32[s];
+    }
+  }
+};
+
+template <typename Real>
+__device__ __forceinline__ const Real* resolve(const SlotPtrs& sp, Ref r) {
   const int s = static_cast<int>(r >> kRefShift);
   const int64_t off = static_cast<int64_t>(r & kRefMask);
-  const double* base;
-  switch (s) {
-    case kSlotX: base = sp.x; break;
-    case kSlotY: base = sp.y; break;
-    case kSlotCombo: base = sp.combo; break;
-    case kSlotOnes: base = sp.ones; break;
-    default: base = sp.table[s]; break;
-  }
-  return base + off;
+  return Tables<Real>::get(sp, s) + off;
 }
 
 __device__ __forceinline__ double fmaR(double a, double b, double c) { return fma(a, b, c); }
@@ -28,15 +49,15 @@ __device__ __forceinline__ float fmaR(float a, float b, float c) { return fmaf(a
 
 // acc[ii][jj] (rows i0 + ii, ii < r; columns j0 + jj, jj < c) += one entry of a term.
 template <typename Real>
-__device__ __forceinline__ void sandwich_item(Real (&acc)[kSub][kSub], const Term& T, const double* __restrict__ A,
-                                              const double* __restrict__ B, const double* __restrict__ C, Real al,
-                                              int i0, int j0, int r, int c) {
+__device__ __forceinline__ void sandwich_item(Real (&acc)[kSub][kSub], const Term& T, const Real* __restrict__ A,
+                                              const Real* __restrict__ B, const Real* __restrict__ C, Real al, int i0,
+                                              int j0, int r, int c) {
   const bool ha = T.flags & kHasA, hc = T.flags & kHasC;
   const bool ta = T.flags & kTransA, tb = T.flags & kTransB, tc = T.flags & kTransC;
   const int64_t lda = T.lda, ldb = T.ldb, ldc = T.ldc;
-  auto opA = [&](int i, int k) { return static_cast<Real>(ta ? A[k + lda * i] : A[i + lda * k]); };
-  auto opB = [&](int k, int l) { return static_cast<Real>(tb ? B[l + ldb * k] : B[k + ldb * l]); };
-  auto opC = [&](int l, int j) { return static_cast<Real>(tc ? C[j + ldc * l] : C[l + ldc * j]); };
+  auto opA = [&](int i, int k) { return ta ? A[k + lda * i] : A[i + lda * k]; };
+  auto opB = [&](int k, int l) { return tb ? B[l + ldb * k] : B[k + ldb * l]; };
+  auto opC = [&](int l, int j) { return tc ? C[j + ldc * l] : C[l + ldc * j]; };
   if (ha && hc) {
     if (T.flags & kLeftFirst) {
       for (int l = 0; l < T.k2; l++) {
@@ -156,28 +177,30 @@ __global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group*
       }
       int t = lo;
       Term T = terms[t];
-      const double* B = resolve(sp, T.b);
-      const double* A0 = (T.flags & kHasA) ? resolve(sp, T.a) : nullptr;
-      const double* C0 = (T.flags & kHasC) ? resolve(sp, T.c) : nullptr;
+      const Real* B = resolve<Real>(sp, T.b);
+      const Real* A0 = (T.flags & kHasA) ? resolve<Real>(sp, T.a) : nullptr;
+      const Real* C0 = (T.flags & kHasC) ? resolve<Real>(sp, T.c) : nullptr;
+      Real alpha = static_cast<Real>(T.alpha);
       for (int item = start; item < stop; item++) {
         int p = item - T.item0;
         if (p >= T.count) {
           T = terms[++t];
-          B = resolve(sp, T.b);
-          A0 = (T.flags & kHasA) ? resolve(sp, T.a) : nullptr;
-          C0 = (T.flags & kHasC) ? resolve(sp, T.c) : nullptr;
+          B = resolve<Real>(sp, T.b);
+          A0 = (T.flags & kHasA) ? resolve<Real>(sp, T.a) : nullptr;
+          C0 = (T.flags & kHasC) ? resolve<Real>(sp, T.c) : nullptr;
+          alpha = static_cast<Real>(T.alpha);
           p = 0;
         }
-        double ratio = 1.0;
-        const double* A = A0;
-        const double* C = C0;
+        Real al = alpha;
+        const Real* A = A0;
+        const Real* C = C0;
         if (T.list >= 0) {
           const BatchEntry e = entries[T.list + p];
-          ratio = e.ratio;
+          if (e.ratio != 1.0) al = static_cast<Real>(T.alpha * e.ratio);
           if (A) A += e.da;
           if (C) C += e.dc;
         }
-        sandwich_item<Real>(acc, T, A, B, C, static_cast<Real>(T.alpha * ratio), i0, j0, r, c);
+        sandwich_item<Real>(acc, T, A, B, C, al, i0, j0, r, c);
       }
     }
   }
@@ -186,7 +209,8 @@ __global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group*
 #pragma unroll
     for (int jj = 0; jj < kSub; jj++) red[tid * kSub * kSub + ii * kSub + jj] = static_cast<double>(acc[ii][jj]);
   __syncthreads();
-  double* O = const_cast<double*>(resolve(sp, G.out));
+  // the output is FP64 in both variants
+  double* O = const_cast<double*>(resolve<double>(sp, G.out));
   const int64_t ldo = G.ldo;
   const bool accum = (G.flags & kAccumulate) != 0;
   for (int e = tid; e < tm * tn; e += kSandwichThreads) {
@@ -200,6 +224,12 @@ __global__ void __launch_bounds__(kSandwichThreads) sandwich_kernel(const Group*
   }
 }
 
+__global__ void to_f32_kernel(float* __restrict__ dst, const double* __restrict__ src, int64_t n) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    dst[i] = static_cast<float>(src[i]);
+}
+
 }  // namespace
 
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
@@ -209,6 +239,14 @@ cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchE
     sandwich_kernel<float><<<ntiles, kSandwichThreads, 0, stream>>>(groups, terms, entries, tiles, sp);
   else
     sandwich_kernel<double><<<ntiles, kSandwichThreads, 0, stream>>>(groups, terms, entries, tiles, sp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_f32(float* dst, const double* src, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  to_f32_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(dst, src, n);
   return cudaGetLastError();
 }
 

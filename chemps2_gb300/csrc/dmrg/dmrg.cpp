@@ -149,6 +149,7 @@ DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool, const st
   mps_dev.assign(L, nullptr);
   ops.resize(L - 1);
   ops_dev.assign(L - 1, nullptr);
+  ops_dev32.assign(L - 1, nullptr);
   isAllocated.assign(L - 1, 0);
   setup_mps(occupancies);
   PreSolve();
@@ -169,6 +170,7 @@ DMRG::~DMRG() {
     }
     for (double* p : mps_dev) rt->release(p);
     for (double* p : ops_dev) rt->release(p);
+    for (float* p : ops_dev32) rt->release(p);
     try {
       rt->sync();
     } catch (...) {
@@ -307,6 +309,28 @@ void DMRG::upload_mps(int site, const std::vector<double>& data) {
   rt->set_slot(c2g::kSlotMpsBase + site, mps_dev[site]);
 }
 
+void DMRG::refresh_f32(const int b) {
+  if (!ops[b] || !ops_dev[b]) return;
+  if (ops_dev32[b]) rt->release(ops_dev32[b]);
+  ops_dev32[b] = rt->alloc_f32(ops[b]->size);
+  C2G_CUDA(c2g::launch_to_f32(ops_dev32[b], ops_dev[b], ops[b]->size, rt->stream()));
+  c2g::count_launches(1);
+  rt->set_slot32(c2g::slot_ops(L, b), ops_dev32[b]);
+}
+
+void DMRG::enable_f32_ops() {
+  if (f32_ops_) return;
+  f32_ops_ = true;
+  for (int b = 0; b < L - 1; b++) refresh_f32(b);
+}
+
+void DMRG::set_precision(int mode, double mixed_tol) {
+  if (mode != 0 && mode != 1) throw std::invalid_argument("precision mode must be 0 or 1");
+  precision_ = mode;
+  mixed_tol_ = mixed_tol;
+  if (mode == 1) enable_f32_ops();
+}
+
 int DMRG::get_num_mps_var() const {
   int n = 0;
   for (int s = 0; s < L; s++) n += static_cast<int>(mps_lay[s]->size());
@@ -318,6 +342,9 @@ void DMRG::delete_all_ops() {
   for (int b = 0; b < L - 1; b++) {
     if (ops_dev[b]) rt->release(ops_dev[b]);
     ops_dev[b] = nullptr;
+    if (ops_dev32[b]) rt->release(ops_dev32[b]);
+    ops_dev32[b] = nullptr;
+    rt->set_slot32(c2g::slot_ops(L, b), nullptr);
     ops[b].reset();
     rt->set_slot(c2g::slot_ops(L, b), nullptr);
     isAllocated[b] = 0;
@@ -367,6 +394,7 @@ void DMRG::update_moving_right(const int index) {
                            [&] { return c2g::compile_update_program(ctx); });
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
+  if (f32_ops_) refresh_f32(index);
   rt->sync();
   stats_.t_update += now() - t0;
 }
@@ -396,6 +424,7 @@ void DMRG::update_moving_left(const int index) {
                            [&] { return c2g::compile_update_program(ctx); });
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
+  if (f32_ops_) refresh_f32(index);
   rt->sync();
   stats_.t_update += now() - t0;
 }
@@ -500,7 +529,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   float mv_ms = 0.f;
   auto matvec = [&](const double* x, double* y, c2g::Precision prec) {
     C2G_CUDA(cudaEventRecord(e0, s));
-    rt->run(*dph, const_cast<double*>(x), y, prec);
+    rt->run(*dph, const_cast<double*>(x), y, prec, veclen);
     C2G_CUDA(cudaEventRecord(e1, s));
     C2G_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -745,7 +774,8 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   double* flush = nullptr;
   const int64_t nflush = flush_bytes > 0 ? (flush_bytes + 7) / 8 : 0;
   if (nflush > 0) flush = rt->alloc(nflush);
-  for (int i = 0; i < warmup; i++) rt->run(*c.program, x, y, prec);
+  if (prec == c2g::Precision::kFP32) enable_f32_ops();
+  for (int i = 0; i < warmup; i++) rt->run(*c.program, x, y, prec, veclen);
   rt->sync();
   const long long l0 = c2g::kernel_launches();
   cudaEvent_t e0, e1;
@@ -755,7 +785,7 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   for (int i = 0; i < steps; i++) {
     if (flush) C2G_CUDA(cudaMemsetAsync(flush, i & 0xff, sizeof(double) * nflush, s));  // evicts L2
     C2G_CUDA(cudaEventRecord(e0, s));
-    rt->run(*c.program, x, y, prec);
+    rt->run(*c.program, x, y, prec, veclen);
     C2G_CUDA(cudaEventRecord(e1, s));
     C2G_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -805,7 +835,8 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
   } else {
     C2G_CUDA(cudaMemcpyAsync(c.xbuf, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
   }
-  rt->run(*c.program, c.xbuf, c.ybuf, precision == 1 ? c2g::Precision::kFP32 : c2g::Precision::kFP64);
+  if (precision == 1) enable_f32_ops();
+  rt->run(*c.program, c.xbuf, c.ybuf, precision == 1 ? c2g::Precision::kFP32 : c2g::Precision::kFP64, veclen);
   C2G_CUDA(cudaMemcpyAsync(y, c.ybuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   if (diag) {
     int maxdim = 1;

@@ -28,6 +28,7 @@ DevProgram::~DevProgram() {
   if (rt) {
     if (blob) rt->release(blob);
     if (combo) rt->release(combo);
+    if (combo32) rt->release(combo32);
   }
 }
 
@@ -45,15 +46,19 @@ Runtime::Runtime(int L, int device) : L_(L) {
   uint64_t threshold = UINT64_MAX;
   C2G_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
   host_slots_.assign(kMaxSlots, nullptr);
+  host_slots32_.assign(kMaxSlots, nullptr);
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots_), sizeof(double*) * kMaxSlots));
+  C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots32_), sizeof(float*) * kMaxSlots));
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&partial_), sizeof(double) * (kDotBlocks * 64 + 4096)));
 }
 
 Runtime::~Runtime() {
   if (stream_) cudaStreamSynchronize(stream_);
   if (ones_) cudaFreeAsync(ones_, stream_);
+  if (x32_) cudaFreeAsync(x32_, stream_);
   if (stream_) cudaStreamSynchronize(stream_);
   cudaFree(dev_slots_);
+  cudaFree(dev_slots32_);
   cudaFree(partial_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -81,9 +86,25 @@ void Runtime::set_slot(int slot, double* p) {
   }
 }
 
+void Runtime::set_slot32(int slot, float* p) {
+  if (slot < 0 || slot >= kMaxSlots) throw std::out_of_range("slot");
+  if (host_slots32_[slot] != p) {
+    host_slots32_[slot] = p;
+    slots_dirty_ = true;
+  }
+}
+
+float* Runtime::alloc_f32(int64_t n) {
+  void* p = nullptr;
+  C2G_CUDA(cudaMallocAsync(&p, sizeof(float) * static_cast<size_t>(std::max<int64_t>(n, 1)), stream_));
+  return static_cast<float*>(p);
+}
+
 void Runtime::flush_slots() {
   if (!slots_dirty_) return;
   C2G_CUDA(cudaMemcpyAsync(dev_slots_, host_slots_.data(), sizeof(double*) * kMaxSlots, cudaMemcpyHostToDevice,
+                           stream_));
+  C2G_CUDA(cudaMemcpyAsync(dev_slots32_, host_slots32_.data(), sizeof(float*) * kMaxSlots, cudaMemcpyHostToDevice,
                            stream_));
   // The host vector may change before the copy runs: wait for it.
   C2G_CUDA(cudaStreamSynchronize(stream_));
@@ -109,6 +130,10 @@ SlotPtrs Runtime::ptrs(double* x, double* y, double* combo) {
   sp.y = y;
   sp.combo = combo;
   sp.ones = ones_;
+  sp.table32 = dev_slots32_;
+  sp.x32 = nullptr;
+  sp.combo32 = nullptr;
+  sp.ones32 = nullptr;
   return sp;
 }
 
@@ -185,11 +210,32 @@ void Runtime::prepare(DevProgram& p) {
     if (ds.ntiles) count_launches(1);
   }
   p.prepared = true;
+  p.combo32_ready = false;
 }
 
-void Runtime::run(DevProgram& p, double* x, double* y, Precision prec) {
+void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t xlen) {
   prepare(p);
-  const SlotPtrs sp = ptrs(x, y, p.combo);
+  SlotPtrs sp = ptrs(x, y, p.combo);
+  if (prec == Precision::kFP32) {
+    if (p.combo_size > 0 && !p.combo32_ready) {
+      if (!p.combo32) p.combo32 = alloc_f32(p.combo_size);
+      C2G_CUDA(launch_to_f32(p.combo32, p.combo, p.combo_size, stream_));
+      count_launches(1);
+      p.combo32_ready = true;
+    }
+    sp.combo32 = p.combo32;
+    if (x) {
+      if (xlen <= 0) throw std::invalid_argument("Runtime::run: an FP32 run needs the length of X");
+      if (xlen > x32_cap_) {
+        if (x32_) release(x32_);
+        x32_cap_ = xlen;
+        x32_ = alloc_f32(x32_cap_);
+      }
+      C2G_CUDA(launch_to_f32(x32_, x, xlen, stream_));
+      count_launches(1);
+      sp.x32 = x32_;
+    }
+  }
   for (size_t s = p.first_repeat; s < p.stages.size(); s++) {
     const DevStage& ds = p.stages[s];
     C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));

@@ -49,7 +49,9 @@ struct DevProgram {
   int64_t nterms = 0, nentries = 0, bytes = 0;
   void* blob = nullptr;
   double* combo = nullptr;
+  float* combo32 = nullptr;     // FP32 copy of the combined blocks for FP32 runs
   bool prepared = false;
+  bool combo32_ready = false;
   DevProgram() = default;
   DevProgram(const DevProgram&) = delete;
   DevProgram& operator=(const DevProgram&) = delete;
@@ -75,12 +77,18 @@ class Runtime {
   // Slot table (slots other than X, Y, Combo and Ones).
   void set_slot(int slot, double* p);
   double* slot(int s) const { return host_slots_[s]; }
+  // FP32 copy of a slot's buffer, read by FP32 runs (nullptr: none).
+  void set_slot32(int slot, float* p);
+  float* slot32(int s) const { return host_slots32_[s]; }
+  float* alloc_f32(int64_t n_floats);
 
   std::unique_ptr<DevProgram> upload(const Program& p);
   void prepare(DevProgram& p);
   // Runs the repeat stages (preparing first if needed). The combination stage always runs
-  // in FP64; prec selects the arithmetic of the repeat stages.
-  void run(DevProgram& p, double* x, double* y, Precision prec = Precision::kFP64);
+  // in FP64; prec selects the arithmetic of the repeat stages. An FP32 run converts X
+  // (xlen elements) and the combined blocks to FP32 first and reads the FP32 slot copies
+  // (set_slot32) of every other operand.
+  void run(DevProgram& p, double* x, double* y, Precision prec = Precision::kFP64, int64_t xlen = 0);
 
   const double* ones(int64_t n);
   void sync();
@@ -96,8 +104,12 @@ class Runtime {
   int L_;
   cudaStream_t stream_ = nullptr;
   std::vector<double*> host_slots_;
+  std::vector<float*> host_slots32_;
   const double** dev_slots_ = nullptr;
+  const float** dev_slots32_ = nullptr;
   bool slots_dirty_ = true;
+  float* x32_ = nullptr;  // FP32 copy of the X vector of an FP32 run
+  int64_t x32_cap_ = 0;
   double* ones_ = nullptr;
   int64_t ones_cap_ = 0;
   double* partial_ = nullptr;

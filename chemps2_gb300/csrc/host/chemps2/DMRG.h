@@ -64,10 +64,7 @@ class DMRG {
   // expands its subspace with FP32-arithmetic matvecs down to residual `mixed_tol`, then
   // finishes with FP64 matvecs to the instruction's tolerance, so energies and
   // eigenvectors are FP64 results.
-  void set_precision(int mode, double mixed_tol = 1e-5) {
-    precision_ = mode;
-    mixed_tol_ = mixed_tol;
-  }
+  void set_precision(int mode, double mixed_tol = 1e-5);
   int get_precision() const { return precision_; }
 
   // One two-site step at sites (index, index + 1): Join, Davidson, Split. Returns the
@@ -126,6 +123,10 @@ class DMRG {
   std::vector<double*> mps_dev;
   std::vector<std::unique_ptr<c2g::BoundaryOps>> ops;
   std::vector<double*> ops_dev;
+  std::vector<float*> ops_dev32;  // FP32 copies of the operators, for FP32 matvecs
+  bool f32_ops_ = false;          // keep ops_dev32 current
+  void refresh_f32(const int boundary);
+  void enable_f32_ops();
   std::vector<int> isAllocated;  // 0 none, 1 moving right, 2 moving left
   double TotalMinEnergy = 1e8;
   double LastMinEnergy = 1e8;
