@@ -66,6 +66,17 @@ enum class Precision : int { kFP64 = 0, kFP32 = 1 };
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
                             int ntiles, const SlotPtrs& sp, cudaStream_t stream, Precision prec = Precision::kFP64);
 
+// The cooperative variant for large output tiles and inner dimensions (sandwich_tile.cu):
+// one 256-thread CTA per tile evaluating every item as shared-memory tiled GEMMs.
+cudaError_t launch_sandwich_tiles(const Group* groups, const Term* terms, const BatchEntry* entries,
+                                  const TileDesc* tiles, int ntiles, const SlotPtrs& sp, cudaStream_t stream,
+                                  Precision prec = Precision::kFP64);
+
+// Groups whose tiles hold at least this many elements and whose items average at least
+// kLargeItemFlops go to the cooperative variant.
+constexpr int kLargeTileElems = 256;
+constexpr int64_t kLargeItemFlops = 4096;
+
 // out[j] = sum_i A[i + lda * j] * x[i] for j < ncol (A has n rows). Uses `partial`
 // (at least ncol * kDotBlocks doubles) as scratch.
 constexpr int kDotBlocks = 152;

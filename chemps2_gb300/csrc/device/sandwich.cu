@@ -6,46 +6,11 @@
 // bottleneck of the FP64 variant); the lane reduction and the update of the FP64 output
 // stay in FP64.
 #include "kernels.cuh"
+#include "slots.cuh"
 
 namespace c2g {
 
 namespace {
-
-template <typename Real>
-struct Tables;
-template <>
-struct Tables<double> {
-  __device__ static const double* get(const SlotPtrs& sp, int s) {
-    switch (s) {
-      case kSlotX: return sp.x;
-      case kSlotY: return sp.y;
-      case kSlotCombo: return sp.combo;
-      case kSlotOnes: return sp.ones;
-      default: return sp.table[s];
-    }
-  }
-};
-template <>
-struct Tables<float> {
-  __device__ static const float* get(const SlotPtrs& sp, int s) {
-    switch (s) {
-      case kSlotX: return sp.x32;
-      case kSlotCombo: return sp.combo32;
-      case kSlotOnes: return sp.ones32;
-      default: return sp.table32[s];
-    }
-  }
-};
-
-template <typename Real>
-__device__ __forceinline__ const Real* resolve(const SlotPtrs& sp, Ref r) {
-  const int s = static_cast<int>(r >> kRefShift);
-  const int64_t off = static_cast<int64_t>(r & kRefMask);
-  return Tables<Real>::get(sp, s) + off;
-}
-
-__device__ __forceinline__ double fmaR(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
 
 // acc[ii][jj] (rows i0 + ii, ii < r; columns j0 + jj, jj < c) += one entry of a term.
 template <typename Real>

@@ -143,7 +143,8 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   dp->first_repeat = p.first_repeat_stage;
   dp->combo_size = p.combo_size;
   // Tile lists: every group cut into 32 x 32 tiles, the groups with the most work first.
-  std::vector<std::vector<TileDesc>> tiles(p.stages.size());
+  // Groups with large tiles and heavy items go to the cooperative variant.
+  std::vector<std::vector<TileDesc>> tiles(p.stages.size()), tiles_large(p.stages.size());
   int64_t bytes = align256(sizeof(BatchEntry) * p.entries.size());
   for (size_t s = 0; s < p.stages.size(); s++) {
     const Stage& st = p.stages[s];
@@ -156,14 +157,18 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
       if (G.m <= 0 || G.n <= 0) continue;
       const int tm = (G.m + kTile - 1) / kTile, tn = (G.n + kTile - 1) / kTile;
       if (tm >= 32768 || tn >= 65536) throw std::invalid_argument("output block too large for the tile index");
+      int64_t items = 0;
+      for (int t = G.t0; t < G.t1; t++) items += st.terms[t].count;
+      const bool large = std::min(G.m, kTile) * std::min(G.n, kTile) >= kLargeTileElems &&
+                         G.work >= kLargeItemFlops * std::max<int64_t>(items, 1);
       for (int i = 0; i < tm; i++)
         for (int j = 0; j < tn; j++) {
           const int rows = std::min(kTile, G.m - i * kTile), cols = std::min(kTile, G.n - j * kTile);
-          tiles[s].push_back(TileDesc{g, (i << 16) | j, sandwich_grid(rows, cols), 0});
+          (large ? tiles_large : tiles)[s].push_back(TileDesc{g, (i << 16) | j, sandwich_grid(rows, cols), 0});
         }
     }
     bytes += align256(sizeof(Group) * st.groups.size()) + align256(sizeof(Term) * st.terms.size()) +
-             align256(sizeof(TileDesc) * tiles[s].size());
+             align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size());
   }
   std::vector<char> host(static_cast<size_t>(std::max<int64_t>(bytes, 256)));
   C2G_CUDA(cudaMallocAsync(&dp->blob, std::max<int64_t>(bytes, 256), stream_));
@@ -189,6 +194,9 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     ds.groups = static_cast<const Group*>(put(st.groups.data(), sizeof(Group) * st.groups.size()));
     ds.terms = static_cast<const Term*>(put(st.terms.data(), sizeof(Term) * st.terms.size()));
     ds.tiles = static_cast<const TileDesc*>(put(tiles[s].data(), sizeof(TileDesc) * tiles[s].size()));
+    ds.ntiles_large = static_cast<int>(tiles_large[s].size());
+    ds.tiles_large =
+        static_cast<const TileDesc*>(put(tiles_large[s].data(), sizeof(TileDesc) * tiles_large[s].size()));
     dp->nterms += ds.nterms;
     if (static_cast<int>(s) < dp->first_repeat) dp->flops_once += ds.flops;
     else dp->flops_repeat += ds.flops;
@@ -206,8 +214,9 @@ void Runtime::prepare(DevProgram& p) {
   const SlotPtrs sp = ptrs(nullptr, nullptr, p.combo);
   for (int s = 0; s < p.first_repeat; s++) {
     const DevStage& ds = p.stages[s];
+    C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_));
     C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_));
-    if (ds.ntiles) count_launches(1);
+    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0));
   }
   p.prepared = true;
   p.combo32_ready = false;
@@ -238,8 +247,10 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
   }
   for (size_t s = p.first_repeat; s < p.stages.size(); s++) {
     const DevStage& ds = p.stages[s];
+    C2G_CUDA(
+        launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
     C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
-    if (ds.ntiles) count_launches(1);
+    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0));
   }
 }
 

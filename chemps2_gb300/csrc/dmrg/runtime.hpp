@@ -33,8 +33,9 @@ class Runtime;
 struct DevStage {
   const Group* groups = nullptr;
   const Term* terms = nullptr;
-  const TileDesc* tiles = nullptr;
-  int ngroups = 0, nterms = 0, ntiles = 0;
+  const TileDesc* tiles = nullptr;        // item-parallel variant
+  const TileDesc* tiles_large = nullptr;  // cooperative variant
+  int ngroups = 0, nterms = 0, ntiles = 0, ntiles_large = 0;
   int64_t flops = 0, items = 0;
   std::string name;
 };
