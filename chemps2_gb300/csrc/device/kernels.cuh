@@ -77,6 +77,16 @@ cudaError_t launch_sandwich_tiles(const Group* groups, const Term* terms, const 
 constexpr int kLargeTileElems = 256;
 constexpr int64_t kLargeItemFlops = 4096;
 
+// The team variant for tiles up to kWarpTile x kWarpTile (sandwich_warp.cu): TileDesc::pos
+// counts kWarpTile units and TileDesc::grid holds the tile's capacity class.
+constexpr int kWarpTile = 16;
+__host__ __device__ constexpr int warp_class_id(int rc, int cc) {
+  return (rc <= 2 ? 0 : rc <= 4 ? 1 : rc <= 8 ? 2 : 3) * 4 + (cc <= 2 ? 0 : cc <= 4 ? 1 : cc <= 8 ? 2 : 3);
+}
+cudaError_t launch_sandwich_warp(const Group* groups, const Term* terms, const BatchEntry* entries,
+                                 const TileDesc* tiles, int ntiles, const SlotPtrs& sp, cudaStream_t stream,
+                                 Precision prec = Precision::kFP64);
+
 // out[j] = sum_i A[i + lda * j] * x[i] for j < ncol (A has n rows). Uses `partial`
 // (at least ncol * kDotBlocks doubles) as scratch.
 constexpr int kDotBlocks = 152;

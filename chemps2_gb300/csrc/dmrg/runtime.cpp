@@ -2,9 +2,11 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <sstream>
+#include <tuple>
 
 namespace c2g {
 
@@ -142,12 +144,33 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   dp->rt = this;
   dp->first_repeat = p.first_repeat_stage;
   dp->combo_size = p.combo_size;
-  // Tile lists: every group cut into 32 x 32 tiles, the groups with the most work first.
-  // Groups with large tiles and heavy items go to the cooperative variant.
-  std::vector<std::vector<TileDesc>> tiles(p.stages.size()), tiles_large(p.stages.size());
+  // Tile lists, the groups with the most work first. Groups of at most kWarpTile x
+  // kWarpTile, and larger groups with light items, go to the team variant in kWarpTile
+  // tiles; larger groups with heavy items go to the cooperative variant in kTile tiles.
+  // (C2G_SANDWICH=item routes the light groups to the item-parallel variant instead.)
+  const char* env = std::getenv("C2G_SANDWICH");
+  const bool use_item = env && std::string(env) == "item";
+  const size_t ns = p.stages.size();
+  std::vector<std::vector<TileDesc>> tiles(ns), tiles_large(ns), tiles_warp(ns);
+  // Terms of each group ordered by shape (flags, k1, k2), so that neighbouring items of
+  // the team variant share their loop structure.
+  std::vector<std::vector<Term>> terms(ns);
   int64_t bytes = align256(sizeof(BatchEntry) * p.entries.size());
-  for (size_t s = 0; s < p.stages.size(); s++) {
+  for (size_t s = 0; s < ns; s++) {
     const Stage& st = p.stages[s];
+    terms[s] = st.terms;
+    for (const Group& G : st.groups) {
+      auto first = terms[s].begin() + G.t0, last = terms[s].begin() + G.t1;
+      std::stable_sort(first, last, [](const Term& a, const Term& b) {
+        return std::make_tuple(a.flags, a.k1, a.k2) < std::make_tuple(b.flags, b.k1, b.k2);
+      });
+      int32_t item0 = 0;
+      for (auto it = first; it != last; ++it) {
+        if (it->count < 1) throw std::invalid_argument("task term without items");
+        it->item0 = item0;
+        item0 += it->count;
+      }
+    }
     std::vector<int> order(st.groups.size());
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
@@ -155,20 +178,32 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     for (int g : order) {
       const Group& G = st.groups[g];
       if (G.m <= 0 || G.n <= 0) continue;
-      const int tm = (G.m + kTile - 1) / kTile, tn = (G.n + kTile - 1) / kTile;
-      if (tm >= 32768 || tn >= 65536) throw std::invalid_argument("output block too large for the tile index");
+      if (G.m >= 32768 * kWarpTile || G.n >= 65536 * kWarpTile)
+        throw std::invalid_argument("output block too large for the tile index");
       int64_t items = 0;
       for (int t = G.t0; t < G.t1; t++) items += st.terms[t].count;
-      const bool large = std::min(G.m, kTile) * std::min(G.n, kTile) >= kLargeTileElems &&
+      const bool small = G.m <= kWarpTile && G.n <= kWarpTile;
+      const bool large = !small && std::min(G.m, kTile) * std::min(G.n, kTile) >= kLargeTileElems &&
                          G.work >= kLargeItemFlops * std::max<int64_t>(items, 1);
-      for (int i = 0; i < tm; i++)
-        for (int j = 0; j < tn; j++) {
-          const int rows = std::min(kTile, G.m - i * kTile), cols = std::min(kTile, G.n - j * kTile);
-          (large ? tiles_large : tiles)[s].push_back(TileDesc{g, (i << 16) | j, sandwich_grid(rows, cols), 0});
-        }
+      if (large || use_item) {
+        const int tm = (G.m + kTile - 1) / kTile, tn = (G.n + kTile - 1) / kTile;
+        for (int i = 0; i < tm; i++)
+          for (int j = 0; j < tn; j++) {
+            const int rows = std::min(kTile, G.m - i * kTile), cols = std::min(kTile, G.n - j * kTile);
+            (large ? tiles_large : tiles)[s].push_back(TileDesc{g, (i << 16) | j, sandwich_grid(rows, cols), 0});
+          }
+      } else {
+        const int tm = (G.m + kWarpTile - 1) / kWarpTile, tn = (G.n + kWarpTile - 1) / kWarpTile;
+        for (int i = 0; i < tm; i++)
+          for (int j = 0; j < tn; j++) {
+            const int rows = std::min(kWarpTile, G.m - i * kWarpTile), cols = std::min(kWarpTile, G.n - j * kWarpTile);
+            tiles_warp[s].push_back(TileDesc{g, (i << 16) | j, warp_class_id(rows, cols), 0});
+          }
+      }
     }
     bytes += align256(sizeof(Group) * st.groups.size()) + align256(sizeof(Term) * st.terms.size()) +
-             align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size());
+             align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size()) +
+             align256(sizeof(TileDesc) * tiles_warp[s].size());
   }
   std::vector<char> host(static_cast<size_t>(std::max<int64_t>(bytes, 256)));
   C2G_CUDA(cudaMallocAsync(&dp->blob, std::max<int64_t>(bytes, 256), stream_));
@@ -192,11 +227,14 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     ds.flops = st.flops;
     ds.items = st.items;
     ds.groups = static_cast<const Group*>(put(st.groups.data(), sizeof(Group) * st.groups.size()));
-    ds.terms = static_cast<const Term*>(put(st.terms.data(), sizeof(Term) * st.terms.size()));
+    ds.terms = static_cast<const Term*>(put(terms[s].data(), sizeof(Term) * terms[s].size()));
     ds.tiles = static_cast<const TileDesc*>(put(tiles[s].data(), sizeof(TileDesc) * tiles[s].size()));
     ds.ntiles_large = static_cast<int>(tiles_large[s].size());
     ds.tiles_large =
         static_cast<const TileDesc*>(put(tiles_large[s].data(), sizeof(TileDesc) * tiles_large[s].size()));
+    ds.ntiles_warp = static_cast<int>(tiles_warp[s].size());
+    ds.tiles_warp =
+        static_cast<const TileDesc*>(put(tiles_warp[s].data(), sizeof(TileDesc) * tiles_warp[s].size()));
     dp->nterms += ds.nterms;
     if (static_cast<int>(s) < dp->first_repeat) dp->flops_once += ds.flops;
     else dp->flops_repeat += ds.flops;
@@ -215,8 +253,9 @@ void Runtime::prepare(DevProgram& p) {
   for (int s = 0; s < p.first_repeat; s++) {
     const DevStage& ds = p.stages[s];
     C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_));
+    C2G_CUDA(launch_sandwich_warp(ds.groups, ds.terms, p.entries, ds.tiles_warp, ds.ntiles_warp, sp, stream_));
     C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_));
-    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0));
+    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + (ds.ntiles_warp > 0));
   }
   p.prepared = true;
   p.combo32_ready = false;
@@ -249,8 +288,9 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
     const DevStage& ds = p.stages[s];
     C2G_CUDA(
         launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
+    C2G_CUDA(launch_sandwich_warp(ds.groups, ds.terms, p.entries, ds.tiles_warp, ds.ntiles_warp, sp, stream_, prec));
     C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
-    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0));
+    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + (ds.ntiles_warp > 0));
   }
 }
 

@@ -35,7 +35,8 @@ struct DevStage {
   const Term* terms = nullptr;
   const TileDesc* tiles = nullptr;        // item-parallel variant
   const TileDesc* tiles_large = nullptr;  // cooperative variant
-  int ngroups = 0, nterms = 0, ntiles = 0, ntiles_large = 0;
+  const TileDesc* tiles_warp = nullptr;   // team variant
+  int ngroups = 0, nterms = 0, ntiles = 0, ntiles_large = 0, ntiles_warp = 0;
   int64_t flops = 0, items = 0;
   std::string name;
 };
