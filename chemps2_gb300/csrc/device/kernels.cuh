@@ -77,15 +77,78 @@ cudaError_t launch_sandwich_tiles(const Group* groups, const Term* terms, const 
 constexpr int kLargeTileElems = 256;
 constexpr int64_t kLargeItemFlops = 4096;
 
-// The team variant for tiles up to kWarpTile x kWarpTile (sandwich_warp.cu): TileDesc::pos
-// counts kWarpTile units and TileDesc::grid holds the tile's capacity class.
+// The team variant for tiles up to kWarpTile x kWarpTile (sandwich_warp.cuh). Its tile
+// class is (row class * kWarpColClasses + column class); row capacities 2, 4, 6, 8, 12,
+// 16, column capacities 2, 4, 8, 12, 16. A tile whose items are split over `nsplit` CTAs
+// (split-items) has its partial sums written to `partials` (split s at part + s * rows *
+// cols) and summed, in split order, by the CTA that finishes last (per-tile arrival
+// counter, reset by that CTA).
 constexpr int kWarpTile = 16;
-__host__ __device__ constexpr int warp_class_id(int rc, int cc) {
-  return (rc <= 2 ? 0 : rc <= 4 ? 1 : rc <= 8 ? 2 : 3) * 4 + (cc <= 2 ? 0 : cc <= 4 ? 1 : cc <= 8 ? 2 : 3);
+constexpr int kWarpColClasses = 5;
+constexpr int kWarpRowClasses = 6;
+inline int warp_class_id(int rows, int cols) {
+  const int rc = rows <= 2 ? 0 : rows <= 4 ? 1 : rows <= 6 ? 2 : rows <= 8 ? 3 : rows <= 12 ? 4 : 5;
+  const int cc = cols <= 2 ? 0 : cols <= 4 ? 1 : cols <= 8 ? 2 : cols <= 12 ? 3 : 4;
+  return rc * kWarpColClasses + cc;
 }
-cudaError_t launch_sandwich_warp(const Group* groups, const Term* terms, const BatchEntry* entries,
-                                 const TileDesc* tiles, int ntiles, const SlotPtrs& sp, cudaStream_t stream,
-                                 Precision prec = Precision::kFP64);
+inline int warp_row_class(int class_id) { return class_id / kWarpColClasses; }
+
+struct WarpTile {   // 48 bytes
+  int32_t group;
+  int32_t pos;      // row << 16 | col, in units of kWarpTile
+  int32_t cls;      // tile class
+  int32_t item0, item1;  // the CTA's items [item0, item1) of the group
+  int32_t nsplit, split;
+  int32_t counter;  // arrival counter of a split tile
+  int64_t part;     // first double of the tile's partial sums (split tiles)
+  int64_t pad;
+};
+
+struct WarpLaunch {
+  const Group* groups;
+  const Term* terms;
+  const BatchEntry* entries;
+  const WarpTile* tiles;   // ordered by row class
+  double* partials;
+  unsigned int* counters;  // zero between launches
+};
+
+// Kernel of row class R (sandwich_warp_r<R>.cu) over `ntiles` tiles of that class.
+template <int R>
+cudaError_t launch_sandwich_warp_class(const WarpLaunch& w, const WarpTile* tiles, int ntiles, const SlotPtrs& sp,
+                                       cudaStream_t stream, Precision prec);
+extern template cudaError_t launch_sandwich_warp_class<0>(const WarpLaunch&, const WarpTile*, int, const SlotPtrs&,
+                                                          cudaStream_t, Precision);
+extern template cudaError_t launch_sandwich_warp_class<1>(const WarpLaunch&, const WarpTile*, int, const SlotPtrs&,
+                                                          cudaStream_t, Precision);
+extern template cudaError_t launch_sandwich_warp_class<2>(const WarpLaunch&, const WarpTile*, int, const SlotPtrs&,
+                                                          cudaStream_t, Precision);
+extern template cudaError_t launch_sandwich_warp_class<3>(const WarpLaunch&, const WarpTile*, int, const SlotPtrs&,
+                                                          cudaStream_t, Precision);
+extern template cudaError_t launch_sandwich_warp_class<4>(const WarpLaunch&, const WarpTile*, int, const SlotPtrs&,
+                                                          cudaStream_t, Precision);
+extern template cudaError_t launch_sandwich_warp_class<5>(const WarpLaunch&, const WarpTile*, int, const SlotPtrs&,
+                                                          cudaStream_t, Precision);
+
+// The team variant over w.tiles (counts[r] tiles of row class r, in class order); returns
+// the number of kernels launched in *launched.
+inline cudaError_t launch_sandwich_warp(const WarpLaunch& w, const int (&counts)[kWarpRowClasses], const SlotPtrs& sp,
+                                        cudaStream_t stream, Precision prec, int* launched) {
+  using Fn = cudaError_t (*)(const WarpLaunch&, const WarpTile*, int, const SlotPtrs&, cudaStream_t, Precision);
+  static constexpr Fn fns[kWarpRowClasses] = {launch_sandwich_warp_class<0>, launch_sandwich_warp_class<1>,
+                                              launch_sandwich_warp_class<2>, launch_sandwich_warp_class<3>,
+                                              launch_sandwich_warp_class<4>, launch_sandwich_warp_class<5>};
+  *launched = 0;
+  int off = 0;
+  for (int r = 0; r < kWarpRowClasses; r++) {
+    if (counts[r] <= 0) continue;
+    const cudaError_t e = fns[r](w, w.tiles + off, counts[r], sp, stream, prec);
+    if (e != cudaSuccess) return e;
+    off += counts[r];
+    ++*launched;
+  }
+  return cudaSuccess;
+}
 
 // out[j] = sum_i A[i + lda * j] * x[i] for j < ncol (A has n rows). Uses `partial`
 // (at least ncol * kDotBlocks doubles) as scratch.

@@ -13,6 +13,28 @@ namespace c2g {
 namespace {
 std::atomic<int64_t> g_launches{0};
 inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
+
+// A team-variant tile before its items are split.
+struct PendingTile {
+  int group, pos, rows, cols;
+  int64_t work;
+};
+
+// Scheduling weight of one item of a term on a rows x cols tile: its flops plus a fixed
+// per-item cost (term lookup, batch entry, pointer setup).
+int64_t item_cost(const Term& t, int rows, int cols) { return term_flops(t, rows, cols) + 64; }
+
+// Slots (concurrently evaluated items) of a team-variant CTA of tile class `cls`.
+int warp_slots(int cls) {
+  static const int gr[kWarpRowClasses] = {1, 1, 2, 2, 4, 4};
+  static const int gc[kWarpColClasses] = {1, 2, 4, 4, 8};
+  return 4 * 32 / (gr[warp_row_class(cls)] * gc[cls % kWarpColClasses]);
+}
+
+// The team variant spreads a stage over at least this many CTA-sized pieces of work, and
+// splits a tile over at most kWarpMaxSplit CTAs.
+constexpr int64_t kWarpCtaTarget = 2048;
+constexpr int kWarpMaxSplit = 64;
 }  // namespace
 
 int64_t kernel_launches() { return g_launches.load(); }
@@ -31,6 +53,8 @@ DevProgram::~DevProgram() {
     if (blob) rt->release(blob);
     if (combo) rt->release(combo);
     if (combo32) rt->release(combo32);
+    if (partials) rt->release(partials);
+    if (counters) rt->release(counters);
   }
 }
 
@@ -151,7 +175,9 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   const char* env = std::getenv("C2G_SANDWICH");
   const bool use_item = env && std::string(env) == "item";
   const size_t ns = p.stages.size();
-  std::vector<std::vector<TileDesc>> tiles(ns), tiles_large(ns), tiles_warp(ns);
+  std::vector<std::vector<TileDesc>> tiles(ns), tiles_large(ns);
+  std::vector<std::vector<WarpTile>> tiles_warp(ns);
+  int64_t part_doubles = 0, ncounters = 0;
   // Terms of each group ordered by shape (flags, k1, k2), so that neighbouring items of
   // the team variant share their loop structure.
   std::vector<std::vector<Term>> terms(ns);
@@ -171,6 +197,8 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
         item0 += it->count;
       }
     }
+    std::vector<PendingTile> pending;
+    int64_t warp_work = 0;
     std::vector<int> order(st.groups.size());
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
@@ -197,13 +225,70 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
         for (int i = 0; i < tm; i++)
           for (int j = 0; j < tn; j++) {
             const int rows = std::min(kWarpTile, G.m - i * kWarpTile), cols = std::min(kWarpTile, G.n - j * kWarpTile);
-            tiles_warp[s].push_back(TileDesc{g, (i << 16) | j, warp_class_id(rows, cols), 0});
+            pending.push_back(PendingTile{g, (i << 16) | j, rows, cols, 0});
+            for (int t = G.t0; t < G.t1; t++)
+              pending.back().work += terms[s][t].count * item_cost(terms[s][t], rows, cols);
+            warp_work += pending.back().work;
           }
       }
     }
+    // Team-variant tiles: heavy tiles have their items split over several CTAs so that the
+    // stage's work is spread over at least kWarpCtaTarget CTA-sized pieces.
+    const int64_t piece = std::max<int64_t>(warp_work / kWarpCtaTarget, 1);
+    int64_t part_off = 0, counter = 0;
+    for (const PendingTile& pt : pending) {
+      const Group& G = st.groups[pt.group];
+      const int cls = warp_class_id(pt.rows, pt.cols);
+      const int total = G.t1 > G.t0 ? terms[s][G.t1 - 1].item0 + terms[s][G.t1 - 1].count : 0;
+      const int min_items = 2 * warp_slots(cls);
+      int nsplit = static_cast<int>(std::min<int64_t>((pt.work + piece - 1) / piece, kWarpMaxSplit));
+      nsplit = std::max(1, std::min(nsplit, total / std::max(min_items, 1)));
+      WarpTile wt{};
+      wt.group = pt.group;
+      wt.pos = pt.pos;
+      wt.cls = cls;
+      wt.nsplit = nsplit;
+      if (nsplit > 1) {
+        wt.part = part_off;
+        wt.counter = static_cast<int32_t>(counter++);
+        part_off += static_cast<int64_t>(nsplit) * pt.rows * pt.cols;
+      }
+      // item boundaries at equal shares of the tile's work
+      int t = G.t0;
+      int64_t before = 0;  // work of the items before term t
+      int start = 0;
+      for (int k = 0; k < nsplit; k++) {
+        int stop = total;
+        if (k + 1 < nsplit) {
+          const int64_t target = pt.work * (k + 1) / nsplit;
+          while (t < G.t1 && before + terms[s][t].count * item_cost(terms[s][t], pt.rows, pt.cols) < target) {
+            before += terms[s][t].count * item_cost(terms[s][t], pt.rows, pt.cols);
+            t++;
+          }
+          stop = total;
+          if (t < G.t1) {
+            const int64_t c = item_cost(terms[s][t], pt.rows, pt.cols);
+            const int64_t inside = (target - before + c - 1) / c;
+            stop = terms[s][t].item0 + static_cast<int>(std::min<int64_t>(inside, terms[s][t].count));
+          }
+          stop = std::max(stop, start);
+        }
+        wt.split = k;
+        wt.item0 = start;
+        wt.item1 = stop;
+        tiles_warp[s].push_back(wt);
+        start = stop;
+      }
+    }
+    part_doubles = std::max(part_doubles, part_off);
+    ncounters = std::max(ncounters, counter);
+    // team-variant tiles ordered by row class (one kernel per class), work order kept
+    std::stable_sort(tiles_warp[s].begin(), tiles_warp[s].end(), [](const WarpTile& a, const WarpTile& b) {
+      return warp_row_class(a.cls) < warp_row_class(b.cls);
+    });
     bytes += align256(sizeof(Group) * st.groups.size()) + align256(sizeof(Term) * st.terms.size()) +
              align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size()) +
-             align256(sizeof(TileDesc) * tiles_warp[s].size());
+             align256(sizeof(WarpTile) * tiles_warp[s].size());
   }
   std::vector<char> host(static_cast<size_t>(std::max<int64_t>(bytes, 256)));
   C2G_CUDA(cudaMallocAsync(&dp->blob, std::max<int64_t>(bytes, 256), stream_));
@@ -233,8 +318,9 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     ds.tiles_large =
         static_cast<const TileDesc*>(put(tiles_large[s].data(), sizeof(TileDesc) * tiles_large[s].size()));
     ds.ntiles_warp = static_cast<int>(tiles_warp[s].size());
+    for (const WarpTile& wt : tiles_warp[s]) ds.nwarp[warp_row_class(wt.cls)]++;
     ds.tiles_warp =
-        static_cast<const TileDesc*>(put(tiles_warp[s].data(), sizeof(TileDesc) * tiles_warp[s].size()));
+        static_cast<const WarpTile*>(put(tiles_warp[s].data(), sizeof(WarpTile) * tiles_warp[s].size()));
     dp->nterms += ds.nterms;
     if (static_cast<int>(s) < dp->first_repeat) dp->flops_once += ds.flops;
     else dp->flops_repeat += ds.flops;
@@ -244,6 +330,11 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   C2G_CUDA(cudaMemcpyAsync(dp->blob, host.data(), bytes, cudaMemcpyHostToDevice, stream_));
   C2G_CUDA(cudaStreamSynchronize(stream_));  // `host` goes out of scope
   if (dp->combo_size > 0) dp->combo = alloc(dp->combo_size);
+  if (part_doubles > 0) dp->partials = alloc(part_doubles);
+  if (ncounters > 0) {
+    C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dp->counters), sizeof(unsigned) * ncounters, stream_));
+    C2G_CUDA(cudaMemsetAsync(dp->counters, 0, sizeof(unsigned) * ncounters, stream_));
+  }
   return dp;
 }
 
@@ -253,9 +344,11 @@ void Runtime::prepare(DevProgram& p) {
   for (int s = 0; s < p.first_repeat; s++) {
     const DevStage& ds = p.stages[s];
     C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_));
-    C2G_CUDA(launch_sandwich_warp(ds.groups, ds.terms, p.entries, ds.tiles_warp, ds.ntiles_warp, sp, stream_));
+    int nw = 0;
+    const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, p.partials, p.counters};
+    C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, Precision::kFP64, &nw));
     C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_));
-    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + (ds.ntiles_warp > 0));
+    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
   }
   p.prepared = true;
   p.combo32_ready = false;
@@ -288,9 +381,11 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
     const DevStage& ds = p.stages[s];
     C2G_CUDA(
         launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
-    C2G_CUDA(launch_sandwich_warp(ds.groups, ds.terms, p.entries, ds.tiles_warp, ds.ntiles_warp, sp, stream_, prec));
+    int nw = 0;
+    const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, p.partials, p.counters};
+    C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, prec, &nw));
     C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
-    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + (ds.ntiles_warp > 0));
+    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
   }
 }
 

@@ -35,8 +35,9 @@ struct DevStage {
   const Term* terms = nullptr;
   const TileDesc* tiles = nullptr;        // item-parallel variant
   const TileDesc* tiles_large = nullptr;  // cooperative variant
-  const TileDesc* tiles_warp = nullptr;   // team variant
+  const WarpTile* tiles_warp = nullptr;   // team variant, ordered by row class
   int ngroups = 0, nterms = 0, ntiles = 0, ntiles_large = 0, ntiles_warp = 0;
+  int nwarp[kWarpRowClasses] = {};        // team-variant tiles per row class
   int64_t flops = 0, items = 0;
   std::string name;
 };
@@ -52,6 +53,8 @@ struct DevProgram {
   void* blob = nullptr;
   double* combo = nullptr;
   float* combo32 = nullptr;     // FP32 copy of the combined blocks for FP32 runs
+  double* partials = nullptr;   // partial sums of split team-variant tiles (shared by the stages)
+  unsigned int* counters = nullptr;  // their arrival counters
   bool prepared = false;
   bool combo32_ready = false;
   DevProgram() = default;
