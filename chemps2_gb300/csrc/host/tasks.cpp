@@ -20,8 +20,6 @@ inline Shape op_shape(const Blk& b, bool t) { return t ? Shape{b.cols, b.rows} :
   throw std::logic_error(std::string("task compiler: inconsistent block shapes in ") + what);
 }
 
-void append_bytes(std::string& s, const void* p, size_t n) { s.append(static_cast<const char*>(p), n); }
-
 inline uint64_t fmix(uint64_t x) {
   x ^= x >> 33;
   x *= 0xff51afd7ed558ccdull;
@@ -152,21 +150,28 @@ void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha
 Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int rows, int cols,
                          const std::vector<bool>* transposed) {
   if (parts.empty()) return Blk();
-  std::string key;
-  key.reserve(parts.size() * 24 + 8);
+  std::vector<uint64_t>& key = key_scratch_;
+  key.clear();
   for (size_t i = 0; i < parts.size(); i++) {
     const bool t = transposed ? (*transposed)[i] : false;
     const Shape s = op_shape(parts[i].second, t);
     if (s.r != rows || s.c != cols) shape_error("combine");
-    append_bytes(key, &parts[i].first, sizeof(double));
-    append_bytes(key, &parts[i].second.ref, sizeof(Ref));
-    append_bytes(key, &parts[i].second.ld, sizeof(int));
-    key.push_back(t ? 'T' : 'N');
+    uint64_t a;
+    std::memcpy(&a, &parts[i].first, sizeof(a));
+    key.push_back(a);
+    key.push_back(parts[i].second.ref);
+    key.push_back((uint64_t(uint32_t(parts[i].second.ld)) << 1) | (t ? 1u : 0u));
   }
-  append_bytes(key, &rows, sizeof(int));
-  append_bytes(key, &cols, sizeof(int));
-  auto it = combo_cache_.find(key);
-  if (it != combo_cache_.end()) return it->second;
+  key.push_back((uint64_t(uint32_t(rows)) << 32) | uint32_t(cols));
+  uint64_t h = 0x243f6a8885a308d3ull;
+  for (uint64_t w : key) h = mix(h, w);
+  auto range = combo_index_.equal_range(h);
+  for (auto it = range.first; it != range.second; ++it) {
+    const ComboEntry& e = combo_entries_[it->second];
+    if (e.nwords == static_cast<int32_t>(key.size()) &&
+        std::memcmp(combo_words_.data() + e.word0, key.data(), sizeof(uint64_t) * key.size()) == 0)
+      return e.out;
+  }
   for (const auto& pr : parts) note_operand(pr.second);
   const Blk out = Blk::make(make_ref(kSlotCombo, combo_size_), rows, cols);
   combo_size_ = align4(combo_size_ + int64_t(rows) * cols);
@@ -174,7 +179,9 @@ Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int r
     const bool t = transposed ? (*transposed)[i] : false;
     add(combo_, false, out, parts[i].first, Blk(), false, parts[i].second, t, Blk(), false, false);
   }
-  combo_cache_.emplace(std::move(key), out);
+  combo_index_.emplace(h, static_cast<int32_t>(combo_entries_.size()));
+  combo_entries_.push_back(ComboEntry{static_cast<int64_t>(combo_words_.size()), static_cast<int32_t>(key.size()), out});
+  combo_words_.insert(combo_words_.end(), key.begin(), key.end());
   return out;
 }
 
@@ -228,11 +235,10 @@ void TaskBuilder::next_stage(const std::string& name) {
 }
 
 Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<BatchEntry>& table,
-                         std::unordered_map<std::string, int32_t>& lists) {
+                         std::unordered_multimap<uint64_t, int32_t>& lists) {
   Stage st;
   st.name = name;
   st.groups = sb.groups;
-  std::string key;
   for (size_t g = 0; g < sb.groups.size(); g++) {
     Group& G = st.groups[g];
     G.t0 = static_cast<int32_t>(st.terms.size());
@@ -246,19 +252,34 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
         if (ab < bc) t.flags |= kLeftFirst;
       }
       if (!pt.entries.empty()) {
-        key.clear();
+        // the list is entry 0 (the term itself) followed by pt.entries
         const BatchEntry first{0, 0, 1.0};
-        append_bytes(key, &first, sizeof(BatchEntry));
-        append_bytes(key, pt.entries.data(), sizeof(BatchEntry) * pt.entries.size());
-        auto it = lists.find(key);
-        if (it == lists.end()) {
-          const int32_t off = static_cast<int32_t>(table.size());
+        const size_t n = pt.entries.size();
+        uint64_t h = mix(0x13198a2e03707344ull, n);
+        for (const BatchEntry& e : pt.entries) {
+          uint64_t r;
+          std::memcpy(&r, &e.ratio, sizeof(r));
+          h = mix(mix(mix(h, static_cast<uint64_t>(e.da)), static_cast<uint64_t>(e.dc)), r);
+        }
+        int32_t found = -1;
+        auto range = lists.equal_range(h);
+        for (auto it = range.first; it != range.second && found < 0; ++it) {
+          if (it->second + 1 + n > table.size()) continue;
+          const BatchEntry* l = table.data() + it->second;
+          bool same = l[0].da == 0 && l[0].dc == 0 && l[0].ratio == 1.0;
+          for (size_t q = 0; same && q < n; q++)
+            same = l[q + 1].da == pt.entries[q].da && l[q + 1].dc == pt.entries[q].dc &&
+                   std::memcmp(&l[q + 1].ratio, &pt.entries[q].ratio, sizeof(double)) == 0;
+          if (same) found = it->second;
+        }
+        if (found < 0) {
+          found = static_cast<int32_t>(table.size());
           table.push_back(first);
           table.insert(table.end(), pt.entries.begin(), pt.entries.end());
-          it = lists.emplace(key, off).first;
+          lists.emplace(h, found);
         }
-        t.list = it->second;
-        t.count = static_cast<int32_t>(pt.entries.size()) + 1;
+        t.list = found;
+        t.count = static_cast<int32_t>(n) + 1;
       }
       items += t.count;
       st.items += t.count;
@@ -273,7 +294,7 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
 
 Program TaskBuilder::finalize(bool keep_empty) {
   Program p;
-  std::unordered_map<std::string, int32_t> lists;
+  std::unordered_multimap<uint64_t, int32_t> lists;
   if (!combo_.groups.empty() || keep_empty) {
     p.stages.push_back(lower(combo_, "combine", p.entries, lists));
     p.first_repeat_stage = 1;
@@ -301,38 +322,70 @@ Program merge_programs(std::vector<Program>& parts) {
   }
   if (eb > INT32_MAX) throw std::length_error("merge_programs: batch table too large");
   out.combo_size = cb;
-  out.entries.reserve(eb);
-  for (auto& p : parts) {
-    out.entries.insert(out.entries.end(), p.entries.begin(), p.entries.end());
-    std::vector<BatchEntry>().swap(p.entries);
+  out.entries.resize(eb);
+  {
+    auto copy_entries = [&](size_t i) {
+      std::copy(parts[i].entries.begin(), parts[i].entries.end(), out.entries.begin() + entry_base[i]);
+      std::vector<BatchEntry>().swap(parts[i].entries);
+    };
+    std::vector<std::thread> th;
+    for (size_t i = 0; i < parts.size(); i++) {
+      if (eb < 65536) copy_entries(i);
+      else th.emplace_back(copy_entries, i);
+    }
+    for (auto& t : th) t.join();
   }
   auto reloc = [&](Ref r, size_t i) -> Ref {
     if (r != 0 && ref_slot(r) == kSlotCombo) return make_ref(kSlotCombo, ref_off(r) + combo_base[i]);
     return r;
   };
+  // Stage by stage: the parts' groups and terms are relocated into their final positions
+  // by one thread per part.
+  const size_t np = parts.size();
   for (size_t s = 0; s < ns; s++) {
     Stage st;
     st.name = parts[0].stages[s].name;
-    for (size_t i = 0; i < parts.size(); i++) {
+    std::vector<size_t> gbase(np + 1, 0), tbase(np + 1, 0);
+    for (size_t i = 0; i < np; i++) {
+      gbase[i + 1] = gbase[i] + parts[i].stages[s].groups.size();
+      tbase[i + 1] = tbase[i] + parts[i].stages[s].terms.size();
+      st.flops += parts[i].stages[s].flops;
+      st.items += parts[i].stages[s].items;
+    }
+    if (tbase[np] > size_t(INT32_MAX)) throw std::length_error("merge_programs: too many terms in a stage");
+    st.groups.resize(gbase[np]);
+    st.terms.resize(tbase[np]);
+    auto relocate = [&](size_t i) {
       Stage& ps = parts[i].stages[s];
-      const int32_t toff = static_cast<int32_t>(st.terms.size());
-      for (Group g : ps.groups) {
+      const int32_t toff = static_cast<int32_t>(tbase[i]);
+      Group* gd = st.groups.data() + gbase[i];
+      for (size_t k = 0; k < ps.groups.size(); k++) {
+        Group g = ps.groups[k];
         g.out = reloc(g.out, i);
         g.t0 += toff;
         g.t1 += toff;
-        st.groups.push_back(g);
+        gd[k] = g;
       }
-      for (Term t : ps.terms) {
+      Term* td = st.terms.data() + tbase[i];
+      const int32_t lbase = static_cast<int32_t>(entry_base[i]);
+      for (size_t k = 0; k < ps.terms.size(); k++) {
+        Term t = ps.terms[k];
         if (t.flags & kHasA) t.a = reloc(t.a, i);
         t.b = reloc(t.b, i);
         if (t.flags & kHasC) t.c = reloc(t.c, i);
-        if (t.list >= 0) t.list += static_cast<int32_t>(entry_base[i]);
-        st.terms.push_back(t);
+        if (t.list >= 0) t.list += lbase;
+        td[k] = t;
       }
-      st.flops += ps.flops;
-      st.items += ps.items;
       std::vector<Group>().swap(ps.groups);
       std::vector<Term>().swap(ps.terms);
+    };
+    if (tbase[np] < 65536 || np == 1) {
+      for (size_t i = 0; i < np; i++) relocate(i);
+    } else {
+      std::vector<std::thread> th;
+      th.reserve(np);
+      for (size_t i = 0; i < np; i++) th.emplace_back(relocate, i);
+      for (auto& t : th) t.join();
     }
     const bool once = (s == 0 && parts[0].first_repeat_stage == 1);
     if (st.groups.empty()) continue;

@@ -200,7 +200,17 @@ class TaskBuilder {
 
   StageBuf combo_;
   int64_t combo_size_ = 0;
-  std::unordered_map<std::string, Blk> combo_cache_;
+  // Combination cache: key words of every combined block in one arena, looked up by hash
+  // and compared exactly.
+  struct ComboEntry {
+    int64_t word0;
+    int32_t nwords;
+    Blk out;
+  };
+  std::unordered_multimap<uint64_t, int32_t> combo_index_;
+  std::vector<ComboEntry> combo_entries_;
+  std::vector<uint64_t> combo_words_;
+  std::vector<uint64_t> key_scratch_;
   std::vector<StageBuf> stages_;
   std::unordered_map<BatchKey, int, BatchKeyHash> open_;  // term index within its group
   std::unordered_map<Ref, bool> written_;                  // outputs written by closed stages
@@ -217,8 +227,9 @@ class TaskBuilder {
   int group_for(StageBuf& sb, const Blk& out, bool accumulate);
   void add(StageBuf& sb, bool batchable, const Blk& out, double alpha, const Blk& A, bool ta, const Blk& B, bool tb,
            const Blk& C, bool tc, bool accumulate);
+  // lists: batch lists already in `table`, by hash of their entries
   static Stage lower(StageBuf& sb, const std::string& name, std::vector<BatchEntry>& table,
-                     std::unordered_map<std::string, int32_t>& lists);
+                     std::unordered_multimap<uint64_t, int32_t>& lists);
 };
 
 // Concatenates programs compiled (with keep_empty) from disjoint output shards into one
