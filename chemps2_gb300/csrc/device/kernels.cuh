@@ -173,6 +173,14 @@ cudaError_t launch_reverse_columns(double* dst, const double* src, int rows, int
 // Davidson device steps (CheMPS2/Davidson.cpp). `sc` is a small device scratch of
 // scalars; layout documented in kernels.cu.
 cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream);
+// Batched Jacobi eigendecompositions of the Gram matrices of the truncation step, one CTA
+// per job (n <= kBatchedEigMax); offsets in doubles from `base` (jobs on the device).
+constexpr int kBatchedEigMax = 32;
+struct EigJob {
+  int32_t n, pad;
+  int64_t offG, offE, offU;
+};
+cudaError_t launch_batched_eig(const EigJob* jobs, int njobs, double* base, cudaStream_t stream);
 cudaError_t launch_residual(double* t, const double* u, const double* evals, int64_t n, cudaStream_t stream);
 cudaError_t launch_precond_w(double* w, const double* u, const double* diag, const double* evals, double cutoff,
                              int64_t n, cudaStream_t stream);

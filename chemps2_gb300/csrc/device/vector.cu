@@ -177,18 +177,36 @@ __global__ void mxm_row_kernel(double* mxm, int ld, int row, const double* dots,
 // Parallel (round-robin) ordering: every round rotates n/2 disjoint planes at once.
 // Eigenvalues ascending in evals[0..n), eigenvectors in the columns of evecs (ld).
 constexpr int kEigMax = 32;
-__global__ void __launch_bounds__(256) small_eig_kernel(const double* __restrict__ mat, int n, int ld,
-                                                        double* __restrict__ evals, double* __restrict__ evecs) {
-  __shared__ double A[kEigMax][kEigMax + 1];
-  __shared__ double B[kEigMax][kEigMax + 1];
-  __shared__ double Vm[kEigMax][kEigMax + 1];
-  __shared__ double W[kEigMax][kEigMax + 1];
-  __shared__ double cs[kEigMax / 2], sn[kEigMax / 2];
-  __shared__ int pp[kEigMax / 2], qq[kEigMax / 2];
-  __shared__ int role[kEigMax];  // pair index * 2 + (0: p, 1: q), or -1
-  __shared__ int pos[kEigMax];
-  __shared__ double offn, totn;
-  __shared__ int order[kEigMax];
+struct EigSmem {
+  double A[kEigMax][kEigMax + 1];
+  double B[kEigMax][kEigMax + 1];
+  double Vm[kEigMax][kEigMax + 1];
+  double W[kEigMax][kEigMax + 1];
+  double cs[kEigMax / 2], sn[kEigMax / 2];
+  int pp[kEigMax / 2], qq[kEigMax / 2];
+  int role[kEigMax];  // pair index * 2 + (0: p, 1: q), or -1
+  int pos[kEigMax];
+  double offn, totn;
+  int order[kEigMax];
+};
+
+// Cyclic Jacobi diagonalisation of the symmetric n x n matrix mat (n <= kEigMax) by one CTA
+// (round-robin pairing, n / 2 rotations per round). On return sm.A is diagonal, sm.Vm holds
+// the eigenvectors and sm.order lists the eigenvalues in ascending order.
+__device__ void jacobi_eig(EigSmem& sm, const double* __restrict__ mat, int n, int ld) {
+  double (&A)[kEigMax][kEigMax + 1] = sm.A;
+  double (&B)[kEigMax][kEigMax + 1] = sm.B;
+  double (&Vm)[kEigMax][kEigMax + 1] = sm.Vm;
+  double (&W)[kEigMax][kEigMax + 1] = sm.W;
+  double* cs = sm.cs;
+  double* sn = sm.sn;
+  int* pp = sm.pp;
+  int* qq = sm.qq;
+  int* role = sm.role;
+  int* pos = sm.pos;
+  double& offn = sm.offn;
+  double& totn = sm.totn;
+  int* order = sm.order;
   const int tid = threadIdx.x;
   for (int e = tid; e < n * n; e += blockDim.x) {
     const int i = e % n, j = e / n;
@@ -295,10 +313,48 @@ __global__ void __launch_bounds__(256) small_eig_kernel(const double* __restrict
     }
   }
   __syncthreads();
-  if (tid < n) evals[tid] = A[order[tid]][order[tid]];
+}
+
+__global__ void __launch_bounds__(256) small_eig_kernel(const double* __restrict__ mat, int n, int ld,
+                                                        double* __restrict__ evals, double* __restrict__ evecs) {
+  __shared__ EigSmem sm;
+  jacobi_eig(sm, mat, n, ld);
+  const int tid = threadIdx.x;
+  if (tid < n) evals[tid] = sm.A[sm.order[tid]][sm.order[tid]];
   for (int e = tid; e < n * n; e += blockDim.x) {
     const int i = e % n, j = e / n;
-    evecs[i + ld * j] = Vm[i][order[j]];
+    evecs[i + ld * j] = sm.Vm[i][sm.order[j]];
+  }
+}
+
+// One CTA per job: Jacobi eigendecomposition of the n x n Gram matrix at base + offG; the
+// eigenvalues go to base + offE in ascending order and the eigenvectors to base + offU in
+// descending order of the eigenvalue, each with the sign that makes its largest-magnitude
+// entry (the first one on ties) positive -- the layout launch_reverse_columns produces.
+__global__ void __launch_bounds__(256) batched_eig_kernel(const EigJob* __restrict__ jobs, double* __restrict__ base) {
+  __shared__ EigSmem sm;
+  __shared__ double sgn[kEigMax];
+  const EigJob jb = jobs[blockIdx.x];
+  const int n = jb.n;
+  jacobi_eig(sm, base + jb.offG, n, n);
+  const int tid = threadIdx.x;
+  if (tid < n) {
+    base[jb.offE + tid] = sm.A[sm.order[tid]][sm.order[tid]];
+    const int col = sm.order[n - 1 - tid];  // output column tid
+    double best = -1.0, v = 0.0;
+    for (int i = 0; i < n; i++) {
+      const double a = fabs(sm.Vm[i][col]);
+      if (a > best) {
+        best = a;
+        v = sm.Vm[i][col];
+      }
+    }
+    sgn[tid] = (v < 0.0) ? -1.0 : 1.0;
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int i = e % n, j = e / n;
+    base[jb.offU + i + static_cast<int64_t>(n) * j] = sgn[j] * sm.Vm[i][sm.order[n - 1 - j]];
   }
 }
 
@@ -411,6 +467,12 @@ cudaError_t launch_reverse_columns(double* dst, const double* src, int rows, int
 cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream) {
   if (n < 1 || n > kEigMax || ld < n) return cudaErrorInvalidValue;
   small_eig_kernel<<<1, 256, 0, stream>>>(mat, n, ld, evals, evecs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batched_eig(const EigJob* jobs, int njobs, double* base, cudaStream_t stream) {
+  if (njobs <= 0) return cudaSuccess;
+  batched_eig_kernel<<<njobs, 256, 0, stream>>>(jobs, base);
   return cudaGetLastError();
 }
 

@@ -161,6 +161,7 @@ DMRG::~DMRG() {
       rt->sync();
     } catch (...) {
     }
+    if (solver_) cusolverDnDestroy(static_cast<cusolverDnHandle_t>(solver_));
     pcache_.reset();
     if (heff_cache_) {
       heff_cache_->program.reset();
@@ -583,12 +584,29 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     });
     rt->run(dp, svec, nullptr);
   }
-  // Eigendecomposition of every Gram matrix (FP64, cuSOLVER syevd).
-  cusolverDnHandle_t sh;
-  check_solver(cusolverDnCreate(&sh), "create");
-  check_solver(cusolverDnSetStream(sh, s), "stream");
+  // Eigendecomposition of every Gram matrix (FP64): sectors up to kBatchedEigMax in one
+  // batched Jacobi launch, larger ones with cuSOLVER syevd.
+  std::vector<c2g::EigJob> jobs;
+  for (const auto& c : plan.centers)
+    if (c.cd > 0 && c.g <= c2g::kBatchedEigMax) jobs.push_back(c2g::EigJob{c.g, 0, c.offG, c.offE, c.offU});
+  if (!jobs.empty()) {
+    c2g::EigJob* djobs = nullptr;
+    C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&djobs), sizeof(c2g::EigJob) * jobs.size(), s));
+    C2G_CUDA(cudaMemcpyAsync(djobs, jobs.data(), sizeof(c2g::EigJob) * jobs.size(), cudaMemcpyHostToDevice, s));
+    C2G_CUDA(c2g::launch_batched_eig(djobs, static_cast<int>(jobs.size()), work, s));
+    c2g::count_launches(1);
+    rt->sync();  // `jobs` is pageable host memory
+    C2G_CUDA(cudaFreeAsync(djobs, s));
+  }
+  if (!solver_) {
+    cusolverDnHandle_t h = nullptr;
+    check_solver(cusolverDnCreate(&h), "create");
+    solver_ = h;
+    check_solver(cusolverDnSetStream(h, s), "stream");
+  }
+  cusolverDnHandle_t sh = static_cast<cusolverDnHandle_t>(solver_);
   int gmax = 0;
-  for (const auto& c : plan.centers) gmax = std::max(gmax, c.cd > 0 ? c.g : 0);
+  for (const auto& c : plan.centers) gmax = std::max(gmax, (c.cd > 0 && c.g > c2g::kBatchedEigMax) ? c.g : 0);
   int lwork = 0;
   double* dwork = nullptr;
   int* dinfo = nullptr;
@@ -602,7 +620,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   }
   for (size_t ic = 0; ic < plan.centers.size(); ic++) {
     const auto& c = plan.centers[ic];
-    if (c.cd <= 0) continue;
+    if (c.cd <= 0 || c.g <= c2g::kBatchedEigMax) continue;
     int lw = 0;
     check_solver(cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, c.g, work + c.offG,
                                              c.g, work + c.offE, &lw),
@@ -629,7 +647,6 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   rt->sync();
   for (size_t ic = 0; ic < plan.centers.size(); ic++)
     if (info[ic] != 0) throw std::runtime_error("Split: eigensolver failed for a center sector");
-  cusolverDnDestroy(sh);
   if (dwork) rt->release(dwork);
   C2G_CUDA(cudaFreeAsync(dinfo, s));
 

@@ -119,6 +119,7 @@ class DMRG {
   double mixed_tol_ = 1e-5;
   std::unique_ptr<SyBookkeeper> denBK;
   std::unique_ptr<c2g::Runtime> rt;
+  void* solver_ = nullptr;  // cuSOLVER handle of the truncation step (created on first use)
   std::vector<std::unique_ptr<c2g::MpsLayout>> mps_lay;
   std::vector<double*> mps_dev;
   std::vector<std::unique_ptr<c2g::BoundaryOps>> ops;
