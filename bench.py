@@ -144,7 +144,7 @@ def measured_peaks():
 def profiled_traffic():
     """DRAM bytes per Heff launch from the committed ncu summary (scaled to this workload)."""
     try:
-        prof = json.loads((ROOT / "profiles" / "heff_sandwich_l24_d1000.json").read_text())
+        prof = json.loads((ROOT / "profiles" / "heff_team_kernel_l24_d1000.json").read_text())
         return prof.get("dram_bytes_per_matvec")
     except (OSError, ValueError):
         return None
@@ -237,7 +237,7 @@ def run_ours(args):
     res32 = dmrg.bench_heff(MID, 0, args.steps, L2_FLUSH_BYTES, precision="fp32")
     mixed = {"matvec_per_s": 1e3 / res32["ms_per_matvec"], "ms_per_matvec": res32["ms_per_matvec"],
              "speedup_vs_fp64": ms / res32["ms_per_matvec"],
-             "arithmetic": "FP32 products and lane sums, FP64 operands, lane reduction and output"}
+             "arithmetic": "FP32 operand copies, products and per-slot sums; FP64 slot reduction and output"}
     if world > 1:
         t = torch.tensor([total_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -260,12 +260,24 @@ def run_ours(args):
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     achieved = res["bytes"] / (ms * 1e-3) / 1e9
+    # The kernel is bound by the FP64 pipe, not by HBM: the compute roofline sits beside the
+    # HBM one. FP64 peak = ncu's device peak of 608 FP64 flops per cycle (2 DFMA lanes per SM
+    # and cycle) at the maximum SM clock; FP32 peak likewise 38912 flops per cycle.
+    sm_hz = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    fp64_peak = 608 * sm_hz / 1e9
+    fp32_peak = 38912 * sm_hz / 1e9
+    gflops = res["flops"] / (ms * 1e-3) / 1e9
+    gflops32 = res32["flops"] / (res32["ms_per_matvec"] * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm if hbm else 6800.0,
                 "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "traffic": profiled_traffic(),
                 "peak_source": "measured" if hbm else "fallback",
-                "kernel": "sandwich_kernel (FP64 block sandwich, c2g::launch_sandwich)",
+                "kernel": "sandwich_warp_kernel<double, R> (team block sandwich, one launch per row class)",
                 "ledger_bytes_per_matvec": res["bytes"], "ledger_flops_per_matvec": res["flops"],
-                "fp64_gflops": res["flops"] / (ms * 1e-3) / 1e9}
+                "compute": {"pipe": "fp64", "achieved_gflops": gflops, "peak_gflops": fp64_peak,
+                            "frac": gflops / fp64_peak,
+                            "peak_source": "ncu device peak 608 FP64 flop/cycle x max SM clock"},
+                "compute_fp32_variant": {"pipe": "fp32", "achieved_gflops": gflops32, "peak_gflops": fp32_peak,
+                                         "frac": gflops32 / fp32_peak}}
     dmrg.close()
     sweep = None
     if rank == 0 and not args.no_sweep:
@@ -315,7 +327,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
