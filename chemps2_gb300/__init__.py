@@ -360,6 +360,14 @@ class DMRG:
         _check(load().c2g_dmrg_heff_apply_fp32(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
         return y
 
+    def heff_apply_noalloc(self, index, x):
+        """y = Heff x (FP64) staged through the library's static device array (no device
+        allocation); needs a prior heff_apply at this index and state."""
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(xx)
+        _check(load().c2g_dmrg_heff_apply_noalloc(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
+        return y
+
     def set_precision(self, mode="fp64", mixed_tol=1e-5):
         """'fp64' (the reference's arithmetic) or 'mixed' (FP32 Davidson expansion, FP64 finish)."""
         m = {"fp64": 0, "mixed": 1}[mode] if isinstance(mode, str) else int(mode)

@@ -449,5 +449,11 @@ int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64
     d->d->heff_apply_host(index, false, x, y, nullptr, n, 1);
   });
 }
+int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n) {
+  return guarded([&] {
+    NEED(d);
+    d->d->heff_apply_noalloc(index, x, y, n);
+  });
+}
 
 }  // extern "C"

@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cusolverDn.h>
+
+#include "static_scratch.hpp"
 #include <unordered_map>
 
 #include "davidson.hpp"
@@ -863,6 +865,31 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
     C2G_CUDA(cudaMemcpyAsync(diag, c.ybuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   }
   rt->sync();
+}
+
+void DMRG::heff_apply_noalloc(const int index, const double* x, double* y, const long long n) {
+  if (!x || !y) throw std::invalid_argument("heff_apply_noalloc: null buffer");
+  if (index < 0 || index > L - 2) throw std::out_of_range("heff_apply_noalloc: index");
+  HeffCache& c = *heff_cache_;
+  if (!(c.index == index && c.version == version_ && c.program))
+    throw std::invalid_argument("heff_apply_noalloc: no Heff program for this index and state (call heff_apply first)");
+  const int64_t veclen = c.S->size();
+  if (n != veclen) throw std::invalid_argument("heff_apply_noalloc: vector length differs from the two-site object size");
+  const int64_t ystart = (veclen + 31) / 32 * 32;  // y starts on a 256-byte boundary
+  if (ystart + veclen > c2g::kStaticScratchDoubles)
+    throw std::invalid_argument("heff_apply_noalloc: two-site object too large for the static scratch");
+  double* base = nullptr;
+  C2G_CUDA(c2g::static_scratch(&base));
+  double* dx = base;
+  double* dy = base + ystart;
+  cudaStream_t s = rt->stream();
+  C2G_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
+  // the program writes every output block; y is cleared so that no earlier caller's data
+  // can survive in it
+  C2G_CUDA(cudaMemsetAsync(dy, 0, sizeof(double) * veclen, s));
+  rt->run(*c.program, dx, dy);
+  C2G_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
+  rt->sync();  // the scratch is free for the next caller once this returns
 }
 
 }  // namespace CheMPS2

@@ -1,0 +1,42 @@
+// A file-scope device array used as staging memory by the allocation-free host-buffer
+// matvec (DMRG::heff_apply_noalloc). Its device address is looked up once per device with
+// cudaGetSymbolAddress and cached.
+//
+// Races: there is one array per device for the whole process. Two calls that use it at
+// the same time (two host threads, or two DMRG objects whose streams overlap) overwrite
+// each other's vectors. Every user synchronises its stream before it returns, so calls
+// issued one after another from any number of DMRG objects are safe; concurrent calls
+// are not and must be serialised by the caller.
+#include "static_scratch.hpp"
+
+#include <mutex>
+
+namespace c2g {
+
+namespace {
+
+__device__ __align__(256) double g_static_scratch[kStaticScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mutex;
+double* g_addr[kMaxDevices] = {};
+
+}  // namespace
+
+cudaError_t static_scratch(double** ptr) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_addr[dev] = static_cast<double*>(p);
+  }
+  *ptr = g_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace c2g

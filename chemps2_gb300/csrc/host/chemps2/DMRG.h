@@ -89,6 +89,10 @@ class DMRG {
   // precision 1: FP32 arithmetic for the matvec (the diagonal stays FP64).
   void heff_apply_host(const int index, const bool join_into_x, double* x, double* y, double* diag,
                        const long long n, const int precision = 0);
+  // y = Heff x (FP64) with no device allocation: x and y are staged through a static
+  // device array shared by the process (not safe for concurrent calls). The Heff program
+  // at `index` must already exist for the current state (a heff_apply_host call there).
+  void heff_apply_noalloc(const int index, const double* x, double* y, const long long n);
 
  private:
   struct HeffCache;

@@ -134,6 +134,14 @@ int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, doub
 /* As c2g_dmrg_heff_apply with the matvec in FP32 arithmetic (operands converted on load,
  * lane sums in FP32, the output in FP64). No counterpart in the reference. */
 int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64_t n);
+/* No counterpart in the reference. As c2g_dmrg_heff_apply (FP64, no join, no diagonal)
+ * without any device allocation: x and y are staged through a static device array of
+ * 2 M doubles shared by the whole process (n up to about 1 M). The Heff program at `index`
+ * must already exist for the current state (a c2g_dmrg_heff_apply call there), otherwise
+ * C2G_ERR_INVALID; n too large for the array: C2G_ERR_INVALID. Not safe for concurrent
+ * calls from several threads or DMRG objects: the array is shared; each call
+ * synchronises before returning, so sequential calls are safe. */
+int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n);
 
 #ifdef __cplusplus
 }
