@@ -274,12 +274,38 @@ class ConvergenceScheme:
         return self._instr[i][4]
 
 
+class TwoDM:
+    """CheMPS2::TwoDM: the spin-summed 2-RDMs A[a,b,c,d] and B[a,b,c,d] of a DMRG state
+    (CheMPS2/include/chemps2/TwoDM.h), as numpy arrays, with trace() and energy()."""
+
+    def __init__(self, A, B, trace, energy):
+        self.A, self.B = A, B
+        self._trace, self._energy = trace, energy
+
+    def getTwoDMA(self, a, b, c, d):
+        return float(self.A[a, b, c, d])
+
+    def getTwoDMB(self, a, b, c, d):
+        return float(self.B[a, b, c, d])
+
+    def get1RDM(self, N):
+        """1-RDM: sum_r A[a, r, b, r] / (N - 1)."""
+        return np.einsum("arbr->ab", self.A) / (N - 1.0)
+
+    def trace(self):
+        return self._trace
+
+    def energy(self):
+        return self._energy
+
+
 class DMRG:
     """CheMPS2::DMRG (PyDMRG): the sweep runs on the GPU."""
 
     def __init__(self, Probl: Problem, OptScheme: ConvergenceScheme, makechkpt=False, tmpfolder="/tmp",
                  occupancies=None):
         self._prob, self._scheme = Probl, OptScheme
+        self._L = Probl.gL()
         self._d = C.c_void_p()
         occ = None
         if occupancies is not None:
@@ -359,6 +385,22 @@ class DMRG:
         y = np.zeros_like(xx)
         _check(load().c2g_dmrg_heff_apply_fp32(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
         return y
+
+    def calc2DMandCorrelations(self):
+        """The two-particle density matrices of the current state (DMRG::calc2DMandCorrelations)."""
+        _check(load().c2g_dmrg_calc_2dm(self._d))
+
+    def get2DM(self, ham_order=False):
+        """(A, B) 2-RDMs as L x L x L x L arrays indexed [a, b, c, d] (DMRG orbital order unless
+        ham_order), plus trace and energy: TwoDM.getTwoDMA_DMRG etc."""
+        L = self._L
+        A = np.zeros(L ** 4)
+        B = np.zeros(L ** 4)
+        _check(load().c2g_dmrg_get_2dm(self._d, int(bool(ham_order)), _dp(A), _dp(B)))
+        tr, en = C.c_double(), C.c_double()
+        _check(load().c2g_dmrg_2dm_trace_energy(self._d, C.byref(tr), C.byref(en)))
+        # element (a,b,c,d) at a + L*(b + L*(c + L*d)): Fortran order
+        return TwoDM(A.reshape((L, L, L, L), order="F"), B.reshape((L, L, L, L), order="F"), tr.value, en.value)
 
     def heff_apply_noalloc(self, index, x):
         """y = Heff x (FP64) staged through the library's static device array (no device

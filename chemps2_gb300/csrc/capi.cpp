@@ -449,6 +449,37 @@ int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64
     d->d->heff_apply_host(index, false, x, y, nullptr, n, 1);
   });
 }
+int c2g_dmrg_calc_2dm(c2g_dmrg* d) {
+  return guarded([&] {
+    NEED(d);
+    d->d->calc2DMandCorrelations();
+  });
+}
+int c2g_dmrg_get_2dm(const c2g_dmrg* d, int ham_order, double* A, double* B) {
+  return guarded([&] {
+    NEED(d);
+    const CheMPS2::TwoDM* dm = d->d->get2DM();
+    if (!dm) throw std::invalid_argument("get_2dm: no 2-RDM computed (call c2g_dmrg_calc_2dm)");
+    const int L = dm->gL();
+    for (int a = 0; a < L; a++)
+      for (int b = 0; b < L; b++)
+        for (int c = 0; c < L; c++)
+          for (int e = 0; e < L; e++) {
+            const size_t at = a + static_cast<size_t>(L) * (b + static_cast<size_t>(L) * (c + static_cast<size_t>(L) * e));
+            if (A) A[at] = ham_order ? dm->getTwoDMA_HAM(a, b, c, e) : dm->getTwoDMA_DMRG(a, b, c, e);
+            if (B) B[at] = ham_order ? dm->getTwoDMB_HAM(a, b, c, e) : dm->getTwoDMB_DMRG(a, b, c, e);
+          }
+  });
+}
+int c2g_dmrg_2dm_trace_energy(const c2g_dmrg* d, double* trace, double* energy) {
+  return guarded([&] {
+    NEED(d);
+    const CheMPS2::TwoDM* dm = d->d->get2DM();
+    if (!dm) throw std::invalid_argument("2dm_trace_energy: no 2-RDM computed (call c2g_dmrg_calc_2dm)");
+    if (trace) *trace = dm->trace();
+    if (energy) *energy = dm->energy();
+  });
+}
 int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n) {
   return guarded([&] {
     NEED(d);

@@ -13,6 +13,8 @@
 #include <unordered_map>
 
 #include "davidson.hpp"
+#include "gauge.hpp"
+#include "twodm.hpp"
 #include "compile.hpp"
 #include "heff.hpp"
 #include "layout.hpp"
@@ -227,80 +229,108 @@ void DMRG::setup_mps(int* occupancies) {
 }
 
 // CheMPS2/TensorT.cpp:188-289 (QR per right sector, Householder, Q kept) as used by
-// DMRG::left_normalize(site, NULL). Initialisation only.
+// DMRG::left_normalize(site, NULL). Initialisation.
 void DMRG::left_normalize_host(int site, std::vector<double>& data) {
-  const MpsLayout& lay = *mps_lay[site];
-  const SyBookkeeper& bk = *denBK;
-  for (int NR = bk.gNmin(site + 1); NR <= bk.gNmax(site + 1); NR++)
-    for (int TwoSR = bk.gTwoSmin(site + 1, NR); TwoSR <= bk.gTwoSmax(site + 1, NR); TwoSR += 2)
-      for (int IR = 0; IR < bk.getNumberOfIrreps(); IR++) {
-        const int dimR = bk.gCurrentDim(site + 1, NR, TwoSR, IR);
-        if (dimR <= 0) continue;
-        std::vector<int> blocks;
-        int m = 0;
-        for (int k = 0; k < lay.nkappa; k++)
-          if (lay.NR[k] == NR && lay.TwoSR[k] == TwoSR && lay.IR[k] == IR && lay.rows[k] > 0) {
-            blocks.push_back(k);
-            m += lay.rows[k];
-          }
-        if (m == 0) continue;
-        const int n = dimR;
-        std::vector<double> a(static_cast<size_t>(m) * n);
-        int r0 = 0;
-        for (int k : blocks) {
-          for (int l = 0; l < lay.rows[k]; l++)
-            for (int r = 0; r < n; r++) a[r0 + l + static_cast<size_t>(m) * r] = data[lay.k2i[k] + l + lay.rows[k] * r];
-          r0 += lay.rows[k];
-        }
-        // Householder QR (dgeqr2 conventions), then Q = H_1 ... H_kk applied to I (dorg2r).
-        const int kk = std::min(m, n);
-        std::vector<double> tau(kk, 0.0);
-        for (int j = 0; j < kk; j++) {
-          double* x = &a[j + static_cast<size_t>(m) * j];
-          const int len = m - j;
-          double xnorm = 0.0;
-          for (int i = 1; i < len; i++) xnorm += x[i] * x[i];
-          xnorm = std::sqrt(xnorm);
-          if (xnorm == 0.0) {
-            tau[j] = 0.0;
-            continue;
-          }
-          const double alpha = x[0];
-          const double beta = -std::copysign(std::hypot(alpha, xnorm), alpha);
-          tau[j] = (beta - alpha) / beta;
-          const double scal = 1.0 / (alpha - beta);
-          for (int i = 1; i < len; i++) x[i] *= scal;
-          x[0] = beta;
-          for (int c = j + 1; c < n; c++) {  // apply H_j to the trailing columns
-            double* y = &a[j + static_cast<size_t>(m) * c];
-            double s = y[0];
-            for (int i = 1; i < len; i++) s += x[i] * y[i];
-            s *= tau[j];
-            y[0] -= s;
-            for (int i = 1; i < len; i++) y[i] -= s * x[i];
-          }
-        }
-        std::vector<double> q(static_cast<size_t>(m) * n, 0.0);
-        for (int c = 0; c < kk; c++) q[c + static_cast<size_t>(m) * c] = 1.0;
-        for (int j = kk - 1; j >= 0; j--) {
-          const double* v = &a[j + static_cast<size_t>(m) * j];
-          const int len = m - j;
-          for (int c = j; c < kk; c++) {
-            double* y = &q[j + static_cast<size_t>(m) * c];
-            double s = y[0];
-            for (int i = 1; i < len; i++) s += v[i] * y[i];
-            s *= tau[j];
-            y[0] -= s;
-            for (int i = 1; i < len; i++) y[i] -= s * v[i];
-          }
-        }
-        r0 = 0;
-        for (int k : blocks) {
-          for (int l = 0; l < lay.rows[k]; l++)
-            for (int r = 0; r < n; r++) data[lay.k2i[k] + l + lay.rows[k] * r] = q[r0 + l + static_cast<size_t>(m) * r];
-          r0 += lay.rows[k];
-        }
-      }
+  c2g::left_normalize(*denBK, site, *mps_lay[site], data);
+}
+
+void DMRG::download_mps(int site, std::vector<double>& data) {
+  data.resize(static_cast<size_t>(mps_lay[site]->size()));
+  if (!data.empty())
+    C2G_CUDA(cudaMemcpyAsync(data.data(), mps_dev[site], sizeof(double) * data.size(), cudaMemcpyDeviceToHost,
+                             rt->stream()));
+  rt->sync();
+}
+
+// CheMPS2/DMRGtechnics.cpp:276-298
+void DMRG::gauge_left_normalize(int site, bool into_next) {
+  std::vector<double> t, n;
+  download_mps(site, t);
+  if (into_next) {
+    download_mps(site + 1, n);
+    c2g::left_normalize(*denBK, site, *mps_lay[site], t, mps_lay[site + 1].get(), &n);
+    upload_mps(site + 1, n);
+  } else {
+    c2g::left_normalize(*denBK, site, *mps_lay[site], t);
+  }
+  upload_mps(site, t);
+  version_++;
+}
+
+// CheMPS2/DMRGtechnics.cpp:300-322: LQ of MPS[site], L into MPS[site - 1]
+void DMRG::gauge_right_normalize(int site) {
+  std::vector<double> t, p;
+  download_mps(site, t);
+  download_mps(site - 1, p);
+  c2g::right_normalize(*denBK, site, *mps_lay[site], t, mps_lay[site - 1].get(), &p);
+  upload_mps(site, t);
+  upload_mps(site - 1, p);
+  version_++;
+}
+
+// CheMPS2/TwoDM.cpp:445-628 for one site, as device task programs (chunked so that the
+// products of one program fit a work budget).
+void DMRG::fill_2dm_site(int site) {
+  if (site > 0 && isAllocated[site - 1] != 1) throw std::logic_error("2-RDM: left operators missing");
+  if (site < L - 1 && isAllocated[site] != 2) throw std::logic_error("2-RDM: right operators missing");
+  c2g::TwoDMContext ctx;
+  ctx.bk = denBK.get();
+  ctx.L = L;
+  ctx.site = site;
+  ctx.T = mps_tensor(mps_lay[site].get(), site);
+  ctx.left = (site > 0) ? ops[site - 1].get() : nullptr;
+  ctx.right = (site < L - 1) ? ops[site].get() : nullptr;
+  const std::vector<c2g::TwoDMInstance> inst = c2g::twodm_instances(ctx);
+  const int nvalues = inst.back().value0 + c2g::twodm_num_values(inst.back().kind);
+  std::vector<double> values(nvalues, 0.0);
+  constexpr int64_t kWorkBudget = int64_t(1) << 25;  // doubles (256 MB) of products per program
+  size_t first = 0;
+  while (first < inst.size()) {
+    size_t last = first;
+    int64_t work = 0;
+    while (last < inst.size() && (last == first || work + inst[last].work <= kWorkBudget)) work += inst[last++].work;
+    TaskBuilder tb;
+    c2g::compile_twodm(tb, ctx, inst, first, last);
+    auto dp = rt->upload(tb.finalize());
+    const int v0 = inst[first].value0;
+    const int nv = inst[last - 1].value0 + c2g::twodm_num_values(inst[last - 1].kind) - v0;
+    double* dwork = rt->alloc(std::max<int64_t>(work, 1));
+    double* dy = rt->alloc(nv);
+    rt->zero(dy, nv);
+    rt->set_slot(c2g::kSlotWork, dwork);
+    rt->run(*dp, nullptr, dy);
+    C2G_CUDA(cudaMemcpyAsync(values.data() + v0, dy, sizeof(double) * nv, cudaMemcpyDeviceToHost, rt->stream()));
+    rt->sync();
+    rt->set_slot(c2g::kSlotWork, nullptr);
+    rt->release(dwork);
+    rt->release(dy);
+    first = last;
+  }
+  c2g::twodm_assemble(*two_dm_, site, inst, values);
+}
+
+// CheMPS2/DMRGtechnics.cpp:40-120 (the 2-RDM part of calc_rdms_and_correlations)
+void DMRG::calc2DMandCorrelations() {
+  if (L < 2) throw std::invalid_argument("calc2DMandCorrelations: at least two orbitals");
+  // the whole MPS left-canonical, then the left operators of boundary L - 2
+  gauge_left_normalize(L - 2, true);
+  gauge_left_normalize(L - 1, false);
+  update_moving_right(L - 2);
+  two_dm_ = std::make_unique<TwoDM>(Prob, L);
+  for (int site = L - 1; site >= 0; site--) {
+    fill_2dm_site(site);
+    if (site > 0) {
+      gauge_right_normalize(site);
+      update_moving_left(site - 1);
+    }
+  }
+  two_dm_->correct_higher_multiplicities();
+  // back to the state of a finished right sweep: MPS[0 .. L-2] left-normalised, the
+  // left operators of boundaries 0 .. L-3
+  for (int site = 0; site < L - 1; site++) {
+    gauge_left_normalize(site, true);
+    if (site <= L - 3) update_moving_right(site);
+  }
 }
 
 void DMRG::upload_mps(int site, const std::vector<double>& data) {

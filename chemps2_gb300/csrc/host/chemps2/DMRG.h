@@ -15,6 +15,7 @@
 #include "ConvergenceScheme.h"
 #include "Problem.h"
 #include "SyBookkeeper.h"
+#include "TwoDM.h"
 
 namespace c2g {
 class Runtime;
@@ -94,6 +95,14 @@ class DMRG {
   // at `index` must already exist for the current state (a heff_apply_host call there).
   void heff_apply_noalloc(const int index, const double* x, double* y, const long long n);
 
+  // CheMPS2/DMRG.h calc2DMandCorrelations (CheMPS2/DMRGtechnics.cpp:40-120): the
+  // two-particle density matrix of the current state, one site at a time from the right
+  // with the MPS brought into mixed-canonical form around it; afterwards the MPS is left-
+  // canonical again and the operators are those of a finished right sweep, so Solve() can
+  // continue. get2DM() returns it (null before the first call).
+  void calc2DMandCorrelations();
+  const TwoDM* get2DM() const { return two_dm_.get(); }
+
  private:
   struct HeffCache;
   HeffCache& heff_program(const int index, const bool with_diag);
@@ -108,6 +117,12 @@ class DMRG {
   c2g::DevProgram& program(const std::string& key, const std::function<c2g::Compiled()>& build,
                            long long* operand_bytes = nullptr);
   std::string dims_key(const char* kind, const int index, const int bmin, const int bmax, const int extra = 0) const;
+
+  std::unique_ptr<TwoDM> two_dm_;
+  void download_mps(int site, std::vector<double>& data);
+  void gauge_left_normalize(int site, bool into_next);
+  void gauge_right_normalize(int site);
+  void fill_2dm_site(int site);
 
   void setup_mps(int* occupancies);
   void left_normalize_host(int site, std::vector<double>& data);

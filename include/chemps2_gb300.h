@@ -134,6 +134,17 @@ int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, doub
 /* As c2g_dmrg_heff_apply with the matvec in FP32 arithmetic (operands converted on load,
  * lane sums in FP32, the output in FP64). No counterpart in the reference. */
 int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64_t n);
+/* DMRG::calc2DMandCorrelations (CheMPS2/DMRGtechnics.cpp:40-120; the 2-RDM part): the
+ * spin-summed two-particle density matrices A and B of the current state
+ * (CheMPS2/TwoDM.cpp:445-640). The state and the operators afterwards are those of a
+ * finished right sweep, so c2g_dmrg_solve may continue. */
+int c2g_dmrg_calc_2dm(c2g_dmrg* d);
+/* The 2-RDMs as L^4 arrays, element (a,b,c,d) at a + L*(b + L*(c + L*d)); ham_order != 0:
+ * Hamiltonian orbital order (TwoDM::getTwoDMA_HAM), else DMRG order (getTwoDMA_DMRG).
+ * A or B may be NULL. */
+int c2g_dmrg_get_2dm(const c2g_dmrg* d, int ham_order, double* A, double* B);
+/* TwoDM::trace (= N(N-1)) and TwoDM::energy (Econst + 1/2 sum A h). */
+int c2g_dmrg_2dm_trace_energy(const c2g_dmrg* d, double* trace, double* energy);
 /* No counterpart in the reference. As c2g_dmrg_heff_apply (FP64, no join, no diagonal)
  * without any device allocation: x and y are staged through a static device array of
  * 2 M doubles shared by the whole process (n up to about 1 M). The Heff program at `index`

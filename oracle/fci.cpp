@@ -152,8 +152,25 @@ const char* oracle_fci_last_error() { return g_fci_err.c_str(); }
 
 // Lowest eigenvalue of H (plus econst) in the (N_up, N_down, irrep) determinant space.
 // tmat: L x L; vmat: L^4 physics notation, (i,j,k,l) at i + L*(j + L*(k + L*l)).
+// With A / B non-null, also the spin-summed 2-RDMs of that eigenvector
+// (CheMPS2/include/chemps2/TwoDM.h definitions, same index layout as vmat):
+//   A_ijkl = sum_st <a+_is a+_jt a_lt a_ks>,
+//   B_ijkl = sum_s (<a+_is a+_js a_ls a_ks> - <a+_is a+_j-s a_l-s a_ks>),
+// from <a+_is a+_jt a_lt a_ks> = <E^s_ik E^t_jl> - delta_jk delta_st <E^s_il> with
+// E^s_pq = a+_ps a_qs.
+int oracle_fci_state(int L, const int* orb_irrep, const double* tmat, const double* vmat, double econst, int n_up,
+                     int n_down, int irrep, double tol, int max_iter, double* energy, int64_t* dim, double* A,
+                     double* B);
+
 int oracle_fci_ground_state(int L, const int* orb_irrep, const double* tmat, const double* vmat, double econst,
                             int n_up, int n_down, int irrep, double tol, int max_iter, double* energy, int64_t* dim) {
+  return oracle_fci_state(L, orb_irrep, tmat, vmat, econst, n_up, n_down, irrep, tol, max_iter, energy, dim, nullptr,
+                          nullptr);
+}
+
+int oracle_fci_state(int L, const int* orb_irrep, const double* tmat, const double* vmat, double econst, int n_up,
+                     int n_down, int irrep, double tol, int max_iter, double* energy, int64_t* dim, double* A,
+                     double* B) {
   try {
     if (L > 24) throw std::invalid_argument("FCI oracle: at most 24 orbitals");
     FCI f;
@@ -276,6 +293,60 @@ int oracle_fci_ground_state(int L, const int* orb_irrep, const double* tmat, con
       }
     }
     *energy = theta + econst;
+    if (A || B) {
+      double nr = 0.0;
+      for (double x : ritz) nr += x * x;
+      nr = std::sqrt(nr);
+      for (double& x : ritz) x /= nr;
+      // Es[s][p + L q] = E^s_pq |c>, s = 0 up, 1 down
+      const size_t nb = f.B.str.size();
+      std::vector<std::vector<double>> Es[2];
+      for (int sp = 0; sp < 2; sp++) Es[sp].assign(size_t(L) * L, std::vector<double>(n, 0.0));
+      for (size_t d = 0; d < n; d++) {
+        const double cd = ritz[d];
+        if (cd == 0.0) continue;
+        const int ia = f.dets[d].first, ib = f.dets[d].second;
+        for (int p = 0; p < L; p++)
+          for (int q = 0; q < L; q++) {
+            for (const auto& e : f.exA[ia][p + size_t(L) * q]) {
+              const int64_t t = f.det_of[size_t(e.to) * nb + ib];
+              if (t >= 0) Es[0][p + size_t(L) * q][t] += e.sign * cd;
+            }
+            for (const auto& e : f.exB[ib][p + size_t(L) * q]) {
+              const int64_t t = f.det_of[size_t(ia) * nb + e.to];
+              if (t >= 0) Es[1][p + size_t(L) * q][t] += e.sign * cd;
+            }
+          }
+      }
+      auto dot = [&](const std::vector<double>& x, const std::vector<double>& y) {
+        double s = 0.0;
+        for (size_t q = 0; q < n; q++) s += x[q] * y[q];
+        return s;
+      };
+      // one-body <E^s_il> = c . E^s_il c
+      std::vector<double> one[2];
+      for (int sp = 0; sp < 2; sp++) {
+        one[sp].assign(size_t(L) * L, 0.0);
+        for (int p = 0; p < L; p++)
+          for (int q = 0; q < L; q++) one[sp][p + size_t(L) * q] = dot(ritz, Es[sp][p + size_t(L) * q]);
+      }
+      for (int i = 0; i < L; i++)
+        for (int j = 0; j < L; j++)
+          for (int k = 0; k < L; k++)
+            for (int l = 0; l < L; l++) {
+              double g[2][2];
+              for (int s1 = 0; s1 < 2; s1++)
+                for (int s2 = 0; s2 < 2; s2++) {
+                  // <E^s1_ik E^s2_jl> = (E^s1_ki c) . (E^s2_jl c)
+                  double v = dot(Es[s1][k + size_t(L) * i], Es[s2][j + size_t(L) * l]);
+                  if (j == k && s1 == s2) v -= one[s1][i + size_t(L) * l];
+                  g[s1][s2] = v;
+                }
+              const size_t at = i + size_t(L) * (j + size_t(L) * (k + size_t(L) * l));
+              if (A) A[at] = g[0][0] + g[0][1] + g[1][0] + g[1][1];
+              if (B) B[at] = g[0][0] + g[1][1] - g[0][1] - g[1][0];
+            }
+    }
     return 0;
   } catch (const std::exception& e) {
     g_fci_err = e.what();

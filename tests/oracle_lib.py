@@ -46,6 +46,20 @@ def fci_energy(model: Model, n_up: int, n_down: int, irrep: int, tol=1e-10) -> f
     return e.value
 
 
+def fci_2rdm(model: Model, n_up: int, n_down: int, irrep: int, tol=1e-11):
+    """FCI ground state energy and its spin-summed 2-RDMs A, B as [a, b, c, d] arrays."""
+    L = model.L
+    e = C.c_double()
+    dim = C.c_int64()
+    A = np.zeros(L ** 4)
+    B = np.zeros(L ** 4)
+    rc = lib().oracle_fci_state(L, _ip(model.irreps), _dp(model.tflat()), _dp(model.vflat()), C.c_double(model.econst),
+                                n_up, n_down, irrep, C.c_double(tol), 600, C.byref(e), C.byref(dim), _dp(A), _dp(B))
+    if rc != 0:
+        raise RuntimeError(lib().oracle_fci_last_error().decode())
+    return e.value, A.reshape((L, L, L, L), order="F"), B.reshape((L, L, L, L), order="F")
+
+
 class OracleDMRG:
     """CPU DMRG of the oracle. schedule: list of (D, econv, max_sweeps, noise, rtol)."""
 

@@ -136,3 +136,25 @@ def test_executor_rejects_out_of_bounds_programs():
     x, y, _ = d.heff_apply(4)  # in bounds: fine
     with pytest.raises(RuntimeError, match="outside slot|not bound|check failed"):
         d.heff_apply(4, x=x[: len(x) // 2])
+
+
+@pytest.mark.parametrize("make,n_up,n_down,irrep", [
+    (lambda: models.hubbard(6, 4.0), 3, 3, 0),
+    (lambda: models.synthetic_ab_initio(6, 5, 3), 3, 2, 0),
+])
+def test_fci_2rdm_identities(make, n_up, n_down, irrep):
+    """The oracle's FCI 2-RDM obeys trace A = N(N-1), Econst + 1/2 sum A h = E (h the
+    reference's matrix elements, CheMPS2/Problem.cpp:351-384) and the (ab)(cd), (ac)(bd)
+    exchange symmetries of the reference's TwoDM::set_2rdm_A/B_DMRG."""
+    m = make()
+    L, N = m.L, n_up + n_down
+    E, A, B = ol.fci_2rdm(m, n_up, n_down, irrep)
+    assert abs(E - ol.fci_energy(m, n_up, n_down, irrep)) < 1e-9
+    assert abs(np.einsum("abab->", A) - N * (N - 1)) < 1e-9
+    h = m.vmat.copy()
+    eye = np.eye(L)
+    h += (np.einsum("ac,bd->abcd", eye, m.tmat) + np.einsum("bd,ac->abcd", eye, m.tmat)) / (N - 1)
+    assert abs(0.5 * np.sum(A * h) + m.econst - E) < 1e-9
+    for X in (A, B):
+        assert np.allclose(X, X.transpose(1, 0, 3, 2), atol=1e-10)
+        assert np.allclose(X, X.transpose(2, 3, 0, 1), atol=1e-10)
