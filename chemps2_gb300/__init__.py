@@ -402,6 +402,19 @@ class DMRG:
         # element (a,b,c,d) at a + L*(b + L*(c + L*d)): Fortran order
         return TwoDM(A.reshape((L, L, L, L), order="F"), B.reshape((L, L, L, L), order="F"), tr.value, en.value)
 
+    def getCorrelations(self, ham_order=False):
+        """Correlation tables and mutual information (CheMPS2::Correlations) as a dict of
+        L x L arrays [row, col] plus the single-orbital entropies."""
+        L = self._L
+        arrs = {k: np.zeros(L * L) for k in ("Cspin", "Cdens", "Cspinflip", "Cdirad", "MutInfo")}
+        ent = np.zeros(L)
+        _check(load().c2g_dmrg_get_correlations(self._d, int(bool(ham_order)), _dp(arrs["Cspin"]), _dp(arrs["Cdens"]),
+                                                _dp(arrs["Cspinflip"]), _dp(arrs["Cdirad"]), _dp(arrs["MutInfo"]),
+                                                _dp(ent)))
+        out = {k: v.reshape((L, L), order="F") for k, v in arrs.items()}
+        out["SingleOrbitalEntropy"] = ent
+        return out
+
     def heff_apply_noalloc(self, index, x):
         """y = Heff x (FP64) staged through the library's static device array (no device
         allocation); needs a prior heff_apply at this index and state."""

@@ -480,6 +480,26 @@ int c2g_dmrg_2dm_trace_energy(const c2g_dmrg* d, double* trace, double* energy) 
     if (energy) *energy = dm->energy();
   });
 }
+int c2g_dmrg_get_correlations(const c2g_dmrg* d, int ham_order, double* cspin, double* cdens, double* cspinflip,
+                              double* cdirad, double* mutinfo, double* entropy) {
+  return guarded([&] {
+    NEED(d);
+    const CheMPS2::Correlations* c = d->d->getCorrelations();
+    if (!c) throw std::invalid_argument("get_correlations: none computed (call c2g_dmrg_calc_2dm)");
+    const int L = c->gL();
+    for (int r = 0; r < L; r++) {
+      if (entropy) entropy[r] = ham_order ? c->SingleOrbitalEntropy_HAM(r) : c->SingleOrbitalEntropy_DMRG(r);
+      for (int q = 0; q < L; q++) {
+        const size_t at = r + static_cast<size_t>(L) * q;
+        if (cspin) cspin[at] = ham_order ? c->getCspin_HAM(r, q) : c->getCspin_DMRG(r, q);
+        if (cdens) cdens[at] = ham_order ? c->getCdens_HAM(r, q) : c->getCdens_DMRG(r, q);
+        if (cspinflip) cspinflip[at] = ham_order ? c->getCspinflip_HAM(r, q) : c->getCspinflip_DMRG(r, q);
+        if (cdirad) cdirad[at] = ham_order ? c->getCdirad_HAM(r, q) : c->getCdirad_DMRG(r, q);
+        if (mutinfo) mutinfo[at] = ham_order ? c->getMutualInformation_HAM(r, q) : c->getMutualInformation_DMRG(r, q);
+      }
+    }
+  });
+}
 int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n) {
   return guarded([&] {
     NEED(d);

@@ -13,6 +13,7 @@
 #include <unordered_map>
 
 #include "davidson.hpp"
+#include "correlations.hpp"
 #include "gauge.hpp"
 #include "twodm.hpp"
 #include "compile.hpp"
@@ -325,12 +326,59 @@ void DMRG::calc2DMandCorrelations() {
     }
   }
   two_dm_->correct_higher_multiplicities();
-  // back to the state of a finished right sweep: MPS[0 .. L-2] left-normalised, the
-  // left operators of boundaries 0 .. L-3
+  // Correlation pass from the left (CheMPS2/DMRGtechnics.cpp:157-176), which also brings
+  // the state back to that of a finished right sweep: MPS[0 .. L-2] left-normalised, the
+  // left operators of boundaries 0 .. L-3.
+  corr_ = std::make_unique<Correlations>(Prob, two_dm_.get());
+  std::unique_ptr<c2g::CorrTensors> cprev;
+  double* dprev = nullptr;
   for (int site = 0; site < L - 1; site++) {
     gauge_left_normalize(site, true);
+    const int s = site + 1;  // the orthogonality centre
+    auto cnext = std::make_unique<c2g::CorrTensors>();
+    const int slot = (s % 2 == 0) ? c2g::kSlotCorr0 : c2g::kSlotCorr1;
+    c2g::allocate_corr(*cnext, *denBK, s, slot);
+    double* dnext = rt->alloc(std::max<int64_t>(cnext->size, 1));
+    rt->zero(dnext, cnext->size);
+    rt->set_slot(slot, dnext);
+    {
+      TaskBuilder tb;
+      c2g::compile_corr_update(tb, *denBK, *Prob, L, s, cprev.get(), *cnext, mps_tensor(mps_lay[site].get(), site));
+      auto dp = rt->upload(tb.finalize());
+      rt->run(*dp, nullptr, nullptr);
+    }
+    {
+      TaskBuilder tb;
+      const int64_t work = c2g::compile_corr_fill(tb, *denBK, s, mps_tensor(mps_lay[s].get(), s), *cnext);
+      auto dp = rt->upload(tb.finalize());
+      const int nv = s * c2g::kCorrValues;
+      double* dwork = rt->alloc(std::max<int64_t>(work, 1));
+      double* dy = rt->alloc(nv);
+      rt->zero(dy, nv);
+      rt->set_slot(c2g::kSlotWork, dwork);
+      rt->run(*dp, nullptr, dy);
+      std::vector<double> values(nv);
+      C2G_CUDA(cudaMemcpyAsync(values.data(), dy, sizeof(double) * nv, cudaMemcpyDeviceToHost, rt->stream()));
+      rt->sync();
+      rt->set_slot(c2g::kSlotWork, nullptr);
+      rt->release(dwork);
+      rt->release(dy);
+      for (int p = 0; p < s; p++) corr_->fill_pair(p, s, values.data() + p * c2g::kCorrValues);
+    }
+    if (dprev) {
+      rt->set_slot((s % 2 == 0) ? c2g::kSlotCorr1 : c2g::kSlotCorr0, nullptr);
+      rt->release(dprev);
+    }
+    cprev = std::move(cnext);
+    dprev = dnext;
     if (site <= L - 3) update_moving_right(site);
   }
+  if (dprev) {
+    rt->sync();
+    rt->release(dprev);
+  }
+  rt->set_slot(c2g::kSlotCorr0, nullptr);
+  rt->set_slot(c2g::kSlotCorr1, nullptr);
 }
 
 void DMRG::upload_mps(int site, const std::vector<double>& data) {

@@ -15,6 +15,7 @@
 #include "ConvergenceScheme.h"
 #include "Problem.h"
 #include "SyBookkeeper.h"
+#include "Correlations.h"
 #include "TwoDM.h"
 
 namespace c2g {
@@ -95,13 +96,15 @@ class DMRG {
   // at `index` must already exist for the current state (a heff_apply_host call there).
   void heff_apply_noalloc(const int index, const double* x, double* y, const long long n);
 
-  // CheMPS2/DMRG.h calc2DMandCorrelations (CheMPS2/DMRGtechnics.cpp:40-120): the
-  // two-particle density matrix of the current state, one site at a time from the right
-  // with the MPS brought into mixed-canonical form around it; afterwards the MPS is left-
-  // canonical again and the operators are those of a finished right sweep, so Solve() can
-  // continue. get2DM() returns it (null before the first call).
+  // CheMPS2/DMRG.h calc2DMandCorrelations (CheMPS2/DMRGtechnics.cpp:40-262 without the
+  // 3-RDM): the two-particle density matrix of the current state, one site at a time from
+  // the right with the MPS brought into mixed-canonical form around it, then the
+  // correlation functions and the two-orbital mutual information in a pass from the left
+  // (which also restores a left-canonical MPS and the operators of a finished right sweep,
+  // so Solve() can continue). get2DM() / getCorrelations() return them (null before).
   void calc2DMandCorrelations();
   const TwoDM* get2DM() const { return two_dm_.get(); }
+  const Correlations* getCorrelations() const { return corr_.get(); }
 
  private:
   struct HeffCache;
@@ -119,6 +122,7 @@ class DMRG {
   std::string dims_key(const char* kind, const int index, const int bmin, const int bmax, const int extra = 0) const;
 
   std::unique_ptr<TwoDM> two_dm_;
+  std::unique_ptr<Correlations> corr_;
   void download_mps(int site, std::vector<double>& data);
   void gauge_left_normalize(int site, bool into_next);
   void gauge_right_normalize(int site);

@@ -993,6 +993,12 @@ struct Emit {
 }  // namespace
 
 // CheMPS2/DMRGoperators.cpp:243-575 (updateMovingRight) and :576-908 (updateMovingLeft)
+void emit_generic_update(TaskBuilder& tb, const SyBookkeeper& bk, const Problem& prob, const MpsT& T, int L,
+                         const OpT& out, const OpT& prev) {
+  Emit e{tb, bk, prob, T, L};
+  e.generic_update(out, prev);
+}
+
 void compile_update(TaskBuilder& tb, const UpdateContext& ctx) {
   const SyBookkeeper& bk = *ctx.bk;
   const Problem& prob = *ctx.prob;

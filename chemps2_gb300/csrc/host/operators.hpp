@@ -91,6 +91,12 @@ struct UpdateContext {
   int shard = 0, nshards = 1;
 };
 
+// The generic TensorOperator::update (CheMPS2/TensorOperator.cpp:163-405) of `out`, at the
+// boundary of its layout, from `prev` at the previous boundary in out's direction, through
+// the MPS tensor T of the site between them.
+void emit_generic_update(TaskBuilder& tb, const CheMPS2::SyBookkeeper& bk, const CheMPS2::Problem& prob,
+                         const MpsT& T, int L, const OpT& out, const OpT& prev);
+
 // Records the whole operator update of one boundary. Stage 1 builds every tensor from
 // the previous boundary; stage 2 adds the freshly made pair operators into the
 // complementary A/B/C/D tensors (CheMPS2/DMRGoperators.cpp:370-403, :703-736).

@@ -49,6 +49,8 @@ enum Slot : int {
   kSlotCombo = 3,   // combined blocks of the program being run
   kSlotWork = 4,    // truncation workspace (assembled sector matrices, Gram, eigvecs)
   kSlotOnes = 5,    // a vector of 1.0, at least as long as the largest sector dimension
+  kSlotCorr0 = 6,   // correlation-pass tensors of alternating boundaries
+  kSlotCorr1 = 7,
   kSlotMpsBase = 8, // + site: MPS tensors
 };
 inline int slot_ops(int L, int boundary) { return kSlotMpsBase + L + boundary; }

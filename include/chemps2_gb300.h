@@ -145,6 +145,12 @@ int c2g_dmrg_calc_2dm(c2g_dmrg* d);
 int c2g_dmrg_get_2dm(const c2g_dmrg* d, int ham_order, double* A, double* B);
 /* TwoDM::trace (= N(N-1)) and TwoDM::energy (Econst + 1/2 sum A h). */
 int c2g_dmrg_2dm_trace_energy(const c2g_dmrg* d, double* trace, double* energy);
+/* DMRG::getCorrelations (CheMPS2/Correlations.cpp), filled by c2g_dmrg_calc_2dm: L x L
+ * tables (row + L*col) Cspin, Cdens, Cspinflip, Cdirad and the two-orbital mutual
+ * information, and the L single-orbital entropies; ham_order as c2g_dmrg_get_2dm. Any
+ * pointer may be NULL. */
+int c2g_dmrg_get_correlations(const c2g_dmrg* d, int ham_order, double* cspin, double* cdens, double* cspinflip,
+                              double* cdirad, double* mutinfo, double* entropy);
 /* No counterpart in the reference. As c2g_dmrg_heff_apply (FP64, no join, no diagonal)
  * without any device allocation: x and y are staged through a static device array of
  * 2 M doubles shared by the whole process (n up to about 1 M). The Heff program at `index`

@@ -10,6 +10,8 @@
 // every spin >= S; the tests use systems whose lowest state in it has spin S.
 #include <algorithm>
 #include <cmath>
+#include <functional>
+#include <map>
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
@@ -168,9 +170,14 @@ int oracle_fci_ground_state(int L, const int* orb_irrep, const double* tmat, con
                           nullptr);
 }
 
-int oracle_fci_state(int L, const int* orb_irrep, const double* tmat, const double* vmat, double econst, int n_up,
-                     int n_down, int irrep, double tol, int max_iter, double* energy, int64_t* dim, double* A,
-                     double* B) {
+}  // extern "C"
+
+namespace {
+// The ground state of the determinant space; `extra` sees the solver and the normalised
+// eigenvector.
+int fci_core(int L, const int* orb_irrep, const double* tmat, const double* vmat, double econst, int n_up,
+             int n_down, int irrep, double tol, int max_iter, double* energy, int64_t* dim, double* A, double* B,
+             const std::function<void(FCI&, const std::vector<double>&)>& extra) {
   try {
     if (L > 24) throw std::invalid_argument("FCI oracle: at most 24 orbitals");
     FCI f;
@@ -347,11 +354,198 @@ int oracle_fci_state(int L, const int* orb_irrep, const double* tmat, const doub
               if (B) B[at] = g[0][0] + g[1][1] - g[0][1] - g[1][0];
             }
     }
+    if (extra) {
+      double nr = 0.0;
+      for (double x : ritz) nr += x * x;
+      nr = std::sqrt(nr);
+      std::vector<double> v(ritz);
+      for (double& x : v) x /= nr;
+      extra(f, v);
+    }
     return 0;
   } catch (const std::exception& e) {
     g_fci_err = e.what();
     return -1;
   }
+}
+
+// Eigenvalues of a symmetric n x n matrix (cyclic Jacobi).
+std::vector<double> sym_eig(std::vector<double> a, int n) {
+  for (int sw = 0; sw < 100; sw++) {
+    double off = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++)
+        if (i != j) off += a[i + n * j] * a[i + n * j];
+    if (off < 1e-32) break;
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double apq = a[p + n * q];
+        if (apq == 0.0) continue;
+        const double tau = (a[q + n * q] - a[p + n * p]) / (2 * apq);
+        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1 + tau * tau));
+        const double c = 1 / std::sqrt(1 + t * t), sn = t * c;
+        for (int j = 0; j < n; j++) {
+          const double x = a[p + n * j], y = a[q + n * j];
+          a[p + n * j] = c * x - sn * y;
+          a[q + n * j] = sn * x + c * y;
+        }
+        for (int i = 0; i < n; i++) {
+          const double x = a[i + n * p], y = a[i + n * q];
+          a[i + n * p] = c * x - sn * y;
+          a[i + n * q] = sn * x + c * y;
+        }
+      }
+  }
+  std::vector<double> ev(n);
+  for (int i = 0; i < n; i++) ev[i] = a[i + n * i];
+  return ev;
+}
+
+double entropy_of(const std::vector<double>& ev) {
+  double e = 0.0;
+  for (double x : ev)
+    if (x > 1e-100) e -= x * std::log(x);
+  return e;
+}
+
+// Reduced density matrix of a set of spin orbitals ("modes", global index o for up and
+// L + o for down; the fermionic order is all up modes, then all down modes), in the basis
+// c+_i |vac> with c+_i the product of the creators of configuration i in ascending mode
+// order: rho_ij = <psi| c+_i P_vac c_j |psi>, P_vac the projector on the empty modes.
+std::vector<double> mode_rdm(FCI& f, const std::vector<double>& psi, const std::vector<int>& modes) {
+  const int L = f.L, nm = static_cast<int>(modes.size()), dim = 1 << nm;
+  const size_t nb = f.B.str.size();
+  std::vector<double> rho(size_t(dim) * dim, 0.0);
+  auto det_mask = [&](size_t d) {
+    return f.A.str[f.dets[d].first] | (f.B.str[f.dets[d].second] << L);
+  };
+  auto find = [&](uint64_t m) -> int64_t {
+    const uint64_t a = m & ((uint64_t(1) << L) - 1), b = m >> L;
+    const int ia = f.A.index_of[a], ib = f.B.index_of[b];
+    if (ia < 0 || ib < 0) return -1;
+    return f.det_of[size_t(ia) * nb + ib];
+  };
+  auto sign_before = [](uint64_t m, int k) { return (__builtin_popcountll(m & ((uint64_t(1) << k) - 1)) & 1) ? -1 : 1; };
+  for (size_t d = 0; d < f.dets.size(); d++) {
+    const double cd = psi[d];
+    if (cd == 0.0) continue;
+    const uint64_t m0 = det_mask(d);
+    // configuration j of the modes in this determinant; c_j = (c+_j)^+ applies the
+    // annihilator of the lowest mode first
+    int j = 0;
+    for (int t = 0; t < nm; t++)
+      if (m0 >> modes[t] & 1) j |= 1 << t;
+    int sgn = 1;
+    uint64_t m = m0;
+    for (int t = 0; t < nm; t++)
+      if (j >> t & 1) {
+        sgn *= sign_before(m, modes[t]);
+        m &= ~(uint64_t(1) << modes[t]);
+      }
+    // c+_i creates configuration i in ascending order applied right to left: the last
+    // creator acts first
+    for (int i = 0; i < dim; i++) {
+      int s2 = sgn;
+      uint64_t mm = m;
+      for (int t = nm - 1; t >= 0; t--)
+        if (i >> t & 1) {
+          s2 *= sign_before(mm, modes[t]);
+          mm |= uint64_t(1) << modes[t];
+        }
+      const int64_t e = find(mm);
+      if (e < 0) continue;
+      rho[i + size_t(dim) * j] += psi[e] * s2 * cd;
+    }
+  }
+  return rho;
+}
+}  // namespace
+
+extern "C" {
+
+int oracle_fci_state(int L, const int* orb_irrep, const double* tmat, const double* vmat, double econst, int n_up,
+                     int n_down, int irrep, double tol, int max_iter, double* energy, int64_t* dim, double* A,
+                     double* B) {
+  return fci_core(L, orb_irrep, tmat, vmat, econst, n_up, n_down, irrep, tol, max_iter, energy, dim, A, B, nullptr);
+}
+
+// Two-orbital density matrix of orbitals p < q as the plain partial trace in the orbital
+// tensor-product basis: amplitudes in the orbital-major fermionic order (0 up, 0 down,
+// 1 up, ...) grouped by the configuration of the other orbitals, with no Jordan-Wigner
+// string for the orbitals between p and q.
+std::vector<double> orbital_pair_rdm(FCI& f, const std::vector<double>& psi, int p, int q) {
+  const int L = f.L;
+  std::map<std::pair<uint64_t, uint64_t>, std::vector<std::pair<int, double>>> env;
+  for (size_t d = 0; d < f.dets.size(); d++) {
+    if (psi[d] == 0.0) continue;
+    const uint64_t a = f.A.str[f.dets[d].first], b = f.B.str[f.dets[d].second];
+    // sign of reordering all-up-then-all-down into orbital-major order
+    int swaps = 0;
+    for (int i = 0; i < L; i++)
+      if (b >> i & 1) swaps += __builtin_popcountll(a >> (i + 1));
+    const double amp = (swaps & 1) ? -psi[d] : psi[d];
+    const int cfg = int(a >> p & 1) + 2 * int(b >> p & 1) + 4 * int(a >> q & 1) + 8 * int(b >> q & 1);
+    const uint64_t clear = ~((uint64_t(1) << p) | (uint64_t(1) << q));
+    env[{a & clear, b & clear}].push_back({cfg, amp});
+  }
+  std::vector<double> rho(256, 0.0);
+  for (const auto& kv : env)
+    for (const auto& x : kv.second)
+      for (const auto& y : kv.second) rho[x.first + 16 * y.first] += x.second * y.second;
+  return rho;
+}
+
+// Single-orbital entropies s1[L] and the mutual information mi[L*L] (row + L col):
+// I_pq = (s_p + s_q - s_pq) / 2 from the one- and two-orbital reduced density matrices
+// of the FCI ground state (the quantities of CheMPS2/Correlations.cpp:165-351), averaged
+// over the spin multiplet like the reference's (its density matrices carry the factor
+// 1 / (2S + 1)): for n_up != n_down the density matrices of the state and of its spin
+// partner with n_up and n_down exchanged are averaged, which is the multiplet average
+// for a doublet (the case this oracle covers besides singlets).
+// jw != 0: the fermionic two-orbital RDM (mode operators, the parity of the orbitals
+// between p and q included); jw == 0: the tensor-product partial trace without it, the
+// definition the reference's correlation tensors follow (TensorGYZ / TensorKM are
+// updated without the Jordan-Wigner phase, CheMPS2/TensorKM.cpp:27-30).
+int oracle_fci_mutual_information(int L, const int* orb_irrep, const double* tmat, const double* vmat,
+                                  double econst, int n_up, int n_down, int irrep, double tol, int max_iter, int jw,
+                                  double* energy, double* s1, double* mi) {
+  if (std::abs(n_up - n_down) > 1) {
+    g_fci_err = "FCI oracle: mutual information only for singlets and doublets";
+    return -1;
+  }
+  std::vector<std::vector<double>> r1(L, std::vector<double>(16, 0.0));
+  std::vector<std::vector<double>> r2(size_t(L) * L, std::vector<double>(256, 0.0));
+  const int nstates = (n_up == n_down) ? 1 : 2;
+  for (int st = 0; st < nstates; st++) {
+    const int nu = st == 0 ? n_up : n_down, nd = st == 0 ? n_down : n_up;
+    int64_t dim = 0;
+    double e = 0.0;
+    const int rc = fci_core(L, orb_irrep, tmat, vmat, econst, nu, nd, irrep, tol, max_iter, &e, &dim, nullptr, nullptr,
+                            [&](FCI& f, const std::vector<double>& psi) {
+                              for (int p = 0; p < L; p++) {
+                                const std::vector<double> r = mode_rdm(f, psi, {p, L + p});
+                                for (int k = 0; k < 16; k++) r1[p][k] += r[k] / nstates;
+                                for (int q = p + 1; q < L; q++) {
+                                  const std::vector<double> rr =
+                                      jw ? mode_rdm(f, psi, {p, q, L + p, L + q}) : orbital_pair_rdm(f, psi, p, q);
+                                  for (int k = 0; k < 256; k++) r2[p + size_t(L) * q][k] += rr[k] / nstates;
+                                }
+                              }
+                            });
+    if (rc != 0) return rc;
+    if (st == 0) *energy = e;
+  }
+  std::vector<double> s(L);
+  for (int p = 0; p < L; p++) s[p] = entropy_of(sym_eig(r1[p], 4));
+  for (int p = 0; p < L; p++) {
+    s1[p] = s[p];
+    mi[p + size_t(L) * p] = 0.0;
+    for (int q = p + 1; q < L; q++) {
+      const double spq = entropy_of(sym_eig(r2[p + size_t(L) * q], 16));
+      mi[p + size_t(L) * q] = mi[q + size_t(L) * p] = 0.5 * (s[p] + s[q] - spq);
+    }
+  }
+  return 0;
 }
 
 }  // extern "C"

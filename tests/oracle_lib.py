@@ -60,6 +60,22 @@ def fci_2rdm(model: Model, n_up: int, n_down: int, irrep: int, tol=1e-11):
     return e.value, A.reshape((L, L, L, L), order="F"), B.reshape((L, L, L, L), order="F")
 
 
+def fci_mutual_information(model: Model, n_up: int, n_down: int, irrep: int, tol=1e-11, jw=False):
+    """FCI energy, single-orbital entropies [L] and mutual information [L, L]; jw: with the
+    parity string of the orbitals between the pair (fermionic RDM), otherwise the
+    tensor-product partial trace of the reference's definition."""
+    L = model.L
+    e = C.c_double()
+    s1 = np.zeros(L)
+    mi = np.zeros(L * L)
+    rc = lib().oracle_fci_mutual_information(L, _ip(model.irreps), _dp(model.tflat()), _dp(model.vflat()),
+                                             C.c_double(model.econst), n_up, n_down, irrep, C.c_double(tol), 600,
+                                             int(bool(jw)), C.byref(e), _dp(s1), _dp(mi))
+    if rc != 0:
+        raise RuntimeError(lib().oracle_fci_last_error().decode())
+    return e.value, s1, mi.reshape((L, L), order="F")
+
+
 class OracleDMRG:
     """CPU DMRG of the oracle. schedule: list of (D, econv, max_sweeps, noise, rtol)."""
 

@@ -158,3 +158,22 @@ def test_fci_2rdm_identities(make, n_up, n_down, irrep):
     for X in (A, B):
         assert np.allclose(X, X.transpose(1, 0, 3, 2), atol=1e-10)
         assert np.allclose(X, X.transpose(2, 3, 0, 1), atol=1e-10)
+
+
+def test_fci_mutual_information_consistent_with_2rdm():
+    """The oracle's single-orbital entropies from fermionic mode RDMs equal the formula of
+    CheMPS2/Correlations.cpp:165-177 evaluated on its FCI 2-RDM; the mutual information is
+    symmetric and non-negative."""
+    m = models.hubbard(6, 4.0)
+    E1, s1, mi = ol.fci_mutual_information(m, 3, 3, 0)
+    E2, A, _ = ol.fci_2rdm(m, 3, 3, 0)
+    assert abs(E1 - E2) < 1e-10
+    N = 6
+    g1 = np.einsum("arbr->ab", A) / (N - 1)
+    for i in range(m.L):
+        v4 = 0.5 * A[i, i, i, i]
+        v23 = 0.5 * (g1[i, i] - A[i, i, i, i])
+        v1 = 1 - v4 - 2 * v23
+        s = -sum(x * np.log(x) for x in (v1, v23, v23, v4) if x > 1e-100)
+        assert abs(s - s1[i]) < 1e-9
+    assert np.allclose(mi, mi.T) and mi.min() >= -1e-12
