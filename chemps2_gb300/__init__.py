@@ -386,6 +386,14 @@ class DMRG:
         _check(load().c2g_dmrg_heff_apply_fp32(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
         return y
 
+    def activateExcitations(self, maxExcIn):
+        """DMRG::activateExcitations: allow up to maxExcIn stored lower states."""
+        _check(load().c2g_dmrg_activate_excitations(self._d, int(maxExcIn)))
+
+    def newExcitation(self, EshiftIn):
+        """DMRG::newExcitation: store the current state; Solve() then targets the next one."""
+        _check(load().c2g_dmrg_new_excitation(self._d, C.c_double(EshiftIn)))
+
     def calc2DMandCorrelations(self):
         """The two-particle density matrices of the current state (DMRG::calc2DMandCorrelations)."""
         _check(load().c2g_dmrg_calc_2dm(self._d))

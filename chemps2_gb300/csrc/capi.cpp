@@ -449,6 +449,18 @@ int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64
     d->d->heff_apply_host(index, false, x, y, nullptr, n, 1);
   });
 }
+int c2g_dmrg_activate_excitations(c2g_dmrg* d, int max_exc) {
+  return guarded([&] {
+    NEED(d);
+    d->d->activateExcitations(max_exc);
+  });
+}
+int c2g_dmrg_new_excitation(c2g_dmrg* d, double eshift) {
+  return guarded([&] {
+    NEED(d);
+    d->d->newExcitation(eshift);
+  });
+}
 int c2g_dmrg_calc_2dm(c2g_dmrg* d) {
   return guarded([&] {
     NEED(d);

@@ -14,6 +14,7 @@
 
 #include "davidson.hpp"
 #include "correlations.hpp"
+#include "excite.hpp"
 #include "gauge.hpp"
 #include "twodm.hpp"
 #include "compile.hpp"
@@ -138,6 +139,18 @@ struct DMRG::HeffCache {
   int64_t xbuf_len = 0;
 };
 
+// A stored (lower) state of the excited-state machinery: its bookkeeper and MPS, and its
+// overlap tensors with the current MPS at every boundary.
+struct DMRG::ExcState {
+  std::unique_ptr<SyBookkeeper> bk;
+  std::vector<std::unique_ptr<MpsLayout>> lay;
+  std::vector<double*> mps;
+  double eshift = 0.0;
+  std::vector<std::unique_ptr<c2g::OverlapLayout>> olay;  // [reference index b]: boundary b + 1
+  std::vector<double*> odev;
+  std::vector<int> odir;  // 1 moving right, 2 moving left, 0 none
+};
+
 DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool, const std::string, int* occupancies)
     : Prob(ProbIn), OptScheme(OptSchemeIn) {
   heff_cache_ = std::make_unique<HeffCache>();
@@ -175,6 +188,9 @@ DMRG::~DMRG() {
       rt->release(heff_cache_->ybuf);
     }
     for (double* p : mps_dev) rt->release(p);
+    release_overlaps();
+    for (auto& st : exc_)
+      for (double* p : st->mps) rt->release(p);
     for (double* p : ops_dev) rt->release(p);
     for (float* p : ops_dev32) rt->release(p);
     try {
@@ -241,6 +257,92 @@ void DMRG::download_mps(int site, std::vector<double>& data) {
     C2G_CUDA(cudaMemcpyAsync(data.data(), mps_dev[site], sizeof(double) * data.size(), cudaMemcpyDeviceToHost,
                              rt->stream()));
   rt->sync();
+}
+
+int DMRG::exc_slot(int state, bool overlap, int idx) const {
+  return c2g::num_slots(L) + state * 2 * L + (overlap ? L : 0) + idx;
+}
+
+// CheMPS2/DMRG.cpp:464-473
+void DMRG::activateExcitations(const int maxExcIn) {
+  if (maxExcIn < 1) throw std::invalid_argument("activateExcitations: at least one state");
+  if (c2g::num_slots(L) + maxExcIn * 2 * L > c2g::kMaxSlots)
+    throw std::invalid_argument("activateExcitations: too many states for the device slot table");
+  exc_active_ = true;
+  max_exc_ = maxExcIn;
+}
+
+// CheMPS2/DMRG.cpp:475-505
+void DMRG::newExcitation(const double EshiftIn) {
+  if (!exc_active_) throw std::logic_error("newExcitation: excitations are not activated");
+  if (static_cast<int>(exc_.size()) >= max_exc_) throw std::logic_error("newExcitation: maximum number of states");
+  two_dm_.reset();
+  corr_.reset();
+  delete_all_ops();
+  release_overlaps();
+  auto st = std::make_unique<ExcState>();
+  st->eshift = EshiftIn;
+  st->bk = std::move(denBK);
+  st->lay = std::move(mps_lay);
+  st->mps = std::move(mps_dev);
+  st->olay.resize(L - 1);
+  st->odev.assign(L - 1, nullptr);
+  st->odir.assign(L - 1, 0);
+  const int k = static_cast<int>(exc_.size());
+  for (int site = 0; site < L; site++) {
+    rt->set_slot(exc_slot(k, false, site), st->mps[site]);
+    rt->set_slot(c2g::kSlotMpsBase + site, nullptr);
+  }
+  exc_.push_back(std::move(st));
+  mps_lay.clear();
+  mps_lay.resize(L);
+  mps_dev.assign(L, nullptr);
+  setup_mps(nullptr);
+  PreSolve();
+}
+
+void DMRG::release_overlaps() {
+  for (size_t k = 0; k < exc_.size(); k++)
+    for (int b = 0; b < L - 1; b++) {
+      ExcState& st = *exc_[k];
+      if (st.odev[b]) rt->release(st.odev[b]);
+      st.odev[b] = nullptr;
+      st.odir[b] = 0;
+      st.olay[b].reset();
+      rt->set_slot(exc_slot(static_cast<int>(k), true, b), nullptr);
+    }
+}
+
+// The overlap tensors of boundary index + 1 with every stored state, after the operator
+// update of that boundary (CheMPS2/DMRGoperators.cpp:556-566, :889-899).
+void DMRG::update_overlaps(const int index, const bool moving_right) {
+  for (size_t k = 0; k < exc_.size(); k++) {
+    ExcState& st = *exc_[k];
+    const int site = moving_right ? index : index + 1;
+    const int pidx = moving_right ? index - 1 : index + 1;
+    const bool edge = moving_right ? (index == 0) : (index == L - 2);
+    if (!edge && st.odir[pidx] != (moving_right ? 1 : 2))
+      throw std::logic_error("excited states: overlap tensors of the previous boundary missing");
+    auto lay = std::make_unique<c2g::OverlapLayout>();
+    lay->build(*denBK, *st.bk, index + 1);
+    if (st.odev[index]) rt->release(st.odev[index]);
+    st.odev[index] = rt->alloc(std::max<int64_t>(lay->size(), 1));
+    rt->zero(st.odev[index], lay->size());
+    const int slot = exc_slot(static_cast<int>(k), true, index);
+    rt->set_slot(slot, st.odev[index]);
+    c2g::OverlapT out{lay.get(), c2g::make_ref(slot, 0)};
+    c2g::OverlapT prev;
+    if (!edge) prev = c2g::OverlapT{st.olay[pidx].get(), c2g::make_ref(exc_slot(static_cast<int>(k), true, pidx), 0)};
+    const MpsT tdown{st.lay[site].get(), c2g::make_ref(exc_slot(static_cast<int>(k), false, site), 0)};
+    TaskBuilder tb;
+    c2g::compile_overlap_update(tb, *denBK, *st.bk, moving_right, index, edge ? nullptr : &prev, out,
+                                mps_tensor(mps_lay[site].get(), site), tdown);
+    auto dp = rt->upload(tb.finalize());
+    rt->run(*dp, nullptr, nullptr);
+    rt->sync();
+    st.olay[index] = std::move(lay);
+    st.odir[index] = moving_right ? 1 : 2;
+  }
 }
 
 // CheMPS2/DMRGtechnics.cpp:276-298
@@ -477,6 +579,7 @@ void DMRG::update_moving_right(const int index) {
   rt->run(dp, nullptr, nullptr);
   if (f32_ops_) refresh_f32(index);
   rt->sync();
+  if (!exc_.empty()) update_overlaps(index, true);
   stats_.t_update += now() - t0;
 }
 
@@ -507,6 +610,7 @@ void DMRG::update_moving_left(const int index) {
   rt->run(dp, nullptr, nullptr);
   if (f32_ops_) refresh_f32(index);
   rt->sync();
+  if (!exc_.empty()) update_overlaps(index, false);
   stats_.t_update += now() - t0;
 }
 
@@ -608,9 +712,52 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   C2G_CUDA(cudaEventCreate(&e0));
   C2G_CUDA(cudaEventCreate(&e1));
   float mv_ms = 0.f;
+  // Projection vectors of the stored lower states (CheMPS2/DMRGtechnics.cpp:509-620):
+  // y += sum_s (V_s . x) V_s after every matvec (CheMPS2/HeffDiagrams1.cpp:65-86).
+  const int nexc = static_cast<int>(exc_.size());
+  double* vmat = nullptr;
+  double* vcoef = nullptr;
+  if (nexc > 0) {
+    vmat = rt->alloc(veclen * nexc);
+    vcoef = rt->alloc(std::max(nexc, 1));
+    for (int k = 0; k < nexc; k++) {
+      ExcState& st = *exc_[k];
+      TwoSiteLayout Sk;
+      Sk.build(*st.bk, index);
+      double* sup = rt->alloc(std::max<int64_t>(Sk.size(), 1));
+      {
+        TaskBuilder tb;
+        c2g::compile_join(tb, *st.bk, Sk, MpsT{st.lay[index].get(), c2g::make_ref(exc_slot(k, false, index), 0)},
+                          MpsT{st.lay[index + 1].get(), c2g::make_ref(exc_slot(k, false, index + 1), 0)});
+        auto dp = rt->upload(tb.finalize());
+        rt->run(*dp, nullptr, sup);
+      }
+      {
+        if (index > 0 && st.odir[index - 1] != 1) throw std::logic_error("excited states: left overlaps missing");
+        if (index + 1 < L - 1 && st.odir[index + 1] != 2) throw std::logic_error("excited states: right overlaps missing");
+        c2g::OverlapT ol, orr;
+        if (index > 0) ol = c2g::OverlapT{st.olay[index - 1].get(), c2g::make_ref(exc_slot(k, true, index - 1), 0)};
+        if (index + 1 < L - 1)
+          orr = c2g::OverlapT{st.olay[index + 1].get(), c2g::make_ref(exc_slot(k, true, index + 1), 0)};
+        TaskBuilder tb;
+        c2g::compile_veff(tb, S, Sk, c2g::make_ref(c2g::kSlotX, 0), index > 0 ? &ol : nullptr,
+                          index + 1 < L - 1 ? &orr : nullptr, std::sqrt(st.eshift) / (Prob->gTwoS() + 1.0),
+                          c2g::make_ref(c2g::kSlotY, 0));
+        auto dp = rt->upload(tb.finalize());
+        rt->run(*dp, sup, vmat + static_cast<int64_t>(k) * veclen);
+      }
+      rt->sync();
+      rt->release(sup);
+    }
+  }
   auto matvec = [&](const double* x, double* y, c2g::Precision prec) {
     C2G_CUDA(cudaEventRecord(e0, s));
     rt->run(*dph, const_cast<double*>(x), y, prec, veclen);
+    if (nexc > 0) {
+      C2G_CUDA(c2g::launch_multi_dot(vmat, veclen, nexc, x, veclen, rt->partial(), vcoef, s));
+      C2G_CUDA(c2g::launch_combine(y, 1.0, vmat, veclen, vcoef, nexc, veclen, s));
+      c2g::count_launches(3);
+    }
     C2G_CUDA(cudaEventRecord(e1, s));
     C2G_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -622,6 +769,8 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   rt->release(diag);
+  if (vmat) rt->release(vmat);
+  if (vcoef) rt->release(vcoef);
   stats_.n_matvec += ds.n_matvec;
   stats_.n_davidson++;
   stats_.t_matvec += 1e-3 * mv_ms;

@@ -106,6 +106,13 @@ class DMRG {
   const TwoDM* get2DM() const { return two_dm_.get(); }
   const Correlations* getCorrelations() const { return corr_.get(); }
 
+  // CheMPS2/DMRG.h activateExcitations / newExcitation (CheMPS2/DMRG.cpp:464-505): after
+  // newExcitation(E_shift) the current state is stored and Solve() targets the next one,
+  // every stored state s adding E_shift_s |V_s><V_s| to the effective Hamiltonian
+  // (CheMPS2/HeffDiagrams1.cpp:65-86); at most maxExcIn stored states.
+  void activateExcitations(const int maxExcIn);
+  void newExcitation(const double EshiftIn);
+
  private:
   struct HeffCache;
   HeffCache& heff_program(const int index, const bool with_diag);
@@ -120,6 +127,14 @@ class DMRG {
   c2g::DevProgram& program(const std::string& key, const std::function<c2g::Compiled()>& build,
                            long long* operand_bytes = nullptr);
   std::string dims_key(const char* kind, const int index, const int bmin, const int bmax, const int extra = 0) const;
+
+  struct ExcState;
+  std::vector<std::unique_ptr<ExcState>> exc_;
+  bool exc_active_ = false;
+  int max_exc_ = 0;
+  int exc_slot(int state, bool overlap, int idx) const;
+  void update_overlaps(int index, bool moving_right);
+  void release_overlaps();
 
   std::unique_ptr<TwoDM> two_dm_;
   std::unique_ptr<Correlations> corr_;

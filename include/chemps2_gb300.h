@@ -134,6 +134,11 @@ int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, doub
 /* As c2g_dmrg_heff_apply with the matvec in FP32 arithmetic (operands converted on load,
  * lane sums in FP32, the output in FP64). No counterpart in the reference. */
 int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64_t n);
+/* DMRG::activateExcitations (CheMPS2/DMRG.cpp:464-473): allow up to max_exc stored states. */
+int c2g_dmrg_activate_excitations(c2g_dmrg* d, int max_exc);
+/* DMRG::newExcitation (CheMPS2/DMRG.cpp:475-505): store the current state; the next
+ * c2g_dmrg_solve targets the next state with the stored ones shifted up by eshift. */
+int c2g_dmrg_new_excitation(c2g_dmrg* d, double eshift);
 /* DMRG::calc2DMandCorrelations (CheMPS2/DMRGtechnics.cpp:40-120; the 2-RDM part): the
  * spin-summed two-particle density matrices A and B of the current state
  * (CheMPS2/TwoDM.cpp:445-640). The state and the operators afterwards are those of a

@@ -6,7 +6,8 @@ outputs are committed so that the tests never read the reference at run time.
   * N2.STO3G.FCIDUMP    copied from tests/matrixelements/N2.STO3G.FCIDUMP (the input of
                         the reference's tests/test1.cpp.in and tests/test5.cpp.in)
   * golden.json         energies the reference's tests assert, parsed from their sources:
-                        tests/test5.cpp.in (N2 STO-3G ground state, D = 1000) and
+                        tests/test5.cpp.in (N2 STO-3G ground and two excited states,
+                        D = 1000) and
                         tests/test12.cpp.in (the BCS pairing model, L = 8)
 """
 from __future__ import annotations
@@ -39,6 +40,9 @@ def main(reference: Path) -> None:
             "reorder": "d2h",
             "schedule": [[1000, 1e-12, 100, 0.0, 1e-5]],
             "energy": -e5[0],
+            # the two excited states of the same test: newExcitation(20.0) twice
+            "excited_eshift": 20.0,
+            "excited_energies": [-e5[1], -e5[2]],
             "tolerance": 1e-8,
         },
         "bcs_l8": {

@@ -246,3 +246,28 @@ def test_program_cache_reuses_programs_across_sweeps():
     gpu.close()
     assert abs(e3 - e2) < 1e-9 and abs(e2 - e1) < 1e-7
     assert t3 <= 0.2 * t2 + 0.05
+
+
+def test_n2_sto3g_excited_states_golden_of_reference_test5():
+    """The reference's tests/test5.cpp.in: ground state, then two excited states of the same
+    symmetry with newExcitation(20.0) each, energies to 1e-8 of its goldens."""
+    g = GOLDEN["n2_sto3g"]
+    ham = c2g.Hamiltonian(0, g["group"], [], filename=str(GOLDEN_DIR / g["fcidump"]))
+    prob = c2g.Problem(ham, g["two_s"], g["n"], g["irrep"])
+    prob.SetupReorderD2h()
+    scheme = c2g.ConvergenceScheme(1)
+    scheme.set_instruction(0, *g["schedule"][0])
+    c2g.srand(1)
+    gpu = c2g.DMRG(prob, scheme)
+    try:
+        e0 = gpu.Solve()
+        assert abs(e0 - g["energy"]) < g["tolerance"]
+        gpu.activateExcitations(10)
+        energies = []
+        for _ in g["excited_energies"]:
+            gpu.newExcitation(g["excited_eshift"])
+            energies.append(gpu.Solve())
+    finally:
+        gpu.close()
+    for e, ref in zip(energies, g["excited_energies"]):
+        assert abs(e - ref) < g["tolerance"], (energies, g["excited_energies"])
