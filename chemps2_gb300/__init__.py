@@ -310,9 +310,9 @@ class DMRG:
         occ = None
         if occupancies is not None:
             occ = np.ascontiguousarray(occupancies, dtype=np.int32)
-        _check(load().c2g_dmrg_create(Probl._p, OptScheme._s,
-                                      occ.ctypes.data_as(C.POINTER(C.c_int)) if occ is not None else None,
-                                      C.byref(self._d)))
+        _check(load().c2g_dmrg_create_chkpt(Probl._p, OptScheme._s, int(bool(makechkpt)),
+                                            occ.ctypes.data_as(C.POINTER(C.c_int)) if occ is not None else None,
+                                            C.byref(self._d)))
 
     def close(self):
         if getattr(self, "_d", None) and _LIB is not None:
@@ -385,6 +385,16 @@ class DMRG:
         y = np.zeros_like(xx)
         _check(load().c2g_dmrg_heff_apply_fp32(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
         return y
+
+    def loadedMPS(self):
+        """True when the MPS was loaded from a checkpoint file (makechkpt)."""
+        v = C.c_int()
+        _check(load().c2g_dmrg_loaded_mps(self._d, C.byref(v)))
+        return bool(v.value)
+
+    def deleteStoredMPS(self):
+        """DMRG::deleteStoredMPS: remove the checkpoint files of this working directory."""
+        _check(load().c2g_dmrg_delete_stored_mps(self._d))
 
     def activateExcitations(self, maxExcIn):
         """DMRG::activateExcitations: allow up to maxExcIn stored lower states."""

@@ -342,6 +342,30 @@ int c2g_dmrg_create(c2g_problem* p, c2g_scheme* s, const int* occupancies, c2g_d
     *out = d.release();
   });
 }
+int c2g_dmrg_create_chkpt(c2g_problem* p, c2g_scheme* s, int makechkpt, const int* occupancies, c2g_dmrg** out) {
+  return guarded([&] {
+    NEED(p);
+    NEED(s);
+    NEED(out);
+    auto d = std::make_unique<c2g_dmrg>();
+    d->d = std::make_unique<CheMPS2::DMRG>(p->p.get(), s->s.get(), makechkpt != 0, "/tmp",
+                                           const_cast<int*>(occupancies));
+    *out = d.release();
+  });
+}
+int c2g_dmrg_loaded_mps(const c2g_dmrg* d, int* loaded) {
+  return guarded([&] {
+    NEED(d);
+    NEED(loaded);
+    *loaded = d->d->loadedMPS() ? 1 : 0;
+  });
+}
+int c2g_dmrg_delete_stored_mps(c2g_dmrg* d) {
+  return guarded([&] {
+    NEED(d);
+    d->d->deleteStoredMPS();
+  });
+}
 int c2g_dmrg_destroy(c2g_dmrg* d) {
   return guarded([&] { delete d; });
 }

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <cusolverDn.h>
 
 #include "static_scratch.hpp"
@@ -151,8 +152,8 @@ struct DMRG::ExcState {
   std::vector<int> odir;  // 1 moving right, 2 moving left, 0 none
 };
 
-DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool, const std::string, int* occupancies)
-    : Prob(ProbIn), OptScheme(OptSchemeIn) {
+DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool makechkpt, const std::string, int* occupancies)
+    : Prob(ProbIn), OptScheme(OptSchemeIn), makecheckpoints_(makechkpt) {
   heff_cache_ = std::make_unique<HeffCache>();
   pcache_ = std::make_unique<ProgramCache>();
   pcache_->limit = 16LL << 30;
@@ -201,9 +202,102 @@ DMRG::~DMRG() {
 }
 
 // CheMPS2/DMRG.cpp:100-256 (setupBookkeeperAndMPS) with CheMPS2/TensorT.cpp:167-173.
+namespace {
+constexpr char kMpsMagic[8] = {'C', '2', 'G', 'M', 'P', 'S', '0', '1'};
+}  // namespace
+
+// CheMPS2/DMRGmpsio.cpp:27-94 (saveMPS): header, virtual dimensions of every boundary in
+// bookkeeper order, converged flag, then the tensors of every site.
+void DMRG::save_mps(bool converged) const {
+  std::FILE* f = std::fopen(mps_storage_name_.c_str(), "wb");
+  if (!f) throw std::runtime_error("saveMPS: cannot open " + mps_storage_name_);
+  auto put = [&](const void* p, size_t n) {
+    if (std::fwrite(p, 1, n, f) != n) {
+      std::fclose(f);
+      throw std::runtime_error("saveMPS: write failed for " + mps_storage_name_);
+    }
+  };
+  const int32_t head[7] = {L, Prob->gN(), Prob->gTwoS(), Prob->gIrrep(), denBK->getNumberOfIrreps(),
+                           converged ? 1 : 0, 0};
+  put(kMpsMagic, 8);
+  put(head, sizeof(head));
+  const SyBookkeeper& bk = *denBK;
+  for (int b = 0; b <= L; b++)
+    for (int n = bk.gNmin(b); n <= bk.gNmax(b); n++)
+      for (int s2 = bk.gTwoSmin(b, n); s2 <= bk.gTwoSmax(b, n); s2 += 2)
+        for (int i = 0; i < bk.getNumberOfIrreps(); i++) {
+          const int32_t d = bk.gCurrentDim(b, n, s2, i);
+          put(&d, sizeof(d));
+        }
+  for (int site = 0; site < L; site++) {
+    std::vector<double> data(static_cast<size_t>(mps_lay[site]->size()));
+    if (!data.empty())
+      C2G_CUDA(cudaMemcpyAsync(data.data(), mps_dev[site], sizeof(double) * data.size(), cudaMemcpyDeviceToHost,
+                               rt->stream()));
+    rt->sync();
+    const int64_t n = static_cast<int64_t>(data.size());
+    put(&n, sizeof(n));
+    put(data.data(), sizeof(double) * data.size());
+  }
+  std::fclose(f);
+}
+
+// CheMPS2/DMRGmpsio.cpp:96-162 (loadDIM, loadMPS). False when the file does not exist.
+bool DMRG::load_mps() {
+  std::FILE* f = std::fopen(mps_storage_name_.c_str(), "rb");
+  if (!f) return false;
+  auto get = [&](void* p, size_t n) {
+    if (std::fread(p, 1, n, f) != n) {
+      std::fclose(f);
+      throw std::runtime_error("loadMPS: " + mps_storage_name_ + " is truncated");
+    }
+  };
+  char magic[8];
+  get(magic, 8);
+  int32_t head[7];
+  get(head, sizeof(head));
+  if (std::memcmp(magic, kMpsMagic, 8) != 0 || head[0] != L || head[1] != Prob->gN() || head[2] != Prob->gTwoS() ||
+      head[3] != Prob->gIrrep() || head[4] != denBK->getNumberOfIrreps()) {
+    std::fclose(f);
+    throw std::runtime_error("loadMPS: " + mps_storage_name_ + " belongs to another problem");
+  }
+  SyBookkeeper& bk = *denBK;
+  for (int b = 0; b <= L; b++)
+    for (int n = bk.gNmin(b); n <= bk.gNmax(b); n++)
+      for (int s2 = bk.gTwoSmin(b, n); s2 <= bk.gTwoSmax(b, n); s2 += 2)
+        for (int i = 0; i < bk.getNumberOfIrreps(); i++) {
+          int32_t d = 0;
+          get(&d, sizeof(d));
+          if (b > 0 && b < L) bk.SetDim(b, n, s2, i, d);
+        }
+  for (int site = 0; site < L; site++) {
+    mps_lay[site] = std::make_unique<MpsLayout>();
+    mps_lay[site]->build(bk, site);
+    int64_t n = 0;
+    get(&n, sizeof(n));
+    if (n != mps_lay[site]->size()) {
+      std::fclose(f);
+      throw std::runtime_error("loadMPS: tensor sizes in " + mps_storage_name_ + " differ from its dimensions");
+    }
+    std::vector<double> data(static_cast<size_t>(n));
+    get(data.data(), sizeof(double) * data.size());
+    upload_mps(site, data);
+  }
+  std::fclose(f);
+  return true;
+}
+
+// CheMPS2/DMRGmpsio.cpp:164-173
+void DMRG::deleteStoredMPS() {
+  for (int k = 0; k <= static_cast<int>(exc_.size()); k++) std::remove(("CheMPS2_MPS" + std::to_string(k) + ".c2g").c_str());
+}
+
 void DMRG::setup_mps(int* occupancies) {
   denBK = std::make_unique<SyBookkeeper>(Prob, OptScheme->get_D(0));
   if (!denBK->IsPossible()) throw std::invalid_argument("DMRG: the targeted symmetry sector is impossible");
+  mps_storage_name_ = "CheMPS2_MPS" + std::to_string(exc_.size()) + ".c2g";
+  loaded_mps_ = makecheckpoints_ && load_mps();
+  if (loaded_mps_) return;
   std::vector<int> occ;
   if (occupancies) {
     occ.assign(occupancies, occupancies + L);
@@ -629,6 +723,7 @@ double DMRG::Solve() {
       if (verbose)
         std::printf("instruction %d sweep %d: E = %.15f  max discarded weight = %.3e\n", instruction, nIterations,
                     Energy, MaxDiscWeightLastSweep);
+      if (makecheckpoints_) save_mps(false);
       nIterations++;
     }
   }

@@ -113,6 +113,15 @@ class DMRG {
   void activateExcitations(const int maxExcIn);
   void newExcitation(const double EshiftIn);
 
+  // MPS checkpoints (CheMPS2/DMRGmpsio.cpp:27-173, CheMPS2/DMRG.cpp:106-158,334): with
+  // makechkpt, the MPS of the current state is written to CheMPS2_MPS<state>.c2g in the
+  // working directory after every left+right sweep, and a DMRG constructed (or a new
+  // excitation set up) while that file exists starts from it. The file holds the same
+  // content as the reference's HDF5 file (virtual dimensions, MPS tensors, a converged flag)
+  // in a flat binary layout. deleteStoredMPS removes the files.
+  void deleteStoredMPS();
+  bool loadedMPS() const { return loaded_mps_; }
+
  private:
   struct HeffCache;
   HeffCache& heff_program(const int index, const bool with_diag);
@@ -127,6 +136,12 @@ class DMRG {
   c2g::DevProgram& program(const std::string& key, const std::function<c2g::Compiled()>& build,
                            long long* operand_bytes = nullptr);
   std::string dims_key(const char* kind, const int index, const int bmin, const int bmax, const int extra = 0) const;
+
+  bool makecheckpoints_ = false;
+  bool loaded_mps_ = false;
+  std::string mps_storage_name_;
+  void save_mps(bool converged) const;
+  bool load_mps();
 
   struct ExcState;
   std::vector<std::unique_ptr<ExcState>> exc_;

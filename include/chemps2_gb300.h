@@ -94,6 +94,14 @@ int c2g_wigner9j(int a, int b, int c, int d, int e, int f, int g, int h, int i, 
 /* CheMPS2::DMRG (CheMPS2/include/chemps2/DMRG.h:93-162, CheMPS2/DMRG.cpp:36-452). The
  * constructor builds the random initial MPS and all renormalized operators on the GPU. */
 int c2g_dmrg_create(c2g_problem* p, c2g_scheme* s, const int* occupancies, c2g_dmrg** out);
+/* DMRG(Prob, OptScheme, makechkpt, tmpfolder, occupancies) (CheMPS2/DMRG.cpp:37-158) with
+ * checkpoints: makechkpt != 0 loads CheMPS2_MPS<state>.c2g from the working directory when
+ * it exists and writes it after every sweep (CheMPS2/DMRGmpsio.cpp). */
+int c2g_dmrg_create_chkpt(c2g_problem* p, c2g_scheme* s, int makechkpt, const int* occupancies, c2g_dmrg** out);
+/* 1 when the MPS was loaded from a checkpoint file (the reference's loadedMPS). */
+int c2g_dmrg_loaded_mps(const c2g_dmrg* d, int* loaded);
+/* DMRG::deleteStoredMPS (CheMPS2/DMRGmpsio.cpp:164-173): removes the checkpoint files. */
+int c2g_dmrg_delete_stored_mps(c2g_dmrg* d);
 int c2g_dmrg_destroy(c2g_dmrg* d);
 int c2g_dmrg_solve(c2g_dmrg* d, double* energy);            /* DMRG::Solve    */
 int c2g_dmrg_presolve(c2g_dmrg* d);                         /* DMRG::PreSolve */

@@ -271,3 +271,30 @@ def test_n2_sto3g_excited_states_golden_of_reference_test5():
         gpu.close()
     for e, ref in zip(energies, g["excited_energies"]):
         assert abs(e - ref) < g["tolerance"], (energies, g["excited_energies"])
+
+
+def test_mps_checkpoint_restart(tmp_path, monkeypatch):
+    """makechkpt (CheMPS2/DMRGmpsio.cpp, CheMPS2/DMRG.cpp:106-158,334): a DMRG writes its MPS
+    after every sweep; a new DMRG in the same directory starts from that file and, already
+    converged, reproduces the energy in its first sweep."""
+    monkeypatch.chdir(tmp_path)
+    m = models.synthetic_ab_initio(8, 5, 11)
+    ham, prob, scheme = gpu_objects(m, 0, 8, 0, [(64, 1e-10, 4, 0.0, 1e-9)])
+    c2g.srand(5)
+    first = c2g.DMRG(prob, scheme, makechkpt=True)
+    assert not first.loadedMPS()
+    e1 = first.Solve()
+    first.close()
+    assert (tmp_path / "CheMPS2_MPS0.c2g").exists()
+    scheme2 = c2g.ConvergenceScheme(1)
+    scheme2.set_instruction(0, 64, 1e-10, 1, 0.0, 1e-9)
+    second = c2g.DMRG(prob, scheme2, makechkpt=True)
+    try:
+        assert second.loadedMPS()
+        second.reset_stats()
+        e2 = second.Solve()
+        assert abs(e2 - e1) < 1e-8
+        second.deleteStoredMPS()
+    finally:
+        second.close()
+    assert not (tmp_path / "CheMPS2_MPS0.c2g").exists()
