@@ -171,28 +171,39 @@ def cpu_baseline_sample(model, n_matvec=1):
 
 
 def sweep_seconds():
-    """Seconds per left+right sweep of the Hubbard chain L = 16, U = 4, D = 200."""
+    """The Hubbard chain L = 16, U = 4, D = 200 with 4 left+right sweeps (the reference's
+    CPU-runnable configuration), plain FP64 and mixed precision: seconds per sweep over the
+    whole run (compilation and the first sweeps from the random start included) and the
+    energy difference between the two."""
     import chemps2_gb300 as c2g
     from chemps2_gb300.models import hubbard
 
     L = 16
     m = hubbard(L, 4.0)
-    ham = c2g.Hamiltonian(L, 0, m.irreps)
-    for i in range(L - 1):
-        ham.setTmat(i, i + 1, -1.0)
-    for i in range(L):
-        ham.setVmat(i, i, i, i, 4.0)
-    prob = c2g.Problem(ham, 0, L, 0)
-    scheme = c2g.ConvergenceScheme(1)
-    scheme.set_instruction(0, 200, 1e-14, 1, 0.0, 1e-8)
-    c2g.srand(1)
-    d = c2g.DMRG(prob, scheme)
-    d.Solve()  # warm-up sweep: dims grow from the initial distribution
-    t0 = time.perf_counter()
-    e = d.Solve()
-    dt = time.perf_counter() - t0
-    d.close()
-    return {"config": "hubbard L=16 N=16 U=4 D=200", "s_per_sweep": dt, "energy": e}
+    out = {"config": "hubbard L=16 N=16 U=4 D=200, 4 sweeps, Davidson rtol 1e-8"}
+    for mode in ("fp64", "mixed"):
+        ham = c2g.Hamiltonian(L, 0, m.irreps)
+        for i in range(L - 1):
+            ham.setTmat(i, i + 1, -1.0)
+        for i in range(L):
+            ham.setVmat(i, i, i, i, 4.0)
+        prob = c2g.Problem(ham, 0, L, 0)
+        scheme = c2g.ConvergenceScheme(1)
+        scheme.set_instruction(0, 200, 1e-14, 4, 0.0, 1e-8)
+        c2g.srand(1)
+        d = c2g.DMRG(prob, scheme)
+        d.set_precision(mode)
+        t0 = time.perf_counter()
+        e = d.Solve()
+        dt = time.perf_counter() - t0
+        st = d.stats()
+        d.close()
+        out[mode] = {"s_per_sweep": dt / 4, "energy": e, "matvecs": st["n_matvec"],
+                     "fp32_matvecs": st["n_matvec_fp32"]}
+    out["s_per_sweep"] = out["fp64"]["s_per_sweep"]
+    out["mixed_speedup"] = out["fp64"]["s_per_sweep"] / out["mixed"]["s_per_sweep"]
+    out["mixed_energy_error"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"])
+    return out
 
 
 def run_ours(args):

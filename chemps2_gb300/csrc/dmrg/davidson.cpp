@@ -19,6 +19,11 @@ constexpr int kLowdin = 2200;   // keep x keep Loewdin matrix
 constexpr int kSumSq = 2216;    // one sum of squares
 constexpr int kSmall = 2304;
 constexpr int kLd = 32;
+// Mixed-precision refinement: cycles, FP32 expansions per cycle, and the residual
+// reduction (relative to the cycle's exact first residual) that ends a cycle.
+constexpr int kRefineCycles = 8;
+constexpr int kRefineExpand = 12;
+constexpr double kRefineRel = 1e-3;
 }  // namespace
 
 DeviceDavidson::DeviceDavidson(Runtime& rt, int64_t n, int max_vec, int keep, double rtol, double cutoff)
@@ -139,6 +144,48 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
   }
 }
 
+bool DeviceDavidson::refine_cycle(const double* diag, const MatVec& matvec, double tol, int max_expand, double rel,
+                                  DavidsonStats& st, double* r_exact) {
+  cudaStream_t s = rt_.stream();
+  double* t = W(0);
+  double* u = W(1);
+  double* w = W(2);
+  int nv = 0;
+  add_new_vec(t, nv);
+  matvec(V(0), HV(0), Precision::kFP64);
+  st.n_matvec++;
+  double r0 = 0.0;
+  for (int it = 0;; it++) {
+    multi_dot(HV_, nv + 1, V(nv), sm_ + kDots);
+    C2G_CUDA(launch_mxm_row(sm_ + kMxM, kLd, nv, sm_ + kDots, nv + 1, s));
+    nv++;
+    C2G_CUDA(launch_small_eig(sm_ + kMxM, nv, kLd, sm_ + kEvals, sm_ + kEvecs, s));
+    C2G_CUDA(launch_combine(t, 0.0, HV_, n_, sm_ + kEvecs, nv, n_, s));
+    C2G_CUDA(launch_combine(u, 0.0, V_, n_, sm_ + kEvecs, nv, n_, s));
+    C2G_CUDA(launch_residual(t, u, sm_ + kEvals, n_, s));
+    count_launches(5);
+    const double rnorm = std::sqrt(norm2(t));
+    st.n_iter++;
+    st.rnorm = rnorm;
+    if (it == 0) {
+      // V = {u} with its FP64 product: the exact residual
+      r0 = rnorm;
+      *r_exact = rnorm;
+      if (!(rnorm > tol)) return true;
+    } else if (rnorm <= rel * r0 || it >= max_expand || nv >= max_vec_) {
+      return false;
+    }
+    C2G_CUDA(launch_precond_w(w, u, diag, sm_ + kEvals, cutoff_, n_, s));
+    multi_dot(W(0), 2, w, sm_ + kDots2);
+    C2G_CUDA(launch_precond_t(t, u, diag, sm_ + kEvals, sm_ + kDots2, cutoff_, n_, s));
+    count_launches(2);
+    add_new_vec(t, nv);
+    matvec(V(nv), HV(nv), Precision::kFP32);
+    st.n_matvec++;
+    st.n_matvec_fp32++;
+  }
+}
+
 DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const MatVec& matvec, bool mixed,
                                     double lo_tol) {
   cudaStream_t s = rt_.stream();
@@ -153,12 +200,22 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
     C2G_CUDA(cudaMemcpyAsync(t, r.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
     rt_.sync();
   }
+  bool done = false;
   if (mixed) {
     run(diag, matvec, Precision::kFP32, std::max(lo_tol, rtol_), true, st);
-    // restart in FP64 from the FP32 Ritz vector
-    C2G_CUDA(cudaMemcpyAsync(t, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+    // refinement cycles from the FP32 Ritz vector; a cycle that cannot improve (for
+    // example an FP32 floor above the target) leaves it to the FP64 Davidson below
+    double last = 1e300;
+    for (int cycle = 0; cycle < kRefineCycles && !done; cycle++) {
+      C2G_CUDA(cudaMemcpyAsync(t, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+      double r = 0.0;
+      done = refine_cycle(diag, matvec, rtol_, kRefineExpand, kRefineRel, st, &r);
+      if (!done && r > 0.5 * last) break;  // the exact residual no longer drops
+      last = r;
+    }
+    if (!done) C2G_CUDA(cudaMemcpyAsync(t, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
   }
-  run(diag, matvec, Precision::kFP64, rtol_, false, st);
+  if (!done) run(diag, matvec, Precision::kFP64, rtol_, false, st);
   C2G_CUDA(cudaMemcpyAsync(guess, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
   C2G_CUDA(cudaMemcpyAsync(host_, sm_ + kEvals, sizeof(double), cudaMemcpyDeviceToHost, s));
   rt_.sync();

@@ -10,8 +10,12 @@
 // applies one modified Gram-Schmidt pass; both are exact in exact arithmetic).
 //
 // Mixed precision: the matvec is requested in FP32 until the residual reaches a looser
-// tolerance (or stops improving), then the solver restarts from that Ritz vector with
-// FP64 matvecs and the caller's tolerance, so the returned eigenpair is an FP64 one.
+// tolerance (or stops improving). Refinement cycles follow: each restarts the subspace from
+// the current Ritz vector u with its FP64 product H u, so the first Rayleigh-Ritz step of a
+// cycle gives the exact residual of u (the convergence test), and expands it with FP32
+// products; the cross terms with u use the exact H u, so only the small correction
+// coefficients carry FP32 error and every cycle reduces the residual by orders of
+// magnitude at the cost of one FP64 matvec. The returned eigenpair is an FP64 one.
 #pragma once
 
 #include <functional>
@@ -53,6 +57,11 @@ class DeviceDavidson {
   // One Davidson run from the vector in W(0); the Ritz vector ends in W(1).
   void run(const double* diag, const MatVec& matvec, Precision prec, double tol, bool stop_on_stall,
            DavidsonStats& st);
+  // One refinement cycle from the vector in W(0) (first product FP64, then FP32, at most
+  // max_expand expansions, until the residual estimate falls below rel * the exact first
+  // residual); true when that exact first residual is <= tol. The Ritz vector ends in W(1).
+  bool refine_cycle(const double* diag, const MatVec& matvec, double tol, int max_expand, double rel,
+                    DavidsonStats& st, double* r_exact);
 
   Runtime& rt_;
   int64_t n_;
