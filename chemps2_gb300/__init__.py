@@ -22,9 +22,9 @@ C2G_ERR_CUDA = -2
 C2G_ERR_NO_DEVICE = -3
 C2G_ERR_INTERNAL = -4
 C2G_ERR_OTHER = -5
-NUM_STATS = 12
+NUM_STATS = 13
 STAT_NAMES = ("n_matvec", "n_davidson", "t_join", "t_solve", "t_split", "t_update", "t_matvec", "t_compile",
-              "matvec_flops", "matvec_bytes", "last_energy", "n_matvec_fp32")
+              "matvec_flops", "matvec_bytes", "last_energy", "n_matvec_fp32", "t_upload")
 
 
 class Chemps2Error(RuntimeError):

@@ -435,7 +435,7 @@ int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n) {
     const double v[C2G_NUM_STATS] = {static_cast<double>(s.n_matvec), static_cast<double>(s.n_davidson),
                                      s.t_join, s.t_solve, s.t_split, s.t_update, s.t_matvec, s.t_compile,
                                      s.matvec_flops, s.matvec_bytes, s.last_energy,
-                                     static_cast<double>(s.n_matvec_fp32)};
+                                     static_cast<double>(s.n_matvec_fp32), s.t_upload};
     for (int i = 0; i < n && i < C2G_NUM_STATS; i++) out[i] = v[i];
   });
 }

@@ -108,7 +108,9 @@ DevProgram& DMRG::program(const std::string& key, const std::function<c2g::Compi
   c2g::Compiled c = build();
   stats_.t_compile += now() - tc;
   ProgramCache::Entry e;
+  const double tu = now();
   e.dp = rt->upload(c.program);
+  stats_.t_upload += now() - tu;
   e.operand_bytes = c.operand_bytes;
   e.last_use = pc.clock;
   const long long size = e.dp->bytes + 8 * e.dp->combo_size;
@@ -1079,7 +1081,9 @@ DMRG::HeffCache& DMRG::heff_program(const int index, const bool with_diag) {
     const double tc = now();
     c2g::Compiled ch = c2g::compile_heff_program(ctx, true);
     stats_.t_compile += now() - tc;
+    const double tu = now();
     c.program = rt->upload(ch.program);
+    stats_.t_upload += now() - tu;
     rt->prepare(*c.program);
     c.operand_bytes = ch.operand_bytes;
     c.index = index;

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <numeric>
 #include <sstream>
+#include <thread>
 #include <tuple>
 
 namespace c2g {
@@ -86,6 +87,7 @@ Runtime::~Runtime() {
   cudaFree(dev_slots_);
   cudaFree(dev_slots32_);
   cudaFree(partial_);
+  if (staging_) cudaFreeHost(staging_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -163,6 +165,19 @@ SlotPtrs Runtime::ptrs(double* x, double* y, double* combo) {
   return sp;
 }
 
+void Runtime::reserve_staging(int64_t bytes, int64_t keep) {
+  if (bytes <= staging_cap_) return;
+  const int64_t cap = std::max<int64_t>(bytes, staging_cap_ + staging_cap_ / 2);
+  char* fresh = nullptr;
+  C2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&fresh), static_cast<size_t>(cap)));
+  if (staging_) {
+    if (keep > 0) std::memcpy(fresh, staging_, static_cast<size_t>(keep));
+    C2G_CUDA(cudaFreeHost(staging_));
+  }
+  staging_ = fresh;
+  staging_cap_ = cap;
+}
+
 std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   auto dp = std::make_unique<DevProgram>();
   dp->rt = this;
@@ -178,25 +193,81 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   std::vector<std::vector<TileDesc>> tiles(ns), tiles_large(ns);
   std::vector<std::vector<WarpTile>> tiles_warp(ns);
   int64_t part_doubles = 0, ncounters = 0;
-  // Terms of each group ordered by shape (flags, k1, k2), so that neighbouring items of
-  // the team variant share their loop structure.
-  std::vector<std::vector<Term>> terms(ns);
-  int64_t bytes = align256(sizeof(BatchEntry) * p.entries.size());
+  // Blob layout: the batch table, then per stage its groups and terms, then the tile lists
+  // of every stage. It is assembled in the runtime's pinned staging buffer: the terms of
+  // each group are copied there in shape order (flags, k1, k2), so that neighbouring items
+  // of the team variant share their loop structure, by all host threads.
+  int64_t head = align256(sizeof(BatchEntry) * p.entries.size());
+  std::vector<int64_t> off_groups(ns), off_terms(ns);
+  for (size_t s = 0; s < ns; s++) {
+    off_groups[s] = head;
+    head += align256(sizeof(Group) * p.stages[s].groups.size());
+    off_terms[s] = head;
+    head += align256(sizeof(Term) * p.stages[s].terms.size());
+  }
+  reserve_staging(head, 0);
+  if (!p.entries.empty()) std::memcpy(staging_, p.entries.data(), sizeof(BatchEntry) * p.entries.size());
+  std::vector<Term*> terms(ns);
   for (size_t s = 0; s < ns; s++) {
     const Stage& st = p.stages[s];
-    terms[s] = st.terms;
-    for (const Group& G : st.groups) {
-      auto first = terms[s].begin() + G.t0, last = terms[s].begin() + G.t1;
-      std::stable_sort(first, last, [](const Term& a, const Term& b) {
-        return std::make_tuple(a.flags, a.k1, a.k2) < std::make_tuple(b.flags, b.k1, b.k2);
-      });
-      int32_t item0 = 0;
-      for (auto it = first; it != last; ++it) {
-        if (it->count < 1) throw std::invalid_argument("task term without items");
-        it->item0 = item0;
-        item0 += it->count;
+    if (!st.groups.empty()) std::memcpy(staging_ + off_groups[s], st.groups.data(), sizeof(Group) * st.groups.size());
+    terms[s] = reinterpret_cast<Term*>(staging_ + off_terms[s]);
+  }
+  {
+    // (stage, first group, last group) chunks of about equal term counts
+    struct Chunk {
+      size_t s;
+      size_t g0, g1;
+    };
+    std::vector<Chunk> chunks;
+    const int nthreads = std::max(1, compile_threads());
+    int64_t total_terms = 0;
+    for (const Stage& st : p.stages) total_terms += static_cast<int64_t>(st.terms.size());
+    const int64_t per = std::max<int64_t>(total_terms / (4 * nthreads), 4096);
+    for (size_t s = 0; s < ns; s++) {
+      const Stage& st = p.stages[s];
+      size_t g0 = 0;
+      int64_t acc = 0;
+      for (size_t g = 0; g < st.groups.size(); g++) {
+        acc += st.groups[g].t1 - st.groups[g].t0;
+        if (acc >= per || g + 1 == st.groups.size()) {
+          chunks.push_back(Chunk{s, g0, g + 1});
+          g0 = g + 1;
+          acc = 0;
+        }
       }
     }
+    std::atomic<size_t> next{0};
+    std::atomic<bool> bad{false};
+    auto work = [&] {
+      for (size_t c = next++; c < chunks.size(); c = next++) {
+        const Stage& st = p.stages[chunks[c].s];
+        Term* out = terms[chunks[c].s];
+        for (size_t g = chunks[c].g0; g < chunks[c].g1; g++) {
+          const Group& G = st.groups[g];
+          std::memcpy(out + G.t0, st.terms.data() + G.t0, sizeof(Term) * (G.t1 - G.t0));
+          std::stable_sort(out + G.t0, out + G.t1, [](const Term& x, const Term& y) {
+            return std::make_tuple(x.flags, x.k1, x.k2) < std::make_tuple(y.flags, y.k1, y.k2);
+          });
+          int32_t item0 = 0;
+          for (Term* it = out + G.t0; it != out + G.t1; ++it) {
+            if (it->count < 1) bad = true;
+            it->item0 = item0;
+            item0 += it->count;
+          }
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    const int nt = static_cast<int>(std::min<size_t>(nthreads, chunks.size()));
+    for (int i = 1; i < nt; i++) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    if (bad) throw std::invalid_argument("task term without items");
+  }
+  int64_t tile_bytes = 0;
+  for (size_t s = 0; s < ns; s++) {
+    const Stage& st = p.stages[s];
     std::vector<PendingTile> pending;
     int64_t warp_work = 0;
     std::vector<int> order(st.groups.size());
@@ -286,23 +357,23 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     std::stable_sort(tiles_warp[s].begin(), tiles_warp[s].end(), [](const WarpTile& a, const WarpTile& b) {
       return warp_row_class(a.cls) < warp_row_class(b.cls);
     });
-    bytes += align256(sizeof(Group) * st.groups.size()) + align256(sizeof(Term) * st.terms.size()) +
-             align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size()) +
-             align256(sizeof(WarpTile) * tiles_warp[s].size());
+    tile_bytes += align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size()) +
+                  align256(sizeof(WarpTile) * tiles_warp[s].size());
   }
-  std::vector<char> host(static_cast<size_t>(std::max<int64_t>(bytes, 256)));
+  const int64_t bytes = head + tile_bytes;
+  reserve_staging(bytes, head);  // keeps the part already assembled
   C2G_CUDA(cudaMallocAsync(&dp->blob, std::max<int64_t>(bytes, 256), stream_));
   char* dbase = static_cast<char*>(dp->blob);
-  int64_t off = 0;
+  int64_t off = head;
   auto put = [&](const void* src, size_t n) -> const void* {
-    if (n) std::memcpy(host.data() + off, src, n);
+    if (n) std::memcpy(staging_ + off, src, n);
     const void* d = dbase + off;
     off += align256(static_cast<int64_t>(n));
     return d;
   };
-  dp->entries = static_cast<const BatchEntry*>(put(p.entries.data(), sizeof(BatchEntry) * p.entries.size()));
+  dp->entries = reinterpret_cast<const BatchEntry*>(dbase);
   dp->nentries = static_cast<int64_t>(p.entries.size());
-  for (size_t s = 0; s < p.stages.size(); s++) {
+  for (size_t s = 0; s < ns; s++) {
     const Stage& st = p.stages[s];
     DevStage ds;
     ds.name = st.name;
@@ -311,8 +382,8 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     ds.ntiles = static_cast<int>(tiles[s].size());
     ds.flops = st.flops;
     ds.items = st.items;
-    ds.groups = static_cast<const Group*>(put(st.groups.data(), sizeof(Group) * st.groups.size()));
-    ds.terms = static_cast<const Term*>(put(terms[s].data(), sizeof(Term) * terms[s].size()));
+    ds.groups = reinterpret_cast<const Group*>(dbase + off_groups[s]);
+    ds.terms = reinterpret_cast<const Term*>(dbase + off_terms[s]);
     ds.tiles = static_cast<const TileDesc*>(put(tiles[s].data(), sizeof(TileDesc) * tiles[s].size()));
     ds.ntiles_large = static_cast<int>(tiles_large[s].size());
     ds.tiles_large =
@@ -327,8 +398,8 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     dp->stages.push_back(ds);
   }
   dp->bytes = bytes;
-  C2G_CUDA(cudaMemcpyAsync(dp->blob, host.data(), bytes, cudaMemcpyHostToDevice, stream_));
-  C2G_CUDA(cudaStreamSynchronize(stream_));  // `host` goes out of scope
+  C2G_CUDA(cudaMemcpyAsync(dp->blob, staging_, bytes, cudaMemcpyHostToDevice, stream_));
+  C2G_CUDA(cudaStreamSynchronize(stream_));  // the staging buffer is reused by the next upload
   if (dp->combo_size > 0) dp->combo = alloc(dp->combo_size);
   if (part_doubles > 0) dp->partials = alloc(part_doubles);
   if (ncounters > 0) {

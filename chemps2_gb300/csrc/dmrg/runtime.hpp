@@ -118,6 +118,11 @@ class Runtime {
   double* ones_ = nullptr;
   int64_t ones_cap_ = 0;
   double* partial_ = nullptr;
+  // pinned host buffer in which upload assembles a program before the copy to the device
+  char* staging_ = nullptr;
+  int64_t staging_cap_ = 0;
+  // grows the staging buffer to at least `bytes`, keeping its first `keep` bytes
+  void reserve_staging(int64_t bytes, int64_t keep);
 };
 
 // Number of kernels this library has launched in this process (all runtimes).

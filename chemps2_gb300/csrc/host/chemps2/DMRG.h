@@ -35,6 +35,7 @@ struct DMRGStats {
   double t_join = 0, t_solve = 0, t_split = 0, t_update = 0;  // seconds, host wall clock
   double t_matvec = 0;            // seconds inside Heff applications (device time)
   double t_compile = 0;           // seconds in the host task compiler
+  double t_upload = 0;            // seconds uploading compiled programs (host work and copy)
   double matvec_flops = 0;        // ledger flops of all Heff applications
   double matvec_bytes = 0;        // ledger bytes of all Heff applications
   double last_energy = 0;

@@ -73,14 +73,14 @@ int64_t TaskBuilder::operand_bytes() const {
 
 int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
   if (&sb == last_sb_ && out.ref == last_out_) return last_group_;
-  auto it = sb.group_of.find(out.ref);
-  if (it != sb.group_of.end()) {
-    const Group& g = sb.groups[it->second];
+  const int found = sb.group_of.find(out.ref);
+  if (found >= 0) {
+    const Group& g = sb.groups[found];
     if (g.m != out.rows || g.n != out.cols || g.ldo != out.ld) shape_error("output group");
     last_sb_ = &sb;
     last_out_ = out.ref;
-    last_group_ = it->second;
-    return it->second;
+    last_group_ = found;
+    return found;
   }
   Group g{};
   g.out = out.ref;
@@ -92,7 +92,7 @@ int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
   sb.groups.push_back(g);
   sb.terms.emplace_back();
   const int id = static_cast<int>(sb.groups.size()) - 1;
-  sb.group_of[out.ref] = id;
+  sb.group_of.insert(out.ref, id);
   last_sb_ = &sb;
   last_out_ = out.ref;
   last_group_ = id;
@@ -165,13 +165,17 @@ Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int r
   key.push_back((uint64_t(uint32_t(rows)) << 32) | uint32_t(cols));
   uint64_t h = 0x243f6a8885a308d3ull;
   for (uint64_t w : key) h = mix(h, w);
-  auto range = combo_index_.equal_range(h);
-  for (auto it = range.first; it != range.second; ++it) {
-    const ComboEntry& e = combo_entries_[it->second];
+  int32_t hit = -1;
+  combo_index_.visit(h, [&](int32_t idx) {
+    const ComboEntry& e = combo_entries_[idx];
     if (e.nwords == static_cast<int32_t>(key.size()) &&
-        std::memcmp(combo_words_.data() + e.word0, key.data(), sizeof(uint64_t) * key.size()) == 0)
-      return e.out;
-  }
+        std::memcmp(combo_words_.data() + e.word0, key.data(), sizeof(uint64_t) * key.size()) == 0) {
+      hit = idx;
+      return true;
+    }
+    return false;
+  });
+  if (hit >= 0) return combo_entries_[hit].out;
   for (const auto& pr : parts) note_operand(pr.second);
   const Blk out = Blk::make(make_ref(kSlotCombo, combo_size_), rows, cols);
   combo_size_ = align4(combo_size_ + int64_t(rows) * cols);
@@ -179,7 +183,7 @@ Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int r
     const bool t = transposed ? (*transposed)[i] : false;
     add(combo_, false, out, parts[i].first, Blk(), false, parts[i].second, t, Blk(), false, false);
   }
-  combo_index_.emplace(h, static_cast<int32_t>(combo_entries_.size()));
+  combo_index_.insert(h, static_cast<int32_t>(combo_entries_.size()));
   combo_entries_.push_back(ComboEntry{static_cast<int64_t>(combo_words_.size()), static_cast<int32_t>(key.size()), out});
   combo_words_.insert(combo_words_.end(), key.begin(), key.end());
   return out;
@@ -235,7 +239,7 @@ void TaskBuilder::next_stage(const std::string& name) {
 }
 
 Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<BatchEntry>& table,
-                         std::unordered_multimap<uint64_t, int32_t>& lists) {
+                         FlatIndex& lists) {
   Stage st;
   st.name = name;
   st.groups = sb.groups;
@@ -262,21 +266,21 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
           h = mix(mix(mix(h, static_cast<uint64_t>(e.da)), static_cast<uint64_t>(e.dc)), r);
         }
         int32_t found = -1;
-        auto range = lists.equal_range(h);
-        for (auto it = range.first; it != range.second && found < 0; ++it) {
-          if (it->second + 1 + n > table.size()) continue;
-          const BatchEntry* l = table.data() + it->second;
+        lists.visit(h, [&](int32_t off) {
+          if (off + 1 + n > table.size()) return false;
+          const BatchEntry* l = table.data() + off;
           bool same = l[0].da == 0 && l[0].dc == 0 && l[0].ratio == 1.0;
           for (size_t q = 0; same && q < n; q++)
             same = l[q + 1].da == pt.entries[q].da && l[q + 1].dc == pt.entries[q].dc &&
                    std::memcmp(&l[q + 1].ratio, &pt.entries[q].ratio, sizeof(double)) == 0;
-          if (same) found = it->second;
-        }
+          if (same) found = off;
+          return same;
+        });
         if (found < 0) {
           found = static_cast<int32_t>(table.size());
           table.push_back(first);
           table.insert(table.end(), pt.entries.begin(), pt.entries.end());
-          lists.emplace(h, found);
+          lists.insert(h, found);
         }
         t.list = found;
         t.count = static_cast<int32_t>(n) + 1;
@@ -294,7 +298,7 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
 
 Program TaskBuilder::finalize(bool keep_empty) {
   Program p;
-  std::unordered_multimap<uint64_t, int32_t> lists;
+  FlatIndex lists;
   if (!combo_.groups.empty() || keep_empty) {
     p.stages.push_back(lower(combo_, "combine", p.entries, lists));
     p.first_repeat_stage = 1;

@@ -25,6 +25,7 @@
 // of a group are summed in a fixed order, so results are deterministic.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <unordered_map>
@@ -135,6 +136,69 @@ struct Program {
 // Flops of one entry of a term (2 per multiply-add; m * n for a plain scaled copy).
 int64_t term_flops(const Term& t, int m, int n);
 
+// Open-addressing index from 64-bit keys to non-negative int32 values (several values per
+// key allowed, visited in insertion order), for the compiler's large lookup tables.
+class FlatIndex {
+ public:
+  // Calls f(value) for the values stored under key until f returns true; true if it did.
+  template <class F>
+  bool visit(uint64_t key, F&& f) const {
+    if (vals_.empty()) return false;
+    for (size_t i = slot(key);; i = (i + 1) & mask_) {
+      if (vals_[i] < 0) return false;
+      if (keys_[i] == key && f(vals_[i])) return true;
+    }
+  }
+  // The first value stored under key, or -1.
+  int32_t find(uint64_t key) const {
+    int32_t out = -1;
+    visit(key, [&](int32_t v) {
+      out = v;
+      return true;
+    });
+    return out;
+  }
+  void insert(uint64_t key, int32_t value) {
+    if ((size_ + 1) * 2 > vals_.size()) grow();
+    size_t i = slot(key);
+    while (vals_[i] >= 0) i = (i + 1) & mask_;
+    keys_[i] = key;
+    vals_[i] = value;
+    size_++;
+  }
+  void clear() {
+    keys_.clear();
+    vals_.clear();
+    mask_ = 0;
+    size_ = 0;
+  }
+  size_t size() const { return size_; }
+
+ private:
+  std::vector<uint64_t> keys_;
+  std::vector<int32_t> vals_;  // -1: empty
+  size_t mask_ = 0, size_ = 0;
+  size_t slot(uint64_t k) const {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    return static_cast<size_t>(k) & mask_;
+  }
+  void grow() {
+    std::vector<uint64_t> ok;
+    std::vector<int32_t> ov;
+    ok.swap(keys_);
+    ov.swap(vals_);
+    const size_t cap = std::max<size_t>(1024, ov.size() * 2);
+    keys_.assign(cap, 0);
+    vals_.assign(cap, -1);
+    mask_ = cap - 1;
+    size_ = 0;
+    for (size_t i = 0; i < ov.size(); i++)  // old probe order keeps equal keys in order
+      if (ov[i] >= 0) insert(ok[i], ov[i]);
+  }
+};
+
 // Records contractions and lowers them into a Program.
 class TaskBuilder {
  public:
@@ -184,7 +248,7 @@ class TaskBuilder {
   struct StageBuf {
     std::vector<Group> groups;
     std::vector<std::vector<PendingTerm>> terms;  // per group
-    std::unordered_map<Ref, int> group_of;
+    FlatIndex group_of;  // output reference -> group
     std::string name;
   };
   struct BatchKey {
@@ -209,7 +273,7 @@ class TaskBuilder {
     int32_t nwords;
     Blk out;
   };
-  std::unordered_multimap<uint64_t, int32_t> combo_index_;
+  FlatIndex combo_index_;
   std::vector<ComboEntry> combo_entries_;
   std::vector<uint64_t> combo_words_;
   std::vector<uint64_t> key_scratch_;
@@ -231,7 +295,7 @@ class TaskBuilder {
            const Blk& C, bool tc, bool accumulate);
   // lists: batch lists already in `table`, by hash of their entries
   static Stage lower(StageBuf& sb, const std::string& name, std::vector<BatchEntry>& table,
-                     std::unordered_multimap<uint64_t, int32_t>& lists);
+                     FlatIndex& lists);
 };
 
 // Concatenates programs compiled (with keep_empty) from disjoint output shards into one

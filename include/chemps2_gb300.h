@@ -118,9 +118,9 @@ int c2g_dmrg_solve_site(c2g_dmrg* d, int index, double dvdson_rtol, double noise
                         int change, double* energy);
 int c2g_dmrg_update(c2g_dmrg* d, int index, int moving_right);
 /* Statistics, in this order: n_matvec, n_davidson, t_join, t_solve, t_split, t_update,
- * t_matvec, t_compile, matvec_flops, matvec_bytes, last_energy, n_matvec_fp32 (seconds,
- * flops, bytes). */
-#define C2G_NUM_STATS 12
+ * t_matvec, t_compile, matvec_flops, matvec_bytes, last_energy, n_matvec_fp32, t_upload
+ * (seconds, flops, bytes). */
+#define C2G_NUM_STATS 13
 int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n);
 int c2g_dmrg_reset_stats(c2g_dmrg* d);
 /* Heff applications at sites (index, index + 1) on the current MPS (CheMPS2/Heff.cpp:43-248):
