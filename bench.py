@@ -53,6 +53,23 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(seconds, world, device="cuda"):
+    """The slowest rank's time: every rank runs the same replica workload and the job ends
+    with the slowest one (no data-path collective; this is the only exchange)."""
+    if world <= 1:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, steps, seconds):
+    """Whole-job units per second: `steps` units on each of `world` replicas."""
+    return world * steps / seconds
+
+
 def make_model():
     from chemps2_gb300.models import synthetic_ab_initio
 
@@ -249,12 +266,10 @@ def run_ours(args):
     mixed = {"matvec_per_s": 1e3 / res32["ms_per_matvec"], "ms_per_matvec": res32["ms_per_matvec"],
              "speedup_vs_fp64": ms / res32["ms_per_matvec"],
              "arithmetic": "FP32 operand copies, products and per-slot sums; FP64 slot reduction and output"}
+    total_s = max_over_ranks(total_s, world)
     if world > 1:
-        t = torch.tensor([total_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
         torch.distributed.barrier()
-    value = world * args.steps / total_s
+    value = replica_throughput(world, args.steps, total_s)
     # end to end through the C-ABI with host buffers
     rng = np.random.default_rng(0)
     x = rng.standard_normal(n)
@@ -263,11 +278,8 @@ def run_ours(args):
     for _ in range(args.steps):
         dmrg.heff_apply(MID, x)
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e = {"value": replica_throughput(world, args.steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     achieved = res["bytes"] / (ms * 1e-3) / 1e9
