@@ -455,6 +455,39 @@ class DMRG:
         return {"ms_per_matvec": ms.value, "flops": fl.value, "bytes": by.value, "launches": nl.value}
 
 
+def solve_batch(problems, schemes, seeds, workers=8, raise_on_error=True):
+    """Solves independent problems on one GPU (no counterpart in the reference, whose
+    callers loop over problems): problems[i] with schemes[i] and the random start that
+    srand(seeds[i]) gives, at most `workers` at a time, each on its own host thread and CUDA
+    stream. Returns one dict per problem with its energy, matvec count, seconds and status
+    (0 or the C-ABI error code). When a problem failed, all others are still solved; the
+    call then raises unless raise_on_error is False."""
+    n = len(problems)
+    if len(schemes) != n or len(seeds) != n:
+        raise ValueError("problems, schemes and seeds differ in length")
+    P = (C.c_void_p * max(n, 1))(*[p._p.value for p in problems])
+    S = (C.c_void_p * max(n, 1))(*[s._s.value for s in schemes])
+    sd = np.ascontiguousarray(seeds, dtype=np.uint32)
+    energies = np.zeros(n)
+    matvecs = np.zeros(n, dtype=np.int64)
+    seconds = np.zeros(n)
+    statuses = np.zeros(n, dtype=np.int32)
+    rc = load().c2g_batch_solve(int(n), P, S, sd.ctypes.data_as(C.POINTER(C.c_uint)), int(workers), _dp(energies),
+                                matvecs.ctypes.data_as(C.POINTER(C.c_longlong)), _dp(seconds),
+                                statuses.ctypes.data_as(C.POINTER(C.c_int)))
+    if raise_on_error or not statuses.any():
+        _check(rc)
+    return [{"energy": float(energies[i]), "matvecs": int(matvecs[i]), "seconds": float(seconds[i]),
+             "status": int(statuses[i])} for i in range(n)]
+
+
+def host_rand_sample(seed: int, n: int) -> np.ndarray:
+    """The first n draws of a batch member's private generator seeded with `seed`."""
+    out = np.zeros(n, dtype=np.int32)
+    _check(load().c2g_host_rand_sample(C.c_uint(seed), int(n), out.ctypes.data_as(C.POINTER(C.c_int))))
+    return out
+
+
 # Names of the reference's Cython module.
 PyHamiltonian = Hamiltonian
 PyProblem = Problem
@@ -462,5 +495,5 @@ PyConvergenceScheme = ConvergenceScheme
 PyDMRG = DMRG
 
 __all__ = ["Hamiltonian", "Problem", "ConvergenceScheme", "DMRG", "PyHamiltonian", "PyProblem",
-           "PyConvergenceScheme", "PyDMRG", "srand", "wigner6j", "wigner9j", "kernel_launches", "load",
+           "PyConvergenceScheme", "PyDMRG", "srand", "solve_batch", "host_rand_sample", "wigner6j", "wigner9j", "kernel_launches", "load",
            "Chemps2Error", "NoDeviceError"]

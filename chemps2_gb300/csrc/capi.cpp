@@ -7,14 +7,17 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "dmrg/runtime.hpp"
+#include "host/chemps2/Batch.h"
 #include "host/chemps2/ConvergenceScheme.h"
 #include "host/chemps2/DMRG.h"
 #include "host/chemps2/Hamiltonian.h"
 #include "host/chemps2/Problem.h"
 #include "host/chemps2/SyBookkeeper.h"
 #include "host/layout.hpp"
+#include "host/rng.hpp"
 #include "host/symm.hpp"
 
 struct c2g_hamiltonian {
@@ -540,6 +543,56 @@ int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double*
   return guarded([&] {
     NEED(d);
     d->d->heff_apply_noalloc(index, x, y, n);
+  });
+}
+
+int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* schemes, const unsigned int* seeds,
+                    int workers, double* energies, long long* matvecs, double* seconds, int* statuses) {
+  std::vector<CheMPS2::BatchResult> res;
+  const int rc = guarded([&] {
+    if (n < 0) throw std::invalid_argument("c2g_batch_solve: negative problem count");
+    if (n > 0) {
+      NEED(problems);
+      NEED(schemes);
+      NEED(seeds);
+    }
+    std::vector<CheMPS2::Problem*> ps(n);
+    std::vector<CheMPS2::ConvergenceScheme*> ss(n);
+    for (int i = 0; i < n; i++) {
+      NEED(problems[i]);
+      NEED(schemes[i]);
+      ps[i] = problems[i]->p.get();
+      ss[i] = schemes[i]->s.get();
+    }
+    res = CheMPS2::SolveBatch(ps, ss, std::vector<unsigned>(seeds, seeds + n), workers);
+  });
+  if (rc != C2G_OK) return rc;
+  int first = C2G_OK;
+  std::string first_error;
+  for (int i = 0; i < n; i++) {
+    const auto& r = res[i];
+    // the same codes the single-problem calls return for these failures
+    static const int kCode[5] = {C2G_OK, C2G_ERR_INVALID, C2G_ERR_CUDA, C2G_ERR_NO_DEVICE, C2G_ERR_OTHER};
+    const int code = (r.status >= 0 && r.status < 5) ? kCode[r.status] : C2G_ERR_OTHER;
+    if (energies) energies[i] = r.energy;
+    if (matvecs) matvecs[i] = r.n_matvec;
+    if (seconds) seconds[i] = r.seconds;
+    if (statuses) statuses[i] = code;
+    if (code != C2G_OK && first == C2G_OK) {
+      first = code;
+      first_error = "problem " + std::to_string(i) + ": " + r.error;
+    }
+  }
+  if (first != C2G_OK) return fail(first, first_error);
+  return C2G_OK;
+}
+
+int c2g_host_rand_sample(unsigned int seed, int n, int* out) {
+  return guarded([&] {
+    if (n < 0) throw std::invalid_argument("c2g_host_rand_sample: negative count");
+    if (n > 0) NEED(out);
+    c2g::HostRand r(seed);
+    for (int i = 0; i < n; i++) out[i] = r.next();
   });
 }
 

@@ -35,7 +35,7 @@ DeviceDavidson::DeviceDavidson(Runtime& rt, int64_t n, int max_vec, int keep, do
   W_ = rt_.alloc(n_ * (3 + keep_));
   sm_ = rt_.alloc(kSmall);
   rt_.zero(sm_, kSmall);
-  C2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&host_), sizeof(double) * 8));
+  host_ = rt_.pinned_scalars();
 }
 
 DeviceDavidson::~DeviceDavidson() {
@@ -43,7 +43,6 @@ DeviceDavidson::~DeviceDavidson() {
   rt_.release(HV_);
   rt_.release(W_);
   rt_.release(sm_);
-  if (host_) cudaFreeHost(host_);
 }
 
 void DeviceDavidson::multi_dot(const double* A, int ncol, const double* x, double* out) {
@@ -196,7 +195,9 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
   // SafetyCheckGuess (CheMPS2/Davidson.cpp:204-214)
   if (norm2(t) == 0.0) {
     std::vector<double> r(n_);
-    for (int64_t i = 0; i < n_; i++) r[i] = static_cast<double>(std::rand()) / RAND_MAX;
+    HostRand libc;
+    HostRand& g = rand_ ? *rand_ : libc;
+    for (int64_t i = 0; i < n_; i++) r[i] = g.unit();
     C2G_CUDA(cudaMemcpyAsync(t, r.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
     rt_.sync();
   }

@@ -20,6 +20,7 @@
 
 #include <functional>
 
+#include "rng.hpp"
 #include "runtime.hpp"
 
 namespace c2g {
@@ -46,6 +47,8 @@ class DeviceDavidson {
   // down to residual lo_tol (never below rtol).
   DavidsonStats solve(double* guess, const double* diag, const MatVec& matvec, bool mixed = false,
                       double lo_tol = 1e-5);
+  // source of the random start that replaces a zero guess (the C library's rand() unless set)
+  void set_rand(HostRand* r) { rand_ = r; }
 
  private:
   double* V(int i) { return V_ + n_ * i; }
@@ -71,7 +74,8 @@ class DeviceDavidson {
   double* HV_ = nullptr;
   double* W_ = nullptr;   // columns: 0 t, 1 u, 2 w, 3.. deflation vectors
   double* sm_ = nullptr;  // small device scalars (layout in davidson.cpp)
-  double* host_ = nullptr;  // pinned host scalars
+  double* host_ = nullptr;  // pinned host scalars of the runtime
+  HostRand* rand_ = nullptr;
 };
 
 }  // namespace c2g

@@ -22,6 +22,7 @@
 #include "heff.hpp"
 #include "layout.hpp"
 #include "operators.hpp"
+#include "rng.hpp"
 #include "runtime.hpp"
 #include "sobject.hpp"
 #include "symm.hpp"
@@ -156,6 +157,17 @@ struct DMRG::ExcState {
 
 DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const bool makechkpt, const std::string, int* occupancies)
     : Prob(ProbIn), OptScheme(OptSchemeIn), makecheckpoints_(makechkpt) {
+  rng_ = std::make_unique<c2g::HostRand>();
+  construct(occupancies);
+}
+
+DMRG::DMRG(Problem* ProbIn, ConvergenceScheme* OptSchemeIn, const DMRGOptions& options)
+    : Prob(ProbIn), OptScheme(OptSchemeIn), makecheckpoints_(options.makechkpt) {
+  rng_ = options.private_seed ? std::make_unique<c2g::HostRand>(options.seed) : std::make_unique<c2g::HostRand>();
+  construct(options.occupancies);
+}
+
+void DMRG::construct(int* occupancies) {
   heff_cache_ = std::make_unique<HeffCache>();
   pcache_ = std::make_unique<ProgramCache>();
   pcache_->limit = 16LL << 30;
@@ -315,7 +327,7 @@ void DMRG::setup_mps(int* occupancies) {
     mps_lay[site]->build(*denBK, site);
     const MpsLayout& lay = *mps_lay[site];
     std::vector<double> data(lay.size());
-    for (auto& v : data) v = (2 * static_cast<double>(std::rand()) / RAND_MAX) - 1.0;
+    for (auto& v : data) v = 2 * rng_->unit() - 1.0;
     if (occupancies) {
       const int right_n = left_n + occ[site];
       const int right_i = (occ[site] == 1) ? c2g::irrep_prod(left_i, Prob->gIrrep(site)) : left_i;
@@ -805,6 +817,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   DevProgram* dph = &dph_ref;
   rt->prepare(*dph);
   c2g::DeviceDavidson dav(*rt, veclen, kDavidsonNumVec, kDavidsonNumVecKeep, dvdson_rtol, kDavidsonPrecondCutoff);
+  dav.set_rand(rng_.get());
   cudaEvent_t e0, e1;
   C2G_CUDA(cudaEventCreate(&e0));
   C2G_CUDA(cudaEventCreate(&e1));
@@ -887,7 +900,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     for (int k = 0; k < S.nkappa; k++) {
       const double f = std::sqrt(S.TwoSR[k] + 1.0);
       for (int64_t c = S.k2i[k]; c < S.k2i[k + 1]; c++)
-        noise[c] = f * noise_level * (static_cast<double>(std::rand()) / RAND_MAX - 0.5);
+        noise[c] = f * noise_level * (rng_->unit() - 0.5);
     }
     double* dn = rt->alloc(veclen);
     C2G_CUDA(cudaMemcpyAsync(dn, noise.data(), sizeof(double) * veclen, cudaMemcpyHostToDevice, s));

@@ -77,6 +77,7 @@ Runtime::Runtime(int L, int device) : L_(L) {
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots_), sizeof(double*) * kMaxSlots));
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots32_), sizeof(float*) * kMaxSlots));
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&partial_), sizeof(double) * (kDotBlocks * 64 + 4096)));
+  C2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&pinned_), sizeof(double) * 8));
 }
 
 Runtime::~Runtime() {
@@ -88,6 +89,7 @@ Runtime::~Runtime() {
   cudaFree(dev_slots32_);
   cudaFree(partial_);
   if (staging_) cudaFreeHost(staging_);
+  if (pinned_) cudaFreeHost(pinned_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 

@@ -100,6 +100,9 @@ class Runtime {
 
   // Scratch for reductions and small Davidson quantities.
   double* partial() { return partial_; }
+  // eight pinned host doubles for synchronising scalar reads on this stream (allocated with
+  // the runtime: pinned allocations and frees synchronise the whole device)
+  double* pinned_scalars() { return pinned_; }
 
  private:
   friend struct DevProgram;
@@ -118,6 +121,7 @@ class Runtime {
   double* ones_ = nullptr;
   int64_t ones_cap_ = 0;
   double* partial_ = nullptr;
+  double* pinned_ = nullptr;
   // pinned host buffer in which upload assembles a program before the copy to the device
   char* staging_ = nullptr;
   int64_t staging_cap_ = 0;

@@ -20,6 +20,7 @@
 
 namespace c2g {
 class Runtime;
+class HostRand;
 struct BoundaryOps;
 struct MpsLayout;
 struct DevProgram;
@@ -41,10 +42,22 @@ struct DMRGStats {
   double last_energy = 0;
 };
 
+// Extension: construction options for DMRG objects that run on concurrent host threads
+// (the batch entry point). With `private_seed` set, the object's random draws (MPS start,
+// noise, Davidson guess fallback) come from its own generator seeded with `seed`: the
+// sequence srand(seed) and rand() give, without the shared state of rand().
+struct DMRGOptions {
+  bool private_seed = false;
+  unsigned seed = 1;
+  bool makechkpt = false;
+  int* occupancies = nullptr;
+};
+
 class DMRG {
  public:
   DMRG(Problem* Prob, ConvergenceScheme* OptScheme, const bool makechkpt = false,
        const std::string tmpfolder = "/tmp", int* occupancies = nullptr);
+  DMRG(Problem* Prob, ConvergenceScheme* OptScheme, const DMRGOptions& options);
   ~DMRG();
   DMRG(const DMRG&) = delete;
   DMRG& operator=(const DMRG&) = delete;
@@ -159,6 +172,8 @@ class DMRG {
   void gauge_right_normalize(int site);
   void fill_2dm_site(int site);
 
+  std::unique_ptr<c2g::HostRand> rng_;
+  void construct(int* occupancies);
   void setup_mps(int* occupancies);
   void left_normalize_host(int site, std::vector<double>& data);
   void upload_mps(int site, const std::vector<double>& data);

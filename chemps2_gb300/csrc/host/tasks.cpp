@@ -399,7 +399,14 @@ Program merge_programs(std::vector<Program>& parts) {
   return out;
 }
 
+namespace {
+thread_local int t_compile_threads = 0;
+}  // namespace
+
+void set_thread_compile_threads(int n) { t_compile_threads = std::max(0, std::min(n, 256)); }
+
 int compile_threads() {
+  if (t_compile_threads > 0) return t_compile_threads;
   if (const char* e = std::getenv("C2G_COMPILE_THREADS")) {
     const int n = std::atoi(e);
     if (n > 0) return std::min(n, 256);

@@ -303,7 +303,11 @@ class TaskBuilder {
 // batch lists. Empty stages are dropped.
 Program merge_programs(std::vector<Program>& parts);
 
-// Number of compile threads (C2G_COMPILE_THREADS overrides the hardware count).
+// Number of compile threads: the calling thread's own setting if it made one, else
+// C2G_COMPILE_THREADS, else the hardware count.
 int compile_threads();
+// Sets the calling thread's compile thread count (0 clears it). Concurrent solves give
+// each worker thread a share of the cores.
+void set_thread_compile_threads(int n);
 
 }  // namespace c2g

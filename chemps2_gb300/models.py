@@ -71,3 +71,32 @@ def bcs(eps, g, power):
     L = len(eps)
     return L, [(o1, o2, g * abs(eps[o1] * eps[o2]) ** power, (eps[o1] + eps[o2]) / (L - 1))
                for o1 in range(L) for o2 in range(L)]
+
+
+BATCH_BOND_DIMS = (64, 128, 256, 512)
+
+
+def batch_members(count=64, seed=2024):
+    """The independent problems of the batching workload: L uniform in {8..20}, N = L,
+    half Hubbard chains (t = 1, U uniform in [1, 8], C1) and half synthetic_ab_initio (D2h,
+    irreps round robin), D drawn from BATCH_BOND_DIMS. The spin is drawn from {0, 1} for
+    even N; odd N cannot have integer spin, so it takes 2S from {1, 3} there. Target irrep
+    0. Returns dicts with the model, two_s, n, irrep, D, kind and a per-problem seed."""
+    rng = np.random.default_rng(seed)
+    kinds = np.array(["hubbard"] * (count // 2) + ["abinit"] * (count - count // 2))
+    rng.shuffle(kinds)
+    out = []
+    for k in range(count):
+        L = int(rng.integers(8, 21))
+        spin_bit = int(rng.integers(0, 2))
+        D = int(rng.choice(BATCH_BOND_DIMS))
+        n = L
+        two_s = (n % 2) + 2 * spin_bit
+        if kinds[k] == "hubbard":
+            U = float(rng.uniform(1.0, 8.0))
+            model = hubbard(L, U)
+        else:
+            model = synthetic_ab_initio(L, 7, int(rng.integers(0, 2**31 - 1)))
+        out.append({"model": model, "two_s": two_s, "n": n, "irrep": 0, "D": D, "kind": str(kinds[k]),
+                    "seed": int(rng.integers(1, 2**31 - 1))})
+    return out

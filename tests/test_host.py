@@ -252,3 +252,43 @@ def test_convergence_scheme_checks():
             sc.set_instruction(*bad)
     with pytest.raises(c2g.Chemps2Error):
         c2g.ConvergenceScheme(0)
+
+
+def test_private_random_stream_equals_srand_rand():
+    """A batch member's private generator gives the C library's srand(seed); rand()
+    sequence, so a batch reproduces the random starts of sequential runs."""
+    libc = C.CDLL(None)
+    if not hasattr(libc, "gnu_get_libc_version"):
+        pytest.skip("not the GNU C library")
+    libc.rand.restype = C.c_int
+    for seed in (0, 1, 7, 12345, 2**31 - 1, 2**31, 4000000000):
+        ours = c2g.host_rand_sample(seed, 5000)
+        libc.srand(C.c_uint(seed))
+        theirs = np.array([libc.rand() for _ in range(5000)], dtype=np.int32)
+        assert np.array_equal(ours, theirs), seed
+
+
+def test_batch_argument_errors_are_status_codes():
+    lib = c2g.load()
+    with pytest.raises(c2g.Chemps2Error):
+        c2g._check(lib.c2g_batch_solve(-1, None, None, None, 1, None, None, None, None))
+    with pytest.raises(c2g.Chemps2Error):
+        c2g._check(lib.c2g_batch_solve(2, None, None, None, 1, None, None, None, None))
+    assert lib.c2g_batch_solve(0, None, None, None, 4, None, None, None, None) == 0
+    with pytest.raises(ValueError):
+        c2g.solve_batch([], [None], [])
+
+
+def test_batch_without_device_reports_each_problem():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    ham = c2g.Hamiltonian(4, 0, np.zeros(4, dtype=np.int32))
+    probs = [c2g.Problem(ham, 0, 4, 0) for _ in range(3)]
+    sc = c2g.ConvergenceScheme(1)
+    sc.set_instruction(0, 10, 1e-8, 1, 0.0, 1e-6)
+    with pytest.raises(c2g.NoDeviceError):
+        c2g.solve_batch(probs, [sc] * 3, [1, 2, 3], workers=2)
+    with pytest.raises(c2g.Chemps2Error):
+        c2g.solve_batch([probs[0], probs[0]], [sc, sc], [1, 2])  # a Problem twice
