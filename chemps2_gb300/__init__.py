@@ -472,13 +472,14 @@ def solve_batch(problems, schemes, seeds, workers=8, raise_on_error=True):
     matvecs = np.zeros(n, dtype=np.int64)
     seconds = np.zeros(n)
     statuses = np.zeros(n, dtype=np.int32)
+    stats = np.zeros((max(n, 1), NUM_STATS))
     rc = load().c2g_batch_solve(int(n), P, S, sd.ctypes.data_as(C.POINTER(C.c_uint)), int(workers), _dp(energies),
                                 matvecs.ctypes.data_as(C.POINTER(C.c_longlong)), _dp(seconds),
-                                statuses.ctypes.data_as(C.POINTER(C.c_int)))
+                                statuses.ctypes.data_as(C.POINTER(C.c_int)), _dp(stats))
     if raise_on_error or not statuses.any():
         _check(rc)
     return [{"energy": float(energies[i]), "matvecs": int(matvecs[i]), "seconds": float(seconds[i]),
-             "status": int(statuses[i])} for i in range(n)]
+             "status": int(statuses[i]), "stats": dict(zip(STAT_NAMES, stats[i].tolist()))} for i in range(n)]
 
 
 def host_rand_sample(seed: int, n: int) -> np.ndarray:

@@ -68,6 +68,15 @@ int guarded(F&& f) {
   }
 }
 
+// The C2G_NUM_STATS layout of c2g_dmrg_stats.
+void fill_stats(const CheMPS2::DMRGStats& s, double* out, int n) {
+  const double v[C2G_NUM_STATS] = {static_cast<double>(s.n_matvec), static_cast<double>(s.n_davidson),
+                                   s.t_join, s.t_solve, s.t_split, s.t_update, s.t_matvec, s.t_compile,
+                                   s.matvec_flops, s.matvec_bytes, s.last_energy,
+                                   static_cast<double>(s.n_matvec_fp32), s.t_upload};
+  for (int i = 0; i < n && i < C2G_NUM_STATS; i++) out[i] = v[i];
+}
+
 #define NEED(x)                                                        \
   do {                                                                 \
     if (!(x)) throw std::invalid_argument("null argument: " #x);       \
@@ -434,12 +443,7 @@ int c2g_dmrg_stats(const c2g_dmrg* d, double* out, int n) {
   return guarded([&] {
     NEED(d);
     NEED(out);
-    const CheMPS2::DMRGStats& s = d->d->stats();
-    const double v[C2G_NUM_STATS] = {static_cast<double>(s.n_matvec), static_cast<double>(s.n_davidson),
-                                     s.t_join, s.t_solve, s.t_split, s.t_update, s.t_matvec, s.t_compile,
-                                     s.matvec_flops, s.matvec_bytes, s.last_energy,
-                                     static_cast<double>(s.n_matvec_fp32), s.t_upload};
-    for (int i = 0; i < n && i < C2G_NUM_STATS; i++) out[i] = v[i];
+    fill_stats(d->d->stats(), out, n);
   });
 }
 int c2g_dmrg_reset_stats(c2g_dmrg* d) {
@@ -547,7 +551,8 @@ int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double*
 }
 
 int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* schemes, const unsigned int* seeds,
-                    int workers, double* energies, long long* matvecs, double* seconds, int* statuses) {
+                    int workers, double* energies, long long* matvecs, double* seconds, int* statuses,
+                    double* stats) {
   std::vector<CheMPS2::BatchResult> res;
   const int rc = guarded([&] {
     if (n < 0) throw std::invalid_argument("c2g_batch_solve: negative problem count");
@@ -578,6 +583,7 @@ int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* sche
     if (matvecs) matvecs[i] = r.n_matvec;
     if (seconds) seconds[i] = r.seconds;
     if (statuses) statuses[i] = code;
+    if (stats) fill_stats(r.stats, stats + static_cast<size_t>(i) * C2G_NUM_STATS, C2G_NUM_STATS);
     if (code != C2G_OK && first == C2G_OK) {
       first = code;
       first_error = "problem " + std::to_string(i) + ": " + r.error;

@@ -66,8 +66,9 @@ std::vector<BatchResult> SolveBatch(const std::vector<Problem*>& problems,
       opt.seed = seeds[i];
       DMRG d(problems[i], schemes[i], opt);
       r.energy = d.Solve();
-      r.n_matvec = d.stats().n_matvec;
-      r.matvec_seconds = d.stats().t_matvec;
+      r.stats = d.stats();
+      r.n_matvec = r.stats.n_matvec;
+      r.matvec_seconds = r.stats.t_matvec;
     } catch (const c2g::CudaError& e) {
       r.status = (e.code == cudaErrorNoDevice || e.code == cudaErrorInsufficientDriver) ? 3 : 2;
       r.error = e.what();

@@ -110,7 +110,7 @@ DevProgram& DMRG::program(const std::string& key, const std::function<c2g::Compi
   stats_.t_compile += now() - tc;
   ProgramCache::Entry e;
   const double tu = now();
-  e.dp = rt->upload(c.program);
+  e.dp = c.parts.empty() ? rt->upload(c.program) : rt->upload(c.parts);
   stats_.t_upload += now() - tu;
   e.operand_bytes = c.operand_bytes;
   e.last_use = pc.clock;
@@ -682,7 +682,7 @@ void DMRG::update_moving_right(const int index) {
   ctx.next = ops[index].get();
   ctx.mps = mps_tensor(mps_lay[index].get(), index);
   DevProgram& dp = program(dims_key("update", index, index, index + 2, ctx.moving_right ? 1 : 0),
-                           [&] { return c2g::compile_update_program(ctx); });
+                           [&] { return c2g::compile_update_program(ctx, false); });
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
   if (f32_ops_) refresh_f32(index);
@@ -713,7 +713,7 @@ void DMRG::update_moving_left(const int index) {
   ctx.next = ops[index].get();
   ctx.mps = mps_tensor(mps_lay[index + 1].get(), index + 1);
   DevProgram& dp = program(dims_key("update", index, index, index + 2, ctx.moving_right ? 1 : 0),
-                           [&] { return c2g::compile_update_program(ctx); });
+                           [&] { return c2g::compile_update_program(ctx, false); });
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
   if (f32_ops_) refresh_f32(index);
@@ -809,11 +809,11 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   rt->ones(maxdim);
   double* diag = rt->alloc(veclen);
   DevProgram& dpd = program(dims_key("diag", index, index, index + 2, 0),
-                            [&] { return c2g::compile_heff_diag_program(ctx); });
+                            [&] { return c2g::compile_heff_diag_program(ctx, false); });
   rt->run(dpd, nullptr, diag);
   long long heff_operand_bytes = 0;
   DevProgram& dph_ref = program(dims_key("heff", index, index, index + 2, 0),
-                                [&] { return c2g::compile_heff_program(ctx, true); }, &heff_operand_bytes);
+                                [&] { return c2g::compile_heff_program(ctx, true, false); }, &heff_operand_bytes);
   DevProgram* dph = &dph_ref;
   rt->prepare(*dph);
   c2g::DeviceDavidson dav(*rt, veclen, kDavidsonNumVec, kDavidsonNumVecKeep, dvdson_rtol, kDavidsonPrecondCutoff);
@@ -1092,10 +1092,10 @@ DMRG::HeffCache& DMRG::heff_program(const int index, const bool with_diag) {
     ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
     ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
     const double tc = now();
-    c2g::Compiled ch = c2g::compile_heff_program(ctx, true);
+    c2g::Compiled ch = c2g::compile_heff_program(ctx, true, false);
     stats_.t_compile += now() - tc;
     const double tu = now();
-    c.program = rt->upload(ch.program);
+    c.program = ch.parts.empty() ? rt->upload(ch.program) : rt->upload(ch.parts);
     stats_.t_upload += now() - tu;
     rt->prepare(*c.program);
     c.operand_bytes = ch.operand_bytes;
@@ -1109,7 +1109,8 @@ DMRG::HeffCache& DMRG::heff_program(const int index, const bool with_diag) {
     ctx.S = c.S.get();
     ctx.left = (index > 0) ? ops[index - 1].get() : nullptr;
     ctx.right = (index + 1 < L - 1) ? ops[index + 1].get() : nullptr;
-    c.diag = rt->upload(c2g::compile_heff_diag_program(ctx).program);
+    c2g::Compiled cd = c2g::compile_heff_diag_program(ctx, false);
+    c.diag = cd.parts.empty() ? rt->upload(cd.program) : rt->upload(cd.parts);
   }
   return c;
 }

@@ -1,9 +1,12 @@
 #include "runtime.hpp"
 
 #include <algorithm>
+#include <climits>
+#include <cstdint>
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <sstream>
 #include <thread>
@@ -16,10 +19,6 @@ std::atomic<int64_t> g_launches{0};
 inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
 
 // A team-variant tile before its items are split.
-struct PendingTile {
-  int group, pos, rows, cols;
-  int64_t work;
-};
 
 // Scheduling weight of one item of a term on a rows x cols tile: its flops plus a fixed
 // per-item cost (term lookup, batch entry, pointer setup).
@@ -180,18 +179,83 @@ void Runtime::reserve_staging(int64_t bytes, int64_t keep) {
   staging_cap_ = cap;
 }
 
-std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
+std::unique_ptr<DevProgram> Runtime::upload(const Program& p) { return upload_parts(&p, 1); }
+
+std::unique_ptr<DevProgram> Runtime::upload(const std::vector<Program>& parts) {
+  if (parts.empty()) throw std::invalid_argument("upload: no program");
+  return upload_parts(parts.data(), parts.size());
+}
+
+// Uploads the concatenation of programs compiled from disjoint output shards (the same
+// stage lists; see merge_programs) without building the merged program on the host: each
+// shard's groups, terms and batch lists go straight to their place in the staging buffer,
+// with combination-scratch references and batch-list offsets relocated on the way.
+std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t np) {
   auto dp = std::make_unique<DevProgram>();
   dp->rt = this;
-  dp->first_repeat = p.first_repeat_stage;
-  dp->combo_size = p.combo_size;
+  const size_t nsrc = parts[0].stages.size();
+  for (size_t i = 0; i < np; i++)
+    if (parts[i].stages.size() != nsrc) throw std::logic_error("upload: shards with different stage lists");
+  std::vector<int64_t> combo_base(np), entry_base(np);
+  int64_t cb = 0, eb = 0;
+  for (size_t i = 0; i < np; i++) {
+    combo_base[i] = cb;
+    entry_base[i] = eb;
+    cb = (np == 1) ? parts[i].combo_size : ((cb + parts[i].combo_size + 3) & ~int64_t(3));
+    eb += static_cast<int64_t>(parts[i].entries.size());
+  }
+  if (eb > INT32_MAX) throw std::length_error("upload: batch table too large");
+  dp->combo_size = cb;
+  auto reloc = [&](Ref r, size_t i) -> Ref {
+    if (r != 0 && ref_slot(r) == kSlotCombo) return make_ref(kSlotCombo, ref_off(r) + combo_base[i]);
+    return r;
+  };
+  // The merged stages: groups relocated, each with its shard; empty stages dropped.
+  struct MergedStage {
+    std::string name;
+    size_t src = 0;
+    std::vector<Group> groups;
+    std::vector<int32_t> part;     // shard of each group
+    std::vector<int64_t> tbase;    // first merged term of each shard
+    int64_t nterms = 0, flops = 0, items = 0;
+  };
+  std::vector<MergedStage> stages;
+  for (size_t s = 0; s < nsrc; s++) {
+    MergedStage m;
+    m.name = parts[0].stages[s].name;
+    m.src = s;
+    m.tbase.resize(np);
+    size_t ng = 0;
+    for (size_t i = 0; i < np; i++) ng += parts[i].stages[s].groups.size();
+    if (ng == 0) continue;
+    m.groups.reserve(ng);
+    m.part.reserve(ng);
+    for (size_t i = 0; i < np; i++) {
+      const Stage& ps = parts[i].stages[s];
+      m.tbase[i] = m.nterms;
+      for (const Group& g0 : ps.groups) {
+        Group g = g0;
+        g.out = reloc(g.out, i);
+        g.t0 += static_cast<int32_t>(m.nterms);
+        g.t1 += static_cast<int32_t>(m.nterms);
+        m.groups.push_back(g);
+        m.part.push_back(static_cast<int32_t>(i));
+      }
+      m.nterms += static_cast<int64_t>(ps.terms.size());
+      m.flops += ps.flops;
+      m.items += ps.items;
+      if (m.nterms > INT32_MAX) throw std::length_error("upload: too many terms in a stage");
+    }
+    if (s == 0 && parts[0].first_repeat_stage == 1) dp->first_repeat = 1;
+    stages.push_back(std::move(m));
+  }
   // Tile lists, the groups with the most work first. Groups of at most kWarpTile x
   // kWarpTile, and larger groups with light items, go to the team variant in kWarpTile
   // tiles; larger groups with heavy items go to the cooperative variant in kTile tiles.
   // (C2G_SANDWICH=item routes the light groups to the item-parallel variant instead.)
   const char* env = std::getenv("C2G_SANDWICH");
   const bool use_item = env && std::string(env) == "item";
-  const size_t ns = p.stages.size();
+  const size_t ns = stages.size();
   std::vector<std::vector<TileDesc>> tiles(ns), tiles_large(ns);
   std::vector<std::vector<WarpTile>> tiles_warp(ns);
   int64_t part_doubles = 0, ncounters = 0;
@@ -199,35 +263,37 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
   // of every stage. It is assembled in the runtime's pinned staging buffer: the terms of
   // each group are copied there in shape order (flags, k1, k2), so that neighbouring items
   // of the team variant share their loop structure, by all host threads.
-  int64_t head = align256(sizeof(BatchEntry) * p.entries.size());
+  int64_t head = align256(sizeof(BatchEntry) * eb);
   std::vector<int64_t> off_groups(ns), off_terms(ns);
   for (size_t s = 0; s < ns; s++) {
     off_groups[s] = head;
-    head += align256(sizeof(Group) * p.stages[s].groups.size());
+    head += align256(sizeof(Group) * stages[s].groups.size());
     off_terms[s] = head;
-    head += align256(sizeof(Term) * p.stages[s].terms.size());
+    head += align256(sizeof(Term) * stages[s].nterms);
   }
   reserve_staging(head, 0);
-  if (!p.entries.empty()) std::memcpy(staging_, p.entries.data(), sizeof(BatchEntry) * p.entries.size());
   std::vector<Term*> terms(ns);
   for (size_t s = 0; s < ns; s++) {
-    const Stage& st = p.stages[s];
-    if (!st.groups.empty()) std::memcpy(staging_ + off_groups[s], st.groups.data(), sizeof(Group) * st.groups.size());
+    const MergedStage& st = stages[s];
+    std::memcpy(staging_ + off_groups[s], st.groups.data(), sizeof(Group) * st.groups.size());
     terms[s] = reinterpret_cast<Term*>(staging_ + off_terms[s]);
   }
   {
-    // (stage, first group, last group) chunks of about equal term counts
+    // work items: the batch table of each shard, and (stage, first group, last group)
+    // chunks of about equal term counts
     struct Chunk {
       size_t s;
       size_t g0, g1;
     };
     std::vector<Chunk> chunks;
+    for (size_t i = 0; i < np; i++)
+      if (!parts[i].entries.empty()) chunks.push_back(Chunk{SIZE_MAX, i, 0});
     const int nthreads = std::max(1, compile_threads());
     int64_t total_terms = 0;
-    for (const Stage& st : p.stages) total_terms += static_cast<int64_t>(st.terms.size());
+    for (const MergedStage& st : stages) total_terms += st.nterms;
     const int64_t per = std::max<int64_t>(total_terms / (4 * nthreads), 4096);
     for (size_t s = 0; s < ns; s++) {
-      const Stage& st = p.stages[s];
+      const MergedStage& st = stages[s];
       size_t g0 = 0;
       int64_t acc = 0;
       for (size_t g = 0; g < st.groups.size(); g++) {
@@ -243,11 +309,29 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     std::atomic<bool> bad{false};
     auto work = [&] {
       for (size_t c = next++; c < chunks.size(); c = next++) {
-        const Stage& st = p.stages[chunks[c].s];
+        if (chunks[c].s == SIZE_MAX) {
+          const Program& pp = parts[chunks[c].g0];
+          std::memcpy(staging_ + sizeof(BatchEntry) * entry_base[chunks[c].g0], pp.entries.data(),
+                      sizeof(BatchEntry) * pp.entries.size());
+          continue;
+        }
+        const MergedStage& st = stages[chunks[c].s];
         Term* out = terms[chunks[c].s];
         for (size_t g = chunks[c].g0; g < chunks[c].g1; g++) {
           const Group& G = st.groups[g];
-          std::memcpy(out + G.t0, st.terms.data() + G.t0, sizeof(Term) * (G.t1 - G.t0));
+          const size_t i = static_cast<size_t>(st.part[g]);
+          const Term* src = parts[i].stages[st.src].terms.data() + (G.t0 - st.tbase[i]);
+          const int32_t lbase = static_cast<int32_t>(entry_base[i]);
+          for (int32_t k = 0; k < G.t1 - G.t0; k++) {
+            Term t = src[k];
+            if (np > 1) {
+              if (t.flags & kHasA) t.a = reloc(t.a, i);
+              t.b = reloc(t.b, i);
+              if (t.flags & kHasC) t.c = reloc(t.c, i);
+              if (t.list >= 0) t.list += lbase;
+            }
+            out[G.t0 + k] = t;
+          }
           std::stable_sort(out + G.t0, out + G.t1, [](const Term& x, const Term& y) {
             return std::make_tuple(x.flags, x.k1, x.k2) < std::make_tuple(y.flags, y.k1, y.k2);
           });
@@ -267,98 +351,207 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     for (auto& t : pool) t.join();
     if (bad) throw std::invalid_argument("task term without items");
   }
+  // Per group of a stage: its tile kind and, for the team variant, the work of a tile of
+  // each of its (at most four) tile shapes. Tiles of one shape in one group have the same
+  // work and the same splits, so both are computed once per shape. Programs can hold
+  // hundreds of thousands of small groups: everything here is linear in groups and terms.
+  struct GroupTiles {
+    int32_t kind = 0;         // 0 none, 1 cooperative / item variant, 2 team variant
+    int32_t large = 0;
+    int32_t tm = 0, tn = 0;   // tile counts
+    int32_t rows[2] = {0, 0}; // full and last tile rows (shape index bit 1)
+    int32_t cols[2] = {0, 0}; // full and last tile columns (shape index bit 0)
+    int64_t work[4] = {0, 0, 0, 0};
+    int32_t nsplit[4] = {1, 1, 1, 1};
+    int32_t bounds[4] = {-1, -1, -1, -1};  // first of nsplit + 1 item boundaries in `splits`
+  };
+  auto present = [](const GroupTiles& gi, int k) {
+    // shapes with a full (not last) tile exist only with more than one tile
+    return !((!(k >> 1) && gi.tm < 2) || (!(k & 1) && gi.tn < 2));
+  };
+  auto shape_of = [](const GroupTiles& gi, int i, int j) {
+    return ((i == gi.tm - 1) ? 2 : 0) | ((j == gi.tn - 1) ? 1 : 0);
+  };
+  const int nthreads = std::max(1, compile_threads());
+  auto parallel_groups = [&](size_t n, int64_t nterms, const std::function<void(size_t, size_t)>& f) {
+    const int nt = (nterms < 200000) ? 1 : static_cast<int>(std::min<size_t>(nthreads, (n + 63) / 64));
+    if (nt <= 1) {
+      f(0, n);
+      return;
+    }
+    std::vector<std::thread> pool;
+    const size_t per = (n + nt - 1) / nt;
+    for (int i = 1; i < nt; i++) pool.emplace_back(f, std::min(n, i * per), std::min(n, (i + 1) * per));
+    f(0, std::min(n, per));
+    for (auto& t : pool) t.join();
+  };
   int64_t tile_bytes = 0;
   for (size_t s = 0; s < ns; s++) {
-    const Stage& st = p.stages[s];
-    std::vector<PendingTile> pending;
-    int64_t warp_work = 0;
-    std::vector<int> order(st.groups.size());
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int b) { return st.groups[a].work > st.groups[b].work; });
-    for (int g : order) {
-      const Group& G = st.groups[g];
-      if (G.m <= 0 || G.n <= 0) continue;
-      if (G.m >= 32768 * kWarpTile || G.n >= 65536 * kWarpTile)
-        throw std::invalid_argument("output block too large for the tile index");
-      int64_t items = 0;
-      for (int t = G.t0; t < G.t1; t++) items += st.terms[t].count;
-      const bool small = G.m <= kWarpTile && G.n <= kWarpTile;
-      const bool large = !small && std::min(G.m, kTile) * std::min(G.n, kTile) >= kLargeTileElems &&
-                         G.work >= kLargeItemFlops * std::max<int64_t>(items, 1);
-      if (large || use_item) {
-        const int tm = (G.m + kTile - 1) / kTile, tn = (G.n + kTile - 1) / kTile;
-        for (int i = 0; i < tm; i++)
-          for (int j = 0; j < tn; j++) {
-            const int rows = std::min(kTile, G.m - i * kTile), cols = std::min(kTile, G.n - j * kTile);
-            (large ? tiles_large : tiles)[s].push_back(TileDesc{g, (i << 16) | j, sandwich_grid(rows, cols), 0});
-          }
-      } else {
-        const int tm = (G.m + kWarpTile - 1) / kWarpTile, tn = (G.n + kWarpTile - 1) / kWarpTile;
-        for (int i = 0; i < tm; i++)
-          for (int j = 0; j < tn; j++) {
-            const int rows = std::min(kWarpTile, G.m - i * kWarpTile), cols = std::min(kWarpTile, G.n - j * kWarpTile);
-            pending.push_back(PendingTile{g, (i << 16) | j, rows, cols, 0});
-            for (int t = G.t0; t < G.t1; t++)
-              pending.back().work += terms[s][t].count * item_cost(terms[s][t], rows, cols);
-            warp_work += pending.back().work;
-          }
+    const MergedStage& st = stages[s];
+    const Term* tt = terms[s];
+    const size_t ng = st.groups.size();
+    std::vector<GroupTiles> info(ng);
+    std::atomic<bool> too_large{false};
+    parallel_groups(ng, st.nterms, [&](size_t g0, size_t g1) {
+      for (size_t g = g0; g < g1; g++) {
+        const Group& G = st.groups[g];
+        GroupTiles& gi = info[g];
+        if (G.m <= 0 || G.n <= 0) continue;
+        if (G.m >= 32768 * kWarpTile || G.n >= 65536 * kWarpTile) {
+          too_large = true;
+          continue;
+        }
+        int64_t items = 0;
+        for (int t = G.t0; t < G.t1; t++) items += tt[t].count;
+        const bool small = G.m <= kWarpTile && G.n <= kWarpTile;
+        gi.large = !small && std::min(G.m, kTile) * std::min(G.n, kTile) >= kLargeTileElems &&
+                   G.work >= kLargeItemFlops * std::max<int64_t>(items, 1);
+        if (gi.large || use_item) {
+          gi.kind = 1;
+          gi.tm = (G.m + kTile - 1) / kTile;
+          gi.tn = (G.n + kTile - 1) / kTile;
+          continue;
+        }
+        gi.kind = 2;
+        gi.tm = (G.m + kWarpTile - 1) / kWarpTile;
+        gi.tn = (G.n + kWarpTile - 1) / kWarpTile;
+        gi.rows[0] = std::min(kWarpTile, G.m);
+        gi.rows[1] = G.m - (gi.tm - 1) * kWarpTile;
+        gi.cols[0] = std::min(kWarpTile, G.n);
+        gi.cols[1] = G.n - (gi.tn - 1) * kWarpTile;
+        for (int k = 0; k < 4; k++) {
+          if (!present(gi, k)) continue;
+          const int r = gi.rows[k >> 1], c = gi.cols[k & 1];
+          for (int t = G.t0; t < G.t1; t++) gi.work[k] += tt[t].count * item_cost(tt[t], r, c);
+        }
       }
+    });
+    if (too_large) throw std::invalid_argument("output block too large for the tile index");
+    int64_t warp_work = 0;
+    for (const GroupTiles& gi : info) {
+      if (gi.kind != 2) continue;
+      // tiles per shape: (tm - 1) full rows and 1 last row, likewise for columns
+      const int64_t nr[2] = {gi.tm - 1, 1}, nc[2] = {gi.tn - 1, 1};
+      for (int k = 0; k < 4; k++)
+        if (present(gi, k)) warp_work += nr[k >> 1] * nc[k & 1] * gi.work[k];
     }
     // Team-variant tiles: heavy tiles have their items split over several CTAs so that the
-    // stage's work is spread over at least kWarpCtaTarget CTA-sized pieces.
+    // stage's work is spread over at least kWarpCtaTarget CTA-sized pieces; the split
+    // points are at equal shares of the tile's work (computed for split shapes only).
     const int64_t piece = std::max<int64_t>(warp_work / kWarpCtaTarget, 1);
-    int64_t part_off = 0, counter = 0;
-    for (const PendingTile& pt : pending) {
-      const Group& G = st.groups[pt.group];
-      const int cls = warp_class_id(pt.rows, pt.cols);
-      const int total = G.t1 > G.t0 ? terms[s][G.t1 - 1].item0 + terms[s][G.t1 - 1].count : 0;
-      const int min_items = 2 * warp_slots(cls);
-      int nsplit = static_cast<int>(std::min<int64_t>((pt.work + piece - 1) / piece, kWarpMaxSplit));
-      nsplit = std::max(1, std::min(nsplit, total / std::max(min_items, 1)));
-      WarpTile wt{};
-      wt.group = pt.group;
-      wt.pos = pt.pos;
-      wt.cls = cls;
-      wt.nsplit = nsplit;
-      if (nsplit > 1) {
-        wt.part = part_off;
-        wt.counter = static_cast<int32_t>(counter++);
-        part_off += static_cast<int64_t>(nsplit) * pt.rows * pt.cols;
-      }
-      // item boundaries at equal shares of the tile's work
-      int t = G.t0;
-      int64_t before = 0;  // work of the items before term t
-      int start = 0;
-      for (int k = 0; k < nsplit; k++) {
-        int stop = total;
-        if (k + 1 < nsplit) {
-          const int64_t target = pt.work * (k + 1) / nsplit;
-          while (t < G.t1 && before + terms[s][t].count * item_cost(terms[s][t], pt.rows, pt.cols) < target) {
-            before += terms[s][t].count * item_cost(terms[s][t], pt.rows, pt.cols);
-            t++;
+    std::vector<int32_t> splits;
+    for (size_t g = 0; g < ng; g++) {
+      GroupTiles& gi = info[g];
+      if (gi.kind != 2) continue;
+      const Group& G = st.groups[g];
+      const int total = G.t1 > G.t0 ? tt[G.t1 - 1].item0 + tt[G.t1 - 1].count : 0;
+      for (int k = 0; k < 4; k++) {
+        if (!present(gi, k)) continue;
+        const int r = gi.rows[k >> 1], c = gi.cols[k & 1];
+        const int64_t work = gi.work[k];
+        const int min_items = 2 * warp_slots(warp_class_id(r, c));
+        int nsplit = static_cast<int>(std::min<int64_t>((work + piece - 1) / piece, kWarpMaxSplit));
+        nsplit = std::max(1, std::min(nsplit, total / std::max(min_items, 1)));
+        gi.nsplit[k] = nsplit;
+        if (nsplit == 1) continue;
+        gi.bounds[k] = static_cast<int32_t>(splits.size());
+        splits.push_back(0);
+        int t = G.t0;
+        int64_t before = 0;  // work of the items before term t
+        for (int q = 0; q < nsplit; q++) {
+          int stop = total;
+          if (q + 1 < nsplit) {
+            const int64_t target = work * (q + 1) / nsplit;
+            while (t < G.t1 && before + tt[t].count * item_cost(tt[t], r, c) < target) {
+              before += tt[t].count * item_cost(tt[t], r, c);
+              t++;
+            }
+            if (t < G.t1) {
+              const int64_t cst = item_cost(tt[t], r, c);
+              const int64_t inside = (target - before + cst - 1) / cst;
+              stop = tt[t].item0 + static_cast<int>(std::min<int64_t>(inside, tt[t].count));
+            }
+            stop = std::max(stop, splits.back());
           }
-          stop = total;
-          if (t < G.t1) {
-            const int64_t c = item_cost(terms[s][t], pt.rows, pt.cols);
-            const int64_t inside = (target - before + c - 1) / c;
-            stop = terms[s][t].item0 + static_cast<int>(std::min<int64_t>(inside, terms[s][t].count));
-          }
-          stop = std::max(stop, start);
+          splits.push_back(stop);
         }
-        wt.split = k;
-        wt.item0 = start;
-        wt.item1 = stop;
-        tiles_warp[s].push_back(wt);
-        start = stop;
+      }
+    }
+    // Tile order: the groups with the most work first (binned by powers of two, in
+    // program order within a bin), row-major within a group. Team-variant tiles are then
+    // grouped by row class (one kernel per class), keeping that order within a class.
+    std::vector<int32_t> order(ng);
+    {
+      auto bin = [&](size_t g) {
+        const int64_t w = st.groups[g].work;
+        return w <= 0 ? 0 : 64 - __builtin_clzll(static_cast<unsigned long long>(w));
+      };
+      int64_t cnt[66] = {0};
+      for (size_t g = 0; g < ng; g++) cnt[65 - bin(g)]++;
+      int64_t at = 0;
+      for (int k = 0; k < 66; k++) {
+        const int64_t c = cnt[k];
+        cnt[k] = at;
+        at += c;
+      }
+      for (size_t g = 0; g < ng; g++) order[cnt[65 - bin(g)]++] = static_cast<int32_t>(g);
+    }
+    int64_t per_class[kWarpRowClasses] = {0};
+    for (size_t g = 0; g < ng; g++) {
+      const GroupTiles& gi = info[g];
+      if (gi.kind != 2) continue;
+      for (int i = 0; i < gi.tm; i++)
+        for (int j = 0; j < gi.tn; j++) {
+          const int k = shape_of(gi, i, j);
+          per_class[warp_row_class(warp_class_id(gi.rows[k >> 1], gi.cols[k & 1]))] += gi.nsplit[k];
+        }
+    }
+    int64_t class_at[kWarpRowClasses];
+    int64_t nwarp_tiles = 0;
+    for (int c = 0; c < kWarpRowClasses; c++) {
+      class_at[c] = nwarp_tiles;
+      nwarp_tiles += per_class[c];
+    }
+    tiles_warp[s].resize(static_cast<size_t>(nwarp_tiles));
+    WarpTile* wout = tiles_warp[s].data();
+    int64_t part_off = 0, counter = 0;
+    for (int g : order) {
+      const Group& G = st.groups[g];
+      const GroupTiles& gi = info[g];
+      if (gi.kind == 1) {
+        for (int i = 0; i < gi.tm; i++)
+          for (int j = 0; j < gi.tn; j++) {
+            const int rows = std::min(kTile, G.m - i * kTile), cols = std::min(kTile, G.n - j * kTile);
+            (gi.large ? tiles_large : tiles)[s].push_back(TileDesc{g, (i << 16) | j, sandwich_grid(rows, cols), 0});
+          }
+      } else if (gi.kind == 2) {
+        const int total = G.t1 > G.t0 ? tt[G.t1 - 1].item0 + tt[G.t1 - 1].count : 0;
+        for (int i = 0; i < gi.tm; i++)
+          for (int j = 0; j < gi.tn; j++) {
+            const int k = shape_of(gi, i, j);
+            const int rows = gi.rows[k >> 1], cols = gi.cols[k & 1];
+            WarpTile wt{};
+            wt.group = g;
+            wt.pos = (i << 16) | j;
+            wt.cls = warp_class_id(rows, cols);
+            wt.nsplit = gi.nsplit[k];
+            if (wt.nsplit > 1) {
+              wt.part = part_off;
+              wt.counter = static_cast<int32_t>(counter++);
+              part_off += static_cast<int64_t>(wt.nsplit) * rows * cols;
+            }
+            int64_t& at = class_at[warp_row_class(wt.cls)];
+            for (int q = 0; q < wt.nsplit; q++) {
+              wt.split = q;
+              wt.item0 = (wt.nsplit == 1) ? 0 : splits[gi.bounds[k] + q];
+              wt.item1 = (wt.nsplit == 1) ? total : splits[gi.bounds[k] + q + 1];
+              wout[at++] = wt;
+            }
+          }
       }
     }
     part_doubles = std::max(part_doubles, part_off);
     ncounters = std::max(ncounters, counter);
-    // team-variant tiles ordered by row class (one kernel per class), work order kept
-    std::stable_sort(tiles_warp[s].begin(), tiles_warp[s].end(), [](const WarpTile& a, const WarpTile& b) {
-      return warp_row_class(a.cls) < warp_row_class(b.cls);
-    });
     tile_bytes += align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size()) +
                   align256(sizeof(WarpTile) * tiles_warp[s].size());
   }
@@ -374,13 +567,13 @@ std::unique_ptr<DevProgram> Runtime::upload(const Program& p) {
     return d;
   };
   dp->entries = reinterpret_cast<const BatchEntry*>(dbase);
-  dp->nentries = static_cast<int64_t>(p.entries.size());
+  dp->nentries = eb;
   for (size_t s = 0; s < ns; s++) {
-    const Stage& st = p.stages[s];
+    const MergedStage& st = stages[s];
     DevStage ds;
     ds.name = st.name;
     ds.ngroups = static_cast<int>(st.groups.size());
-    ds.nterms = static_cast<int>(st.terms.size());
+    ds.nterms = static_cast<int>(st.nterms);
     ds.ntiles = static_cast<int>(tiles[s].size());
     ds.flops = st.flops;
     ds.items = st.items;

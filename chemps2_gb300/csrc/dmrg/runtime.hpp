@@ -88,6 +88,9 @@ class Runtime {
   float* alloc_f32(int64_t n_floats);
 
   std::unique_ptr<DevProgram> upload(const Program& p);
+  // The program made of these shards (compiled with keep_empty from disjoint outputs), as
+  // upload(merge_programs(parts)) gives it, without assembling the merged program.
+  std::unique_ptr<DevProgram> upload(const std::vector<Program>& parts);
   void prepare(DevProgram& p);
   // Runs the repeat stages (preparing first if needed). The combination stage always runs
   // in FP64; prec selects the arithmetic of the repeat stages. An FP32 run converts X
@@ -127,6 +130,7 @@ class Runtime {
   int64_t staging_cap_ = 0;
   // grows the staging buffer to at least `bytes`, keeping its first `keep` bytes
   void reserve_staging(int64_t bytes, int64_t keep);
+  std::unique_ptr<DevProgram> upload_parts(const Program* parts, size_t np);
 };
 
 // Number of kernels this library has launched in this process (all runtimes).

@@ -63,17 +63,6 @@ SyBookkeeper::SyBookkeeper(const Problem* P, const int D)
   if (!IsPossible()) throw std::invalid_argument("SyBookkeeper: the targeted symmetry sector is empty");
 }
 
-int SyBookkeeper::sector_id(const int b, const int n, const int two_s, const int irrep) const {
-  if (b < 0 || b > L) return -1;
-  if (n < Nmin[b] || n > Nmax[b]) return -1;
-  const int smin = TwoSmin[b][n - Nmin[b]];
-  const int smax = TwoSmax[b][n - Nmin[b]];
-  if ((two_s % 2) != (smin % 2)) return -1;
-  if (two_s < smin || two_s > smax) return -1;
-  if (irrep < 0 || irrep >= nirrep) return -1;
-  return sec_base[b][n - Nmin[b]] + ((two_s - smin) / 2) * nirrep + irrep;
-}
-
 void SyBookkeeper::sector_labels(const int b, const int id, int* n, int* two_s, int* irrep) const {
   for (int nn = Nmax[b]; nn >= Nmin[b]; nn--) {
     if (sec_base[b][nn - Nmin[b]] <= id) {
@@ -85,20 +74,6 @@ void SyBookkeeper::sector_labels(const int b, const int id, int* n, int* two_s, 
     }
   }
   *n = *two_s = *irrep = -1;
-}
-
-int SyBookkeeper::dim_private(const std::vector<std::vector<int>>& st, int b, int n, int two_s,
-                              int irrep) const {
-  const int id = sector_id(b, n, two_s, irrep);
-  return id < 0 ? 0 : st[b][id];
-}
-
-int SyBookkeeper::gFCIdim(const int b, const int n, const int s, const int i) const {
-  return dim_private(fci, b, n, s, i);
-}
-
-int SyBookkeeper::gCurrentDim(const int b, const int n, const int s, const int i) const {
-  return dim_private(cur, b, n, s, i);
 }
 
 void SyBookkeeper::SetDim(const int b, const int n, const int s, const int i, const int value) {

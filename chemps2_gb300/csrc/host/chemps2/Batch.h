@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "ConvergenceScheme.h"
+#include "DMRG.h"
 #include "Problem.h"
 
 namespace CheMPS2 {
@@ -22,6 +23,7 @@ struct BatchResult {
   // CUDA device; 4 another failure. `error` says why.
   int status = 0;
   std::string error;
+  DMRGStats stats;             // the DMRG's statistics after Solve()
 };
 
 // Solves problems[i] with schemes[i] for every i. Problem i's random start is the one that

@@ -38,12 +38,27 @@ class SyBookkeeper {
   int gTwoSmax(const int b, const int n) const { return TwoSmax[b][n - Nmin[b]]; }
 
   // Dense sector index at boundary b, or -1 when (N, 2S, I) is outside the ranges.
-  int sector_id(const int b, const int n, const int two_s, const int irrep) const;
+  int sector_id(const int b, const int n, const int two_s, const int irrep) const {
+    if (b < 0 || b > L) return -1;
+    if (n < Nmin[b] || n > Nmax[b]) return -1;
+    const int smin = TwoSmin[b][n - Nmin[b]];
+    const int smax = TwoSmax[b][n - Nmin[b]];
+    if ((two_s % 2) != (smin % 2)) return -1;
+    if (two_s < smin || two_s > smax) return -1;
+    if (irrep < 0 || irrep >= nirrep) return -1;
+    return sec_base[b][n - Nmin[b]] + ((two_s - smin) / 2) * nirrep + irrep;
+  }
   int num_sectors(const int b) const { return nsec[b]; }
   void sector_labels(const int b, const int id, int* n, int* two_s, int* irrep) const;
 
-  int gFCIdim(const int b, const int n, const int two_s, const int irrep) const;
-  int gCurrentDim(const int b, const int n, const int two_s, const int irrep) const;
+  int gFCIdim(const int b, const int n, const int two_s, const int irrep) const {
+    const int id = sector_id(b, n, two_s, irrep);
+    return id < 0 ? 0 : fci[b][id];
+  }
+  int gCurrentDim(const int b, const int n, const int two_s, const int irrep) const {
+    const int id = sector_id(b, n, two_s, irrep);
+    return id < 0 ? 0 : cur[b][id];
+  }
   int cur_dim_by_id(const int b, const int id) const { return id < 0 ? 0 : cur[b][id]; }
   int fci_dim_by_id(const int b, const int id) const { return id < 0 ? 0 : fci[b][id]; }
   void SetDim(const int b, const int n, const int two_s, const int irrep, const int value);
@@ -62,7 +77,10 @@ class SyBookkeeper {
 
   void fill_fci_dim_right(std::vector<std::vector<int>>& st, int start, int stop);
   void fill_fci_dim_left(std::vector<std::vector<int>>& st, int start, int stop);
-  int dim_private(const std::vector<std::vector<int>>& st, int b, int n, int two_s, int irrep) const;
+  int dim_private(const std::vector<std::vector<int>>& st, int b, int n, int two_s, int irrep) const {
+    const int id = sector_id(b, n, two_s, irrep);
+    return id < 0 ? 0 : st[b][id];
+  }
   void scale_cur_dim(int virtual_dim, int start, int stop);
 };
 

@@ -9,7 +9,7 @@ namespace c2g {
 namespace {
 
 template <class F>
-Compiled run_sharded(F emit, bool track = false) {
+Compiled run_sharded(F emit, bool track, bool merge) {
   const int n = compile_threads();
   Compiled out;
   if (n <= 1) {
@@ -21,7 +21,7 @@ Compiled run_sharded(F emit, bool track = false) {
     return out;
   }
   std::vector<Program> parts(n);
-  std::vector<std::unordered_map<Ref, int64_t>> operands(n);
+  std::vector<RefSizes> operands(n);
   std::vector<int64_t> contractions(n, 0);
   std::vector<std::exception_ptr> errors(n);
   std::vector<std::thread> threads;
@@ -41,35 +41,35 @@ Compiled run_sharded(F emit, bool track = false) {
   for (auto& t : threads) t.join();
   for (auto& e : errors)
     if (e) std::rethrow_exception(e);
-  out.program = merge_programs(parts);
-  std::unordered_map<Ref, int64_t> all;
-  for (auto& m : operands)
-    for (auto& kv : m) {
-      int64_t& v = all[kv.first];
-      if (kv.second > v) v = kv.second;
-    }
-  for (auto& kv : all) out.operand_bytes += 8 * kv.second;
+  if (merge) out.program = merge_programs(parts);
+  else out.parts = std::move(parts);
+  if (track) {
+    RefSizes all;
+    for (auto& m : operands) m.for_each([&](Ref r, int64_t v) { all.note(r, v); });
+    out.operand_bytes = 8 * all.total();
+  }
   for (int64_t c : contractions) out.contractions += c;
   return out;
 }
 
 }  // namespace
 
-Compiled compile_heff_program(const HeffContext& ctx, bool track_operands) {
-  return run_sharded([&](TaskBuilder& tb, int shard, int n) { compile_heff(tb, ctx, shard, n); }, track_operands);
+Compiled compile_heff_program(const HeffContext& ctx, bool track_operands, bool merge) {
+  return run_sharded([&](TaskBuilder& tb, int shard, int n) { compile_heff(tb, ctx, shard, n); }, track_operands,
+                     merge);
 }
 
-Compiled compile_heff_diag_program(const HeffContext& ctx) {
-  return run_sharded([&](TaskBuilder& tb, int shard, int n) { compile_heff_diag(tb, ctx, shard, n); });
+Compiled compile_heff_diag_program(const HeffContext& ctx, bool merge) {
+  return run_sharded([&](TaskBuilder& tb, int shard, int n) { compile_heff_diag(tb, ctx, shard, n); }, false, merge);
 }
 
-Compiled compile_update_program(const UpdateContext& ctx) {
+Compiled compile_update_program(const UpdateContext& ctx, bool merge) {
   return run_sharded([&](TaskBuilder& tb, int shard, int n) {
     UpdateContext c = ctx;
     c.shard = shard;
     c.nshards = n;
     compile_update(tb, c);
-  });
+  }, false, merge);
 }
 
 }  // namespace c2g

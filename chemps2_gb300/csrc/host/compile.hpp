@@ -9,14 +9,16 @@
 namespace c2g {
 
 struct Compiled {
-  Program program;
+  Program program;             // the merged program (empty when `parts` is not)
+  std::vector<Program> parts;  // the unmerged shards (merge = false); Runtime::upload takes them
   int64_t operand_bytes = 0;   // distinct MPS / operator bytes the program reads
   int64_t contractions = 0;    // block contractions recorded (before batching)
 };
 
-// track_operands fills Compiled::operand_bytes (costs compile time).
-Compiled compile_heff_program(const HeffContext& ctx, bool track_operands = false);
-Compiled compile_heff_diag_program(const HeffContext& ctx);
-Compiled compile_update_program(const UpdateContext& ctx);
+// track_operands fills Compiled::operand_bytes (costs compile time). With merge = false
+// a program compiled in several shards is left in Compiled::parts.
+Compiled compile_heff_program(const HeffContext& ctx, bool track_operands = false, bool merge = true);
+Compiled compile_heff_diag_program(const HeffContext& ctx, bool merge = true);
+Compiled compile_update_program(const UpdateContext& ctx, bool merge = true);
 
 }  // namespace c2g

@@ -13,7 +13,8 @@ static const Blk kNo;
 static Blk q_plus_l(HeffEmitter& h, const OpT& q, const BoundaryOps* side, const std::vector<int>& sites,
                     int ir, double (*coef)(HeffEmitter&, int), int n1, int s1, int i1, int n2, int s2, int i2,
                     int rows, int cols) {
-  std::vector<std::pair<double, Blk>> parts{{1.0, HeffEmitter::need(q.blk(n1, s1, i1, n2, s2, i2))}};
+  thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+  parts.assign(1, {1.0, HeffEmitter::need(q.blk(n1, s1, i1, n2, s2, i2))});
   for (int l : sites)
     if (h.irr(l) == ir) parts.push_back({coef(h, l), HeffEmitter::need(side->Lop(l).blk(n1, s1, i1, n2, s2, i2))});
   return h.combine(parts, rows, cols);

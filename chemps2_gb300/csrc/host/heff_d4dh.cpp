@@ -19,7 +19,8 @@ inline int ph(int x) { return heff_phase(x); }
 template <class Coef>
 Blk lsum(HeffEmitter& h, const BoundaryOps* side, bool left, int ir, Coef coef, int n1, int s1, int i1, int n2,
          int s2, int i2, int rows, int cols) {
-  std::vector<std::pair<double, Blk>> parts;
+  thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+  parts.clear();
   const int lo = left ? 0 : h.theindex + 2, hi = left ? h.theindex : h.L;
   for (int l = lo; l < hi; l++)
     if (h.irr(l) == ir) parts.push_back({coef(l), HeffEmitter::need(side->Lop(l).blk(n1, s1, i1, n2, s2, i2))});
@@ -149,7 +150,8 @@ void HeffEmitter::d4E() {
       const int kp = kap(nld, SLd, ILd, kn1, kn2, ktj, nrd, SRd, IRd);
       for (int la = 0; la < i; la++) {
         if (irr(la) != Irrep) continue;
-        std::vector<std::pair<double, Blk>> parts;
+        thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+        parts.clear();
         for (int lb = i + 2; lb < L; lb++) {
           if (irr(lb) != Irrep) continue;
           const Blk rb = rdn ? Rt->Lop(lb).blk(nrd, SRd, IRd, NR, TwoSR, IR) : Rt->Lop(lb).blk(NR, TwoSR, IR, nrd, SRd, IRd);
@@ -444,7 +446,8 @@ void HeffEmitter::d4H() {
       const int kp = kap(nld, SLd, ILd, kn1, kn2, ktj, nrd, SRd, IRd);
       for (int la = 0; la < i; la++) {
         if (irr(la) != Irrep) continue;
-        std::vector<std::pair<double, Blk>> parts;
+        thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+        parts.clear();
         for (int lb = i + 2; lb < L; lb++) {
           if (irr(lb) != Irrep) continue;
           const Blk rb = rdn ? Rt->Lop(lb).blk(nrd, SRd, IRd, NR, TwoSR, IR) : Rt->Lop(lb).blk(NR, TwoSR, IR, nrd, SRd, IRd);

@@ -45,7 +45,8 @@ void five_body(HeffEmitter& h, int nld, int SLd, int nrd, int SRd, int kn1, int 
     if (kp == -1) continue;
     for (int la = 0; la < i; la++) {
       if (h.irr(la) != Irrep) continue;
-      std::vector<std::pair<double, Blk>> parts;
+      thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+      parts.clear();
       for (int lb = i + 2; lb < h.L; lb++) {
         if (h.irr(lb) != IrrepTimesMid) continue;
         const Blk rb = rdn ? h.Rt->Lop(lb).blk(nrd, SRd, IRd, h.NR, h.TwoSR, h.IR)

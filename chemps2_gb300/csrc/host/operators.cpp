@@ -563,7 +563,8 @@ struct Emit {
       if (out.moving_right) {
         // case 1
         if (dim(index - 1, n, su, i) > 0 && dim(index - 1, n - 1, sd, id) > 0) {
-          std::vector<std::pair<double, Blk>> parts;
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.clear();
           for (int loca : locs)
             parts.push_back({V(loca, site, index - 1, index - 1), need(Lprev(loca).blk(n - 1, sd, id, n, su, i))});
           const Blk W = tb.combine(parts, dim(index - 1, n - 1, sd, id), dim(index - 1, n, su, i));
@@ -573,7 +574,8 @@ struct Emit {
         }
         // case 2
         if (dim(index - 1, n - 2, su, i) > 0 && dim(index - 1, n - 1, sd, id) > 0) {
-          std::vector<std::pair<double, Blk>> parts;
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.clear();
           for (int loca : locs)
             parts.push_back({2 * V(loca, index - 1, site, index - 1) - V(loca, index - 1, index - 1, site),
                              need(Lprev(loca).blk(n - 2, su, i, n - 1, sd, id))});
@@ -590,7 +592,8 @@ struct Emit {
             const int dlu = dim(index - 1, n - 1, slu, ilu), dld = dim(index - 1, n, sld, ild);
             if (dlu <= 0 || dld <= 0) continue;
             const double factor = ph(su + sld) * std::sqrt((sld + 1) * (su + 1.0)) * wigner6j(su, sd, 1, sld, slu, 1);
-            std::vector<std::pair<double, Blk>> parts;
+            thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+            parts.clear();
             for (int loca : locs) {
               double a = factor * V(loca, index - 1, site, index - 1);
               if (sld == su) a += V(loca, index - 1, index - 1, site);
@@ -604,7 +607,8 @@ struct Emit {
       } else {
         // case 1
         if (dim(index + 1, n + 2, su, i) > 0 && dim(index + 1, n + 1, sd, id) > 0) {
-          std::vector<std::pair<double, Blk>> parts;
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.clear();
           for (int loca : locs)
             parts.push_back({V(site, loca, index, index), need(Lprev(loca).blk(n + 1, sd, id, n + 2, su, i))});
           const Blk W = tb.combine(parts, dim(index + 1, n + 1, sd, id), dim(index + 1, n + 2, su, i));
@@ -614,7 +618,8 @@ struct Emit {
         }
         // case 2
         if (dim(index + 1, n + 2, su, i) > 0 && dim(index + 1, n + 3, sd, id) > 0) {
-          std::vector<std::pair<double, Blk>> parts;
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.clear();
           for (int loca : locs)
             parts.push_back({2 * V(site, index, loca, index) - V(site, index, index, loca),
                              need(Lprev(loca).blk(n + 2, su, i, n + 3, sd, id))});
@@ -633,7 +638,8 @@ struct Emit {
             const double f1 = ph(sd + sru) * std::sqrt((sru + 1.0) / (sd + 1.0)) * (srd + 1) *
                               wigner6j(su, sd, 1, srd, sru, 1);
             const double f2 = (srd + 1.0) / (sd + 1.0);
-            std::vector<std::pair<double, Blk>> parts;
+            thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+            parts.clear();
             for (int loca : locs) {
               double a = f1 * V(site, index, loca, index);
               if (sru == sd) a += f2 * V(site, index, index, loca);
@@ -752,7 +758,8 @@ struct Emit {
           const int dlu = dim(index - 1, n, su, i), dld = dim(index - 1, n, sld, ild);
           if (dlu <= 0 || dld <= 0) continue;
           const double fD = ph(su + sd + 1) * std::sqrt(3.0 * (sld + 1)) * wigner6j(1, 2, 1, su, sd, sld);
-          std::vector<std::pair<double, Blk>> parts{{fD, need(D.blk(n, su, i, n, sld, ild))}};
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.assign(1, {fD, need(D.blk(n, su, i, n, sld, ild))});
           if (sld == su) parts.push_back({std::sqrt(0.5), need(C.blk(n, su, i, n, sld, ild))});
           const Blk M = tb.combine(parts, dlu, dld);
           tb.contract(ob, 1.0, need(T.blk(n, su, i, n, su, i)), true, M, false,
@@ -763,7 +770,8 @@ struct Emit {
           const int dlu = dim(index - 1, n - 1, slu, ilu), dld = dim(index - 1, n - 1, sd, id);
           if (dlu <= 0 || dld <= 0) continue;
           const double fD = ph(slu + sd) * std::sqrt(3.0 * (su + 1)) * wigner6j(1, 2, 1, sd, su, slu);
-          std::vector<std::pair<double, Blk>> parts{{fD, need(D.blk(n - 1, slu, ilu, n - 1, sd, id))}};
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.assign(1, {fD, need(D.blk(n - 1, slu, ilu, n - 1, sd, id))});
           if (slu == sd)
             parts.push_back({ph(sd + 1 - su) * std::sqrt(0.5 * (su + 1.0) / (sd + 1.0)),
                              need(C.blk(n - 1, slu, ilu, n - 1, sd, id))});
@@ -777,7 +785,8 @@ struct Emit {
           const int dru = dim(index + 1, n + 1, sru, iru), drd = dim(index + 1, n + 1, sd, id);
           if (dru <= 0 || drd <= 0) continue;
           const double fD = ph(su + sru + 3) * std::sqrt(3.0 / (sd + 1.0)) * (sru + 1) * wigner6j(1, 1, 2, sru, sd, su);
-          std::vector<std::pair<double, Blk>> parts{{fD, need(D.blk(n + 1, sru, iru, n + 1, sd, id))}};
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.assign(1, {fD, need(D.blk(n + 1, sru, iru, n + 1, sd, id))});
           if (sru == sd) parts.push_back({std::sqrt(0.5), need(C.blk(n + 1, sru, iru, n + 1, sd, id))});
           const Blk M = tb.combine(parts, dru, drd);
           tb.contract(ob, 1.0, need(T.blk(n, su, i, n + 1, sru, iru)), false, M, false,
@@ -789,7 +798,8 @@ struct Emit {
           if (dru <= 0 || drd <= 0) continue;
           const double fD = podd(srd + 1) * std::sqrt(3.0 * (srd + 1.0) * (su + 1.0) / (sd + 1.0)) *
                             wigner6j(1, 1, 2, su, srd, sd);
-          std::vector<std::pair<double, Blk>> parts{{fD, need(D.blk(n + 2, su, i, n + 2, srd, ird))}};
+          thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+          parts.assign(1, {fD, need(D.blk(n + 2, su, i, n + 2, srd, ird))});
           if (srd == su)
             parts.push_back({ph(su + 1 - sd) * std::sqrt(0.5 * (su + 1.0) / (sd + 1.0)),
                              need(C.blk(n + 2, su, i, n + 2, srd, ird))});
@@ -867,7 +877,8 @@ struct Emit {
             M = Qb;
           } else {
             factor = ph(s + 1 - sd2) * std::sqrt((sd2 + 1.0) / (s + 1.0));
-            std::vector<std::pair<double, Blk>> parts{{1.0, Qb}};
+            thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+            parts.assign(1, {1.0, Qb});
             for (int loca = 0; loca < index - 1; loca++)
               if (bk.gIrrep(index - 1) == bk.gIrrep(loca))
                 parts.push_back({V(loca, index - 1, index - 1, index - 1),
@@ -896,7 +907,8 @@ struct Emit {
             M = Qb;
           } else {
             factor = ph(s + 1 - su2) * std::sqrt((su2 + 1.0) / (s + 1.0));
-            std::vector<std::pair<double, Blk>> parts{{1.0, Qb}};
+            thread_local std::vector<std::pair<double, Blk>> parts;  // reused: no allocation per block
+            parts.assign(1, {1.0, Qb});
             for (int loca = index + 1; loca < L; loca++)
               if (bk.gIrrep(index) == bk.gIrrep(loca))
                 parts.push_back({V(index, index, index, loca), need(Lprev(loca).blk(nu, su2, iu, nd, sd2, idn))});

@@ -44,13 +44,32 @@ int64_t term_flops(const Term& t, int m, int n) {
   return int64_t(m) * n;
 }
 
-size_t TaskBuilder::BatchKeyHash::operator()(const BatchKey& k) const {
-  uint64_t h = static_cast<uint64_t>(k.group);
-  h = mix(h, k.b);
-  h = mix(h, (uint64_t(uint32_t(k.flags)) << 32) | uint32_t(k.k1));
-  h = mix(h, (uint64_t(uint32_t(k.k2)) << 32) | uint32_t(k.lda));
-  h = mix(h, (uint64_t(uint32_t(k.ldc)) << 32) | (uint32_t(k.aslot) << 16) | uint32_t(k.cslot & 0xffff));
-  return static_cast<size_t>(h);
+void TaskBuilder::OpenTerms::insert(uint64_t h, int32_t term) {
+  if ((n_ + 1) * 2 > stamps_.size()) {
+    // grow, keeping the current entries (in probe order, so equal hashes keep their order)
+    std::vector<uint32_t> os;
+    std::vector<uint64_t> oh;
+    std::vector<int32_t> ot;
+    os.swap(stamps_);
+    oh.swap(hashes_);
+    ot.swap(terms_);
+    const size_t cap = std::max<size_t>(64, os.size() * 2);
+    stamps_.assign(cap, 0u);
+    hashes_.assign(cap, 0);
+    terms_.assign(cap, -1);
+    mask_ = cap - 1;
+    const uint32_t cur = stamp_;
+    stamp_ = 1;
+    n_ = 0;
+    for (size_t i = 0; i < os.size(); i++)
+      if (os[i] == cur) insert(oh[i], ot[i]);
+  }
+  size_t i = h & mask_;
+  while (stamps_[i] == stamp_) i = (i + 1) & mask_;
+  stamps_[i] = stamp_;
+  hashes_[i] = h;
+  terms_[i] = term;
+  n_++;
 }
 
 TaskBuilder::TaskBuilder(bool track_operands) : track_operands_(track_operands) {
@@ -61,17 +80,15 @@ TaskBuilder::TaskBuilder(bool track_operands) : track_operands_(track_operands) 
 void TaskBuilder::note_operand(const Blk& b) {
   if (!track_operands_ || !b.valid || ref_slot(b.ref) < kSlotMpsBase) return;
   const int64_t n = int64_t(b.rows) * b.cols;
-  int64_t& cur = operands_[b.ref];
-  if (n > cur) cur = n;
+  if (b.ref == last_operand_ && n <= last_operand_n_) return;
+  operands_.note(b.ref, n);
+  last_operand_ = b.ref;
+  last_operand_n_ = n;
 }
 
-int64_t TaskBuilder::operand_bytes() const {
-  int64_t s = 0;
-  for (const auto& kv : operands_) s += kv.second;
-  return 8 * s;
-}
+int64_t TaskBuilder::operand_bytes() const { return 8 * operands_.total(); }
 
-int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
+int TaskBuilder::group_for(StageBuf& sb, const Blk& out) {
   if (&sb == last_sb_ && out.ref == last_out_) return last_group_;
   const int found = sb.group_of.find(out.ref);
   if (found >= 0) {
@@ -82,6 +99,7 @@ int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
     last_group_ = found;
     return found;
   }
+  const bool accumulate = (&sb != &combo_) && written_.find(out.ref) >= 0;
   Group g{};
   g.out = out.ref;
   g.m = out.rows;
@@ -90,7 +108,6 @@ int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
   g.flags = accumulate ? kAccumulate : 0;
   g.work = 0;
   sb.groups.push_back(g);
-  sb.terms.emplace_back();
   const int id = static_cast<int>(sb.groups.size()) - 1;
   sb.group_of.insert(out.ref, id);
   last_sb_ = &sb;
@@ -100,8 +117,8 @@ int TaskBuilder::group_for(StageBuf& sb, const Blk& out, bool accumulate) {
 }
 
 void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha, const Blk& A, bool ta,
-                      const Blk& B, bool tb, const Blk& C, bool tc, bool accumulate) {
-  const int g = group_for(sb, out, accumulate);
+                      const Blk& B, bool tb, const Blk& C, bool tc) {
+  const int g = group_for(sb, out);
   Term t{};
   t.a = A.valid ? A.ref : 0;
   t.b = B.ref;
@@ -118,32 +135,40 @@ void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha
   t.list = -1;
   t.count = 1;
   t.item0 = 0;
-  auto& gt = sb.terms[g];
   Group& G = sb.groups[g];
+  const int32_t idx = static_cast<int32_t>(sb.terms.size());
   if (batchable) {
     // The compilers emit all contractions of one output block consecutively, so only the
-    // current group's terms are kept open for batching: the map stays small.
+    // current group's terms are kept open for batching: the table stays small.
     if (g != open_group_ || &sb != open_sb_) {
       open_.clear();
       open_group_ = g;
       open_sb_ = &sb;
     }
-    const BatchKey key{g, t.b, t.flags, t.k1, t.k2, t.lda, t.ldc, A.valid ? ref_slot(A.ref) : -1,
-                       C.valid ? ref_slot(C.ref) : -1};
-    auto it = open_.find(key);
-    if (it != open_.end()) {
-      PendingTerm& pt = gt[it->second];
+    const int aslot = A.valid ? ref_slot(A.ref) : -1, cslot = C.valid ? ref_slot(C.ref) : -1;
+    uint64_t h = mix(t.b, (uint64_t(uint32_t(t.flags)) << 32) | uint32_t(t.k1));
+    h = mix(h, (uint64_t(uint32_t(t.k2)) << 32) | uint32_t(t.lda));
+    h = mix(h, (uint64_t(uint32_t(t.ldc)) << 32) | (uint32_t(aslot & 0xffff) << 16) | uint32_t(cslot & 0xffff));
+    const int32_t hit = open_.find(h, [&](int32_t k) {
+      const Term& o = sb.terms[k];
+      return o.b == t.b && o.flags == t.flags && o.k1 == t.k1 && o.k2 == t.k2 && o.lda == t.lda && o.ldc == t.ldc &&
+             ((o.flags & kHasA) ? ref_slot(o.a) : -1) == aslot && ((o.flags & kHasC) ? ref_slot(o.c) : -1) == cslot;
+    });
+    if (hit >= 0) {
+      const Term& o = sb.terms[hit];
       BatchEntry e;
-      e.da = A.valid ? static_cast<int64_t>(A.ref - pt.t.a) : 0;
-      e.dc = C.valid ? static_cast<int64_t>(C.ref - pt.t.c) : 0;
-      e.ratio = alpha / pt.t.alpha;
-      pt.entries.push_back(e);
-      G.work += term_flops(pt.t, G.m, G.n);
+      e.da = A.valid ? static_cast<int64_t>(A.ref - o.a) : 0;
+      e.dc = C.valid ? static_cast<int64_t>(C.ref - o.c) : 0;
+      e.ratio = alpha / o.alpha;
+      sb.extra.push_back(e);
+      sb.extra_term.push_back(hit);
+      G.work += term_flops(o, G.m, G.n);
       return;
     }
-    open_.emplace(key, static_cast<int>(gt.size()));
+    open_.insert(h, idx);
   }
-  gt.push_back(PendingTerm{t, {}});
+  sb.terms.push_back(t);
+  sb.term_group.push_back(g);
   G.work += term_flops(t, G.m, G.n);
 }
 
@@ -181,7 +206,7 @@ Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int r
   combo_size_ = align4(combo_size_ + int64_t(rows) * cols);
   for (size_t i = 0; i < parts.size(); i++) {
     const bool t = transposed ? (*transposed)[i] : false;
-    add(combo_, false, out, parts[i].first, Blk(), false, parts[i].second, t, Blk(), false, false);
+    add(combo_, false, out, parts[i].first, Blk(), false, parts[i].second, t, Blk(), false);
   }
   combo_index_.insert(h, static_cast<int32_t>(combo_entries_.size()));
   combo_entries_.push_back(ComboEntry{static_cast<int64_t>(combo_words_.size()), static_cast<int32_t>(key.size()), out});
@@ -191,7 +216,7 @@ Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int r
 
 void TaskBuilder::declare_output(const Blk& out) {
   if (!out.valid || out.rows == 0 || out.cols == 0) return;
-  group_for(stages_.back(), out, written_.count(out.ref) > 0);
+  group_for(stages_.back(), out);
 }
 
 void TaskBuilder::contract(const Blk& out, double alpha, const Blk& A, bool ta, const Blk& B, bool tb, const Blk& C,
@@ -218,18 +243,18 @@ void TaskBuilder::contract(const Blk& out, double alpha, const Blk& A, bool ta, 
   note_operand(B);
   note_operand(C);
   n_contract_++;
-  const bool acc = written_.count(out.ref) > 0;
   StageBuf& st = stages_.back();
   // Zero-sized or zero-weight contractions add nothing; the output still exists.
   if (alpha == 0.0 || m == 0 || n == 0 || sb.r == 0 || sb.c == 0) {
-    if (m > 0 && n > 0) group_for(st, out, acc);
+    if (m > 0 && n > 0) group_for(st, out);
     return;
   }
-  add(st, true, out, alpha, A, ta, B, tb, C, tc, acc);
+  add(st, true, out, alpha, A, ta, B, tb, C, tc);
 }
 
 void TaskBuilder::next_stage(const std::string& name) {
-  for (auto& g : stages_.back().groups) written_[g.out] = true;
+  for (auto& g : stages_.back().groups)
+    if (written_.find(g.out) < 0) written_.insert(g.out, 1);
   open_.clear();
   last_sb_ = nullptr;
   open_sb_ = nullptr;
@@ -243,27 +268,49 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
   Stage st;
   st.name = name;
   st.groups = sb.groups;
-  for (size_t g = 0; g < sb.groups.size(); g++) {
+  const size_t ng = sb.groups.size(), nt = sb.terms.size(), ne = sb.extra.size();
+  // terms by group, entries by term, both in emission order (counting sorts)
+  std::vector<int32_t> gstart(ng + 1, 0), order(nt);
+  for (size_t k = 0; k < nt; k++) gstart[sb.term_group[k] + 1]++;
+  for (size_t g = 0; g < ng; g++) gstart[g + 1] += gstart[g];
+  {
+    std::vector<int32_t> fill(gstart.begin(), gstart.end() - 1);
+    for (size_t k = 0; k < nt; k++) order[fill[sb.term_group[k]]++] = static_cast<int32_t>(k);
+  }
+  std::vector<int32_t> estart(nt + 1, 0);
+  std::vector<BatchEntry> ebuf(ne);
+  for (size_t q = 0; q < ne; q++) estart[sb.extra_term[q] + 1]++;
+  for (size_t k = 0; k < nt; k++) estart[k + 1] += estart[k];
+  {
+    std::vector<int32_t> fill(estart.begin(), estart.end() - 1);
+    for (size_t q = 0; q < ne; q++) ebuf[fill[sb.extra_term[q]]++] = sb.extra[q];
+  }
+  std::vector<BatchEntry>().swap(sb.extra);
+  std::vector<int32_t>().swap(sb.extra_term);
+  st.terms.reserve(nt);
+  for (size_t g = 0; g < ng; g++) {
     Group& G = st.groups[g];
     G.t0 = static_cast<int32_t>(st.terms.size());
     int32_t items = 0;
-    for (PendingTerm& pt : sb.terms[g]) {
-      Term t = pt.t;
+    for (int32_t j = gstart[g]; j < gstart[g + 1]; j++) {
+      const int32_t k = order[j];
+      Term t = sb.terms[k];
       t.item0 = items;
       if ((t.flags & kHasA) && (t.flags & kHasC)) {
         const int64_t ab = int64_t(G.m) * t.k1 * t.k2 + int64_t(G.m) * t.k2 * G.n;
         const int64_t bc = int64_t(t.k1) * t.k2 * G.n + int64_t(G.m) * t.k1 * G.n;
         if (ab < bc) t.flags |= kLeftFirst;
       }
-      if (!pt.entries.empty()) {
-        // the list is entry 0 (the term itself) followed by pt.entries
+      const size_t n = static_cast<size_t>(estart[k + 1] - estart[k]);
+      if (n > 0) {
+        // the list is entry 0 (the term itself) followed by the term's further entries
+        const BatchEntry* pe = ebuf.data() + estart[k];
         const BatchEntry first{0, 0, 1.0};
-        const size_t n = pt.entries.size();
         uint64_t h = mix(0x13198a2e03707344ull, n);
-        for (const BatchEntry& e : pt.entries) {
+        for (size_t q = 0; q < n; q++) {
           uint64_t r;
-          std::memcpy(&r, &e.ratio, sizeof(r));
-          h = mix(mix(mix(h, static_cast<uint64_t>(e.da)), static_cast<uint64_t>(e.dc)), r);
+          std::memcpy(&r, &pe[q].ratio, sizeof(r));
+          h = mix(mix(mix(h, static_cast<uint64_t>(pe[q].da)), static_cast<uint64_t>(pe[q].dc)), r);
         }
         int32_t found = -1;
         lists.visit(h, [&](int32_t off) {
@@ -271,15 +318,15 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
           const BatchEntry* l = table.data() + off;
           bool same = l[0].da == 0 && l[0].dc == 0 && l[0].ratio == 1.0;
           for (size_t q = 0; same && q < n; q++)
-            same = l[q + 1].da == pt.entries[q].da && l[q + 1].dc == pt.entries[q].dc &&
-                   std::memcmp(&l[q + 1].ratio, &pt.entries[q].ratio, sizeof(double)) == 0;
+            same = l[q + 1].da == pe[q].da && l[q + 1].dc == pe[q].dc &&
+                   std::memcmp(&l[q + 1].ratio, &pe[q].ratio, sizeof(double)) == 0;
           if (same) found = off;
           return same;
         });
         if (found < 0) {
           found = static_cast<int32_t>(table.size());
           table.push_back(first);
-          table.insert(table.end(), pt.entries.begin(), pt.entries.end());
+          table.insert(table.end(), pe, pe + n);
           lists.insert(h, found);
         }
         t.list = found;
@@ -291,8 +338,9 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
       st.terms.push_back(t);
     }
     G.t1 = static_cast<int32_t>(st.terms.size());
-    std::vector<PendingTerm>().swap(sb.terms[g]);
   }
+  std::vector<Term>().swap(sb.terms);
+  std::vector<int32_t>().swap(sb.term_group);
   return st;
 }
 

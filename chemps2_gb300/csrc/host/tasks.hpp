@@ -199,6 +199,62 @@ class FlatIndex {
   }
 };
 
+// Open-addressing table from block references (never 0: slot 0 is never tracked) to the
+// largest element count seen for each: the operand footprint of a program.
+class RefSizes {
+ public:
+  void note(Ref r, int64_t n) {
+    if ((size_ + 1) * 2 > keys_.size()) grow();
+    for (size_t i = slot(r);; i = (i + 1) & mask_) {
+      if (keys_[i] == r) {
+        if (n > vals_[i]) vals_[i] = n;
+        return;
+      }
+      if (keys_[i] == 0) {
+        keys_[i] = r;
+        vals_[i] = n;
+        size_++;
+        return;
+      }
+    }
+  }
+  template <class F>
+  void for_each(F&& f) const {
+    for (size_t i = 0; i < keys_.size(); i++)
+      if (keys_[i] != 0) f(keys_[i], vals_[i]);
+  }
+  int64_t total() const {
+    int64_t s = 0;
+    for_each([&](Ref, int64_t v) { s += v; });
+    return s;
+  }
+  size_t size() const { return size_; }
+
+ private:
+  std::vector<Ref> keys_;
+  std::vector<int64_t> vals_;
+  size_t mask_ = 0, size_ = 0;
+  size_t slot(Ref k) const {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    return static_cast<size_t>(k) & mask_;
+  }
+  void grow() {
+    std::vector<Ref> ok;
+    std::vector<int64_t> ov;
+    ok.swap(keys_);
+    ov.swap(vals_);
+    const size_t cap = std::max<size_t>(1024, ok.size() * 2);
+    keys_.assign(cap, 0);
+    vals_.assign(cap, 0);
+    mask_ = cap - 1;
+    size_ = 0;
+    for (size_t i = 0; i < ok.size(); i++)
+      if (ok[i] != 0) note(ok[i], ov[i]);
+  }
+};
+
 // Records contractions and lowers them into a Program.
 class TaskBuilder {
  public:
@@ -238,30 +294,47 @@ class TaskBuilder {
   // Bytes of the distinct MPS / operator blocks the recorded contractions read (each
   // block counted once, FP64), the operand traffic of one execution of the program.
   int64_t operand_bytes() const;
-  const std::unordered_map<Ref, int64_t>& operands() const { return operands_; }
+  const RefSizes& operands() const { return operands_; }
 
  private:
-  struct PendingTerm {
-    Term t;
-    std::vector<BatchEntry> entries;  // beyond entry 0
-  };
+  // Terms and batch entries of a stage in emission order (flat arrays: no allocation
+  // per term); lowering orders them by group, and entries by term, with counting sorts.
   struct StageBuf {
     std::vector<Group> groups;
-    std::vector<std::vector<PendingTerm>> terms;  // per group
+    std::vector<Term> terms;
+    std::vector<int32_t> term_group;
+    std::vector<BatchEntry> extra;      // batch entries beyond entry 0
+    std::vector<int32_t> extra_term;    // the term of each
     FlatIndex group_of;  // output reference -> group
     std::string name;
   };
-  struct BatchKey {
-    int group;
-    Ref b;
-    int32_t flags, k1, k2, lda, ldc, aslot, cslot;
-    bool operator==(const BatchKey& o) const {
-      return group == o.group && b == o.b && flags == o.flags && k1 == o.k1 && k2 == o.k2 && lda == o.lda &&
-             ldc == o.ldc && aslot == o.aslot && cslot == o.cslot;
+  // Terms of the open group that later contractions may join, by hash of the batching
+  // key (B, shapes, leading dimensions, flags, operand slots); cleared in O(1) by stamps.
+  class OpenTerms {
+   public:
+    template <class Eq>
+    int32_t find(uint64_t h, Eq&& eq) const {
+      if (stamps_.empty()) return -1;
+      for (size_t i = h & mask_;; i = (i + 1) & mask_) {
+        if (stamps_[i] != stamp_) return -1;
+        if (hashes_[i] == h && eq(terms_[i])) return terms_[i];
+      }
     }
-  };
-  struct BatchKeyHash {
-    size_t operator()(const BatchKey& k) const;
+    void insert(uint64_t h, int32_t term);
+    void clear() {
+      n_ = 0;
+      if (++stamp_ == 0) {
+        std::fill(stamps_.begin(), stamps_.end(), 0u);
+        stamp_ = 1;
+      }
+    }
+
+   private:
+    std::vector<uint32_t> stamps_;
+    std::vector<uint64_t> hashes_;
+    std::vector<int32_t> terms_;
+    uint32_t stamp_ = 1;
+    size_t mask_ = 0, n_ = 0;
   };
 
   StageBuf combo_;
@@ -278,9 +351,11 @@ class TaskBuilder {
   std::vector<uint64_t> combo_words_;
   std::vector<uint64_t> key_scratch_;
   std::vector<StageBuf> stages_;
-  std::unordered_map<BatchKey, int, BatchKeyHash> open_;  // term index within its group
-  std::unordered_map<Ref, bool> written_;                  // outputs written by closed stages
-  std::unordered_map<Ref, int64_t> operands_;              // footprint of MPS / operator operands
+  OpenTerms open_;                                         // open terms of the open group
+  FlatIndex written_;                                      // outputs written by closed stages
+  RefSizes operands_;                                      // footprint of MPS / operator operands
+  Ref last_operand_ = 0;                                   // the last noted block (repeats are common)
+  int64_t last_operand_n_ = 0;
   int64_t n_contract_ = 0;
   bool track_operands_ = false;
   const StageBuf* open_sb_ = nullptr;  // the group whose terms are open for batching
@@ -290,9 +365,11 @@ class TaskBuilder {
   int last_group_ = -1;
 
   void note_operand(const Blk& b);
-  int group_for(StageBuf& sb, const Blk& out, bool accumulate);
+  // The group of `out` in sb, created on first use: it accumulates onto what earlier
+  // stages wrote (never in the combination stage).
+  int group_for(StageBuf& sb, const Blk& out);
   void add(StageBuf& sb, bool batchable, const Blk& out, double alpha, const Blk& A, bool ta, const Blk& B, bool tb,
-           const Blk& C, bool tc, bool accumulate);
+           const Blk& C, bool tc);
   // lists: batch lists already in `table`, by hash of their entries
   static Stage lower(StageBuf& sb, const std::string& name, std::vector<BatchEntry>& table,
                      FlatIndex& lists);

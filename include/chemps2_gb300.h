@@ -181,10 +181,12 @@ int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double*
  * problems run at once on host threads sharing the current device (workers <= 1: one after
  * another). Every problem is attempted; per-problem outputs (any may be NULL): energies
  * (Solve()), matvecs (Heff applications), seconds (wall clock of construction and Solve),
- * statuses (C2G_OK or the error code of that problem). Returns C2G_OK when all were
- * solved, else the first failed problem's code (c2g_last_error names it). */
+ * statuses (C2G_OK or the error code of that problem), stats (n x C2G_NUM_STATS, the
+ * layout of c2g_dmrg_stats). Returns C2G_OK when all were solved, else the first failed
+ * problem's code (c2g_last_error names it). */
 int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* schemes, const unsigned int* seeds,
-                    int workers, double* energies, long long* matvecs, double* seconds, int* statuses);
+                    int workers, double* energies, long long* matvecs, double* seconds, int* statuses,
+                    double* stats);
 /* The first n draws of the private random generator a batch member seeded with `seed`
  * uses (equal to srand(seed); rand() of the GNU C library). No GPU needed. */
 int c2g_host_rand_sample(unsigned int seed, int n, int* out);

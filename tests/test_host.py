@@ -271,10 +271,10 @@ def test_private_random_stream_equals_srand_rand():
 def test_batch_argument_errors_are_status_codes():
     lib = c2g.load()
     with pytest.raises(c2g.Chemps2Error):
-        c2g._check(lib.c2g_batch_solve(-1, None, None, None, 1, None, None, None, None))
+        c2g._check(lib.c2g_batch_solve(-1, None, None, None, 1, None, None, None, None, None))
     with pytest.raises(c2g.Chemps2Error):
-        c2g._check(lib.c2g_batch_solve(2, None, None, None, 1, None, None, None, None))
-    assert lib.c2g_batch_solve(0, None, None, None, 4, None, None, None, None) == 0
+        c2g._check(lib.c2g_batch_solve(2, None, None, None, 1, None, None, None, None, None))
+    assert lib.c2g_batch_solve(0, None, None, None, 4, None, None, None, None, None) == 0
     with pytest.raises(ValueError):
         c2g.solve_batch([], [None], [])
 
