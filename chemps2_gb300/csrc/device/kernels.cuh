@@ -38,6 +38,52 @@ struct SlotPtrs {
   const float* x32;
   const float* combo32;
   const float* ones32;
+  // intermediate products of the two-pass large-group path (slot kSlotInter), written in
+  // the precision of the run
+  double* inter;
+  float* inter32;
+};
+
+// ---- Two-pass path of large groups (big output blocks with heavy items).
+// A one-pass tile kernel recomputes an item's intermediate product (B C_p, or A_p B) for
+// every output tile it feeds. Here pass 1 forms every intermediate once, as a plain tiled
+// GEMM into the program's intermediate scratch (slot kSlotInter); pass 2 sums the items'
+// products into the output tiles, out += sum_p alpha_p op(L_p) op(R_p), in the fixed item
+// order, with long item lists split over several CTAs whose partial tiles the last CTA to
+// finish adds up in split order. Tiles are 32 or 64 rows by 32 or 64 columns (chosen per
+// block to limit padding), 256 threads each holding a (tile / 16) x (tile / 16) patch.
+constexpr int kGemmThreads = 256;
+constexpr int kGemmMaxSplit = 64;
+constexpr int64_t kGemmCtaTarget = 1216;  // 152 SMs x 8 CTA-sized pieces per stage
+
+struct GemmOperand {   // element (i, k) of op(M): trans ? p[k + ld i] : p[i + ld k]
+  Ref ref;
+  int32_t ld, trans;
+};
+struct InterJob {      // S (m x n, column-major, ld m) = op(L) (m x k) op(R) (k x n)
+  GemmOperand l, r;
+  int32_t m, n, k, pad;
+  int64_t off;         // S at slot kSlotInter + off
+  int64_t pad2;
+};
+struct SumItem {       // out += alpha op(L) (m x k) op(R) (k x n); k == 0: out += alpha op(R)
+  GemmOperand l, r;
+  double alpha;
+  int32_t k, pad;
+};
+struct SumGroup {      // an output block of the path: items [i0, i1)
+  Ref out;
+  int32_t m, n, ldo, flags;
+  int32_t i0, i1;
+};
+struct GemmTile {      // a CTA's work unit of either pass
+  int32_t idx;         // job (pass 1) or sum group (pass 2)
+  int32_t pos;         // tile row << 16 | tile column, in units of the tile shape
+  int32_t shape;       // bit 0: 64 rows (else 32); bit 1: 64 columns (else 32)
+  int32_t nsplit, split;
+  int32_t item0, item1;  // pass 2: this split's items (absolute indices)
+  int32_t counter;       // pass 2 with nsplit > 1: arrival counter
+  int64_t part;          // and its partial tiles (nsplit x 64 x 64 doubles)
 };
 
 // dst[i] = (float)src[i]
@@ -62,6 +108,13 @@ inline int sandwich_grid(int m, int n) {
 // SlotPtrs), products and per-lane sums, with the lane reduction and the FP64 output
 // update in FP64. The FP32 variant issues no FP64 instruction in its item loop.
 enum class Precision : int { kFP64 = 0, kFP32 = 1 };
+
+cudaError_t launch_inter_gemm(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp,
+                              cudaStream_t stream, Precision prec);
+cudaError_t launch_sum_gemm(const SumGroup* groups, const SumItem* items, const GemmTile* tiles, int ntiles,
+                            double* partials, unsigned int* counters, const SlotPtrs& sp, cudaStream_t stream,
+                            Precision prec);
+
 
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
                             int ntiles, const SlotPtrs& sp, cudaStream_t stream, Precision prec = Precision::kFP64);

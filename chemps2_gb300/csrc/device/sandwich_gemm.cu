@@ -1,0 +1,244 @@
+// Two-pass path of large groups (declarations and the scheme in kernels.cuh).
+//
+// Both passes run the same CTA-level GEMM: 256 threads in a 16 x 16 layout, each holding
+// a PM x PN register patch of a (16 PM) x (16 PN) output tile (PM, PN in {2, 4}); the
+// operands are staged through shared memory in chunks of 16 along the inner dimension,
+// loaded with the unit-stride index fastest for either storage order of each operand.
+// In FP64 the GEMM is bound by the FP64 pipe (two FMAs per SM and clock on this GPU),
+// so the kernel's job is to issue no FMA twice: every intermediate is formed once in
+// pass 1 and the tile shapes keep the padding small.
+#include "kernels.cuh"
+#include "slots.cuh"
+
+namespace c2g {
+
+namespace {
+
+constexpr int kKC = 16;
+
+template <typename Real>
+struct Opnd {
+  const Real* p;
+  int64_t ld;
+  bool t;
+  __device__ __forceinline__ Real at(int i, int k) const { return t ? p[k + ld * i] : p[i + ld * k]; }
+  __device__ __forceinline__ Opnd shift(int di, int dk) const {
+    Opnd o = *this;
+    o.p = t ? p + dk + ld * di : p + di + ld * dk;
+    return o;
+  }
+};
+
+template <typename Real>
+__device__ __forceinline__ Opnd<Real> opnd(const SlotPtrs& sp, const GemmOperand& g) {
+  return Opnd<Real>{resolve<Real>(sp, g.ref), g.ld, g.trans != 0};
+}
+
+template <typename Real>
+struct GSmem {
+  Real L[kKC][64 + 1];
+  Real R[kKC][64 + 1];
+};
+
+// part (rows ty + 16 ii, columns tx + 16 jj) = sum_{k < K} L(i, k) R(k, j) over i < M,
+// j < N (zero elsewhere)
+template <typename Real, int PM, int PN>
+__device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>& L, int M, const Opnd<Real>& R,
+                                          int N, int K, GSmem<Real>& sm) {
+  constexpr int TM = 16 * PM, TN = 16 * PN;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+  for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+    for (int jj = 0; jj < PN; jj++) part[ii][jj] = Real(0);
+  for (int k0 = 0; k0 < K; k0 += kKC) {
+#pragma unroll
+    for (int s = 0; s < PM; s++) {
+      const int e = tid + kGemmThreads * s;  // TM x kKC elements
+      int i, kk;
+      if (!L.t) {
+        i = e % TM;
+        kk = e / TM;
+      } else {
+        kk = e % kKC;
+        i = e / kKC;
+      }
+      sm.L[kk][i] = (i < M && k0 + kk < K) ? L.at(i, k0 + kk) : Real(0);
+    }
+#pragma unroll
+    for (int s = 0; s < PN; s++) {
+      const int e = tid + kGemmThreads * s;  // kKC x TN elements
+      int j, kk;
+      if (!R.t) {
+        kk = e % kKC;
+        j = e / kKC;
+      } else {
+        j = e % TN;
+        kk = e / TN;
+      }
+      sm.R[kk][j] = (j < N && k0 + kk < K) ? R.at(k0 + kk, j) : Real(0);
+    }
+    __syncthreads();
+    const int kn = min(kKC, K - k0);
+    for (int kk = 0; kk < kn; kk++) {
+      Real a[PM], b[PN];
+#pragma unroll
+      for (int ii = 0; ii < PM; ii++) a[ii] = sm.L[kk][ty + 16 * ii];
+#pragma unroll
+      for (int jj = 0; jj < PN; jj++) b[jj] = sm.R[kk][tx + 16 * jj];
+#pragma unroll
+      for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+        for (int jj = 0; jj < PN; jj++) part[ii][jj] = fmaR(a[ii], b[jj], part[ii][jj]);
+    }
+    __syncthreads();
+  }
+}
+
+template <typename Real, int PM, int PN>
+__device__ __forceinline__ void inter_tile(const InterJob& J, int pos, const SlotPtrs& sp, GSmem<Real>& sm) {
+  constexpr int TM = 16 * PM, TN = 16 * PN;
+  const int row0 = (pos >> 16) * TM, col0 = (pos & 0xffff) * TN;
+  const int tm = min(TM, J.m - row0), tn = min(TN, J.n - col0);
+  Real part[PM][PN];
+  tile_gemm<Real, PM, PN>(part, opnd<Real>(sp, J.l).shift(row0, 0), tm, opnd<Real>(sp, J.r).shift(0, col0), tn, J.k,
+                          sm);
+  Real* S = const_cast<Real*>(Tables<Real>::get(sp, kSlotInter)) + J.off;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+  for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+    for (int jj = 0; jj < PN; jj++) {
+      const int r = ty + 16 * ii, c = tx + 16 * jj;
+      if (r < tm && c < tn) S[(row0 + r) + static_cast<int64_t>(J.m) * (col0 + c)] = part[ii][jj];
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kGemmThreads, 2)
+    inter_gemm_kernel(const InterJob* __restrict__ jobs, const GemmTile* __restrict__ tiles, SlotPtrs sp) {
+  __shared__ GSmem<Real> sm;
+  const GemmTile T = tiles[blockIdx.x];
+  const InterJob J = jobs[T.idx];
+  switch (T.shape) {
+    case 0: inter_tile<Real, 2, 2>(J, T.pos, sp, sm); break;
+    case 1: inter_tile<Real, 4, 2>(J, T.pos, sp, sm); break;
+    case 2: inter_tile<Real, 2, 4>(J, T.pos, sp, sm); break;
+    default: inter_tile<Real, 4, 4>(J, T.pos, sp, sm); break;
+  }
+}
+
+template <typename Real, int PM, int PN>
+__device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, const SumItem* __restrict__ items,
+                                         double* partials, unsigned int* counters, const SlotPtrs& sp,
+                                         GSmem<Real>& sm) {
+  constexpr int TM = 16 * PM, TN = 16 * PN;
+  const int row0 = (T.pos >> 16) * TM, col0 = (T.pos & 0xffff) * TN;
+  const int tm = min(TM, G.m - row0), tn = min(TN, G.n - col0);
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  double acc[PM][PN];
+#pragma unroll
+  for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+    for (int jj = 0; jj < PN; jj++) acc[ii][jj] = 0.0;
+  for (int it = T.item0; it < T.item1; it++) {
+    const SumItem I = items[it];
+    const Opnd<Real> R = opnd<Real>(sp, I.r);
+    Real part[PM][PN];
+    if (I.k > 0) {
+      tile_gemm<Real, PM, PN>(part, opnd<Real>(sp, I.l).shift(row0, 0), tm, R.shift(0, col0), tn, I.k, sm);
+    } else {
+#pragma unroll
+      for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+        for (int jj = 0; jj < PN; jj++) {
+          const int r = ty + 16 * ii, c = tx + 16 * jj;
+          part[ii][jj] = (r < tm && c < tn) ? R.at(row0 + r, col0 + c) : Real(0);
+        }
+    }
+#pragma unroll
+    for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+      for (int jj = 0; jj < PN; jj++) acc[ii][jj] = fma(I.alpha, static_cast<double>(part[ii][jj]), acc[ii][jj]);
+  }
+  if (T.nsplit > 1) {
+    // store this split's partial tile; the last split to arrive adds them up in split order
+    double* part = partials + T.part;
+    constexpr int te = TM * TN;
+#pragma unroll
+    for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+      for (int jj = 0; jj < PN; jj++)
+        __stcg(part + static_cast<int64_t>(T.split) * te + (ty + 16 * ii) + TM * (tx + 16 * jj), acc[ii][jj]);
+    __threadfence();
+    __shared__ int is_last;
+    __syncthreads();
+    if (tid == 0) is_last = atomicAdd(counters + T.counter, 1u) == static_cast<unsigned>(T.nsplit - 1);
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+#pragma unroll
+    for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+      for (int jj = 0; jj < PN; jj++) {
+        double v = 0.0;
+        for (int s = 0; s < T.nsplit; s++)
+          v += __ldcg(part + static_cast<int64_t>(s) * te + (ty + 16 * ii) + TM * (tx + 16 * jj));
+        acc[ii][jj] = v;
+      }
+    if (tid == 0) counters[T.counter] = 0u;  // ready for the next launch
+  }
+  double* O = const_cast<double*>(resolve<double>(sp, G.out));
+  const int64_t ldo = G.ldo;
+  const bool accum = (G.flags & kAccumulate) != 0;
+#pragma unroll
+  for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+    for (int jj = 0; jj < PN; jj++) {
+      const int r = ty + 16 * ii, c = tx + 16 * jj;
+      if (r < tm && c < tn) {
+        const int64_t idx = (row0 + r) + ldo * (col0 + c);
+        O[idx] = accum ? O[idx] + acc[ii][jj] : acc[ii][jj];
+      }
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kGemmThreads, 2)
+    sum_gemm_kernel(const SumGroup* __restrict__ groups, const SumItem* __restrict__ items,
+                    const GemmTile* __restrict__ tiles, double* partials, unsigned int* counters, SlotPtrs sp) {
+  __shared__ GSmem<Real> sm;
+  const GemmTile T = tiles[blockIdx.x];
+  const SumGroup G = groups[T.idx];
+  switch (T.shape) {
+    case 0: sum_tile<Real, 2, 2>(T, G, items, partials, counters, sp, sm); break;
+    case 1: sum_tile<Real, 4, 2>(T, G, items, partials, counters, sp, sm); break;
+    case 2: sum_tile<Real, 2, 4>(T, G, items, partials, counters, sp, sm); break;
+    default: sum_tile<Real, 4, 4>(T, G, items, partials, counters, sp, sm); break;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_inter_gemm(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp,
+                              cudaStream_t stream, Precision prec) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (prec == Precision::kFP32)
+    inter_gemm_kernel<float><<<ntiles, kGemmThreads, 0, stream>>>(jobs, tiles, sp);
+  else
+    inter_gemm_kernel<double><<<ntiles, kGemmThreads, 0, stream>>>(jobs, tiles, sp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_gemm(const SumGroup* groups, const SumItem* items, const GemmTile* tiles, int ntiles,
+                            double* partials, unsigned int* counters, const SlotPtrs& sp, cudaStream_t stream,
+                            Precision prec) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (prec == Precision::kFP32)
+    sum_gemm_kernel<float><<<ntiles, kGemmThreads, 0, stream>>>(groups, items, tiles, partials, counters, sp);
+  else
+    sum_gemm_kernel<double><<<ntiles, kGemmThreads, 0, stream>>>(groups, items, tiles, partials, counters, sp);
+  return cudaGetLastError();
+}
+
+}  // namespace c2g

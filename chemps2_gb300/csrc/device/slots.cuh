@@ -16,6 +16,7 @@ struct Tables<double> {
       case kSlotY: return sp.y;
       case kSlotCombo: return sp.combo;
       case kSlotOnes: return sp.ones;
+      case kSlotInter: return sp.inter;
       default: return sp.table[s];
     }
   }
@@ -27,6 +28,7 @@ struct Tables<float> {
       case kSlotX: return sp.x32;
       case kSlotCombo: return sp.combo32;
       case kSlotOnes: return sp.ones32;
+      case kSlotInter: return sp.inter32;
       default: return sp.table32[s];
     }
   }

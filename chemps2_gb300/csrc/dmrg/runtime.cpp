@@ -55,6 +55,9 @@ DevProgram::~DevProgram() {
     if (combo32) rt->release(combo32);
     if (partials) rt->release(partials);
     if (counters) rt->release(counters);
+    if (inter) rt->release(inter);
+    if (gemm_partials) rt->release(gemm_partials);
+    if (gemm_counters) rt->release(gemm_counters);
   }
 }
 
@@ -163,6 +166,8 @@ SlotPtrs Runtime::ptrs(double* x, double* y, double* combo) {
   sp.x32 = nullptr;
   sp.combo32 = nullptr;
   sp.ones32 = nullptr;
+  sp.inter = nullptr;
+  sp.inter32 = nullptr;
   return sp;
 }
 
@@ -259,6 +264,19 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
   std::vector<std::vector<TileDesc>> tiles(ns), tiles_large(ns);
   std::vector<std::vector<WarpTile>> tiles_warp(ns);
   int64_t part_doubles = 0, ncounters = 0;
+  // Two-pass path of large groups (C2G_LARGE=tile keeps them on the one-pass cooperative
+  // kernel instead).
+  const char* lenv = std::getenv("C2G_LARGE");
+  const bool one_pass_large = lenv && std::string(lenv) == "tile";
+  struct TwoPass {
+    std::vector<InterJob> jobs;
+    std::vector<GemmTile> jtiles;
+    std::vector<SumGroup> groups;
+    std::vector<SumItem> items;
+    std::vector<GemmTile> stiles;
+  };
+  std::vector<TwoPass> twopass(ns);
+  int64_t inter_doubles = 0, gemm_part_doubles = 0, gemm_counters = 0;
   // Blob layout: the batch table, then per stage its groups and terms, then the tile lists
   // of every stage. It is assembled in the runtime's pinned staging buffer: the terms of
   // each group are copied there in shape order (flags, k1, k2), so that neighbouring items
@@ -480,6 +498,92 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     // Tile order: the groups with the most work first (binned by powers of two, in
     // program order within a bin), row-major within a group. Team-variant tiles are then
     // grouped by row class (one kernel per class), keeping that order within a class.
+    // Large groups: every (term, entry) item becomes a pass-2 product, after a pass-1
+    // intermediate when the item has both outer operands. Tile edges of 32 or 64 (the one
+    // with less padding); long item lists are split at equal shares of the work.
+    TwoPass& tp = twopass[s];
+    int64_t inter_off = 0;
+    auto pick = [](int x) { return ((x + 63) / 64) * 64 <= ((x + 31) / 32) * 32 ? 64 : 32; };
+    auto plan_large = [&](int g) {
+      const Group& G = st.groups[g];
+      const BatchEntry* ents = reinterpret_cast<const BatchEntry*>(staging_);
+      SumGroup sg{};
+      sg.out = G.out;
+      sg.m = G.m;
+      sg.n = G.n;
+      sg.ldo = G.ldo;
+      sg.flags = G.flags;
+      sg.i0 = static_cast<int32_t>(tp.items.size());
+      for (int t = G.t0; t < G.t1; t++) {
+        const Term& T = tt[t];
+        const bool ha = T.flags & kHasA, hc = T.flags & kHasC;
+        const GemmOperand B{T.b, T.ldb, (T.flags & kTransB) ? 1 : 0};
+        for (int p = 0; p < T.count; p++) {
+          double alpha = T.alpha;
+          int64_t da = 0, dc = 0;
+          if (T.list >= 0) {
+            const BatchEntry& e = ents[T.list + p];
+            alpha *= e.ratio;
+            da = e.da;
+            dc = e.dc;
+          }
+          const GemmOperand A{ha ? T.a + static_cast<uint64_t>(da) : 0, T.lda, (T.flags & kTransA) ? 1 : 0};
+          const GemmOperand C{hc ? T.c + static_cast<uint64_t>(dc) : 0, T.ldc, (T.flags & kTransC) ? 1 : 0};
+          SumItem it{};
+          it.alpha = alpha;
+          if (ha && hc) {
+            InterJob J{};
+            J.off = inter_off;
+            const Ref S = make_ref(kSlotInter, inter_off);
+            if (T.flags & kLeftFirst) {  // S = op(A_p) op(B), m x k2; out += alpha S op(C_p)
+              J.l = A;
+              J.r = B;
+              J.m = G.m;
+              J.n = T.k2;
+              J.k = T.k1;
+              it.l = GemmOperand{S, G.m, 0};
+              it.r = C;
+              it.k = T.k2;
+            } else {  // S = op(B) op(C_p), k1 x n; out += alpha op(A_p) S
+              J.l = B;
+              J.r = C;
+              J.m = T.k1;
+              J.n = G.n;
+              J.k = T.k2;
+              it.l = A;
+              it.r = GemmOperand{S, T.k1, 0};
+              it.k = T.k1;
+            }
+            inter_off += (static_cast<int64_t>(J.m) * J.n + 3) & ~int64_t(3);
+            const int jm = pick(J.m), jn = pick(J.n);
+            const int shape = (jm == 64 ? 1 : 0) | (jn == 64 ? 2 : 0);
+            for (int i = 0; i < (J.m + jm - 1) / jm; i++)
+              for (int j = 0; j < (J.n + jn - 1) / jn; j++) {
+                GemmTile gt{};
+                gt.idx = static_cast<int32_t>(tp.jobs.size());
+                gt.pos = (i << 16) | j;
+                gt.shape = shape;
+                tp.jtiles.push_back(gt);
+              }
+            tp.jobs.push_back(J);
+          } else if (ha) {
+            it.l = A;
+            it.r = B;
+            it.k = T.k1;
+          } else if (hc) {
+            it.l = B;
+            it.r = C;
+            it.k = T.k2;
+          } else {
+            it.r = B;
+            it.k = 0;
+          }
+          tp.items.push_back(it);
+        }
+      }
+      sg.i1 = static_cast<int32_t>(tp.items.size());
+      tp.groups.push_back(sg);
+    };
     std::vector<int32_t> order(ng);
     {
       auto bin = [&](size_t g) {
@@ -518,7 +622,9 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     for (int g : order) {
       const Group& G = st.groups[g];
       const GroupTiles& gi = info[g];
-      if (gi.kind == 1) {
+      if (gi.kind == 1 && gi.large && !one_pass_large) {
+        plan_large(g);
+      } else if (gi.kind == 1) {
         for (int i = 0; i < gi.tm; i++)
           for (int j = 0; j < gi.tn; j++) {
             const int rows = std::min(kTile, G.m - i * kTile), cols = std::min(kTile, G.n - j * kTile);
@@ -550,8 +656,67 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
           }
       }
     }
+    if (!tp.groups.empty()) {
+      auto item_cost = [](const SumItem& it, int tm_, int tn_) {
+        return 2 * static_cast<int64_t>(tm_) * tn_ * std::max(it.k, 1) + 8192;
+      };
+      int64_t total = 0;
+      for (const SumGroup& sg : tp.groups) {
+        const int gm = pick(sg.m), gn = pick(sg.n);
+        const int64_t ntile = static_cast<int64_t>((sg.m + gm - 1) / gm) * ((sg.n + gn - 1) / gn);
+        for (int i = sg.i0; i < sg.i1; i++) total += ntile * item_cost(tp.items[i], gm, gn);
+      }
+      const int64_t gpiece = std::max<int64_t>(total / kGemmCtaTarget, 1);
+      int64_t gpart = 0, gcount = 0;
+      std::vector<int32_t> bnd;
+      for (size_t q = 0; q < tp.groups.size(); q++) {
+        const SumGroup& sg = tp.groups[q];
+        const int gm = pick(sg.m), gn = pick(sg.n);
+        const int shape = (gm == 64 ? 1 : 0) | (gn == 64 ? 2 : 0);
+        int64_t work = 0;
+        for (int i = sg.i0; i < sg.i1; i++) work += item_cost(tp.items[i], gm, gn);
+        int nsplit = static_cast<int>(std::min<int64_t>((work + gpiece - 1) / gpiece, kGemmMaxSplit));
+        nsplit = std::max(1, std::min(nsplit, sg.i1 - sg.i0));
+        bnd.assign(1, sg.i0);
+        int64_t before = 0;
+        int i = sg.i0;
+        for (int k = 1; k < nsplit; k++) {
+          const int64_t target = work * k / nsplit;
+          while (i < sg.i1 && before + item_cost(tp.items[i], gm, gn) <= target) before += item_cost(tp.items[i++], gm, gn);
+          bnd.push_back(std::max(i, bnd.back()));
+        }
+        bnd.push_back(sg.i1);
+        for (int r = 0; r < (sg.m + gm - 1) / gm; r++)
+          for (int c = 0; c < (sg.n + gn - 1) / gn; c++) {
+            GemmTile gt{};
+            gt.idx = static_cast<int32_t>(q);
+            gt.pos = (r << 16) | c;
+            gt.shape = shape;
+            gt.nsplit = nsplit;
+            if (nsplit > 1) {
+              gt.counter = static_cast<int32_t>(gcount++);
+              gt.part = gpart;
+              gpart += static_cast<int64_t>(nsplit) * gm * gn;
+            }
+            for (int k = 0; k < nsplit; k++) {
+              gt.split = k;
+              gt.item0 = bnd[k];
+              gt.item1 = bnd[k + 1];
+              tp.stiles.push_back(gt);
+            }
+          }
+      }
+      gemm_part_doubles = std::max(gemm_part_doubles, gpart);
+      gemm_counters = std::max(gemm_counters, gcount);
+      inter_doubles = std::max(inter_doubles, inter_off);
+      if (tp.items.size() > size_t(INT32_MAX) || tp.jobs.size() > size_t(INT32_MAX))
+        throw std::length_error("upload: too many large-group items");
+    }
     part_doubles = std::max(part_doubles, part_off);
     ncounters = std::max(ncounters, counter);
+    tile_bytes += align256(sizeof(InterJob) * tp.jobs.size()) + align256(sizeof(GemmTile) * tp.jtiles.size()) +
+                  align256(sizeof(SumGroup) * tp.groups.size()) + align256(sizeof(SumItem) * tp.items.size()) +
+                  align256(sizeof(GemmTile) * tp.stiles.size());
     tile_bytes += align256(sizeof(TileDesc) * tiles[s].size()) + align256(sizeof(TileDesc) * tiles_large[s].size()) +
                   align256(sizeof(WarpTile) * tiles_warp[s].size());
   }
@@ -587,6 +752,14 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     for (const WarpTile& wt : tiles_warp[s]) ds.nwarp[warp_row_class(wt.cls)]++;
     ds.tiles_warp =
         static_cast<const WarpTile*>(put(tiles_warp[s].data(), sizeof(WarpTile) * tiles_warp[s].size()));
+    const TwoPass& tp = twopass[s];
+    ds.jobs = static_cast<const InterJob*>(put(tp.jobs.data(), sizeof(InterJob) * tp.jobs.size()));
+    ds.jtiles = static_cast<const GemmTile*>(put(tp.jtiles.data(), sizeof(GemmTile) * tp.jtiles.size()));
+    ds.njtiles = static_cast<int>(tp.jtiles.size());
+    ds.sgroups = static_cast<const SumGroup*>(put(tp.groups.data(), sizeof(SumGroup) * tp.groups.size()));
+    ds.sitems = static_cast<const SumItem*>(put(tp.items.data(), sizeof(SumItem) * tp.items.size()));
+    ds.stiles = static_cast<const GemmTile*>(put(tp.stiles.data(), sizeof(GemmTile) * tp.stiles.size()));
+    ds.nstiles = static_cast<int>(tp.stiles.size());
     dp->nterms += ds.nterms;
     if (static_cast<int>(s) < dp->first_repeat) dp->flops_once += ds.flops;
     else dp->flops_repeat += ds.flops;
@@ -597,6 +770,12 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
   C2G_CUDA(cudaStreamSynchronize(stream_));  // the staging buffer is reused by the next upload
   if (dp->combo_size > 0) dp->combo = alloc(dp->combo_size);
   if (part_doubles > 0) dp->partials = alloc(part_doubles);
+  if (inter_doubles > 0) dp->inter = alloc(inter_doubles);
+  if (gemm_part_doubles > 0) dp->gemm_partials = alloc(gemm_part_doubles);
+  if (gemm_counters > 0) {
+    C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dp->gemm_counters), sizeof(unsigned) * gemm_counters, stream_));
+    C2G_CUDA(cudaMemsetAsync(dp->gemm_counters, 0, sizeof(unsigned) * gemm_counters, stream_));
+  }
   if (ncounters > 0) {
     C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dp->counters), sizeof(unsigned) * ncounters, stream_));
     C2G_CUDA(cudaMemsetAsync(dp->counters, 0, sizeof(unsigned) * ncounters, stream_));
@@ -606,16 +785,9 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
 
 void Runtime::prepare(DevProgram& p) {
   if (p.prepared) return;
-  const SlotPtrs sp = ptrs(nullptr, nullptr, p.combo);
-  for (int s = 0; s < p.first_repeat; s++) {
-    const DevStage& ds = p.stages[s];
-    C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_));
-    int nw = 0;
-    const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, p.partials, p.counters};
-    C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, Precision::kFP64, &nw));
-    C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_));
-    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
-  }
+  SlotPtrs sp = ptrs(nullptr, nullptr, p.combo);
+  sp.inter = p.inter;
+  for (int s = 0; s < p.first_repeat; s++) launch_stage(p, p.stages[s], sp, Precision::kFP64);
   p.prepared = true;
   p.combo32_ready = false;
 }
@@ -643,16 +815,23 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
       sp.x32 = x32_;
     }
   }
-  for (size_t s = p.first_repeat; s < p.stages.size(); s++) {
-    const DevStage& ds = p.stages[s];
-    C2G_CUDA(
-        launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
-    int nw = 0;
-    const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, p.partials, p.counters};
-    C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, prec, &nw));
-    C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
-    count_launches((ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
-  }
+  sp.inter = p.inter;
+  sp.inter32 = reinterpret_cast<float*>(p.inter);
+  for (size_t s = p.first_repeat; s < p.stages.size(); s++) launch_stage(p, p.stages[s], sp, prec);
+}
+
+// One stage: the two passes of its large groups, then the one-pass variants (all write
+// disjoint output blocks).
+void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec) {
+  C2G_CUDA(launch_inter_gemm(ds.jobs, ds.jtiles, ds.njtiles, sp, stream_, prec));
+  C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, p.gemm_partials, p.gemm_counters, sp,
+                           stream_, prec));
+  C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
+  int nw = 0;
+  const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, p.partials, p.counters};
+  C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, prec, &nw));
+  C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
+  count_launches((ds.njtiles > 0) + (ds.nstiles > 0) + (ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
 }
 
 void Runtime::sync() { C2G_CUDA(cudaStreamSynchronize(stream_)); }

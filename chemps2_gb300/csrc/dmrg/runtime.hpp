@@ -38,6 +38,13 @@ struct DevStage {
   const WarpTile* tiles_warp = nullptr;   // team variant, ordered by row class
   int ngroups = 0, nterms = 0, ntiles = 0, ntiles_large = 0, ntiles_warp = 0;
   int nwarp[kWarpRowClasses] = {};        // team-variant tiles per row class
+  // two-pass path of large groups: pass-1 jobs and tiles, pass-2 groups, items and tiles
+  const InterJob* jobs = nullptr;
+  const GemmTile* jtiles = nullptr;
+  const SumGroup* sgroups = nullptr;
+  const SumItem* sitems = nullptr;
+  const GemmTile* stiles = nullptr;
+  int njtiles = 0, nstiles = 0;
   int64_t flops = 0, items = 0;
   std::string name;
 };
@@ -55,6 +62,9 @@ struct DevProgram {
   float* combo32 = nullptr;     // FP32 copy of the combined blocks for FP32 runs
   double* partials = nullptr;   // partial sums of split team-variant tiles (shared by the stages)
   unsigned int* counters = nullptr;  // their arrival counters
+  double* inter = nullptr;           // intermediate products of the two-pass path
+  double* gemm_partials = nullptr;   // partial tiles of its split pass-2 tiles
+  unsigned int* gemm_counters = nullptr;
   bool prepared = false;
   bool combo32_ready = false;
   DevProgram() = default;
@@ -111,6 +121,7 @@ class Runtime {
   friend struct DevProgram;
   void flush_slots();
   SlotPtrs ptrs(double* x, double* y, double* combo);
+  void launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec);
 
   int L_;
   cudaStream_t stream_ = nullptr;

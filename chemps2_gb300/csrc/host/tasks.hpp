@@ -47,6 +47,7 @@ inline int64_t ref_off(Ref r) { return static_cast<int64_t>(r & kRefMask); }
 enum Slot : int {
   kSlotX = 0,
   kSlotY = 1,
+  kSlotInter = 2,   // intermediate products of the two-pass large-block path
   kSlotCombo = 3,   // combined blocks of the program being run
   kSlotWork = 4,    // truncation workspace (assembled sector matrices, Gram, eigvecs)
   kSlotOnes = 5,    // a vector of 1.0, at least as long as the largest sector dimension

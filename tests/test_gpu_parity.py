@@ -82,6 +82,38 @@ def test_heff_matches_oracle_on_fresh_state(name, make, two_s, n, irrep):
     gpu.close()
 
 
+@pytest.mark.parametrize("one_pass", [False, True])
+def test_heff_large_blocks_match_oracle(one_pass, monkeypatch):
+    """Heff at the middle of a C1 Hubbard chain whose sector blocks are large (the two-pass
+    large-block path: intermediates once, then split item sums), and with C2G_LARGE=tile
+    the one-pass cooperative kernel, element-wise against the oracle; the FP32 variant of
+    the same program within FP32 rounding."""
+    if one_pass:
+        monkeypatch.setenv("C2G_LARGE", "tile")
+    else:
+        monkeypatch.delenv("C2G_LARGE", raising=False)
+    m = models.hubbard(12, 4.0)
+    sched = [(256, 1e-10, 1, 0.0, 1e-8)]
+    ham, prob, scheme = gpu_objects(m, 0, 12, 0, sched)
+    c2g.srand(9)
+    gpu = c2g.DMRG(prob, scheme)
+    ol.srand(9)
+    cpu = ol.OracleDMRG(m, 0, 12, 0, sched)
+    mid = m.L // 2 - 1
+    for index in range(m.L - 2, mid, -1):
+        gpu.update(index, False)
+        cpu.update(index, False)
+    xg, yg, _ = gpu.heff_apply(mid)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(xg.size)
+    _, yg, _ = gpu.heff_apply(mid, x)
+    _, yc, _ = cpu.heff_apply(mid, x)
+    assert rel_err(yg, yc) < 1e-10
+    y32 = gpu.heff_apply_fp32(mid, x)
+    assert rel_err(y32, yc) < 1e-4
+    gpu.close()
+
+
 @pytest.mark.parametrize("name,make,two_s,n,irrep", CASES)
 def test_sweep_steps_match_oracle(name, make, two_s, n, irrep):
     """One left and one right sweep step by step: per-step energies, then Heff at every
