@@ -50,8 +50,8 @@ struct SlotPtrs {
 // GEMM into the program's intermediate scratch (slot kSlotInter); pass 2 sums the items'
 // products into the output tiles, out += sum_p alpha_p op(L_p) op(R_p), in the fixed item
 // order, with long item lists split over several CTAs whose partial tiles the last CTA to
-// finish adds up in split order. Tiles are 32 or 64 rows by 32 or 64 columns (chosen per
-// block to limit padding), 256 threads each holding a (tile / 16) x (tile / 16) patch.
+// finish adds up in split order. Tiles lie on a 64 x 64 grid; each is 16 PM x 16 PN
+// (PM, PN = 1 .. 4) to cover its part of the block with little padding.
 constexpr int kGemmThreads = 256;
 constexpr int kGemmMaxSplit = 64;
 constexpr int64_t kGemmCtaTarget = 1216;  // 152 SMs x 8 CTA-sized pieces per stage
@@ -78,8 +78,8 @@ struct SumGroup {      // an output block of the path: items [i0, i1)
 };
 struct GemmTile {      // a CTA's work unit of either pass
   int32_t idx;         // job (pass 1) or sum group (pass 2)
-  int32_t pos;         // tile row << 16 | tile column, in units of the tile shape
-  int32_t shape;       // bit 0: 64 rows (else 32); bit 1: 64 columns (else 32)
+  int32_t pos;         // tile row << 16 | tile column, in units of 64
+  int32_t shape;       // (PM - 1) | (PN - 1) << 2: the tile is 16 PM x 16 PN
   int32_t nsplit, split;
   int32_t item0, item1;  // pass 2: this split's items (absolute indices)
   int32_t counter;       // pass 2 with nsplit > 1: arrival counter

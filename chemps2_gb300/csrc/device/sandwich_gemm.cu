@@ -1,12 +1,15 @@
 // Two-pass path of large groups (declarations and the scheme in kernels.cuh).
 //
-// Both passes run the same CTA-level GEMM: 256 threads in a 16 x 16 layout, each holding
-// a PM x PN register patch of a (16 PM) x (16 PN) output tile (PM, PN in {2, 4}); the
+// Both passes run the same CTA-level GEMM on an output tile of at most 64 x 64 placed on
+// a 64 x 64 grid: 256 threads in a 16 x 16 layout, thread (ty, tx) holding rows
+// ty PM .. ty PM + PM - 1 and columns tx + 16 jj (jj < PN) of the tile, where PM and PN
+// (1 to 4) are the tile's extents in units of 16, chosen per tile on the host. The
 // operands are staged through shared memory in chunks of 16 along the inner dimension,
 // loaded with the unit-stride index fastest for either storage order of each operand.
-// In FP64 the GEMM is bound by the FP64 pipe (two FMAs per SM and clock on this GPU),
-// so the kernel's job is to issue no FMA twice: every intermediate is formed once in
-// pass 1 and the tile shapes keep the padding small.
+// In FP64 the GEMM is bound by the FP64 pipe (two FMAs per SM and clock on this GPU), so
+// no FMA may be issued twice or on padding: every intermediate is formed once in pass 1,
+// tile extents follow the block to 16 columns, and warps whose rows lie past the block
+// skip the multiply-adds altogether.
 #include "kernels.cuh"
 #include "slots.cuh"
 
@@ -40,13 +43,15 @@ struct GSmem {
   Real R[kKC][64 + 1];
 };
 
-// part (rows ty + 16 ii, columns tx + 16 jj) = sum_{k < K} L(i, k) R(k, j) over i < M,
-// j < N (zero elsewhere)
+// part (rows ty PM + ii, columns tx + 16 jj) = sum_{k < K} L(i, k) R(k, j) over i < M,
+// j < N (zero elsewhere); M <= 16 PM, N <= 16 PN
 template <typename Real, int PM, int PN>
 __device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>& L, int M, const Opnd<Real>& R,
                                           int N, int K, GSmem<Real>& sm) {
   constexpr int TM = 16 * PM, TN = 16 * PN;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  // a warp holds rows (ty & ~1) PM .. (ty | 1) PM + PM - 1
+  const bool active = (ty & ~1) * PM < M;
 #pragma unroll
   for (int ii = 0; ii < PM; ii++)
 #pragma unroll
@@ -79,17 +84,19 @@ __device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>
       sm.R[kk][j] = (j < N && k0 + kk < K) ? R.at(k0 + kk, j) : Real(0);
     }
     __syncthreads();
-    const int kn = min(kKC, K - k0);
-    for (int kk = 0; kk < kn; kk++) {
-      Real a[PM], b[PN];
+    if (active) {
+      const int kn = min(kKC, K - k0);
+      for (int kk = 0; kk < kn; kk++) {
+        Real a[PM], b[PN];
 #pragma unroll
-      for (int ii = 0; ii < PM; ii++) a[ii] = sm.L[kk][ty + 16 * ii];
+        for (int ii = 0; ii < PM; ii++) a[ii] = sm.L[kk][ty * PM + ii];
 #pragma unroll
-      for (int jj = 0; jj < PN; jj++) b[jj] = sm.R[kk][tx + 16 * jj];
+        for (int jj = 0; jj < PN; jj++) b[jj] = sm.R[kk][tx + 16 * jj];
 #pragma unroll
-      for (int ii = 0; ii < PM; ii++)
+        for (int ii = 0; ii < PM; ii++)
 #pragma unroll
-        for (int jj = 0; jj < PN; jj++) part[ii][jj] = fmaR(a[ii], b[jj], part[ii][jj]);
+          for (int jj = 0; jj < PN; jj++) part[ii][jj] = fmaR(a[ii], b[jj], part[ii][jj]);
+      }
     }
     __syncthreads();
   }
@@ -98,7 +105,7 @@ __device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>
 template <typename Real, int PM, int PN>
 __device__ __forceinline__ void inter_tile(const InterJob& J, int pos, const SlotPtrs& sp, GSmem<Real>& sm) {
   constexpr int TM = 16 * PM, TN = 16 * PN;
-  const int row0 = (pos >> 16) * TM, col0 = (pos & 0xffff) * TN;
+  const int row0 = (pos >> 16) * 64, col0 = (pos & 0xffff) * 64;
   const int tm = min(TM, J.m - row0), tn = min(TN, J.n - col0);
   Real part[PM][PN];
   tile_gemm<Real, PM, PN>(part, opnd<Real>(sp, J.l).shift(row0, 0), tm, opnd<Real>(sp, J.r).shift(0, col0), tn, J.k,
@@ -109,7 +116,7 @@ __device__ __forceinline__ void inter_tile(const InterJob& J, int pos, const Slo
   for (int ii = 0; ii < PM; ii++)
 #pragma unroll
     for (int jj = 0; jj < PN; jj++) {
-      const int r = ty + 16 * ii, c = tx + 16 * jj;
+      const int r = ty * PM + ii, c = tx + 16 * jj;
       if (r < tm && c < tn) S[(row0 + r) + static_cast<int64_t>(J.m) * (col0 + c)] = part[ii][jj];
     }
 }
@@ -120,12 +127,17 @@ __global__ void __launch_bounds__(kGemmThreads, 2)
   __shared__ GSmem<Real> sm;
   const GemmTile T = tiles[blockIdx.x];
   const InterJob J = jobs[T.idx];
+  // shape = (PM - 1) | (PN - 1) << 2
+#define C2G_INTER(pm, pn) \
+  case (pm - 1) | ((pn - 1) << 2): inter_tile<Real, pm, pn>(J, T.pos, sp, sm); break;
   switch (T.shape) {
-    case 0: inter_tile<Real, 2, 2>(J, T.pos, sp, sm); break;
-    case 1: inter_tile<Real, 4, 2>(J, T.pos, sp, sm); break;
-    case 2: inter_tile<Real, 2, 4>(J, T.pos, sp, sm); break;
-    default: inter_tile<Real, 4, 4>(J, T.pos, sp, sm); break;
+    C2G_INTER(1, 1) C2G_INTER(2, 1) C2G_INTER(3, 1) C2G_INTER(4, 1)
+    C2G_INTER(1, 2) C2G_INTER(2, 2) C2G_INTER(3, 2) C2G_INTER(4, 2)
+    C2G_INTER(1, 3) C2G_INTER(2, 3) C2G_INTER(3, 3) C2G_INTER(4, 3)
+    C2G_INTER(1, 4) C2G_INTER(2, 4) C2G_INTER(3, 4) C2G_INTER(4, 4)
+    default: break;
   }
+#undef C2G_INTER
 }
 
 template <typename Real, int PM, int PN>
@@ -133,7 +145,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
                                          double* partials, unsigned int* counters, const SlotPtrs& sp,
                                          GSmem<Real>& sm) {
   constexpr int TM = 16 * PM, TN = 16 * PN;
-  const int row0 = (T.pos >> 16) * TM, col0 = (T.pos & 0xffff) * TN;
+  const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
   const int tm = min(TM, G.m - row0), tn = min(TN, G.n - col0);
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   double acc[PM][PN];
@@ -152,7 +164,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
       for (int ii = 0; ii < PM; ii++)
 #pragma unroll
         for (int jj = 0; jj < PN; jj++) {
-          const int r = ty + 16 * ii, c = tx + 16 * jj;
+          const int r = ty * PM + ii, c = tx + 16 * jj;
           part[ii][jj] = (r < tm && c < tn) ? R.at(row0 + r, col0 + c) : Real(0);
         }
     }
@@ -169,7 +181,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
     for (int ii = 0; ii < PM; ii++)
 #pragma unroll
       for (int jj = 0; jj < PN; jj++)
-        __stcg(part + static_cast<int64_t>(T.split) * te + (ty + 16 * ii) + TM * (tx + 16 * jj), acc[ii][jj]);
+        __stcg(part + static_cast<int64_t>(T.split) * te + (ty * PM + ii) + TM * (tx + 16 * jj), acc[ii][jj]);
     __threadfence();
     __shared__ int is_last;
     __syncthreads();
@@ -183,7 +195,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
       for (int jj = 0; jj < PN; jj++) {
         double v = 0.0;
         for (int s = 0; s < T.nsplit; s++)
-          v += __ldcg(part + static_cast<int64_t>(s) * te + (ty + 16 * ii) + TM * (tx + 16 * jj));
+          v += __ldcg(part + static_cast<int64_t>(s) * te + (ty * PM + ii) + TM * (tx + 16 * jj));
         acc[ii][jj] = v;
       }
     if (tid == 0) counters[T.counter] = 0u;  // ready for the next launch
@@ -195,7 +207,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
   for (int ii = 0; ii < PM; ii++)
 #pragma unroll
     for (int jj = 0; jj < PN; jj++) {
-      const int r = ty + 16 * ii, c = tx + 16 * jj;
+      const int r = ty * PM + ii, c = tx + 16 * jj;
       if (r < tm && c < tn) {
         const int64_t idx = (row0 + r) + ldo * (col0 + c);
         O[idx] = accum ? O[idx] + acc[ii][jj] : acc[ii][jj];
@@ -210,12 +222,16 @@ __global__ void __launch_bounds__(kGemmThreads, 2)
   __shared__ GSmem<Real> sm;
   const GemmTile T = tiles[blockIdx.x];
   const SumGroup G = groups[T.idx];
+#define C2G_SUM(pm, pn) \
+  case (pm - 1) | ((pn - 1) << 2): sum_tile<Real, pm, pn>(T, G, items, partials, counters, sp, sm); break;
   switch (T.shape) {
-    case 0: sum_tile<Real, 2, 2>(T, G, items, partials, counters, sp, sm); break;
-    case 1: sum_tile<Real, 4, 2>(T, G, items, partials, counters, sp, sm); break;
-    case 2: sum_tile<Real, 2, 4>(T, G, items, partials, counters, sp, sm); break;
-    default: sum_tile<Real, 4, 4>(T, G, items, partials, counters, sp, sm); break;
+    C2G_SUM(1, 1) C2G_SUM(2, 1) C2G_SUM(3, 1) C2G_SUM(4, 1)
+    C2G_SUM(1, 2) C2G_SUM(2, 2) C2G_SUM(3, 2) C2G_SUM(4, 2)
+    C2G_SUM(1, 3) C2G_SUM(2, 3) C2G_SUM(3, 3) C2G_SUM(4, 3)
+    C2G_SUM(1, 4) C2G_SUM(2, 4) C2G_SUM(3, 4) C2G_SUM(4, 4)
+    default: break;
   }
+#undef C2G_SUM
 }
 
 }  // namespace

@@ -499,11 +499,13 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     // program order within a bin), row-major within a group. Team-variant tiles are then
     // grouped by row class (one kernel per class), keeping that order within a class.
     // Large groups: every (term, entry) item becomes a pass-2 product, after a pass-1
-    // intermediate when the item has both outer operands. Tile edges of 32 or 64 (the one
-    // with less padding); long item lists are split at equal shares of the work.
+    // intermediate when the item has both outer operands. Tiles lie on a 64 x 64 grid,
+    // each cut to its part of the block rounded up to 16; long item lists are split at
+    // equal shares of the work.
     TwoPass& tp = twopass[s];
     int64_t inter_off = 0;
-    auto pick = [](int x) { return ((x + 63) / 64) * 64 <= ((x + 31) / 32) * 32 ? 64 : 32; };
+    auto ext16 = [](int x) { return std::max(1, std::min(4, (x + 15) / 16)); };  // extent in units of 16
+    auto tile_shape = [&](int rows, int cols) { return (ext16(rows) - 1) | ((ext16(cols) - 1) << 2); };
     auto plan_large = [&](int g) {
       const Group& G = st.groups[g];
       const BatchEntry* ents = reinterpret_cast<const BatchEntry*>(staging_);
@@ -555,14 +557,12 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
               it.k = T.k1;
             }
             inter_off += (static_cast<int64_t>(J.m) * J.n + 3) & ~int64_t(3);
-            const int jm = pick(J.m), jn = pick(J.n);
-            const int shape = (jm == 64 ? 1 : 0) | (jn == 64 ? 2 : 0);
-            for (int i = 0; i < (J.m + jm - 1) / jm; i++)
-              for (int j = 0; j < (J.n + jn - 1) / jn; j++) {
+            for (int i = 0; i < (J.m + 63) / 64; i++)
+              for (int j = 0; j < (J.n + 63) / 64; j++) {
                 GemmTile gt{};
                 gt.idx = static_cast<int32_t>(tp.jobs.size());
                 gt.pos = (i << 16) | j;
-                gt.shape = shape;
+                gt.shape = tile_shape(std::min(64, J.m - 64 * i), std::min(64, J.n - 64 * j));
                 tp.jtiles.push_back(gt);
               }
             tp.jobs.push_back(J);
@@ -660,19 +660,20 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
       auto item_cost = [](const SumItem& it, int tm_, int tn_) {
         return 2 * static_cast<int64_t>(tm_) * tn_ * std::max(it.k, 1) + 8192;
       };
+      // work of an item on a full tile of the group (edge tiles are smaller)
+      auto gm16 = [&](const SumGroup& sg) { return 16 * ext16(std::min(64, sg.m)); };
+      auto gn16 = [&](const SumGroup& sg) { return 16 * ext16(std::min(64, sg.n)); };
       int64_t total = 0;
       for (const SumGroup& sg : tp.groups) {
-        const int gm = pick(sg.m), gn = pick(sg.n);
-        const int64_t ntile = static_cast<int64_t>((sg.m + gm - 1) / gm) * ((sg.n + gn - 1) / gn);
-        for (int i = sg.i0; i < sg.i1; i++) total += ntile * item_cost(tp.items[i], gm, gn);
+        const int64_t ntile = static_cast<int64_t>((sg.m + 63) / 64) * ((sg.n + 63) / 64);
+        for (int i = sg.i0; i < sg.i1; i++) total += ntile * item_cost(tp.items[i], gm16(sg), gn16(sg));
       }
       const int64_t gpiece = std::max<int64_t>(total / kGemmCtaTarget, 1);
       int64_t gpart = 0, gcount = 0;
       std::vector<int32_t> bnd;
       for (size_t q = 0; q < tp.groups.size(); q++) {
         const SumGroup& sg = tp.groups[q];
-        const int gm = pick(sg.m), gn = pick(sg.n);
-        const int shape = (gm == 64 ? 1 : 0) | (gn == 64 ? 2 : 0);
+        const int gm = gm16(sg), gn = gn16(sg);
         int64_t work = 0;
         for (int i = sg.i0; i < sg.i1; i++) work += item_cost(tp.items[i], gm, gn);
         int nsplit = static_cast<int>(std::min<int64_t>((work + gpiece - 1) / gpiece, kGemmMaxSplit));
@@ -686,17 +687,18 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
           bnd.push_back(std::max(i, bnd.back()));
         }
         bnd.push_back(sg.i1);
-        for (int r = 0; r < (sg.m + gm - 1) / gm; r++)
-          for (int c = 0; c < (sg.n + gn - 1) / gn; c++) {
+        for (int r = 0; r < (sg.m + 63) / 64; r++)
+          for (int c = 0; c < (sg.n + 63) / 64; c++) {
+            const int rows = std::min(64, sg.m - 64 * r), cols = std::min(64, sg.n - 64 * c);
             GemmTile gt{};
             gt.idx = static_cast<int32_t>(q);
             gt.pos = (r << 16) | c;
-            gt.shape = shape;
+            gt.shape = tile_shape(rows, cols);
             gt.nsplit = nsplit;
             if (nsplit > 1) {
               gt.counter = static_cast<int32_t>(gcount++);
               gt.part = gpart;
-              gpart += static_cast<int64_t>(nsplit) * gm * gn;
+              gpart += static_cast<int64_t>(nsplit) * (16 * ext16(rows)) * (16 * ext16(cols));
             }
             for (int k = 0; k < nsplit; k++) {
               gt.split = k;
