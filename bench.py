@@ -76,7 +76,7 @@ def make_model():
     return synthetic_ab_initio(L_SITES, GROUP, SEED)
 
 
-def build_gpu_dmrg(model, D=D_VIRT):
+def build_gpu_dmrg(model, D=D_VIRT, sweeps=1, right_ops=True):
     import chemps2_gb300 as c2g
 
     L = model.L
@@ -90,11 +90,12 @@ def build_gpu_dmrg(model, D=D_VIRT):
             ham.setVmat(int(i), int(j), int(k), int(l), float(model.vmat[i, j, k, l]))
     prob = c2g.Problem(ham, TWO_S, N_ELEC, IRREP)
     scheme = c2g.ConvergenceScheme(1)
-    scheme.set_instruction(0, D, 1e-10, 1, 0.0, 1e-8)
+    scheme.set_instruction(0, D, 1e-10, sweeps, 0.0, 1e-8)
     c2g.srand(SEED)
     dmrg = c2g.DMRG(prob, scheme)
-    for index in range(L - 2, MID, -1):  # right-hand operators down to the middle
-        dmrg.update(index, False)
+    if right_ops:
+        for index in range(L - 2, MID, -1):  # right-hand operators down to the middle
+            dmrg.update(index, False)
     return ham, prob, scheme, dmrg
 
 
@@ -223,6 +224,40 @@ def sweep_seconds():
     return out
 
 
+def sweep_config2(model, sweeps=2, steps=20):
+    """The headline system (L = 24, D = 1000) swept `sweeps` times from the random start in
+    plain FP64 and in mixed precision: seconds per sweep (first and last sweep, host task
+    compilation included), the energy difference, and the matvec rate at sites (11, 12) on
+    the swept state (sector dimensions after truncation, larger blocks than the initial
+    state), FP64 and FP32."""
+    out = {"config": f"synthetic ab initio L=24 N=24 S=0 D2h D=1000, {sweeps} sweeps, Davidson rtol 1e-8"}
+    for mode in ("fp64", "mixed"):
+        ham, prob, scheme, d = build_gpu_dmrg(model, sweeps=1, right_ops=False)  # one sweep per Solve()
+        d.set_precision(mode)
+        per = []
+        for _ in range(sweeps):
+            d.reset_stats()
+            t0 = time.perf_counter()
+            e = d.Solve()
+            per.append(time.perf_counter() - t0)
+        st = d.stats()
+        res = {"s_per_sweep": per, "energy": e, "last_sweep": {k: v for k, v in st.items() if k.startswith(("t_", "n_"))}}
+        if mode == "fp64":
+            for index in range(L_SITES - 2, MID, -1):
+                d.update(index, False)
+            r64 = d.bench_heff(MID, 3, steps, L2_FLUSH_BYTES)
+            r32 = d.bench_heff(MID, 3, steps, L2_FLUSH_BYTES, precision="fp32")
+            res["swept_state_matvec"] = {
+                "fp64_matvec_per_s": 1e3 / r64["ms_per_matvec"], "fp64_gflops": r64["flops"] / r64["ms_per_matvec"] / 1e6,
+                "fp32_matvec_per_s": 1e3 / r32["ms_per_matvec"], "fp32_gflops": r32["flops"] / r32["ms_per_matvec"] / 1e6,
+                "ledger_flops_per_matvec": r64["flops"], "two_site_vector_length": d.sobject_size(MID)}
+        d.close()
+        out[mode] = res
+    out["mixed_speedup_last_sweep"] = out["fp64"]["s_per_sweep"][-1] / out["mixed"]["s_per_sweep"][-1]
+    out["mixed_energy_error"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"])
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -302,9 +337,10 @@ def run_ours(args):
                 "compute_fp32_variant": {"pipe": "fp32", "achieved_gflops": gflops32, "peak_gflops": fp32_peak,
                                          "frac": gflops32 / fp32_peak}}
     dmrg.close()
-    sweep = None
+    sweep = sweep24 = None
     if rank == 0 and not args.no_sweep:
         sweep = sweep_seconds()
+        sweep24 = sweep_config2(model)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline_sample(model, n_matvec=1)
@@ -318,11 +354,102 @@ def run_ours(args):
                        "group": "D2h", "D": D_VIRT, "two_site_vector_length": n, "l2": "flushed between steps",
                        "parallelism": f"replicas x{world}", "setup_s": setup_s},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
-            "gpu_launches": res["launches"], "sweep": sweep, "mixed": mixed,
+            "gpu_launches": res["launches"], "sweep": sweep, "sweep_l24_d1000": sweep24, "mixed": mixed,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def extra_config3(args):
+    """Precision form: synthetic ab initio L = N = 30, S = 0, D2h, D = 2000, swept in plain
+    FP64 and in mixed precision (FP32 Davidson expansion with FP64 refinement, FP64
+    truncation): seconds per sweep and the energy difference. --sweeps sets the number of
+    sweeps (8 in the reference configuration)."""
+    import chemps2_gb300 as c2g
+    from chemps2_gb300.models import synthetic_ab_initio
+
+    L = 30
+    model = synthetic_ab_initio(L, GROUP, SEED)
+    out = {"config": f"synthetic ab initio L=30 N=30 S=0 D2h D=2000, {args.sweeps} sweeps, Davidson rtol 1e-8"}
+    for mode in ("fp64", "mixed"):
+        ham = c2g.Hamiltonian(L, model.group, model.irreps)
+        for i in range(L):
+            for j in range(i, L):
+                if model.tmat[i, j] != 0.0:
+                    ham.setTmat(i, j, float(model.tmat[i, j]))
+        for i, j, k, l in np.argwhere(model.vmat != 0.0):
+            if i <= j and i <= k:
+                ham.setVmat(int(i), int(j), int(k), int(l), float(model.vmat[i, j, k, l]))
+        prob = c2g.Problem(ham, 0, L, 0)
+        scheme = c2g.ConvergenceScheme(1)
+        scheme.set_instruction(0, 2000, 1e-10, 1, 0.0, 1e-8)
+        c2g.srand(SEED)
+        d = c2g.DMRG(prob, scheme)
+        d.set_precision(mode)
+        per, stats = [], []
+        for _ in range(args.sweeps):
+            d.reset_stats()
+            t0 = time.perf_counter()
+            e = d.Solve()
+            per.append(time.perf_counter() - t0)
+            stats.append({k: v for k, v in d.stats().items() if k.startswith(("t_", "n_"))})
+        d.close()
+        out[mode] = {"s_per_sweep": per, "energy": e, "stats": stats}
+    out["mixed_speedup_last_sweep"] = out["fp64"]["s_per_sweep"][-1] / out["mixed"]["s_per_sweep"][-1]
+    out["mixed_speedup_total"] = sum(out["fp64"]["s_per_sweep"]) / sum(out["mixed"]["s_per_sweep"])
+    out["mixed_energy_error"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"])
+    print(json.dumps({"extra": "precision_l30_d2000", **out}), flush=True)
+
+
+def batch_objects(members, sweeps):
+    import chemps2_gb300 as c2g
+
+    objs = []
+    for mb in members:
+        m = mb["model"]
+        ham = c2g.Hamiltonian(m.L, m.group, m.irreps)
+        for i in range(m.L):
+            for j in range(i, m.L):
+                if m.tmat[i, j] != 0.0:
+                    ham.setTmat(i, j, float(m.tmat[i, j]))
+        for i, j, k, l in np.argwhere(m.vmat != 0.0):
+            if i <= j and i <= k:
+                ham.setVmat(int(i), int(j), int(k), int(l), float(m.vmat[i, j, k, l]))
+        prob = c2g.Problem(ham, mb["two_s"], mb["n"], mb["irrep"])
+        sc = c2g.ConvergenceScheme(1)
+        sc.set_instruction(0, mb["D"], 1e-10, sweeps, 0.0, 1e-8)
+        objs.append((ham, prob, sc))
+    return objs
+
+
+def extra_batch(args):
+    """Batching form: the seeded set of independent problems (L in 8..20, N = L, half
+    Hubbard, half synthetic ab initio, D in {64, 128, 256, 512}, FP64), --batch-count of
+    them (64 in the reference configuration), each swept --sweeps times, solved
+    concurrently through c2g_batch_solve (each problem on its own stream, --workers host
+    threads) and one after another: aggregate Heff matvecs/s both ways, with the energies
+    of the two runs compared."""
+    import chemps2_gb300 as c2g
+    from chemps2_gb300.models import batch_members
+
+    members = batch_members(args.batch_count)
+    out = {"config": f"{args.batch_count} problems, {args.sweeps} sweep(s) each, FP64"}
+    energies = {}
+    for label, workers in (("concurrent", args.workers), ("sequential", 1)):
+        objs = batch_objects(members, args.sweeps)
+        t0 = time.perf_counter()
+        res = c2g.solve_batch([o[1] for o in objs], [o[2] for o in objs], [mb["seed"] for mb in members],
+                              workers=workers)
+        dt = time.perf_counter() - t0
+        mv = sum(r["matvecs"] for r in res)
+        out[label] = {"workers": workers, "seconds": dt, "matvecs": mv, "matvec_per_s": mv / dt,
+                      "device_matvec_seconds": sum(r["stats"]["t_matvec"] for r in res),
+                      "compile_seconds": sum(r["stats"]["t_compile"] for r in res)}
+        energies[label] = [r["energy"] for r in res]
+    out["speedup"] = out["concurrent"]["matvec_per_s"] / out["sequential"]["matvec_per_s"]
+    out["max_energy_difference"] = max(abs(a - b) for a, b in zip(energies["concurrent"], energies["sequential"]))
+    print(json.dumps({"extra": "batch", **out}), flush=True)
 
 
 def run_reference(args):
@@ -355,12 +482,21 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-sweep", action="store_true", help="skip the sweep timing")
+    ap.add_argument("--extra", choices=["config3", "batch"], default=None,
+                    help="run one of the further configurations instead (prints its own JSON line)")
+    ap.add_argument("--sweeps", type=int, default=2, help="sweeps per problem for --extra")
+    ap.add_argument("--batch-count", type=int, default=64, help="problems for --extra batch")
+    ap.add_argument("--workers", type=int, default=16, help="concurrent problems for --extra batch")
     ap.add_argument("--profile", type=int, default=0,
                     help="profiling mode: set up, then run this many matvecs between cudaProfilerStart/Stop")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.extra == "config3":
+        extra_config3(args)
+    elif args.extra == "batch":
+        extra_batch(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -495,9 +495,6 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
         }
       }
     }
-    // Tile order: the groups with the most work first (binned by powers of two, in
-    // program order within a bin), row-major within a group. Team-variant tiles are then
-    // grouped by row class (one kernel per class), keeping that order within a class.
     // Large groups: every (term, entry) item becomes a pass-2 product, after a pass-1
     // intermediate when the item has both outer operands. Tiles lie on a 64 x 64 grid,
     // each cut to its part of the block rounded up to 16; long item lists are split at
@@ -584,21 +581,31 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
       sg.i1 = static_cast<int32_t>(tp.items.size());
       tp.groups.push_back(sg);
     };
+    // Tile order: the groups with the most work first, row-major within a group.
+    // Team-variant tiles are then grouped by row class (one kernel per class), keeping
+    // that order within a class.
     std::vector<int32_t> order(ng);
     {
-      auto bin = [&](size_t g) {
-        const int64_t w = st.groups[g].work;
-        return w <= 0 ? 0 : 64 - __builtin_clzll(static_cast<unsigned long long>(w));
-      };
-      int64_t cnt[66] = {0};
-      for (size_t g = 0; g < ng; g++) cnt[65 - bin(g)]++;
-      int64_t at = 0;
-      for (int k = 0; k < 66; k++) {
-        const int64_t c = cnt[k];
-        cnt[k] = at;
-        at += c;
+      // stable LSD radix sort on the complemented work (descending work, program order
+      // among equal work), 8 bits a pass
+      std::vector<uint64_t> key(ng);
+      uint64_t all = 0;
+      for (size_t g = 0; g < ng; g++) {
+        key[g] = ~static_cast<uint64_t>(std::max<int64_t>(st.groups[g].work, 0));
+        all |= ~key[g];
       }
-      for (size_t g = 0; g < ng; g++) order[cnt[65 - bin(g)]++] = static_cast<int32_t>(g);
+      std::iota(order.begin(), order.end(), 0);
+      std::vector<int32_t> tmp(ng);
+      int passes = 0;
+      while (passes < 8 && (all >> (8 * passes)) != 0) passes++;
+      for (int pass = 0; pass < passes; pass++) {
+        const int sh = 8 * pass;
+        size_t cnt[257] = {0};
+        for (size_t q = 0; q < ng; q++) cnt[((key[order[q]] >> sh) & 255) + 1]++;
+        for (int b = 0; b < 256; b++) cnt[b + 1] += cnt[b];
+        for (size_t q = 0; q < ng; q++) tmp[cnt[(key[order[q]] >> sh) & 255]++] = order[q];
+        order.swap(tmp);
+      }
     }
     int64_t per_class[kWarpRowClasses] = {0};
     for (size_t g = 0; g < ng; g++) {
