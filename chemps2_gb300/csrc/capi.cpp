@@ -593,6 +593,52 @@ int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* sche
   return C2G_OK;
 }
 
+int c2g_truncation_eig(int count, const int* n, const double* mats, double* evals, double* evecs) {
+  return guarded([&] {
+    if (count < 0) throw std::invalid_argument("c2g_truncation_eig: negative count");
+    if (count == 0) return;
+    NEED(n);
+    NEED(mats);
+    NEED(evals);
+    NEED(evecs);
+    std::vector<c2g::EigJob> small, large;
+    int64_t tot = 0, totn = 0;
+    int nmax = 0;
+    for (int i = 0; i < count; i++) {
+      if (n[i] < 1 || n[i] > c2g::kBatchedEigLargeMax)
+        throw std::invalid_argument("c2g_truncation_eig: matrix order outside 1..128");
+      tot += static_cast<int64_t>(n[i]) * n[i];
+      totn += n[i];
+    }
+    // device layout: all matrices (Gram slots), then the eigenvalues, then the eigenvectors
+    int64_t og = 0, oe = tot, ou = tot + totn;
+    for (int i = 0; i < count; i++) {
+      const c2g::EigJob jb{n[i], 0, og, oe, ou};
+      (n[i] <= c2g::kBatchedEigMax ? small : large).push_back(jb);
+      if (n[i] > c2g::kBatchedEigMax) nmax = std::max(nmax, n[i]);
+      og += static_cast<int64_t>(n[i]) * n[i];
+      oe += n[i];
+      ou += static_cast<int64_t>(n[i]) * n[i];
+    }
+    double* d = nullptr;
+    c2g::EigJob* dj = nullptr;
+    C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), sizeof(double) * (2 * tot + totn)));
+    C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dj), sizeof(c2g::EigJob) * count));
+    std::vector<c2g::EigJob> all(small);
+    all.insert(all.end(), large.begin(), large.end());
+    C2G_CUDA(cudaMemcpy(d, mats, sizeof(double) * tot, cudaMemcpyHostToDevice));
+    C2G_CUDA(cudaMemcpy(dj, all.data(), sizeof(c2g::EigJob) * count, cudaMemcpyHostToDevice));
+    if (!small.empty()) C2G_CUDA(c2g::launch_batched_eig(dj, static_cast<int>(small.size()), d, nullptr));
+    if (!large.empty())
+      C2G_CUDA(c2g::launch_batched_eig_large(dj + small.size(), static_cast<int>(large.size()), nmax, d, nullptr));
+    C2G_CUDA(cudaDeviceSynchronize());
+    C2G_CUDA(cudaMemcpy(evals, d + tot, sizeof(double) * totn, cudaMemcpyDeviceToHost));
+    C2G_CUDA(cudaMemcpy(evecs, d + tot + totn, sizeof(double) * tot, cudaMemcpyDeviceToHost));
+    cudaFree(dj);
+    cudaFree(d);
+  });
+}
+
 int c2g_host_rand_sample(unsigned int seed, int n, int* out) {
   return guarded([&] {
     if (n < 0) throw std::invalid_argument("c2g_host_rand_sample: negative count");

@@ -234,6 +234,12 @@ struct EigJob {
   int64_t offG, offE, offU;
 };
 cudaError_t launch_batched_eig(const EigJob* jobs, int njobs, double* base, cudaStream_t stream);
+// The same for kBatchedEigMax < n <= kBatchedEigLargeMax: one 512-thread CTA per matrix
+// with the matrix in dynamic shared memory and the eigenvector columns rotated in place
+// in global memory (the Gram matrix's own slot, which the matrix is read from first).
+// nmax: the largest n among the jobs (sizes the shared memory).
+constexpr int kBatchedEigLargeMax = 128;
+cudaError_t launch_batched_eig_large(const EigJob* jobs, int njobs, int nmax, double* base, cudaStream_t stream);
 cudaError_t launch_residual(double* t, const double* u, const double* evals, int64_t n, cudaStream_t stream);
 cudaError_t launch_precond_w(double* w, const double* u, const double* diag, const double* evals, double cutoff,
                              int64_t n, cudaStream_t stream);

@@ -470,6 +470,173 @@ cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* 
   return cudaGetLastError();
 }
 
+// Cyclic Jacobi as in jacobi_eig, for kBatchedEigMax < n <= kBatchedEigLargeMax: the
+// matrix A (n x (n + 1), padded rows) lives in dynamic shared memory; each round's n / 2
+// disjoint plane rotations update the rows p, q and then the columns p, q of A in place,
+// and the same columns of the eigenvector matrix V, which is kept in global memory at the
+// job's Gram slot (read into A first). Output as batched_eig_kernel: eigenvalues ascending
+// at offE, eigenvectors in descending order of the eigenvalue with the sign gauge at offU.
+constexpr int kEigLargeThreads = 512;
+struct EigLargeShared {
+  double cs[kBatchedEigLargeMax / 2], sn[kBatchedEigLargeMax / 2];
+  int pp[kBatchedEigLargeMax / 2], qq[kBatchedEigLargeMax / 2];
+  int pos[kBatchedEigLargeMax];
+  int order[kBatchedEigLargeMax];
+  double sgn[kBatchedEigLargeMax];
+  double red[2][kEigLargeThreads / 32];
+};
+
+__global__ void __launch_bounds__(kEigLargeThreads) batched_eig_large_kernel(const EigJob* __restrict__ jobs,
+                                                                             double* __restrict__ base) {
+  extern __shared__ double dyn[];
+  __shared__ EigLargeShared sh;
+  const EigJob jb = jobs[blockIdx.x];
+  const int n = jb.n, ldA = n + 1;
+  double* A = dyn;                  // A[i + ldA j] is element (i, j)... stored row-major: A[i * ldA + j]
+  double* V = base + jb.offG;       // V(i, j) = V[i + n j]
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e % n, j = e / n;
+    A[i * ldA + j] = V[i + static_cast<int64_t>(n) * j];
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e % n, j = e / n;
+    V[i + static_cast<int64_t>(n) * j] = (i == j) ? 1.0 : 0.0;
+  }
+  const int m = (n % 2 == 0) ? n : n + 1;
+  const int npair = m / 2;
+  if (tid < m) sh.pos[tid] = tid;
+  __syncthreads();
+  for (int sweep = 0; sweep < 30; sweep++) {
+    double off = 0.0, tot = 0.0;
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e % n, j = e / n;
+      const double v = A[i * ldA + j] * A[i * ldA + j];
+      tot += v;
+      if (i != j) off += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_down_sync(0xffffffffu, off, o);
+      tot += __shfl_down_sync(0xffffffffu, tot, o);
+    }
+    if ((tid & 31) == 0) {
+      sh.red[0][tid >> 5] = off;
+      sh.red[1][tid >> 5] = tot;
+    }
+    __syncthreads();
+    off = 0.0;
+    tot = 0.0;
+    for (int w = 0; w < nt / 32; w++) {
+      off += sh.red[0][w];
+      tot += sh.red[1][w];
+    }
+    __syncthreads();
+    if (!(off > 1e-28 * tot)) break;
+    for (int round = 0; round < m - 1; round++) {
+      if (tid < npair) {
+        int p = sh.pos[tid], q = sh.pos[m - 1 - tid];
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        double c = 1.0, s = 0.0;
+        if (q < n) {
+          const double apq = A[p * ldA + q];
+          if (apq != 0.0) {
+            const double tau = (A[q * ldA + q] - A[p * ldA + p]) / (2.0 * apq);
+            const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        } else {
+          q = p;  // the dummy plane of an odd n: no rotation
+        }
+        sh.cs[tid] = c;
+        sh.sn[tid] = s;
+        sh.pp[tid] = p;
+        sh.qq[tid] = q;
+      }
+      __syncthreads();
+      // rows p, q of every plane: A <- J^T A
+      for (int e = tid; e < npair * n; e += nt) {
+        const int k = e / n, j = e % n;
+        const int p = sh.pp[k], q = sh.qq[k];
+        if (p == q) continue;
+        const double c = sh.cs[k], s = sh.sn[k];
+        const double a = A[p * ldA + j], b = A[q * ldA + j];
+        A[p * ldA + j] = c * a - s * b;
+        A[q * ldA + j] = s * a + c * b;
+      }
+      __syncthreads();
+      // columns p, q: A <- A J, V <- V J
+      for (int e = tid; e < npair * n; e += nt) {
+        const int k = e / n, i = e % n;
+        const int p = sh.pp[k], q = sh.qq[k];
+        if (p == q) continue;
+        const double c = sh.cs[k], s = sh.sn[k];
+        const double a = A[i * ldA + p], b = A[i * ldA + q];
+        A[i * ldA + p] = c * a - s * b;
+        A[i * ldA + q] = s * a + c * b;
+        double* vp = V + static_cast<int64_t>(n) * p;
+        double* vq = V + static_cast<int64_t>(n) * q;
+        const double x = vp[i], y = vq[i];
+        vp[i] = c * x - s * y;
+        vq[i] = s * x + c * y;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const int last = sh.pos[m - 1];
+        for (int k = m - 1; k > 1; k--) sh.pos[k] = sh.pos[k - 1];
+        sh.pos[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  if (tid == 0) {
+    for (int i = 0; i < n; i++) sh.order[i] = i;
+    for (int i = 0; i < n; i++) {  // selection sort, ascending
+      int best = i;
+      for (int j = i + 1; j < n; j++)
+        if (A[sh.order[j] * ldA + sh.order[j]] < A[sh.order[best] * ldA + sh.order[best]]) best = j;
+      const int t = sh.order[i];
+      sh.order[i] = sh.order[best];
+      sh.order[best] = t;
+    }
+  }
+  __syncthreads();
+  if (tid < n) {
+    base[jb.offE + tid] = A[sh.order[tid] * ldA + sh.order[tid]];
+    const double* col = V + static_cast<int64_t>(n) * sh.order[n - 1 - tid];  // output column tid
+    double best = -1.0, v = 0.0;
+    for (int i = 0; i < n; i++) {
+      const double a = fabs(col[i]);
+      if (a > best) {
+        best = a;
+        v = col[i];
+      }
+    }
+    sh.sgn[tid] = (v < 0.0) ? -1.0 : 1.0;
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e % n, j = e / n;
+    base[jb.offU + i + static_cast<int64_t>(n) * j] = sh.sgn[j] * V[i + static_cast<int64_t>(n) * sh.order[n - 1 - j]];
+  }
+}
+
+cudaError_t launch_batched_eig_large(const EigJob* jobs, int njobs, int nmax, double* base, cudaStream_t stream) {
+  if (njobs <= 0) return cudaSuccess;
+  if (nmax > kBatchedEigLargeMax) return cudaErrorInvalidValue;
+  const size_t bytes = sizeof(double) * static_cast<size_t>(nmax) * (nmax + 1);
+  cudaError_t e = cudaFuncSetAttribute(batched_eig_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(bytes));
+  if (e != cudaSuccess) return e;
+  batched_eig_large_kernel<<<njobs, kEigLargeThreads, bytes, stream>>>(jobs, base);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_batched_eig(const EigJob* jobs, int njobs, double* base, cudaStream_t stream) {
   if (njobs <= 0) return cudaSuccess;
   batched_eig_kernel<<<njobs, 256, 0, stream>>>(jobs, base);

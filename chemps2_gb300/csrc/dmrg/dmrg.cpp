@@ -924,16 +924,31 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     rt->run(dp, svec, nullptr);
   }
   // Eigendecomposition of every Gram matrix (FP64): sectors up to kBatchedEigMax in one
-  // batched Jacobi launch, larger ones with cuSOLVER syevd.
+  // batched Jacobi launch, those up to kBatchedEigLargeMax in a second one (all sectors
+  // of a launch at once, one CTA each), larger ones with cuSOLVER syevd.
   std::vector<c2g::EigJob> jobs;
+  int nsmall = 0, nmax_large = 0;
   for (const auto& c : plan.centers)
     if (c.cd > 0 && c.g <= c2g::kBatchedEigMax) jobs.push_back(c2g::EigJob{c.g, 0, c.offG, c.offE, c.offU});
+  nsmall = static_cast<int>(jobs.size());
+  for (const auto& c : plan.centers)
+    if (c.cd > 0 && c.g > c2g::kBatchedEigMax && c.g <= c2g::kBatchedEigLargeMax) {
+      jobs.push_back(c2g::EigJob{c.g, 0, c.offG, c.offE, c.offU});
+      nmax_large = std::max(nmax_large, c.g);
+    }
   if (!jobs.empty()) {
     c2g::EigJob* djobs = nullptr;
     C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&djobs), sizeof(c2g::EigJob) * jobs.size(), s));
     C2G_CUDA(cudaMemcpyAsync(djobs, jobs.data(), sizeof(c2g::EigJob) * jobs.size(), cudaMemcpyHostToDevice, s));
-    C2G_CUDA(c2g::launch_batched_eig(djobs, static_cast<int>(jobs.size()), work, s));
-    c2g::count_launches(1);
+    if (nsmall > 0) {
+      C2G_CUDA(c2g::launch_batched_eig(djobs, nsmall, work, s));
+      c2g::count_launches(1);
+    }
+    const int nlarge = static_cast<int>(jobs.size()) - nsmall;
+    if (nlarge > 0) {
+      C2G_CUDA(c2g::launch_batched_eig_large(djobs + nsmall, nlarge, nmax_large, work, s));
+      c2g::count_launches(1);
+    }
     rt->sync();  // `jobs` is pageable host memory
     C2G_CUDA(cudaFreeAsync(djobs, s));
   }
@@ -945,7 +960,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   }
   cusolverDnHandle_t sh = static_cast<cusolverDnHandle_t>(solver_);
   int gmax = 0;
-  for (const auto& c : plan.centers) gmax = std::max(gmax, (c.cd > 0 && c.g > c2g::kBatchedEigMax) ? c.g : 0);
+  for (const auto& c : plan.centers) gmax = std::max(gmax, (c.cd > 0 && c.g > c2g::kBatchedEigLargeMax) ? c.g : 0);
   int lwork = 0;
   double* dwork = nullptr;
   int* dinfo = nullptr;
@@ -959,7 +974,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   }
   for (size_t ic = 0; ic < plan.centers.size(); ic++) {
     const auto& c = plan.centers[ic];
-    if (c.cd <= 0 || c.g <= c2g::kBatchedEigMax) continue;
+    if (c.cd <= 0 || c.g <= c2g::kBatchedEigLargeMax) continue;
     int lw = 0;
     check_solver(cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, c.g, work + c.offG,
                                              c.g, work + c.offE, &lw),

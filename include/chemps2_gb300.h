@@ -187,6 +187,13 @@ int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double*
 int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* schemes, const unsigned int* seeds,
                     int workers, double* energies, long long* matvecs, double* seconds, int* statuses,
                     double* stats);
+/* The FP64 eigensolver of the truncation step (CheMPS2/Sobject.cpp:418, where the
+ * reference calls dgesdd on the sector matrices; here the Gram matrices are diagonalised)
+ * for matrices of order 1..128, exposed for testing: `count` symmetric matrices of orders
+ * n[i], column-major and concatenated in `mats`; evals receives each matrix's eigenvalues
+ * in ascending order (concatenated), evecs its eigenvectors in descending order of the
+ * eigenvalue, each column signed so that its largest-magnitude entry is positive. */
+int c2g_truncation_eig(int count, const int* n, const double* mats, double* evals, double* evecs);
 /* The first n draws of the private random generator a batch member seeded with `seed`
  * uses (equal to srand(seed); rand() of the GNU C library). No GPU needed. */
 int c2g_host_rand_sample(unsigned int seed, int n, int* out);
