@@ -936,21 +936,27 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
       jobs.push_back(c2g::EigJob{c.g, 0, c.offG, c.offE, c.offU});
       nmax_large = std::max(nmax_large, c.g);
     }
+  // The batched kernels run on the auxiliary stream, overlapping the syevd calls below on
+  // the main one; the main stream joins them before the eigenvalues are read. `jobs`
+  // (pageable) stays alive until that final synchronisation.
+  bool forked = false;
   if (!jobs.empty()) {
+    rt->fork_aux();
+    forked = true;
+    cudaStream_t a = rt->aux_stream();
     c2g::EigJob* djobs = nullptr;
-    C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&djobs), sizeof(c2g::EigJob) * jobs.size(), s));
-    C2G_CUDA(cudaMemcpyAsync(djobs, jobs.data(), sizeof(c2g::EigJob) * jobs.size(), cudaMemcpyHostToDevice, s));
+    C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&djobs), sizeof(c2g::EigJob) * jobs.size(), a));
+    C2G_CUDA(cudaMemcpyAsync(djobs, jobs.data(), sizeof(c2g::EigJob) * jobs.size(), cudaMemcpyHostToDevice, a));
     if (nsmall > 0) {
-      C2G_CUDA(c2g::launch_batched_eig(djobs, nsmall, work, s));
+      C2G_CUDA(c2g::launch_batched_eig(djobs, nsmall, work, a));
       c2g::count_launches(1);
     }
     const int nlarge = static_cast<int>(jobs.size()) - nsmall;
     if (nlarge > 0) {
-      C2G_CUDA(c2g::launch_batched_eig_large(djobs + nsmall, nlarge, nmax_large, work, s));
+      C2G_CUDA(c2g::launch_batched_eig_large(djobs + nsmall, nlarge, nmax_large, work, a));
       c2g::count_launches(1);
     }
-    rt->sync();  // `jobs` is pageable host memory
-    C2G_CUDA(cudaFreeAsync(djobs, s));
+    C2G_CUDA(cudaFreeAsync(djobs, a));
   }
   if (!solver_) {
     cusolverDnHandle_t h = nullptr;
@@ -991,6 +997,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     C2G_CUDA(c2g::launch_reverse_columns(work + c.offU, work + c.offG, c.g, c.g, s));
     c2g::count_launches(1);
   }
+  if (forked) rt->join_aux();
   std::vector<double> evals(plan.work_size > 0 ? plan.work_size : 1);
   std::vector<int> info(std::max<size_t>(plan.centers.size(), 1));
   // only the eigenvalue segments are needed; copy each

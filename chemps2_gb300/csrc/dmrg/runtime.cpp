@@ -92,6 +92,12 @@ Runtime::~Runtime() {
   cudaFree(partial_);
   if (staging_) cudaFreeHost(staging_);
   if (pinned_) cudaFreeHost(pinned_);
+  if (aux_) {
+    cudaStreamSynchronize(aux_);
+    cudaStreamDestroy(aux_);
+  }
+  if (fork_ev_) cudaEventDestroy(fork_ev_);
+  if (join_ev_) cudaEventDestroy(join_ev_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -843,6 +849,30 @@ void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPt
   count_launches((ds.njtiles > 0) + (ds.nstiles > 0) + (ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
 }
 
-void Runtime::sync() { C2G_CUDA(cudaStreamSynchronize(stream_)); }
+void Runtime::sync() {
+  C2G_CUDA(cudaStreamSynchronize(stream_));
+  if (aux_) C2G_CUDA(cudaStreamSynchronize(aux_));
+}
+
+cudaStream_t Runtime::aux_stream() {
+  if (!aux_) {
+    C2G_CUDA(cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking));
+    C2G_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
+    C2G_CUDA(cudaEventCreateWithFlags(&join_ev_, cudaEventDisableTiming));
+  }
+  return aux_;
+}
+
+void Runtime::fork_aux() {
+  cudaStream_t a = aux_stream();
+  C2G_CUDA(cudaEventRecord(fork_ev_, stream_));
+  C2G_CUDA(cudaStreamWaitEvent(a, fork_ev_, 0));
+}
+
+void Runtime::join_aux() {
+  if (!aux_) return;
+  C2G_CUDA(cudaEventRecord(join_ev_, aux_));
+  C2G_CUDA(cudaStreamWaitEvent(stream_, join_ev_, 0));
+}
 
 }  // namespace c2g

@@ -82,6 +82,11 @@ class Runtime {
   Runtime& operator=(const Runtime&) = delete;
 
   cudaStream_t stream() const { return stream_; }
+  // A second stream for work that overlaps the main one (created on first use), and a
+  // fork / join of it with the main stream.
+  cudaStream_t aux_stream();
+  void fork_aux();  // aux waits for everything issued on the main stream so far
+  void join_aux();  // the main stream waits for everything issued on aux so far
   int L() const { return L_; }
 
   // Device memory, stream ordered on this runtime's stream.
@@ -125,6 +130,8 @@ class Runtime {
 
   int L_;
   cudaStream_t stream_ = nullptr;
+  cudaStream_t aux_ = nullptr;
+  cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;
   std::vector<double*> host_slots_;
   std::vector<float*> host_slots32_;
   const double** dev_slots_ = nullptr;
