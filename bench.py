@@ -402,6 +402,55 @@ def extra_config3(args):
     print(json.dumps({"extra": "precision_l30_d2000", **out}), flush=True)
 
 
+def extra_hubbard(args):
+    """Large sector blocks: the Hubbard chain L = N = 20, U = 4, C1, D = 512 swept --sweeps
+    times, right-hand operators renormalized down to the middle, then --steps FP64 and FP32
+    matvecs at sites (9, 10) (the two-pass path of large groups carries most of the work).
+    With --profile n: n FP64 matvecs between cudaProfilerStart/Stop, nothing printed."""
+    import torch
+
+    import chemps2_gb300 as c2g
+    from chemps2_gb300.models import hubbard
+
+    L, mid = 20, 9
+    m = hubbard(L, 4.0)
+    ham = c2g.Hamiltonian(L, 0, m.irreps)
+    for i in range(L - 1):
+        ham.setTmat(i, i + 1, -1.0)
+    for i in range(L):
+        ham.setVmat(i, i, i, i, 4.0)
+    prob = c2g.Problem(ham, 0, L, 0)
+    scheme = c2g.ConvergenceScheme(1)
+    scheme.set_instruction(0, 512, 1e-10, args.sweeps, 0.0, 1e-8)
+    c2g.srand(7)
+    d = c2g.DMRG(prob, scheme)
+    t0 = time.perf_counter()
+    e = d.Solve()
+    solve_s = time.perf_counter() - t0
+    for index in range(L - 2, mid, -1):
+        d.update(index, False)
+    d.bench_heff(mid, args.warmup, 0, 0)
+    if args.profile:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        d.bench_heff(mid, 0, args.profile, 0)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        d.close()
+        return
+    r64 = d.bench_heff(mid, 0, args.steps, L2_FLUSH_BYTES)
+    d.bench_heff(mid, args.warmup, 0, 0, precision="fp32")
+    r32 = d.bench_heff(mid, 0, args.steps, L2_FLUSH_BYTES, precision="fp32")
+    d.close()
+    out = {"config": f"hubbard L=20 N=20 U=4 C1 D=512, {args.sweeps} sweep(s), matvec at sites (9,10)",
+           "solve_s": solve_s, "energy": e,
+           "fp64": {"ms_per_matvec": r64["ms_per_matvec"], "gflops": r64["flops"] / r64["ms_per_matvec"] / 1e6,
+                    "launches_per_matvec": r64["launches"] / max(args.steps, 1)},
+           "fp32": {"ms_per_matvec": r32["ms_per_matvec"], "gflops": r32["flops"] / r32["ms_per_matvec"] / 1e6},
+           "ledger_flops_per_matvec": r64["flops"]}
+    print(json.dumps({"extra": "hubbard_l20_d512", **out}), flush=True)
+
+
 def batch_objects(members, sweeps):
     import chemps2_gb300 as c2g
 
@@ -482,7 +531,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-sweep", action="store_true", help="skip the sweep timing")
-    ap.add_argument("--extra", choices=["config3", "batch"], default=None,
+    ap.add_argument("--extra", choices=["config3", "batch", "hubbard"], default=None,
                     help="run one of the further configurations instead (prints its own JSON line)")
     ap.add_argument("--sweeps", type=int, default=2, help="sweeps per problem for --extra")
     ap.add_argument("--batch-count", type=int, default=64, help="problems for --extra batch")
@@ -496,6 +545,8 @@ def main():
         extra_config3(args)
     elif args.extra == "batch":
         extra_batch(args)
+    elif args.extra == "hubbard":
+        extra_hubbard(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
