@@ -111,6 +111,10 @@ enum class Precision : int { kFP64 = 0, kFP32 = 1 };
 
 cudaError_t launch_inter_gemm(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp,
                               cudaStream_t stream, Precision prec);
+// Pass 1 for the jobs list[0 .. njobs) with m n <= kInterSmallElems: one warp per job.
+constexpr int kInterSmallElems = 256;
+cudaError_t launch_inter_small(const InterJob* jobs, const int32_t* list, int njobs, const SlotPtrs& sp,
+                               cudaStream_t stream, Precision prec);
 cudaError_t launch_sum_gemm(const SumGroup* groups, const SumItem* items, const GemmTile* tiles, int ntiles,
                             double* partials, unsigned int* counters, const SlotPtrs& sp, cudaStream_t stream,
                             Precision prec);

@@ -140,6 +140,56 @@ __global__ void __launch_bounds__(kGemmThreads, 2)
 #undef C2G_INTER
 }
 
+// Pass 1 for small jobs (m n <= 256): one warp per job, each lane a run of output
+// elements, each element a dot product over k read straight from global memory (L1).
+// A tile-shaped CTA would spend most of its time staging a few operand values; here no
+// multiply-add runs on padding except in the last group of 32 elements, and in FP64 two
+// loads per multiply-add stay below what the FP64 pipe consumes.
+template <typename Real, int NQ>
+__device__ __forceinline__ void small_job(const InterJob& J, const SlotPtrs& sp, int lane) {
+  const Opnd<Real> L = opnd<Real>(sp, J.l), R = opnd<Real>(sp, J.r);
+  const int mn = J.m * J.n;
+  int r[NQ], c[NQ];
+  bool v[NQ];
+  Real acc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int e = lane + 32 * q;
+    v[q] = e < mn;
+    r[q] = v[q] ? e % J.m : 0;
+    c[q] = v[q] ? e / J.m : 0;
+    acc[q] = Real(0);
+  }
+  for (int k = 0; k < J.k; k++) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) acc[q] = fmaR(L.at(r[q], k), R.at(k, c[q]), acc[q]);
+  }
+  Real* S = const_cast<Real*>(Tables<Real>::get(sp, kSlotInter)) + J.off;
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+    if (v[q]) S[r[q] + static_cast<int64_t>(J.m) * c[q]] = acc[q];
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(256)
+    inter_small_kernel(const InterJob* __restrict__ jobs, const int32_t* __restrict__ list, int njobs, SlotPtrs sp) {
+  const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (w >= njobs) return;
+  const InterJob J = jobs[list[w]];
+  const int lane = threadIdx.x & 31;
+  switch ((J.m * J.n + 31) / 32) {
+    case 1: small_job<Real, 1>(J, sp, lane); break;
+    case 2: small_job<Real, 2>(J, sp, lane); break;
+    case 3: small_job<Real, 3>(J, sp, lane); break;
+    case 4: small_job<Real, 4>(J, sp, lane); break;
+    case 5: small_job<Real, 5>(J, sp, lane); break;
+    case 6: small_job<Real, 6>(J, sp, lane); break;
+    case 7: small_job<Real, 7>(J, sp, lane); break;
+    case 8: small_job<Real, 8>(J, sp, lane); break;
+    default: break;
+  }
+}
+
 template <typename Real, int PM, int PN>
 __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, const SumItem* __restrict__ items,
                                          double* partials, unsigned int* counters, const SlotPtrs& sp,
@@ -243,6 +293,17 @@ cudaError_t launch_inter_gemm(const InterJob* jobs, const GemmTile* tiles, int n
     inter_gemm_kernel<float><<<ntiles, kGemmThreads, 0, stream>>>(jobs, tiles, sp);
   else
     inter_gemm_kernel<double><<<ntiles, kGemmThreads, 0, stream>>>(jobs, tiles, sp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inter_small(const InterJob* jobs, const int32_t* list, int njobs, const SlotPtrs& sp,
+                               cudaStream_t stream, Precision prec) {
+  if (njobs <= 0) return cudaSuccess;
+  const int grid = (njobs + 7) / 8;
+  if (prec == Precision::kFP32)
+    inter_small_kernel<float><<<grid, 256, 0, stream>>>(jobs, list, njobs, sp);
+  else
+    inter_small_kernel<double><<<grid, 256, 0, stream>>>(jobs, list, njobs, sp);
   return cudaGetLastError();
 }
 

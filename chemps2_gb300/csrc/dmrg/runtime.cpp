@@ -277,6 +277,7 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
   struct TwoPass {
     std::vector<InterJob> jobs;
     std::vector<GemmTile> jtiles;
+    std::vector<int32_t> small;  // jobs of at most kInterSmallElems elements
     std::vector<SumGroup> groups;
     std::vector<SumItem> items;
     std::vector<GemmTile> stiles;
@@ -560,14 +561,18 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
               it.k = T.k1;
             }
             inter_off += (static_cast<int64_t>(J.m) * J.n + 3) & ~int64_t(3);
-            for (int i = 0; i < (J.m + 63) / 64; i++)
-              for (int j = 0; j < (J.n + 63) / 64; j++) {
-                GemmTile gt{};
-                gt.idx = static_cast<int32_t>(tp.jobs.size());
-                gt.pos = (i << 16) | j;
-                gt.shape = tile_shape(std::min(64, J.m - 64 * i), std::min(64, J.n - 64 * j));
-                tp.jtiles.push_back(gt);
-              }
+            if (static_cast<int64_t>(J.m) * J.n <= kInterSmallElems) {
+              tp.small.push_back(static_cast<int32_t>(tp.jobs.size()));
+            } else {
+              for (int i = 0; i < (J.m + 63) / 64; i++)
+                for (int j = 0; j < (J.n + 63) / 64; j++) {
+                  GemmTile gt{};
+                  gt.idx = static_cast<int32_t>(tp.jobs.size());
+                  gt.pos = (i << 16) | j;
+                  gt.shape = tile_shape(std::min(64, J.m - 64 * i), std::min(64, J.n - 64 * j));
+                  tp.jtiles.push_back(gt);
+                }
+            }
             tp.jobs.push_back(J);
           } else if (ha) {
             it.l = A;
@@ -729,6 +734,7 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     }
     part_doubles = std::max(part_doubles, part_off);
     ncounters = std::max(ncounters, counter);
+    tile_bytes += align256(sizeof(int32_t) * tp.small.size());
     tile_bytes += align256(sizeof(InterJob) * tp.jobs.size()) + align256(sizeof(GemmTile) * tp.jtiles.size()) +
                   align256(sizeof(SumGroup) * tp.groups.size()) + align256(sizeof(SumItem) * tp.items.size()) +
                   align256(sizeof(GemmTile) * tp.stiles.size());
@@ -771,6 +777,8 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     ds.jobs = static_cast<const InterJob*>(put(tp.jobs.data(), sizeof(InterJob) * tp.jobs.size()));
     ds.jtiles = static_cast<const GemmTile*>(put(tp.jtiles.data(), sizeof(GemmTile) * tp.jtiles.size()));
     ds.njtiles = static_cast<int>(tp.jtiles.size());
+    ds.jsmall = static_cast<const int32_t*>(put(tp.small.data(), sizeof(int32_t) * tp.small.size()));
+    ds.njsmall = static_cast<int>(tp.small.size());
     ds.sgroups = static_cast<const SumGroup*>(put(tp.groups.data(), sizeof(SumGroup) * tp.groups.size()));
     ds.sitems = static_cast<const SumItem*>(put(tp.items.data(), sizeof(SumItem) * tp.items.size()));
     ds.stiles = static_cast<const GemmTile*>(put(tp.stiles.data(), sizeof(GemmTile) * tp.stiles.size()));
@@ -839,6 +847,7 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
 // disjoint output blocks).
 void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec) {
   C2G_CUDA(launch_inter_gemm(ds.jobs, ds.jtiles, ds.njtiles, sp, stream_, prec));
+  C2G_CUDA(launch_inter_small(ds.jobs, ds.jsmall, ds.njsmall, sp, stream_, prec));
   C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, p.gemm_partials, p.gemm_counters, sp,
                            stream_, prec));
   C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
@@ -846,7 +855,7 @@ void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPt
   const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, p.partials, p.counters};
   C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, prec, &nw));
   C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
-  count_launches((ds.njtiles > 0) + (ds.nstiles > 0) + (ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
+  count_launches((ds.njtiles > 0) + (ds.njsmall > 0) + (ds.nstiles > 0) + (ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
 }
 
 void Runtime::sync() {

@@ -44,7 +44,8 @@ struct DevStage {
   const SumGroup* sgroups = nullptr;
   const SumItem* sitems = nullptr;
   const GemmTile* stiles = nullptr;
-  int njtiles = 0, nstiles = 0;
+  const int32_t* jsmall = nullptr;  // pass-1 jobs run one per warp
+  int njtiles = 0, nstiles = 0, njsmall = 0;
   int64_t flops = 0, items = 0;
   std::string name;
 };
