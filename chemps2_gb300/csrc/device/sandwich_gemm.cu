@@ -2,10 +2,11 @@
 //
 // Both passes run the same CTA-level GEMM on an output tile of at most 64 x 64 placed on
 // a 64 x 64 grid: 256 threads in a 16 x 16 layout, thread (ty, tx) holding rows
-// ty PM .. ty PM + PM - 1 and columns tx + 16 jj (jj < PN) of the tile, where PM and PN
+// ty PM .. ty PM + PM - 1 and columns tx PN .. tx PN + PN - 1 of the tile, where PM and PN
 // (1 to 4) are the tile's extents in units of 16, chosen per tile on the host. The
 // operands are staged through shared memory in chunks of 16 along the inner dimension,
-// loaded with the unit-stride index fastest for either storage order of each operand.
+// loaded with the unit-stride index fastest for either storage order of each operand, and
+// read back as contiguous runs (16-byte reads: one per operand and step for FP32 4 x 4).
 // In FP64 the GEMM is bound by the FP64 pipe (two FMAs per SM and clock on this GPU), so
 // no FMA may be issued twice or on padding: every intermediate is formed once in pass 1,
 // tile extents follow the block to 16 columns, and warps whose rows lie past the block
@@ -37,13 +38,45 @@ __device__ __forceinline__ Opnd<Real> opnd(const SlotPtrs& sp, const GemmOperand
   return Opnd<Real>{resolve<Real>(sp, g.ref), g.ld, g.trans != 0};
 }
 
+// rows of 68 elements keep every row 16-byte aligned for vector reads (FP32 and FP64)
+constexpr int kGLd = 68;
 template <typename Real>
-struct GSmem {
-  Real L[kKC][64 + 1];
-  Real R[kKC][64 + 1];
+struct __align__(16) GSmem {
+  Real L[kKC][kGLd];
+  Real R[kKC][kGLd];
 };
 
-// part (rows ty PM + ii, columns tx + 16 jj) = sum_{k < K} L(i, k) R(k, j) over i < M,
+// v[0 .. P) = p[0 .. P) from shared memory, in 16-byte (or 8-byte) reads where the run's
+// length and alignment allow (p is aligned to P elements)
+template <int P>
+__device__ __forceinline__ void lds_run(float (&v)[P], const float* p) {
+  if constexpr (P == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else if constexpr (P == 2) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x; v[1] = t.y;
+  } else {
+#pragma unroll
+    for (int i = 0; i < P; i++) v[i] = p[i];
+  }
+}
+template <int P>
+__device__ __forceinline__ void lds_run(double (&v)[P], const double* p) {
+  if constexpr (P == 2 || P == 4) {
+#pragma unroll
+    for (int i = 0; i < P; i += 2) {
+      const double2 t = *reinterpret_cast<const double2*>(p + i);
+      v[i] = t.x;
+      v[i + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < P; i++) v[i] = p[i];
+  }
+}
+
+// part (rows ty PM + ii, columns tx PN + jj) = sum_{k < K} L(i, k) R(k, j) over i < M,
 // j < N (zero elsewhere); M <= 16 PM, N <= 16 PN
 template <typename Real, int PM, int PN>
 __device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>& L, int M, const Opnd<Real>& R,
@@ -88,10 +121,8 @@ __device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>
       const int kn = min(kKC, K - k0);
       for (int kk = 0; kk < kn; kk++) {
         Real a[PM], b[PN];
-#pragma unroll
-        for (int ii = 0; ii < PM; ii++) a[ii] = sm.L[kk][ty * PM + ii];
-#pragma unroll
-        for (int jj = 0; jj < PN; jj++) b[jj] = sm.R[kk][tx + 16 * jj];
+        lds_run<PM>(a, &sm.L[kk][ty * PM]);
+        lds_run<PN>(b, &sm.R[kk][tx * PN]);
 #pragma unroll
         for (int ii = 0; ii < PM; ii++)
 #pragma unroll
@@ -116,7 +147,7 @@ __device__ __forceinline__ void inter_tile(const InterJob& J, int pos, const Slo
   for (int ii = 0; ii < PM; ii++)
 #pragma unroll
     for (int jj = 0; jj < PN; jj++) {
-      const int r = ty * PM + ii, c = tx + 16 * jj;
+      const int r = ty * PM + ii, c = tx * PN + jj;
       if (r < tm && c < tn) S[(row0 + r) + static_cast<int64_t>(J.m) * (col0 + c)] = part[ii][jj];
     }
 }
@@ -147,31 +178,40 @@ __global__ void __launch_bounds__(kGemmThreads, 2)
 // loads per multiply-add stay below what the FP64 pipe consumes.
 template <typename Real, int NQ>
 __device__ __forceinline__ void small_job(const InterJob& J, const SlotPtrs& sp, int lane) {
-  const Opnd<Real> L = opnd<Real>(sp, J.l), R = opnd<Real>(sp, J.r);
+  // element (i, k) of op(M) at M + i si + k sk
+  const int64_t lsi = J.l.trans ? J.l.ld : 1, lsk = J.l.trans ? 1 : J.l.ld;
+  const int64_t rsk = J.r.trans ? J.r.ld : 1, rsj = J.r.trans ? 1 : J.r.ld;
+  const Real* L = resolve<Real>(sp, J.l.ref);
+  const Real* R = resolve<Real>(sp, J.r.ref);
   const int mn = J.m * J.n;
-  int r[NQ], c[NQ];
-  bool v[NQ];
+  const Real* lp[NQ];
+  const Real* rp[NQ];
   Real acc[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; q++) {
-    const int e = lane + 32 * q;
-    v[q] = e < mn;
-    r[q] = v[q] ? e % J.m : 0;
-    c[q] = v[q] ? e / J.m : 0;
+    const int e = min(lane + 32 * q, mn - 1);  // lanes past the end repeat the last element
+    lp[q] = L + (e % J.m) * lsi;
+    rp[q] = R + (e / J.m) * rsj;
     acc[q] = Real(0);
   }
   for (int k = 0; k < J.k; k++) {
 #pragma unroll
-    for (int q = 0; q < NQ; q++) acc[q] = fmaR(L.at(r[q], k), R.at(k, c[q]), acc[q]);
+    for (int q = 0; q < NQ; q++) {
+      acc[q] = fmaR(*lp[q], *rp[q], acc[q]);
+      lp[q] += lsk;
+      rp[q] += rsk;
+    }
   }
   Real* S = const_cast<Real*>(Tables<Real>::get(sp, kSlotInter)) + J.off;
 #pragma unroll
-  for (int q = 0; q < NQ; q++)
-    if (v[q]) S[r[q] + static_cast<int64_t>(J.m) * c[q]] = acc[q];
+  for (int q = 0; q < NQ; q++) {
+    const int e = lane + 32 * q;
+    if (e < mn) S[(e % J.m) + static_cast<int64_t>(J.m) * (e / J.m)] = acc[q];
+  }
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
     inter_small_kernel(const InterJob* __restrict__ jobs, const int32_t* __restrict__ list, int njobs, SlotPtrs sp) {
   const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (w >= njobs) return;
@@ -214,7 +254,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
       for (int ii = 0; ii < PM; ii++)
 #pragma unroll
         for (int jj = 0; jj < PN; jj++) {
-          const int r = ty * PM + ii, c = tx + 16 * jj;
+          const int r = ty * PM + ii, c = tx * PN + jj;
           part[ii][jj] = (r < tm && c < tn) ? R.at(row0 + r, col0 + c) : Real(0);
         }
     }
@@ -231,7 +271,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
     for (int ii = 0; ii < PM; ii++)
 #pragma unroll
       for (int jj = 0; jj < PN; jj++)
-        __stcg(part + static_cast<int64_t>(T.split) * te + (ty * PM + ii) + TM * (tx + 16 * jj), acc[ii][jj]);
+        __stcg(part + static_cast<int64_t>(T.split) * te + (ty * PM + ii) + TM * (tx * PN + jj), acc[ii][jj]);
     __threadfence();
     __shared__ int is_last;
     __syncthreads();
@@ -245,7 +285,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
       for (int jj = 0; jj < PN; jj++) {
         double v = 0.0;
         for (int s = 0; s < T.nsplit; s++)
-          v += __ldcg(part + static_cast<int64_t>(s) * te + (ty * PM + ii) + TM * (tx + 16 * jj));
+          v += __ldcg(part + static_cast<int64_t>(s) * te + (ty * PM + ii) + TM * (tx * PN + jj));
         acc[ii][jj] = v;
       }
     if (tid == 0) counters[T.counter] = 0u;  // ready for the next launch
@@ -257,7 +297,7 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
   for (int ii = 0; ii < PM; ii++)
 #pragma unroll
     for (int jj = 0; jj < PN; jj++) {
-      const int r = ty * PM + ii, c = tx + 16 * jj;
+      const int r = ty * PM + ii, c = tx * PN + jj;
       if (r < tm && c < tn) {
         const int64_t idx = (row0 + r) + ldo * (col0 + c);
         O[idx] = accum ? O[idx] + acc[ii][jj] : acc[ii][jj];
