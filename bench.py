@@ -406,7 +406,8 @@ def extra_hubbard(args):
     """Large sector blocks: the Hubbard chain L = N = 20, U = 4, C1, D = 512 swept --sweeps
     times, right-hand operators renormalized down to the middle, then --steps FP64 and FP32
     matvecs at sites (9, 10) (the two-pass path of large groups carries most of the work).
-    With --profile n: n FP64 matvecs between cudaProfilerStart/Stop, nothing printed."""
+    With --profile n: n matvecs (--profile-precision) between cudaProfilerStart/Stop,
+    nothing printed."""
     import torch
 
     import chemps2_gb300 as c2g
@@ -431,9 +432,10 @@ def extra_hubbard(args):
         d.update(index, False)
     d.bench_heff(mid, args.warmup, 0, 0)
     if args.profile:
+        d.bench_heff(mid, args.warmup, 0, 0, precision=args.profile_precision)
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
-        d.bench_heff(mid, 0, args.profile, 0)
+        d.bench_heff(mid, 0, args.profile, 0, precision=args.profile_precision)
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
         d.close()
@@ -536,6 +538,8 @@ def main():
     ap.add_argument("--sweeps", type=int, default=2, help="sweeps per problem for --extra")
     ap.add_argument("--batch-count", type=int, default=64, help="problems for --extra batch")
     ap.add_argument("--workers", type=int, default=16, help="concurrent problems for --extra batch")
+    ap.add_argument("--profile-precision", choices=["fp64", "fp32"], default="fp64",
+                    help="arithmetic of the profiled matvecs of --extra hubbard --profile")
     ap.add_argument("--profile", type=int, default=0,
                     help="profiling mode: set up, then run this many matvecs between cudaProfilerStart/Stop")
     args = ap.parse_args()

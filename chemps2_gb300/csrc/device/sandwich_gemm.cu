@@ -153,7 +153,7 @@ __device__ __forceinline__ void inter_tile(const InterJob& J, int pos, const Slo
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(kGemmThreads, 2)
+__global__ void __launch_bounds__(kGemmThreads, sizeof(Real) == 4 ? 3 : 2)
     inter_gemm_kernel(const InterJob* __restrict__ jobs, const GemmTile* __restrict__ tiles, SlotPtrs sp) {
   __shared__ GSmem<Real> sm;
   const GemmTile T = tiles[blockIdx.x];
@@ -230,6 +230,51 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
+// One 16-deep chunk of the operands of a tile GEMM, staged in registers: the global
+// loads of the next chunk are issued before the current chunk's multiply-adds, so their
+// latency overlaps that work (also across item boundaries in pass 2).
+template <typename Real, int PM, int PN>
+struct ChunkRegs {
+  Real l[PM], r[PN];
+};
+
+template <typename Real, int PM, int PN>
+__device__ __forceinline__ void fetch_chunk(ChunkRegs<Real, PM, PN>& g, const Opnd<Real>& L, int M, const Opnd<Real>& R,
+                                            int N, int K, int k0) {
+  constexpr int TM = 16 * PM, TN = 16 * PN;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < PM; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int i = L.t ? e / kKC : e % TM, kk = L.t ? e % kKC : e / TM;
+    g.l[s] = (i < M && k0 + kk < K) ? L.at(i, k0 + kk) : Real(0);
+  }
+#pragma unroll
+  for (int s = 0; s < PN; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int j = R.t ? e % TN : e / kKC, kk = R.t ? e / TN : e % kKC;
+    g.r[s] = (j < N && k0 + kk < K) ? R.at(k0 + kk, j) : Real(0);
+  }
+}
+
+template <typename Real, int PM, int PN>
+__device__ __forceinline__ void store_chunk(const ChunkRegs<Real, PM, PN>& g, bool lt, bool rt, GSmem<Real>& sm) {
+  constexpr int TM = 16 * PM, TN = 16 * PN;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < PM; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int i = lt ? e / kKC : e % TM, kk = lt ? e % kKC : e / TM;
+    sm.L[kk][i] = g.l[s];
+  }
+#pragma unroll
+  for (int s = 0; s < PN; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int j = rt ? e % TN : e / kKC, kk = rt ? e / TN : e % kKC;
+    sm.R[kk][j] = g.r[s];
+  }
+}
+
 template <typename Real, int PM, int PN>
 __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, const SumItem* __restrict__ items,
                                          double* partials, unsigned int* counters, const SlotPtrs& sp,
@@ -238,30 +283,100 @@ __device__ __forceinline__ void sum_tile(const GemmTile& T, const SumGroup& G, c
   const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
   const int tm = min(TM, G.m - row0), tn = min(TN, G.n - col0);
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const bool active = (ty & ~1) * PM < tm;  // the warp holds rows of the block
   double acc[PM][PN];
 #pragma unroll
   for (int ii = 0; ii < PM; ii++)
 #pragma unroll
     for (int jj = 0; jj < PN; jj++) acc[ii][jj] = 0.0;
-  for (int it = T.item0; it < T.item1; it++) {
-    const SumItem I = items[it];
+  // items without an inner dimension: out += alpha op(R), straight from global memory
+  auto add_copy = [&](const SumItem& I) {
     const Opnd<Real> R = opnd<Real>(sp, I.r);
-    Real part[PM][PN];
-    if (I.k > 0) {
-      tile_gemm<Real, PM, PN>(part, opnd<Real>(sp, I.l).shift(row0, 0), tm, R.shift(0, col0), tn, I.k, sm);
-    } else {
-#pragma unroll
-      for (int ii = 0; ii < PM; ii++)
-#pragma unroll
-        for (int jj = 0; jj < PN; jj++) {
-          const int r = ty * PM + ii, c = tx * PN + jj;
-          part[ii][jj] = (r < tm && c < tn) ? R.at(row0 + r, col0 + c) : Real(0);
-        }
-    }
 #pragma unroll
     for (int ii = 0; ii < PM; ii++)
 #pragma unroll
-      for (int jj = 0; jj < PN; jj++) acc[ii][jj] = fma(I.alpha, static_cast<double>(part[ii][jj]), acc[ii][jj]);
+      for (int jj = 0; jj < PN; jj++) {
+        const int r = ty * PM + ii, c = tx * PN + jj;
+        if (r < tm && c < tn) acc[ii][jj] = fma(I.alpha, static_cast<double>(R.at(row0 + r, col0 + c)), acc[ii][jj]);
+      }
+  };
+  // the GEMM items, chunk by chunk, with the next chunk's loads in flight
+  int it = T.item0;
+  SumItem cur{};
+  bool have = false;
+  for (; it < T.item1; it++) {
+    cur = items[it];
+    if (cur.k > 0) {
+      have = true;
+      break;
+    }
+    add_copy(cur);
+  }
+  if (have) {
+    Opnd<Real> cL = opnd<Real>(sp, cur.l).shift(row0, 0), cR = opnd<Real>(sp, cur.r).shift(0, col0);
+    int k0 = 0;
+    ChunkRegs<Real, PM, PN> g;
+    fetch_chunk<Real, PM, PN>(g, cL, tm, cR, tn, cur.k, 0);
+    Real part[PM][PN];
+#pragma unroll
+    for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+      for (int jj = 0; jj < PN; jj++) part[ii][jj] = Real(0);
+    for (;;) {
+      store_chunk<Real, PM, PN>(g, cL.t, cR.t, sm);
+      __syncthreads();
+      const int kn = min(kKC, cur.k - k0);
+      const bool last = k0 + kKC >= cur.k;
+      SumItem nxt = cur;
+      Opnd<Real> nL = cL, nR = cR;
+      int nk0 = k0 + kKC;
+      bool more = true;
+      if (last) {
+        more = false;
+        for (int j = it + 1; j < T.item1; j++) {
+          const SumItem c2 = items[j];
+          if (c2.k > 0) {
+            nxt = c2;
+            it = j;
+            more = true;
+            break;
+          }
+          add_copy(c2);
+        }
+        if (more) {
+          nL = opnd<Real>(sp, nxt.l).shift(row0, 0);
+          nR = opnd<Real>(sp, nxt.r).shift(0, col0);
+          nk0 = 0;
+        }
+      }
+      if (more) fetch_chunk<Real, PM, PN>(g, nL, tm, nR, tn, nxt.k, nk0);
+      if (active) {
+        for (int kk = 0; kk < kn; kk++) {
+          Real a[PM], b[PN];
+          lds_run<PM>(a, &sm.L[kk][ty * PM]);
+          lds_run<PN>(b, &sm.R[kk][tx * PN]);
+#pragma unroll
+          for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+            for (int jj = 0; jj < PN; jj++) part[ii][jj] = fmaR(a[ii], b[jj], part[ii][jj]);
+        }
+      }
+      if (last) {
+#pragma unroll
+        for (int ii = 0; ii < PM; ii++)
+#pragma unroll
+          for (int jj = 0; jj < PN; jj++) {
+            acc[ii][jj] = fma(cur.alpha, static_cast<double>(part[ii][jj]), acc[ii][jj]);
+            part[ii][jj] = Real(0);
+          }
+      }
+      __syncthreads();
+      if (!more) break;
+      cur = nxt;
+      cL = nL;
+      cR = nR;
+      k0 = nk0;
+    }
   }
   if (T.nsplit > 1) {
     // store this split's partial tile; the last split to arrive adds them up in split order
