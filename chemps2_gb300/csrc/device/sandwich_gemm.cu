@@ -76,12 +76,57 @@ __device__ __forceinline__ void lds_run(double (&v)[P], const double* p) {
   }
 }
 
+// One 16-deep chunk of the operands of a tile GEMM, staged in registers: the global
+// loads of the next chunk are issued before the current chunk's multiply-adds, so their
+// latency overlaps that work (also across item boundaries in pass 2).
+template <typename Real, int PM, int PN>
+struct ChunkRegs {
+  Real l[PM], r[PN];
+};
+
+template <typename Real, int PM, int PN>
+__device__ __forceinline__ void fetch_chunk(ChunkRegs<Real, PM, PN>& g, const Opnd<Real>& L, int M, const Opnd<Real>& R,
+                                            int N, int K, int k0) {
+  constexpr int TM = 16 * PM, TN = 16 * PN;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < PM; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int i = L.t ? e / kKC : e % TM, kk = L.t ? e % kKC : e / TM;
+    g.l[s] = (i < M && k0 + kk < K) ? L.at(i, k0 + kk) : Real(0);
+  }
+#pragma unroll
+  for (int s = 0; s < PN; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int j = R.t ? e % TN : e / kKC, kk = R.t ? e / TN : e % kKC;
+    g.r[s] = (j < N && k0 + kk < K) ? R.at(k0 + kk, j) : Real(0);
+  }
+}
+
+template <typename Real, int PM, int PN>
+__device__ __forceinline__ void store_chunk(const ChunkRegs<Real, PM, PN>& g, bool lt, bool rt, GSmem<Real>& sm) {
+  constexpr int TM = 16 * PM, TN = 16 * PN;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < PM; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int i = lt ? e / kKC : e % TM, kk = lt ? e % kKC : e / TM;
+    sm.L[kk][i] = g.l[s];
+  }
+#pragma unroll
+  for (int s = 0; s < PN; s++) {
+    const int e = tid + kGemmThreads * s;
+    const int j = rt ? e % TN : e / kKC, kk = rt ? e / TN : e % kKC;
+    sm.R[kk][j] = g.r[s];
+  }
+}
+
 // part (rows ty PM + ii, columns tx PN + jj) = sum_{k < K} L(i, k) R(k, j) over i < M,
-// j < N (zero elsewhere); M <= 16 PM, N <= 16 PN
+// j < N (zero elsewhere); M <= 16 PM, N <= 16 PN. The next chunk's loads are in flight
+// while the current chunk is multiplied.
 template <typename Real, int PM, int PN>
 __device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>& L, int M, const Opnd<Real>& R,
                                           int N, int K, GSmem<Real>& sm) {
-  constexpr int TM = 16 * PM, TN = 16 * PN;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   // a warp holds rows (ty & ~1) PM .. (ty | 1) PM + PM - 1
   const bool active = (ty & ~1) * PM < M;
@@ -89,34 +134,13 @@ __device__ __forceinline__ void tile_gemm(Real (&part)[PM][PN], const Opnd<Real>
   for (int ii = 0; ii < PM; ii++)
 #pragma unroll
     for (int jj = 0; jj < PN; jj++) part[ii][jj] = Real(0);
+  if (K <= 0) return;
+  ChunkRegs<Real, PM, PN> g;
+  fetch_chunk<Real, PM, PN>(g, L, M, R, N, K, 0);
   for (int k0 = 0; k0 < K; k0 += kKC) {
-#pragma unroll
-    for (int s = 0; s < PM; s++) {
-      const int e = tid + kGemmThreads * s;  // TM x kKC elements
-      int i, kk;
-      if (!L.t) {
-        i = e % TM;
-        kk = e / TM;
-      } else {
-        kk = e % kKC;
-        i = e / kKC;
-      }
-      sm.L[kk][i] = (i < M && k0 + kk < K) ? L.at(i, k0 + kk) : Real(0);
-    }
-#pragma unroll
-    for (int s = 0; s < PN; s++) {
-      const int e = tid + kGemmThreads * s;  // kKC x TN elements
-      int j, kk;
-      if (!R.t) {
-        kk = e % kKC;
-        j = e / kKC;
-      } else {
-        j = e % TN;
-        kk = e / TN;
-      }
-      sm.R[kk][j] = (j < N && k0 + kk < K) ? R.at(k0 + kk, j) : Real(0);
-    }
+    store_chunk<Real, PM, PN>(g, L.t, R.t, sm);
     __syncthreads();
+    if (k0 + kKC < K) fetch_chunk<Real, PM, PN>(g, L, M, R, N, K, k0 + kKC);
     if (active) {
       const int kn = min(kKC, K - k0);
       for (int kk = 0; kk < kn; kk++) {
@@ -227,51 +251,6 @@ __global__ void __launch_bounds__(256, 2)
     case 7: small_job<Real, 7>(J, sp, lane); break;
     case 8: small_job<Real, 8>(J, sp, lane); break;
     default: break;
-  }
-}
-
-// One 16-deep chunk of the operands of a tile GEMM, staged in registers: the global
-// loads of the next chunk are issued before the current chunk's multiply-adds, so their
-// latency overlaps that work (also across item boundaries in pass 2).
-template <typename Real, int PM, int PN>
-struct ChunkRegs {
-  Real l[PM], r[PN];
-};
-
-template <typename Real, int PM, int PN>
-__device__ __forceinline__ void fetch_chunk(ChunkRegs<Real, PM, PN>& g, const Opnd<Real>& L, int M, const Opnd<Real>& R,
-                                            int N, int K, int k0) {
-  constexpr int TM = 16 * PM, TN = 16 * PN;
-  const int tid = threadIdx.x;
-#pragma unroll
-  for (int s = 0; s < PM; s++) {
-    const int e = tid + kGemmThreads * s;
-    const int i = L.t ? e / kKC : e % TM, kk = L.t ? e % kKC : e / TM;
-    g.l[s] = (i < M && k0 + kk < K) ? L.at(i, k0 + kk) : Real(0);
-  }
-#pragma unroll
-  for (int s = 0; s < PN; s++) {
-    const int e = tid + kGemmThreads * s;
-    const int j = R.t ? e % TN : e / kKC, kk = R.t ? e / TN : e % kKC;
-    g.r[s] = (j < N && k0 + kk < K) ? R.at(k0 + kk, j) : Real(0);
-  }
-}
-
-template <typename Real, int PM, int PN>
-__device__ __forceinline__ void store_chunk(const ChunkRegs<Real, PM, PN>& g, bool lt, bool rt, GSmem<Real>& sm) {
-  constexpr int TM = 16 * PM, TN = 16 * PN;
-  const int tid = threadIdx.x;
-#pragma unroll
-  for (int s = 0; s < PM; s++) {
-    const int e = tid + kGemmThreads * s;
-    const int i = lt ? e / kKC : e % TM, kk = lt ? e % kKC : e / TM;
-    sm.L[kk][i] = g.l[s];
-  }
-#pragma unroll
-  for (int s = 0; s < PN; s++) {
-    const int e = tid + kGemmThreads * s;
-    const int j = rt ? e % TN : e / kKC, kk = rt ? e / TN : e % kKC;
-    sm.R[kk][j] = g.r[s];
   }
 }
 
