@@ -510,21 +510,31 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     int64_t inter_off = 0;
     auto ext16 = [](int x) { return std::max(1, std::min(4, (x + 15) / 16)); };  // extent in units of 16
     auto tile_shape = [&](int rows, int cols) { return (ext16(rows) - 1) | ((ext16(cols) - 1) << 2); };
-    auto plan_large = [&](int g) {
+    // Planning is two passes over the large groups, both parallel: count each group's
+    // items, jobs, job tiles and intermediate size, then fill the arrays at the groups'
+    // prefix offsets (groups in the tile order below).
+    struct Cursor {
+      int64_t item = 0, job = 0, small = 0, jtile = 0, inter = 0;
+    };
+    auto plan_group = [&](int g, Cursor& c, bool fill) {
       const Group& G = st.groups[g];
       const BatchEntry* ents = reinterpret_cast<const BatchEntry*>(staging_);
-      SumGroup sg{};
-      sg.out = G.out;
-      sg.m = G.m;
-      sg.n = G.n;
-      sg.ldo = G.ldo;
-      sg.flags = G.flags;
-      sg.i0 = static_cast<int32_t>(tp.items.size());
       for (int t = G.t0; t < G.t1; t++) {
         const Term& T = tt[t];
         const bool ha = T.flags & kHasA, hc = T.flags & kHasC;
         const GemmOperand B{T.b, T.ldb, (T.flags & kTransB) ? 1 : 0};
         for (int p = 0; p < T.count; p++) {
+          if (!fill) {
+            if (ha && hc) {
+              const int jm = (T.flags & kLeftFirst) ? G.m : T.k1, jn = (T.flags & kLeftFirst) ? T.k2 : G.n;
+              c.inter += (static_cast<int64_t>(jm) * jn + 3) & ~int64_t(3);
+              if (static_cast<int64_t>(jm) * jn <= kInterSmallElems) c.small++;
+              else c.jtile += static_cast<int64_t>((jm + 63) / 64) * ((jn + 63) / 64);
+              c.job++;
+            }
+            c.item++;
+            continue;
+          }
           double alpha = T.alpha;
           int64_t da = 0, dc = 0;
           if (T.list >= 0) {
@@ -539,8 +549,8 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
           it.alpha = alpha;
           if (ha && hc) {
             InterJob J{};
-            J.off = inter_off;
-            const Ref S = make_ref(kSlotInter, inter_off);
+            J.off = c.inter;
+            const Ref S = make_ref(kSlotInter, c.inter);
             if (T.flags & kLeftFirst) {  // S = op(A_p) op(B), m x k2; out += alpha S op(C_p)
               J.l = A;
               J.r = B;
@@ -560,20 +570,20 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
               it.r = GemmOperand{S, T.k1, 0};
               it.k = T.k1;
             }
-            inter_off += (static_cast<int64_t>(J.m) * J.n + 3) & ~int64_t(3);
+            c.inter += (static_cast<int64_t>(J.m) * J.n + 3) & ~int64_t(3);
             if (static_cast<int64_t>(J.m) * J.n <= kInterSmallElems) {
-              tp.small.push_back(static_cast<int32_t>(tp.jobs.size()));
+              tp.small[c.small++] = static_cast<int32_t>(c.job);
             } else {
               for (int i = 0; i < (J.m + 63) / 64; i++)
                 for (int j = 0; j < (J.n + 63) / 64; j++) {
                   GemmTile gt{};
-                  gt.idx = static_cast<int32_t>(tp.jobs.size());
+                  gt.idx = static_cast<int32_t>(c.job);
                   gt.pos = (i << 16) | j;
                   gt.shape = tile_shape(std::min(64, J.m - 64 * i), std::min(64, J.n - 64 * j));
-                  tp.jtiles.push_back(gt);
+                  tp.jtiles[c.jtile++] = gt;
                 }
             }
-            tp.jobs.push_back(J);
+            tp.jobs[c.job++] = J;
           } else if (ha) {
             it.l = A;
             it.r = B;
@@ -586,11 +596,52 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
             it.r = B;
             it.k = 0;
           }
-          tp.items.push_back(it);
+          tp.items[c.item++] = it;
         }
       }
-      sg.i1 = static_cast<int32_t>(tp.items.size());
-      tp.groups.push_back(sg);
+    };
+    auto plan_large_groups = [&](const std::vector<int32_t>& lg) {
+      const size_t nl = lg.size();
+      if (nl == 0) return;
+      int64_t lterms = 0;
+      for (int g : lg) lterms += st.groups[g].t1 - st.groups[g].t0;
+      std::vector<Cursor> cnt(nl), at(nl);
+      parallel_groups(nl, 4 * lterms, [&](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; q++) plan_group(lg[q], cnt[q], false);
+      });
+      Cursor tot;
+      for (size_t q = 0; q < nl; q++) {
+        at[q] = tot;
+        tot.item += cnt[q].item;
+        tot.job += cnt[q].job;
+        tot.small += cnt[q].small;
+        tot.jtile += cnt[q].jtile;
+        tot.inter += cnt[q].inter;
+      }
+      if (tot.item > INT32_MAX || tot.job > INT32_MAX || tot.jtile > INT32_MAX)
+        throw std::length_error("upload: too many large-group items");
+      tp.items.resize(static_cast<size_t>(tot.item));
+      tp.jobs.resize(static_cast<size_t>(tot.job));
+      tp.small.resize(static_cast<size_t>(tot.small));
+      tp.jtiles.resize(static_cast<size_t>(tot.jtile));
+      tp.groups.resize(nl);
+      inter_off = tot.inter;
+      parallel_groups(nl, 4 * lterms, [&](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; q++) {
+          Cursor c = at[q];
+          plan_group(lg[q], c, true);
+          const Group& G = st.groups[lg[q]];
+          SumGroup sg{};
+          sg.out = G.out;
+          sg.m = G.m;
+          sg.n = G.n;
+          sg.ldo = G.ldo;
+          sg.flags = G.flags;
+          sg.i0 = static_cast<int32_t>(at[q].item);
+          sg.i1 = static_cast<int32_t>(at[q].item + cnt[q].item);
+          tp.groups[q] = sg;
+        }
+      });
     };
     // Tile order: the groups with the most work first, row-major within a group.
     // Team-variant tiles are then grouped by row class (one kernel per class), keeping
@@ -634,6 +685,13 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
       class_at[c] = nwarp_tiles;
       nwarp_tiles += per_class[c];
     }
+    {
+      std::vector<int32_t> lg;
+      if (!one_pass_large)
+        for (int g : order)
+          if (info[g].kind == 1 && info[g].large) lg.push_back(g);
+      plan_large_groups(lg);
+    }
     tiles_warp[s].resize(static_cast<size_t>(nwarp_tiles));
     WarpTile* wout = tiles_warp[s].data();
     int64_t part_off = 0, counter = 0;
@@ -641,7 +699,7 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
       const Group& G = st.groups[g];
       const GroupTiles& gi = info[g];
       if (gi.kind == 1 && gi.large && !one_pass_large) {
-        plan_large(g);
+        continue;  // planned above
       } else if (gi.kind == 1) {
         for (int i = 0; i < gi.tm; i++)
           for (int j = 0; j < gi.tn; j++) {
