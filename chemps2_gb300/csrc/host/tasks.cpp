@@ -80,10 +80,18 @@ TaskBuilder::TaskBuilder(bool track_operands) : track_operands_(track_operands) 
 void TaskBuilder::note_operand(const Blk& b) {
   if (!track_operands_ || !b.valid || ref_slot(b.ref) < kSlotMpsBase) return;
   const int64_t n = int64_t(b.rows) * b.cols;
-  if (b.ref == last_operand_ && n <= last_operand_n_) return;
+  if (seen_ref_.empty()) {
+    seen_ref_.assign(kOperandCache, 0);
+    seen_n_.assign(kOperandCache, 0);
+  }
+  const size_t h = static_cast<size_t>((b.ref * 0x9e3779b97f4a7c15ull) >> 52) & (kOperandCache - 1);
+  if (seen_ref_[h] == b.ref) {
+    if (n <= seen_n_[h]) return;  // already noted with at least this size
+  } else {
+    seen_ref_[h] = b.ref;
+  }
+  seen_n_[h] = n;
   operands_.note(b.ref, n);
-  last_operand_ = b.ref;
-  last_operand_n_ = n;
 }
 
 int64_t TaskBuilder::operand_bytes() const { return 8 * operands_.total(); }
@@ -146,9 +154,14 @@ void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha
       open_sb_ = &sb;
     }
     const int aslot = A.valid ? ref_slot(A.ref) : -1, cslot = C.valid ? ref_slot(C.ref) : -1;
-    uint64_t h = mix(t.b, (uint64_t(uint32_t(t.flags)) << 32) | uint32_t(t.k1));
-    h = mix(h, (uint64_t(uint32_t(t.k2)) << 32) | uint32_t(t.lda));
-    h = mix(h, (uint64_t(uint32_t(t.ldc)) << 32) | (uint32_t(aslot & 0xffff) << 16) | uint32_t(cslot & 0xffff));
+    // multiply-xor combination of the key words (independent multiplies), high bits folded
+    // down for the table index
+    uint64_t h = (t.b * 0x9e3779b97f4a7c15ull) ^
+                 (((uint64_t(uint32_t(t.flags)) << 32) | uint32_t(t.k1)) * 0xc2b2ae3d27d4eb4full) ^
+                 (((uint64_t(uint32_t(t.k2)) << 32) | uint32_t(t.lda)) * 0x165667b19e3779f9ull) ^
+                 (((uint64_t(uint32_t(t.ldc)) << 32) | (uint32_t(aslot & 0xffff) << 16) | uint32_t(cslot & 0xffff)) *
+                  0x27d4eb2f165667c5ull);
+    h ^= h >> 29;
     const int32_t hit = open_.find(h, [&](int32_t k) {
       const Term& o = sb.terms[k];
       return o.b == t.b && o.flags == t.flags && o.k1 == t.k1 && o.k2 == t.k2 && o.lda == t.lda && o.ldc == t.ldc &&
@@ -306,11 +319,14 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
         // the list is entry 0 (the term itself) followed by the term's further entries
         const BatchEntry* pe = ebuf.data() + estart[k];
         const BatchEntry first{0, 0, 1.0};
-        uint64_t h = mix(0x13198a2e03707344ull, n);
+        uint64_t h = 0x13198a2e03707344ull ^ (n * 0x9e3779b97f4a7c15ull);
         for (size_t q = 0; q < n; q++) {
           uint64_t r;
           std::memcpy(&r, &pe[q].ratio, sizeof(r));
-          h = mix(mix(mix(h, static_cast<uint64_t>(pe[q].da)), static_cast<uint64_t>(pe[q].dc)), r);
+          h = (h ^ (static_cast<uint64_t>(pe[q].da) * 0xc2b2ae3d27d4eb4full) ^
+               (static_cast<uint64_t>(pe[q].dc) * 0x165667b19e3779f9ull) ^ (r * 0x27d4eb2f165667c5ull)) *
+              0xff51afd7ed558ccdull;
+          h ^= h >> 32;
         }
         int32_t found = -1;
         lists.visit(h, [&](int32_t off) {

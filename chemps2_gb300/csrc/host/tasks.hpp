@@ -355,8 +355,11 @@ class TaskBuilder {
   OpenTerms open_;                                         // open terms of the open group
   FlatIndex written_;                                      // outputs written by closed stages
   RefSizes operands_;                                      // footprint of MPS / operator operands
-  Ref last_operand_ = 0;                                   // the last noted block (repeats are common)
-  int64_t last_operand_n_ = 0;
+  // direct-mapped cache of recently noted blocks in front of operands_ (the same operator
+  // blocks recur across the output blocks of a program)
+  static constexpr int kOperandCache = 4096;
+  std::vector<Ref> seen_ref_;
+  std::vector<int64_t> seen_n_;
   int64_t n_contract_ = 0;
   bool track_operands_ = false;
   const StageBuf* open_sb_ = nullptr;  // the group whose terms are open for batching
