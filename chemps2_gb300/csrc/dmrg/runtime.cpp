@@ -53,11 +53,6 @@ DevProgram::~DevProgram() {
     if (blob) rt->release(blob);
     if (combo) rt->release(combo);
     if (combo32) rt->release(combo32);
-    if (partials) rt->release(partials);
-    if (counters) rt->release(counters);
-    if (inter) rt->release(inter);
-    if (gemm_partials) rt->release(gemm_partials);
-    if (gemm_counters) rt->release(gemm_counters);
   }
 }
 
@@ -91,6 +86,9 @@ Runtime::~Runtime() {
   cudaFree(dev_slots32_);
   cudaFree(partial_);
   if (staging_) cudaFreeHost(staging_);
+  for (int k = 0; k < kTransientKinds; k++)
+    if (transient_[k]) cudaFreeAsync(transient_[k], stream_);
+  if (stream_) cudaStreamSynchronize(stream_);
   if (pinned_) cudaFreeHost(pinned_);
   if (aux_) {
     cudaStreamSynchronize(aux_);
@@ -188,6 +186,31 @@ void Runtime::reserve_staging(int64_t bytes, int64_t keep) {
   }
   staging_ = fresh;
   staging_cap_ = cap;
+}
+
+// Buffers that live only during one stage launch (intermediates of the two-pass path,
+// partial tiles of split tiles, their arrival counters) are shared by all programs of
+// the runtime: programs run one after another on its stream, so the largest need is
+// enough. Growth is stream-ordered; new counters start at zero (a launch leaves its
+// counters at zero again).
+void* Runtime::transient(int kind, int64_t bytes, bool zero) {
+  if (bytes <= transient_cap_[kind]) return transient_[kind];
+  if (transient_[kind]) C2G_CUDA(cudaFreeAsync(transient_[kind], stream_));
+  const int64_t cap = std::max<int64_t>(bytes, transient_cap_[kind] + transient_cap_[kind] / 2);
+  C2G_CUDA(cudaMallocAsync(&transient_[kind], static_cast<size_t>(cap), stream_));
+  if (zero) C2G_CUDA(cudaMemsetAsync(transient_[kind], 0, static_cast<size_t>(cap), stream_));
+  transient_cap_[kind] = cap;
+  return transient_[kind];
+}
+
+double* Runtime::transient_doubles(int kind, int64_t n) {
+  if (n <= 0) return nullptr;
+  return static_cast<double*>(transient(kind, 8 * n, false));
+}
+
+unsigned int* Runtime::transient_counters(int kind, int64_t n) {
+  if (n <= 0) return nullptr;
+  return static_cast<unsigned int*>(transient(kind, static_cast<int64_t>(sizeof(unsigned int)) * n, true));
 }
 
 std::unique_ptr<DevProgram> Runtime::upload(const Program& p) { return upload_parts(&p, 1); }
@@ -850,24 +873,19 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
   C2G_CUDA(cudaMemcpyAsync(dp->blob, staging_, bytes, cudaMemcpyHostToDevice, stream_));
   C2G_CUDA(cudaStreamSynchronize(stream_));  // the staging buffer is reused by the next upload
   if (dp->combo_size > 0) dp->combo = alloc(dp->combo_size);
-  if (part_doubles > 0) dp->partials = alloc(part_doubles);
-  if (inter_doubles > 0) dp->inter = alloc(inter_doubles);
-  if (gemm_part_doubles > 0) dp->gemm_partials = alloc(gemm_part_doubles);
-  if (gemm_counters > 0) {
-    C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dp->gemm_counters), sizeof(unsigned) * gemm_counters, stream_));
-    C2G_CUDA(cudaMemsetAsync(dp->gemm_counters, 0, sizeof(unsigned) * gemm_counters, stream_));
-  }
-  if (ncounters > 0) {
-    C2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dp->counters), sizeof(unsigned) * ncounters, stream_));
-    C2G_CUDA(cudaMemsetAsync(dp->counters, 0, sizeof(unsigned) * ncounters, stream_));
-  }
+  // transient buffers come from the runtime's shared ones at run time (sizes only here)
+  dp->part_size = part_doubles;
+  dp->inter_size = inter_doubles;
+  dp->gemm_part_size = gemm_part_doubles;
+  dp->gemm_counter_count = gemm_counters;
+  dp->counter_count = ncounters;
   return dp;
 }
 
 void Runtime::prepare(DevProgram& p) {
   if (p.prepared) return;
   SlotPtrs sp = ptrs(nullptr, nullptr, p.combo);
-  sp.inter = p.inter;
+  sp.inter = transient_doubles(kTransientInter, p.inter_size);
   for (int s = 0; s < p.first_repeat; s++) launch_stage(p, p.stages[s], sp, Precision::kFP64);
   p.prepared = true;
   p.combo32_ready = false;
@@ -896,8 +914,8 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
       sp.x32 = x32_;
     }
   }
-  sp.inter = p.inter;
-  sp.inter32 = reinterpret_cast<float*>(p.inter);
+  sp.inter = transient_doubles(kTransientInter, p.inter_size);
+  sp.inter32 = reinterpret_cast<float*>(sp.inter);
   for (size_t s = p.first_repeat; s < p.stages.size(); s++) launch_stage(p, p.stages[s], sp, prec);
 }
 
@@ -906,11 +924,15 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
 void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec) {
   C2G_CUDA(launch_inter_gemm(ds.jobs, ds.jtiles, ds.njtiles, sp, stream_, prec));
   C2G_CUDA(launch_inter_small(ds.jobs, ds.jsmall, ds.njsmall, sp, stream_, prec));
-  C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, p.gemm_partials, p.gemm_counters, sp,
+  double* gemm_partials = transient_doubles(kTransientGemmPartials, p.gemm_part_size);
+  unsigned* gemm_counters = transient_counters(kTransientGemmCounters, p.gemm_counter_count);
+  double* partials = transient_doubles(kTransientPartials, p.part_size);
+  unsigned* counters = transient_counters(kTransientCounters, p.counter_count);
+  C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp,
                            stream_, prec));
   C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
   int nw = 0;
-  const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, p.partials, p.counters};
+  const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, partials, counters};
   C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, prec, &nw));
   C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
   count_launches((ds.njtiles > 0) + (ds.njsmall > 0) + (ds.nstiles > 0) + (ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);

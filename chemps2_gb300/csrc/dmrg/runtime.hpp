@@ -61,11 +61,11 @@ struct DevProgram {
   void* blob = nullptr;
   double* combo = nullptr;
   float* combo32 = nullptr;     // FP32 copy of the combined blocks for FP32 runs
-  double* partials = nullptr;   // partial sums of split team-variant tiles (shared by the stages)
-  unsigned int* counters = nullptr;  // their arrival counters
-  double* inter = nullptr;           // intermediate products of the two-pass path
-  double* gemm_partials = nullptr;   // partial tiles of its split pass-2 tiles
-  unsigned int* gemm_counters = nullptr;
+  // sizes of the transient buffers the stages need (the runtime's shared buffers hold
+  // them at run time): partial sums of split team-variant tiles and their arrival
+  // counters, intermediates of the two-pass path, its split partial tiles and counters
+  int64_t part_size = 0, counter_count = 0;
+  int64_t inter_size = 0, gemm_part_size = 0, gemm_counter_count = 0;
   bool prepared = false;
   bool combo32_ready = false;
   DevProgram() = default;
@@ -128,6 +128,13 @@ class Runtime {
   void flush_slots();
   SlotPtrs ptrs(double* x, double* y, double* combo);
   void launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec);
+  enum TransientKind { kTransientInter, kTransientGemmPartials, kTransientGemmCounters, kTransientPartials,
+                       kTransientCounters, kTransientKinds };
+  void* transient_[kTransientKinds] = {};
+  int64_t transient_cap_[kTransientKinds] = {};
+  void* transient(int kind, int64_t bytes, bool zero);
+  double* transient_doubles(int kind, int64_t n);
+  unsigned int* transient_counters(int kind, int64_t n);
 
   int L_;
   cudaStream_t stream_ = nullptr;
