@@ -292,3 +292,23 @@ def test_batch_without_device_reports_each_problem():
         c2g.solve_batch(probs, [sc] * 3, [1, 2, 3], workers=2)
     with pytest.raises(c2g.Chemps2Error):
         c2g.solve_batch([probs[0], probs[0]], [sc, sc], [1, 2])  # a Problem twice
+
+
+def test_batching_workload_generator():
+    """The seeded problem set of the batching form: 64 problems, half Hubbard and half
+    synthetic ab initio, L in 8..20, N = L, D from the four bond dimensions, spins that the
+    electron count allows, identical on every call."""
+    from chemps2_gb300.models import BATCH_BOND_DIMS, batch_members
+
+    a = batch_members(64)
+    b = batch_members(64)
+    assert len(a) == 64
+    assert sum(m["kind"] == "hubbard" for m in a) == 32
+    for x, y in zip(a, b):
+        assert (x["kind"], x["two_s"], x["n"], x["D"], x["seed"]) == (y["kind"], y["two_s"], y["n"], y["D"], y["seed"])
+        assert np.array_equal(x["model"].vmat, y["model"].vmat)
+        L = x["model"].L
+        assert 8 <= L <= 20 and x["n"] == L
+        assert x["D"] in BATCH_BOND_DIMS
+        assert x["two_s"] % 2 == L % 2 and x["two_s"] <= 3
+        assert x["model"].group == (0 if x["kind"] == "hubbard" else 7)
