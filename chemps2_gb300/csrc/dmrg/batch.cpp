@@ -53,8 +53,6 @@ std::vector<BatchResult> SolveBatch(const std::vector<Problem*>& problems,
 
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) device = 0;
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int share = std::max(1, static_cast<int>(hw) / workers);
   std::atomic<size_t> next{0};
 
   auto solve_one = [&](size_t i) {
@@ -91,15 +89,18 @@ std::vector<BatchResult> SolveBatch(const std::vector<Problem*>& problems,
     r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   };
 
+  // Each worker's compilations use an equal share of the host cores among the workers
+  // still solving: when the queue runs dry and workers leave, the last (largest-first
+  // order: longest) problems get more compile threads.
   auto worker = [&] {
     cudaSetDevice(device);
-    if (workers > 1) c2g::set_thread_compile_threads(share);
+    if (workers > 1) c2g::share_compile_threads(true);
     for (;;) {
       const size_t k = next.fetch_add(1);
       if (k >= n) break;
       solve_one(order[k]);
     }
-    c2g::set_thread_compile_threads(0);
+    c2g::share_compile_threads(false);
   };
 
   if (workers == 1) {

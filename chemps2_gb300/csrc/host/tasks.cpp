@@ -1,6 +1,7 @@
 #include "tasks.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstdlib>
 #include <cstring>
@@ -465,11 +466,23 @@ Program merge_programs(std::vector<Program>& parts) {
 
 namespace {
 thread_local int t_compile_threads = 0;
+thread_local bool t_shared = false;
+std::atomic<int> g_sharing{0};  // threads currently sharing the cores
 }  // namespace
 
 void set_thread_compile_threads(int n) { t_compile_threads = std::max(0, std::min(n, 256)); }
 
+void share_compile_threads(bool on) {
+  if (on == t_shared) return;
+  t_shared = on;
+  g_sharing += on ? 1 : -1;
+}
+
 int compile_threads() {
+  if (t_shared) {
+    const int hw = static_cast<int>(std::max(1u, std::min(std::thread::hardware_concurrency(), 64u)));
+    return std::max(1, hw / std::max(1, g_sharing.load()));
+  }
   if (t_compile_threads > 0) return t_compile_threads;
   if (const char* e = std::getenv("C2G_COMPILE_THREADS")) {
     const int n = std::atoi(e);

@@ -390,5 +390,9 @@ int compile_threads();
 // Sets the calling thread's compile thread count (0 clears it). Concurrent solves give
 // each worker thread a share of the cores.
 void set_thread_compile_threads(int n);
+// While on, the calling thread's compilations use an equal share of the cores among all
+// threads that have it on (re-read at every compilation, so the share grows as others
+// turn it off). Concurrent solves turn it on in their worker threads.
+void share_compile_threads(bool on);
 
 }  // namespace c2g
