@@ -144,7 +144,6 @@ void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha
   t.list = -1;
   t.count = 1;
   t.item0 = 0;
-  Group& G = sb.groups[g];
   const int32_t idx = static_cast<int32_t>(sb.terms.size());
   if (batchable) {
     // The compilers emit all contractions of one output block consecutively, so only the
@@ -176,14 +175,12 @@ void TaskBuilder::add(StageBuf& sb, bool batchable, const Blk& out, double alpha
       e.ratio = alpha / o.alpha;
       sb.extra.push_back(e);
       sb.extra_term.push_back(hit);
-      G.work += term_flops(o, G.m, G.n);
       return;
     }
     open_.insert(h, idx);
   }
   sb.terms.push_back(t);
   sb.term_group.push_back(g);
-  G.work += term_flops(t, G.m, G.n);
 }
 
 Blk TaskBuilder::combine(const std::vector<std::pair<double, Blk>>& parts, int rows, int cols,
@@ -281,8 +278,8 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
                          FlatIndex& lists) {
   Stage st;
   st.name = name;
-  st.groups = sb.groups;
-  const size_t ng = sb.groups.size(), nt = sb.terms.size(), ne = sb.extra.size();
+  st.groups = std::move(sb.groups);
+  const size_t ng = st.groups.size(), nt = sb.terms.size(), ne = sb.extra.size();
   // terms by group, entries by term, both in emission order (counting sorts)
   std::vector<int32_t> gstart(ng + 1, 0), order(nt);
   for (size_t k = 0; k < nt; k++) gstart[sb.term_group[k] + 1]++;
@@ -351,7 +348,9 @@ Stage TaskBuilder::lower(StageBuf& sb, const std::string& name, std::vector<Batc
       }
       items += t.count;
       st.items += t.count;
-      st.flops += term_flops(t, G.m, G.n) * t.count;
+      const int64_t f = term_flops(t, G.m, G.n) * t.count;
+      st.flops += f;
+      G.work += f;
       st.terms.push_back(t);
     }
     G.t1 = static_cast<int32_t>(st.terms.size());
