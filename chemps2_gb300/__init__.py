@@ -441,6 +441,13 @@ class DMRG:
         _check(load().c2g_dmrg_heff_apply_noalloc(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
         return y
 
+    def heff_apply_device(self, index, x_ptr, y_ptr, n, precision="fp64", stream=0):
+        """y = Heff x on device buffers given as integer addresses (e.g. torch's data_ptr())
+        of n doubles; `stream` an integer cudaStream_t (0: synchronous)."""
+        p = {"fp64": 0, "fp32": 1}[precision] if isinstance(precision, str) else int(precision)
+        _check(load().c2g_dmrg_heff_apply_device(self._d, int(index), C.c_void_p(int(x_ptr)), C.c_void_p(int(y_ptr)),
+                                                 C.c_int64(int(n)), int(p), C.c_void_p(int(stream) or None)))
+
     def set_precision(self, mode="fp64", mixed_tol=1e-5):
         """'fp64' (the reference's arithmetic) or 'mixed' (FP32 Davidson expansion, FP64 finish)."""
         m = {"fp64": 0, "mixed": 1}[mode] if isinstance(mode, str) else int(mode)

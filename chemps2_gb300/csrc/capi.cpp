@@ -543,6 +543,13 @@ int c2g_dmrg_get_correlations(const c2g_dmrg* d, int ham_order, double* cspin, d
     }
   });
 }
+int c2g_dmrg_heff_apply_device(c2g_dmrg* d, int index, const double* x_dev, double* y_dev, int64_t n, int precision,
+                               void* stream) {
+  return guarded([&] {
+    NEED(d);
+    d->d->heff_apply_device(index, x_dev, y_dev, n, precision, stream);
+  });
+}
 int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n) {
   return guarded([&] {
     NEED(d);

@@ -1229,6 +1229,23 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
   rt->sync();
 }
 
+void DMRG::heff_apply_device(const int index, const double* x_dev, double* y_dev, const long long n,
+                             const int precision, void* stream) {
+  if (!x_dev || !y_dev) throw std::invalid_argument("heff_apply_device: null buffer");
+  if (index < 0 || index > L - 2) throw std::out_of_range("heff_apply_device: index");
+  if (precision != 0 && precision != 1) throw std::invalid_argument("heff_apply_device: precision must be 0 or 1");
+  HeffCache& c = heff_program(index, false);
+  const int64_t veclen = c.S->size();
+  if (n != veclen) throw std::invalid_argument("heff_apply_device: vector length differs from the two-site object size");
+  cudaStream_t u = static_cast<cudaStream_t>(stream);
+  if (u) rt->wait_for(u);  // x is ready once the caller's stream gets here
+  if (precision == 1) enable_f32_ops();
+  rt->run(*c.program, const_cast<double*>(x_dev), y_dev,
+          precision == 1 ? c2g::Precision::kFP32 : c2g::Precision::kFP64, veclen);
+  if (u) rt->signal_to(u);  // the caller's stream waits for y
+  else rt->sync();
+}
+
 void DMRG::heff_apply_noalloc(const int index, const double* x, double* y, const long long n) {
   if (!x || !y) throw std::invalid_argument("heff_apply_noalloc: null buffer");
   if (index < 0 || index > L - 2) throw std::out_of_range("heff_apply_noalloc: index");

@@ -95,6 +95,8 @@ Runtime::~Runtime() {
     cudaStreamDestroy(aux_);
   }
   if (fork_ev_) cudaEventDestroy(fork_ev_);
+  if (ext_in_) cudaEventDestroy(ext_in_);
+  if (ext_out_) cudaEventDestroy(ext_out_);
   if (join_ev_) cudaEventDestroy(join_ev_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -956,6 +958,18 @@ void Runtime::fork_aux() {
   cudaStream_t a = aux_stream();
   C2G_CUDA(cudaEventRecord(fork_ev_, stream_));
   C2G_CUDA(cudaStreamWaitEvent(a, fork_ev_, 0));
+}
+
+void Runtime::wait_for(cudaStream_t other) {
+  if (!ext_in_) C2G_CUDA(cudaEventCreateWithFlags(&ext_in_, cudaEventDisableTiming));
+  C2G_CUDA(cudaEventRecord(ext_in_, other));
+  C2G_CUDA(cudaStreamWaitEvent(stream_, ext_in_, 0));
+}
+
+void Runtime::signal_to(cudaStream_t other) {
+  if (!ext_out_) C2G_CUDA(cudaEventCreateWithFlags(&ext_out_, cudaEventDisableTiming));
+  C2G_CUDA(cudaEventRecord(ext_out_, stream_));
+  C2G_CUDA(cudaStreamWaitEvent(other, ext_out_, 0));
 }
 
 void Runtime::join_aux() {

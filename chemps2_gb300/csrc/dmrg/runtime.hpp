@@ -88,6 +88,10 @@ class Runtime {
   cudaStream_t aux_stream();
   void fork_aux();  // aux waits for everything issued on the main stream so far
   void join_aux();  // the main stream waits for everything issued on aux so far
+  // ordering with a stream of the caller: the main stream waits for what is issued on
+  // `other` so far / `other` waits for what is issued on the main stream so far
+  void wait_for(cudaStream_t other);
+  void signal_to(cudaStream_t other);
   int L() const { return L_; }
 
   // Device memory, stream ordered on this runtime's stream.
@@ -140,6 +144,7 @@ class Runtime {
   cudaStream_t stream_ = nullptr;
   cudaStream_t aux_ = nullptr;
   cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;
+  cudaEvent_t ext_in_ = nullptr, ext_out_ = nullptr;
   std::vector<double*> host_slots_;
   std::vector<float*> host_slots32_;
   const double** dev_slots_ = nullptr;

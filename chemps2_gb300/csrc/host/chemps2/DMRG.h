@@ -109,6 +109,12 @@ class DMRG {
   // device array shared by the process (not safe for concurrent calls). The Heff program
   // at `index` must already exist for the current state (a heff_apply_host call there).
   void heff_apply_noalloc(const int index, const double* x, double* y, const long long n);
+  // Extension: y_dev = Heff x_dev on the caller's device buffers (precision 0: FP64, 1:
+  // FP32 arithmetic). With a CUDA stream the call is ordered after the work already on it
+  // and that stream waits for the result (no host synchronisation); without one the call
+  // returns when y_dev is written.
+  void heff_apply_device(const int index, const double* x_dev, double* y_dev, const long long n,
+                         const int precision, void* stream);
 
   // CheMPS2/DMRG.h calc2DMandCorrelations (CheMPS2/DMRGtechnics.cpp:40-262 without the
   // 3-RDM): the two-particle density matrix of the current state, one site at a time from

@@ -172,6 +172,14 @@ int c2g_dmrg_get_correlations(const c2g_dmrg* d, int ham_order, double* cspin, d
  * calls from several threads or DMRG objects: the array is shared; each call
  * synchronises before returning, so sequential calls are safe. */
 int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n);
+/* No counterpart in the reference (its Heff::makeHeff, CheMPS2/Heff.cpp:43-248, works on
+ * host arrays): y_dev = Heff x_dev at sites (index, index + 1) on the caller's device
+ * buffers of n doubles, FP64 (precision 0) or FP32 arithmetic (precision 1), for the
+ * current MPS and operators. `stream` (a cudaStream_t, or NULL): the call is ordered after
+ * the work already issued on it and that stream waits for y_dev, without a host
+ * synchronisation; with NULL the call returns when y_dev is written. */
+int c2g_dmrg_heff_apply_device(c2g_dmrg* d, int index, const double* x_dev, double* y_dev, int64_t n, int precision,
+                               void* stream);
 
 /* ---- Batches of independent problems (no counterpart in the reference, whose callers
  * loop over problems with one CheMPS2::DMRG each, e.g. CheMPS2/CASSCFnewtonraphson.cpp:

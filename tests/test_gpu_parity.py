@@ -330,3 +330,36 @@ def test_mps_checkpoint_restart(tmp_path, monkeypatch):
     finally:
         second.close()
     assert not (tmp_path / "CheMPS2_MPS0.c2g").exists()
+
+
+def test_heff_apply_on_device_buffers_with_a_stream():
+    """c2g_dmrg_heff_apply_device: the same matvec on the caller's device buffers, both
+    synchronous and ordered on a caller's CUDA stream (FP64 bit-identical to the host-buffer
+    call; FP32 within FP32 rounding)."""
+    torch = pytest.importorskip("torch")
+    m = models.hubbard(8, 4.0)
+    sched = [(64, 1e-10, 1, 0.0, 1e-8)]
+    ham, prob, scheme = gpu_objects(m, 0, 8, 0, sched)
+    c2g.srand(5)
+    gpu = c2g.DMRG(prob, scheme)
+    idx = m.L - 2
+    n = gpu.sobject_size(idx)
+    x = np.random.default_rng(2).standard_normal(n)
+    _, y_host, _ = gpu.heff_apply(idx, x)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    gpu.heff_apply_device(idx, xd.data_ptr(), yd.data_ptr(), n)
+    assert np.array_equal(yd.cpu().numpy(), y_host)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        x2 = xd * 2.0  # produced on the caller's stream right before the call
+        y2 = torch.empty_like(xd)
+    gpu.heff_apply_device(idx, x2.data_ptr(), y2.data_ptr(), n, stream=s.cuda_stream)
+    with torch.cuda.stream(s):
+        y2h = y2.cpu()
+    s.synchronize()
+    assert np.max(np.abs(y2h.numpy() - 2.0 * y_host)) <= 1e-12 * np.max(np.abs(y_host))
+    y32 = torch.empty_like(xd)
+    gpu.heff_apply_device(idx, xd.data_ptr(), y32.data_ptr(), n, precision="fp32")
+    assert np.linalg.norm(y32.cpu().numpy() - y_host) / np.linalg.norm(y_host) < 1e-5
+    gpu.close()
