@@ -85,7 +85,7 @@ void TaskBuilder::note_operand(const Blk& b) {
     seen_ref_.assign(kOperandCache, 0);
     seen_n_.assign(kOperandCache, 0);
   }
-  const size_t h = static_cast<size_t>((b.ref * 0x9e3779b97f4a7c15ull) >> 52) & (kOperandCache - 1);
+  const size_t h = static_cast<size_t>((b.ref * 0x9e3779b97f4a7c15ull) >> 50) & (kOperandCache - 1);
   if (seen_ref_[h] == b.ref) {
     if (n <= seen_n_[h]) return;  // already noted with at least this size
   } else {

@@ -357,7 +357,7 @@ class TaskBuilder {
   RefSizes operands_;                                      // footprint of MPS / operator operands
   // direct-mapped cache of recently noted blocks in front of operands_ (the same operator
   // blocks recur across the output blocks of a program)
-  static constexpr int kOperandCache = 4096;
+  static constexpr int kOperandCache = 16384;
   std::vector<Ref> seen_ref_;
   std::vector<int64_t> seen_n_;
   int64_t n_contract_ = 0;
