@@ -1,16 +1,18 @@
 // Device kernels of the DMRG hot path and their host launchers.
 //
-//   block sandwich     one launch per task-program stage executes every term
-//                      out += alpha sum_p ratio_p op(A_p) op(B) op(C_p) of the stage. One
-//                      CTA per output tile (<= 32 x 32); its 128 threads split into S
-//                      register sub-tiles (<= 4 x 4 elements each) times 128 / S item
-//                      lanes, each lane summing a contiguous range of the group's
-//                      (term, entry) items; the lanes' partial tiles are then reduced in a
-//                      fixed order, so the result is deterministic.
+//   block sandwich     every term out += alpha sum_p ratio_p op(A_p) op(B) op(C_p) of a
+//                      task-program stage, by output tiles, in three variants: the team
+//                      kernel for tiles up to 16 x 16 (one launch per row class,
+//                      sandwich_warp.cuh), the two-pass GEMM path for large groups
+//                      (intermediates once, then split-K item sums; sandwich_gemm.cu)
+//                      and, for comparison only, the one-pass cooperative and
+//                      item-parallel kernels. Item sums run in a fixed order and split
+//                      tiles are reduced in split order, so results are deterministic.
 //   vector kernels     the Davidson eigensolver's dots, linear combinations and
 //                      preconditioner, with deterministic two-pass reductions.
-//   small_eig          Jacobi diagonalisation of the <= 32 x 32 Rayleigh-Ritz matrix in
-//                      one CTA (FP64).
+//   eigensolvers       one-CTA Jacobi for the <= 32 x 32 Rayleigh-Ritz matrix, and
+//                      batched one-CTA Jacobi for the truncation's Gram matrices up to
+//                      order 128 (FP64).
 #pragma once
 
 #include <cstdint>
@@ -123,14 +125,15 @@ cudaError_t launch_sum_gemm(const SumGroup* groups, const SumItem* items, const 
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
                             int ntiles, const SlotPtrs& sp, cudaStream_t stream, Precision prec = Precision::kFP64);
 
-// The cooperative variant for large output tiles and inner dimensions (sandwich_tile.cu):
-// one 256-thread CTA per tile evaluating every item as shared-memory tiled GEMMs.
+// The one-pass cooperative variant for large output tiles (sandwich_tile.cu): one
+// 256-thread CTA per 32 x 32 tile evaluating every item as shared-memory tiled GEMMs
+// (kept for comparison, C2G_LARGE=tile; large groups take the two-pass path).
 cudaError_t launch_sandwich_tiles(const Group* groups, const Term* terms, const BatchEntry* entries,
                                   const TileDesc* tiles, int ntiles, const SlotPtrs& sp, cudaStream_t stream,
                                   Precision prec = Precision::kFP64);
 
 // Groups whose tiles hold at least this many elements and whose items average at least
-// kLargeItemFlops go to the cooperative variant.
+// kLargeItemFlops are large groups (the two-pass path).
 constexpr int kLargeTileElems = 256;
 constexpr int64_t kLargeItemFlops = 4096;
 

@@ -287,7 +287,8 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
   }
   // Tile lists, the groups with the most work first. Groups of at most kWarpTile x
   // kWarpTile, and larger groups with light items, go to the team variant in kWarpTile
-  // tiles; larger groups with heavy items go to the cooperative variant in kTile tiles.
+  // tiles; larger groups with heavy items take the two-pass path (or, with
+  // C2G_LARGE=tile, the one-pass cooperative variant in kTile tiles).
   // (C2G_SANDWICH=item routes the light groups to the item-parallel variant instead.)
   const char* env = std::getenv("C2G_SANDWICH");
   const bool use_item = env && std::string(env) == "item";

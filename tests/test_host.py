@@ -312,3 +312,16 @@ def test_batching_workload_generator():
         assert x["D"] in BATCH_BOND_DIMS
         assert x["two_s"] % 2 == L % 2 and x["two_s"] <= 3
         assert x["model"].group == (0 if x["kind"] == "hubbard" else 7)
+
+
+def test_truncation_eig_argument_errors_are_status_codes():
+    lib = c2g.load()
+    n = np.array([129], dtype=np.int32)
+    buf = np.zeros(129 * 129)
+    ev = np.zeros(129)
+    with pytest.raises(c2g.Chemps2Error):  # order above 128: refused before any device work
+        c2g._check(lib.c2g_truncation_eig(1, n.ctypes.data_as(C.POINTER(C.c_int)), c2g._dp(buf), c2g._dp(ev),
+                                          c2g._dp(buf)))
+    with pytest.raises(c2g.Chemps2Error):
+        c2g._check(lib.c2g_truncation_eig(-1, None, None, None, None))
+    assert lib.c2g_truncation_eig(0, None, None, None, None) == 0
