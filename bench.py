@@ -18,7 +18,7 @@ solver repeats inside every sweep step.
           configuration of the reference's benchmark list), after one warm-up sweep
 
 The reference arm (--impl reference) times the CPU oracle port of the same matvec on
-the host cores (the reference itself needs external BLAS/LAPACK/HDF5 builds and is not
+all the host cores (the reference itself needs external BLAS/LAPACK/HDF5 builds and is not
 compiled here). Multi-GPU runs are independent replicas (the path has no exchange step
 on one problem): each rank runs the full workload on its own GPU.
 """
@@ -169,11 +169,14 @@ def profiled_traffic():
 
 
 def cpu_baseline_sample(model, n_matvec=1):
-    """The CPU oracle port of the same matvec (single host thread), bounded to n_matvec
+    """The CPU oracle port of the same matvec on all host cores (the executor runs the
+    independent output blocks of a stage on parallel threads), bounded to n_matvec
     applications after its own setup."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as ol
 
+    threads = os.cpu_count() or 1
+    ol.set_threads(threads)
     ol.srand(SEED)
     cpu = ol.OracleDMRG(model, TWO_S, N_ELEC, IRREP, [(D_VIRT, 1e-10, 1, 0.0, 1e-8)], check=False)
     for index in range(L_SITES - 2, MID, -1):
@@ -183,9 +186,9 @@ def cpu_baseline_sample(model, n_matvec=1):
     for _ in range(n_matvec):
         cpu.heff_apply(MID, x)
     dt = time.perf_counter() - t0
-    return {"value": n_matvec / dt, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": n_matvec / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{n_matvec} Heff matvec(s) at sites ({MID},{MID + 1}) of the same L=24 D=1000 state "
-                      "(oracle CPU executor, compile excluded, as for the GPU)"}
+                      f"(oracle CPU executor on {threads} threads, compile excluded, as for the GPU)"}
 
 
 def sweep_seconds():

@@ -577,6 +577,12 @@ extern "C" {
 
 const char* oracle_last_error() { return g_err.c_str(); }
 
+// Host threads of the task-program executor (groups of a stage run in parallel).
+int oracle_set_threads(int n) {
+  oracle::CpuExecutor::set_threads(n);
+  return 0;
+}
+
 // Builds a Hamiltonian (tmat L x L, vmat L^4 in physics notation, element (i,j,k,l) at
 // i + L*(j + L*(k + L*l))) or reads an FCIDUMP when fcidump is non-null, the Problem, the
 // ConvergenceScheme and the CPU DMRG (random MPS from the C generator, PreSolve).

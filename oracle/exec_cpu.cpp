@@ -2,7 +2,9 @@
 #include "exec_cpu.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <sstream>
+#include <thread>
 #include <utility>
 
 namespace oracle {
@@ -129,72 +131,103 @@ void CpuExecutor::check(const c2g::Program& p) {
   for (const Stage& st : p.stages) check_stage(st, p.entries);
 }
 
-void CpuExecutor::run_stage(const Stage& st, const std::vector<BatchEntry>& table) {
-  std::vector<double> acc, tmp;
-  for (const Group& G : st.groups) {
-    if (G.m <= 0 || G.n <= 0) continue;
-    const int m = G.m, n = G.n;
-    acc.assign(static_cast<size_t>(m) * n, 0.0);
-    for (int t = G.t0; t < G.t1; t++) {
-      const Term& T = st.terms[t];
-      const bool ha = T.flags & c2g::kHasA, hc = T.flags & c2g::kHasC;
-      const bool ta = T.flags & c2g::kTransA, tb = T.flags & c2g::kTransB, tc = T.flags & c2g::kTransC;
-      const double* B = ptr(T.b);
-      auto opB = [&](int k, int l) { return tb ? B[l + int64_t(T.ldb) * k] : B[k + int64_t(T.ldb) * l]; };
-      for (int p = 0; p < T.count; p++) {
-        const BatchEntry e = entry_of(T, table, p);
-        const double al = T.alpha * e.ratio;
-        const double* A = ha ? ptr(T.a + static_cast<uint64_t>(e.da)) : nullptr;
-        const double* C = hc ? ptr(T.c + static_cast<uint64_t>(e.dc)) : nullptr;
-        auto opA = [&](int i, int k) { return ta ? A[k + int64_t(T.lda) * i] : A[i + int64_t(T.lda) * k]; };
-        auto opC = [&](int l, int j) { return tc ? C[j + int64_t(T.ldc) * l] : C[l + int64_t(T.ldc) * j]; };
-        if (ha && hc) {
-          // tmp = op(B) op(C_p): k1 x n
-          tmp.assign(static_cast<size_t>(T.k1) * n, 0.0);
-          for (int j = 0; j < n; j++)
-            for (int l = 0; l < T.k2; l++) {
-              const double c = opC(l, j);
-              if (c == 0.0) continue;
-              for (int k = 0; k < T.k1; k++) tmp[k + size_t(T.k1) * j] += opB(k, l) * c;
-            }
-          for (int j = 0; j < n; j++)
-            for (int k = 0; k < T.k1; k++) {
-              const double v = al * tmp[k + size_t(T.k1) * j];
-              if (v == 0.0) continue;
-              for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opA(i, k) * v;
-            }
-          flops_done += term_flops(T, m, n);
-        } else if (ha) {
-          for (int j = 0; j < n; j++)
-            for (int k = 0; k < T.k1; k++) {
-              const double v = al * opB(k, j);
-              if (v == 0.0) continue;
-              for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opA(i, k) * v;
-            }
-          flops_done += 2 * int64_t(m) * n * T.k1;
-        } else if (hc) {
-          for (int j = 0; j < n; j++)
-            for (int l = 0; l < T.k2; l++) {
-              const double v = al * opC(l, j);
-              if (v == 0.0) continue;
-              for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opB(i, l) * v;
-            }
-          flops_done += 2 * int64_t(m) * n * T.k2;
-        } else {
-          for (int j = 0; j < n; j++)
-            for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += al * opB(i, j);
-          flops_done += int64_t(m) * n;
-        }
+int64_t CpuExecutor::run_group(const Stage& st, const Group& G, const std::vector<BatchEntry>& table,
+                               std::vector<double>& acc, std::vector<double>& tmp) {
+  int64_t flops = 0;
+  if (G.m <= 0 || G.n <= 0) return 0;
+  const int m = G.m, n = G.n;
+  acc.assign(static_cast<size_t>(m) * n, 0.0);
+  for (int t = G.t0; t < G.t1; t++) {
+    const Term& T = st.terms[t];
+    const bool ha = T.flags & c2g::kHasA, hc = T.flags & c2g::kHasC;
+    const bool ta = T.flags & c2g::kTransA, tb = T.flags & c2g::kTransB, tc = T.flags & c2g::kTransC;
+    const double* B = ptr(T.b);
+    auto opB = [&](int k, int l) { return tb ? B[l + int64_t(T.ldb) * k] : B[k + int64_t(T.ldb) * l]; };
+    for (int p = 0; p < T.count; p++) {
+      const BatchEntry e = entry_of(T, table, p);
+      const double al = T.alpha * e.ratio;
+      const double* A = ha ? ptr(T.a + static_cast<uint64_t>(e.da)) : nullptr;
+      const double* C = hc ? ptr(T.c + static_cast<uint64_t>(e.dc)) : nullptr;
+      auto opA = [&](int i, int k) { return ta ? A[k + int64_t(T.lda) * i] : A[i + int64_t(T.lda) * k]; };
+      auto opC = [&](int l, int j) { return tc ? C[j + int64_t(T.ldc) * l] : C[l + int64_t(T.ldc) * j]; };
+      if (ha && hc) {
+        // tmp = op(B) op(C_p): k1 x n
+        tmp.assign(static_cast<size_t>(T.k1) * n, 0.0);
+        for (int j = 0; j < n; j++)
+          for (int l = 0; l < T.k2; l++) {
+            const double c = opC(l, j);
+            if (c == 0.0) continue;
+            for (int k = 0; k < T.k1; k++) tmp[k + size_t(T.k1) * j] += opB(k, l) * c;
+          }
+        for (int j = 0; j < n; j++)
+          for (int k = 0; k < T.k1; k++) {
+            const double v = al * tmp[k + size_t(T.k1) * j];
+            if (v == 0.0) continue;
+            for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opA(i, k) * v;
+          }
+        flops += term_flops(T, m, n);
+      } else if (ha) {
+        for (int j = 0; j < n; j++)
+          for (int k = 0; k < T.k1; k++) {
+            const double v = al * opB(k, j);
+            if (v == 0.0) continue;
+            for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opA(i, k) * v;
+          }
+        flops += 2 * int64_t(m) * n * T.k1;
+      } else if (hc) {
+        for (int j = 0; j < n; j++)
+          for (int l = 0; l < T.k2; l++) {
+            const double v = al * opC(l, j);
+            if (v == 0.0) continue;
+            for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += opB(i, l) * v;
+          }
+        flops += 2 * int64_t(m) * n * T.k2;
+      } else {
+        for (int j = 0; j < n; j++)
+          for (int i = 0; i < m; i++) acc[i + size_t(m) * j] += al * opB(i, j);
+        flops += int64_t(m) * n;
       }
     }
-    double* O = const_cast<double*>(ptr(G.out));
-    const bool accum = G.flags & c2g::kAccumulate;
-    for (int c = 0; c < n; c++)
-      for (int r = 0; r < m; r++) {
-        double& o = O[r + int64_t(G.ldo) * c];
-        o = accum ? o + acc[r + size_t(m) * c] : acc[r + size_t(m) * c];
-      }
   }
+  double* O = const_cast<double*>(ptr(G.out));
+  const bool accum = G.flags & c2g::kAccumulate;
+  for (int c = 0; c < n; c++)
+    for (int r = 0; r < m; r++) {
+      double& o = O[r + int64_t(G.ldo) * c];
+      o = accum ? o + acc[r + size_t(m) * c] : acc[r + size_t(m) * c];
+    }
+  return flops;
+}
+
+namespace {
+std::atomic<int> g_threads{1};
+}  // namespace
+
+void CpuExecutor::set_threads(int n) { g_threads = std::max(1, std::min(n, 1024)); }
+int CpuExecutor::threads() { return g_threads.load(); }
+
+void CpuExecutor::run_stage(const Stage& st, const std::vector<BatchEntry>& table) {
+  const size_t ng = st.groups.size();
+  const int nt = static_cast<int>(std::min<size_t>(threads(), (ng + 63) / 64));
+  if (nt <= 1) {
+    std::vector<double> acc, tmp;
+    for (const Group& G : st.groups) flops_done += run_group(st, G, table, acc, tmp);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::atomic<int64_t> flops{0};
+  auto work = [&] {
+    std::vector<double> acc, tmp;
+    int64_t f = 0;
+    for (size_t g0 = next.fetch_add(32); g0 < ng; g0 = next.fetch_add(32))
+      for (size_t g = g0; g < std::min(ng, g0 + 32); g++) f += run_group(st, st.groups[g], table, acc, tmp);
+    flops += f;
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < nt; i++) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  flops_done += flops.load();
 }
 
 void CpuExecutor::run(const c2g::Program& p, bool once_stages, bool repeat_stages) {

@@ -36,11 +36,18 @@ class CpuExecutor {
 
   int64_t flops_done = 0;
 
+  // Host threads that execute the groups of a stage (independent outputs); results do not
+  // depend on it (each group is computed by one thread in the fixed term order).
+  static void set_threads(int n);
+  static int threads();
+
  private:
   std::vector<Buffer> slots_;
   std::vector<double> combo_;
   void check_stage(const c2g::Stage& st, const std::vector<c2g::BatchEntry>& table);
   void run_stage(const c2g::Stage& st, const std::vector<c2g::BatchEntry>& table);
+  int64_t run_group(const c2g::Stage& st, const c2g::Group& G, const std::vector<c2g::BatchEntry>& table,
+                    std::vector<double>& acc, std::vector<double>& tmp);
   const double* ptr(c2g::Ref r) const;
 };
 

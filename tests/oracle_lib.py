@@ -162,5 +162,10 @@ class OracleDMRG:
             pass
 
 
+def set_threads(n: int):
+    """Host threads of the oracle's task-program executor (results do not depend on it)."""
+    lib().oracle_set_threads(int(n))
+
+
 def srand(seed: int):
     C.CDLL(None).srand(C.c_uint(seed))
