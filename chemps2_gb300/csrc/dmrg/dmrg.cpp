@@ -686,7 +686,8 @@ void DMRG::update_moving_right(const int index) {
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
   if (f32_ops_) refresh_f32(index);
-  rt->sync();
+  // no synchronisation: the host goes on compiling the next site's programs while the
+  // update runs; everything that reads its results is ordered after it on the stream
   if (!exc_.empty()) update_overlaps(index, true);
   stats_.t_update += now() - t0;
 }
@@ -717,7 +718,7 @@ void DMRG::update_moving_left(const int index) {
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
   if (f32_ops_) refresh_f32(index);
-  rt->sync();
+  // no synchronisation (as in update_moving_right)
   if (!exc_.empty()) update_overlaps(index, false);
   stats_.t_update += now() - t0;
 }
