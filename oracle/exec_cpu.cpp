@@ -208,7 +208,7 @@ int CpuExecutor::threads() { return g_threads.load(); }
 
 void CpuExecutor::run_stage(const Stage& st, const std::vector<BatchEntry>& table) {
   const size_t ng = st.groups.size();
-  const int nt = static_cast<int>(std::min<size_t>(threads(), (ng + 63) / 64));
+  const int nt = static_cast<int>(std::min<size_t>(threads(), (ng + 15) / 16));
   if (nt <= 1) {
     std::vector<double> acc, tmp;
     for (const Group& G : st.groups) flops_done += run_group(st, G, table, acc, tmp);

@@ -177,3 +177,23 @@ def test_fci_mutual_information_consistent_with_2rdm():
         s = -sum(x * np.log(x) for x in (v1, v23, v23, v4) if x > 1e-100)
         assert abs(s - s1[i]) < 1e-9
     assert np.allclose(mi, mi.T) and mi.min() >= -1e-12
+
+
+def test_threaded_executor_gives_identical_results():
+    """The oracle's executor on several host threads (output blocks of a stage in
+    parallel) gives the single-thread matvec bit for bit, and the same sweep energy."""
+    m = models.synthetic_ab_initio(9, 7, 12)
+    sched = [(64, 1e-10, 1, 0.0, 1e-8)]
+    results = {}
+    try:
+        for nt in (1, 4):
+            ol.set_threads(nt)
+            ol.srand(5)
+            cpu = ol.OracleDMRG(m, 1, 9, 3, sched)
+            x = np.random.default_rng(8).standard_normal(cpu.sobject_size(m.L - 2))
+            _, y, _ = cpu.heff_apply(m.L - 2, x)
+            results[nt] = (y, cpu.solve())
+    finally:
+        ol.set_threads(1)
+    assert np.array_equal(results[1][0], results[4][0])
+    assert results[1][1] == results[4][1]
