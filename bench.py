@@ -109,7 +109,9 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = Path(tempfile.mkstemp(prefix="c2g_clocks_", suffix=".csv")[1])
+        fd, name = tempfile.mkstemp(prefix="c2g_clocks_", suffix=".csv")
+        os.close(fd)
+        self.path = Path(name)
 
     def __enter__(self):
         try:
@@ -375,6 +377,43 @@ def extra_config3(args):
     L = 30
     model = synthetic_ab_initio(L, GROUP, SEED)
     out = {"config": f"synthetic ab initio L=30 N=30 S=0 D2h D=2000, {args.sweeps} sweeps, Davidson rtol 1e-8"}
+    if args.profile:
+        # profiling mode: --sweeps FP64 sweeps, right-hand operators down to the middle, then
+        # --profile matvecs at sites (14, 15) in each precision between cudaProfilerStart/Stop
+        import torch
+
+        ham = c2g.Hamiltonian(L, model.group, model.irreps)
+        for i in range(L):
+            for j in range(i, L):
+                if model.tmat[i, j] != 0.0:
+                    ham.setTmat(i, j, float(model.tmat[i, j]))
+        for i, j, k, l in np.argwhere(model.vmat != 0.0):
+            if i <= j and i <= k:
+                ham.setVmat(int(i), int(j), int(k), int(l), float(model.vmat[i, j, k, l]))
+        prob = c2g.Problem(ham, 0, L, 0)
+        scheme = c2g.ConvergenceScheme(1)
+        scheme.set_instruction(0, 2000, 1e-10, args.sweeps, 0.0, 1e-8)
+        c2g.srand(SEED)
+        d = c2g.DMRG(prob, scheme)
+        d.Solve()
+        mid = L // 2 - 1
+        for index in range(L - 2, mid, -1):
+            d.update(index, False)
+        precs = ["fp64", "fp32"]
+        for p in precs:
+            d.bench_heff(mid, args.warmup, 0, 0, precision=p)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        for p in precs:
+            d.bench_heff(mid, 0, args.profile, 0, precision=p)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        for p in precs:
+            r = d.bench_heff(mid, 0, 5, L2_FLUSH_BYTES, precision=p)
+            print(json.dumps({"precision": p, "ms_per_matvec": r["ms_per_matvec"], "ledger_flops": r["flops"],
+                              "ledger_bytes": r["bytes"], "n": d.sobject_size(mid)}), flush=True)
+        d.close()
+        return
     for mode in ("fp64", "mixed"):
         ham = c2g.Hamiltonian(L, model.group, model.irreps)
         for i in range(L):

@@ -433,9 +433,37 @@ class DMRG:
         out["SingleOrbitalEntropy"] = ent
         return out
 
+    def sectors(self, boundary):
+        """Rows (N, 2S, I, FCI dim, current dim) of the object's bookkeeper at `boundary`."""
+        n = C.c_int()
+        _check(load().c2g_dmrg_sectors(self._d, int(boundary), None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 5), dtype=np.int32)
+        _check(load().c2g_dmrg_sectors(self._d, int(boundary), out.ctypes.data_as(C.POINTER(C.c_int)), n.value,
+                                       C.byref(n)))
+        return out[:n.value]
+
+    def get_mps(self, site):
+        """The current MPS tensor of `site` (TensorT storage order) as a host array."""
+        n = C.c_int64()
+        _check(load().c2g_dmrg_get_mps(self._d, int(site), None, C.c_int64(0), C.byref(n)))
+        out = np.zeros(n.value)
+        _check(load().c2g_dmrg_get_mps(self._d, int(site), _dp(out), C.c_int64(n.value), C.byref(n)))
+        return out
+
+    def step_energies(self):
+        """Energies of every two-site step Solve() has run, in order."""
+        n = C.c_int()
+        _check(load().c2g_dmrg_step_energies(self._d, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        _check(load().c2g_dmrg_step_energies(self._d, _dp(out), n.value, C.byref(n)))
+        return out
+
     def heff_apply_noalloc(self, index, x):
-        """y = Heff x (FP64) staged through the library's static device array (no device
-        allocation); needs a prior heff_apply at this index and state."""
+        """y = Heff x (FP64) with no device allocation, for callers that cannot allocate
+        device memory while they run: x and y are staged through the library's one
+        file-scope device array (two-site objects of at most 1 048 544 doubles). Needs a
+        prior heff_apply at this index and state. Calls that overlap on the GPU race for
+        the array; calls made one after another are safe."""
         xx = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros_like(xx)
         _check(load().c2g_dmrg_heff_apply_noalloc(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
@@ -487,6 +515,13 @@ def solve_batch(problems, schemes, seeds, workers=8, raise_on_error=True):
         _check(rc)
     return [{"energy": float(energies[i]), "matvecs": int(matvecs[i]), "seconds": float(seconds[i]),
              "status": int(statuses[i]), "stats": dict(zip(STAT_NAMES, stats[i].tolist()))} for i in range(n)]
+
+
+def device_memory_info(device: int = -1):
+    """(free bytes of the device, bytes in use from its default stream-ordered pool)."""
+    fr, used = C.c_int64(), C.c_int64()
+    _check(load().c2g_device_memory_info(int(device), C.byref(fr), C.byref(used)))
+    return fr.value, used.value
 
 
 def host_rand_sample(seed: int, n: int) -> np.ndarray:

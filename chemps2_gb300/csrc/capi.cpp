@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <memory>
 #include <stdexcept>
@@ -550,6 +551,47 @@ int c2g_dmrg_heff_apply_device(c2g_dmrg* d, int index, const double* x_dev, doub
     d->d->heff_apply_device(index, x_dev, y_dev, n, precision, stream);
   });
 }
+int c2g_dmrg_sectors(const c2g_dmrg* d, int boundary, int* out, int cap, int* count) {
+  return guarded([&] {
+    NEED(d);
+    NEED(count);
+    const CheMPS2::SyBookkeeper& bk = *d->d->get_bookkeeper();
+    if (boundary < 0 || boundary > bk.gL()) throw std::invalid_argument("boundary out of range");
+    const int ns = bk.num_sectors(boundary);
+    *count = ns;
+    if (cap <= 0) return;
+    NEED(out);
+    for (int id = 0; id < ns && id < cap; id++) {
+      int n, s, i;
+      bk.sector_labels(boundary, id, &n, &s, &i);
+      out[5 * id + 0] = n;
+      out[5 * id + 1] = s;
+      out[5 * id + 2] = i;
+      out[5 * id + 3] = bk.fci_dim_by_id(boundary, id);
+      out[5 * id + 4] = bk.cur_dim_by_id(boundary, id);
+    }
+  });
+}
+int c2g_dmrg_get_mps(const c2g_dmrg* d, int site, double* out, int64_t cap, int64_t* n) {
+  return guarded([&] {
+    NEED(d);
+    NEED(n);
+    *n = d->d->mps_size(site);
+    if (cap <= 0) return;
+    if (cap < *n) throw std::invalid_argument("c2g_dmrg_get_mps: buffer shorter than the tensor");
+    d->d->get_mps(site, out, *n);
+  });
+}
+int c2g_dmrg_step_energies(const c2g_dmrg* d, double* out, int cap, int* count) {
+  return guarded([&] {
+    NEED(d);
+    NEED(count);
+    const std::vector<double>& e = d->d->step_energies();
+    *count = static_cast<int>(e.size());
+    if (out)
+      for (int i = 0; i < std::min(cap, *count); i++) out[i] = e[i];
+  });
+}
 int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n) {
   return guarded([&] {
     NEED(d);
@@ -643,6 +685,27 @@ int c2g_truncation_eig(int count, const int* n, const double* mats, double* eval
     C2G_CUDA(cudaMemcpy(evecs, d + tot + totn, sizeof(double) * tot, cudaMemcpyDeviceToHost));
     cudaFree(dj);
     cudaFree(d);
+  });
+}
+
+int c2g_device_memory_info(int device, int64_t* free_bytes, int64_t* pool_used_bytes) {
+  return guarded([&] {
+    NEED(free_bytes);
+    NEED(pool_used_bytes);
+    int cur = 0;
+    C2G_CUDA(cudaGetDevice(&cur));
+    if (device < 0) device = cur;
+    if (device != cur) C2G_CUDA(cudaSetDevice(device));
+    size_t fr = 0, tot = 0;
+    cudaError_t e = cudaMemGetInfo(&fr, &tot);
+    cudaMemPool_t pool = nullptr;
+    uint64_t used = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, device);
+    if (e == cudaSuccess) e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    if (device != cur) cudaSetDevice(cur);
+    C2G_CUDA(e);
+    *free_bytes = static_cast<int64_t>(fr);
+    *pool_used_bytes = static_cast<int64_t>(used);
   });
 }
 

@@ -9,9 +9,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <cusolverDn.h>
+#include <string>
+#include <unistd.h>
+#include <unordered_map>
 
 #include "static_scratch.hpp"
-#include <unordered_map>
 
 #include "davidson.hpp"
 #include "correlations.hpp"
@@ -221,14 +223,18 @@ constexpr char kMpsMagic[8] = {'C', '2', 'G', 'M', 'P', 'S', '0', '1'};
 }  // namespace
 
 // CheMPS2/DMRGmpsio.cpp:27-94 (saveMPS): header, virtual dimensions of every boundary in
-// bookkeeper order, converged flag, then the tensors of every site.
+// bookkeeper order, converged flag, then the tensors of every site. The file is written
+// under a temporary name, flushed to disk and then renamed over the previous checkpoint,
+// so a process killed mid-write leaves the last complete checkpoint in place.
 void DMRG::save_mps(bool converged) const {
-  std::FILE* f = std::fopen(mps_storage_name_.c_str(), "wb");
-  if (!f) throw std::runtime_error("saveMPS: cannot open " + mps_storage_name_);
+  const std::string tmp_name = mps_storage_name_ + ".tmp";
+  std::FILE* f = std::fopen(tmp_name.c_str(), "wb");
+  if (!f) throw std::runtime_error("saveMPS: cannot open " + tmp_name);
   auto put = [&](const void* p, size_t n) {
     if (std::fwrite(p, 1, n, f) != n) {
       std::fclose(f);
-      throw std::runtime_error("saveMPS: write failed for " + mps_storage_name_);
+      std::remove(tmp_name.c_str());
+      throw std::runtime_error("saveMPS: write failed for " + tmp_name);
     }
   };
   const int32_t head[7] = {L, Prob->gN(), Prob->gTwoS(), Prob->gIrrep(), denBK->getNumberOfIrreps(),
@@ -253,7 +259,15 @@ void DMRG::save_mps(bool converged) const {
     put(&n, sizeof(n));
     put(data.data(), sizeof(double) * data.size());
   }
-  std::fclose(f);
+  const bool flushed = std::fflush(f) == 0 && fsync(fileno(f)) == 0;
+  if (std::fclose(f) != 0 || !flushed) {
+    std::remove(tmp_name.c_str());
+    throw std::runtime_error("saveMPS: could not flush " + tmp_name);
+  }
+  if (std::rename(tmp_name.c_str(), mps_storage_name_.c_str()) != 0) {
+    std::remove(tmp_name.c_str());
+    throw std::runtime_error("saveMPS: could not rename " + tmp_name + " to " + mps_storage_name_);
+  }
 }
 
 // CheMPS2/DMRGmpsio.cpp:96-162 (loadDIM, loadMPS). False when the file does not exist.
@@ -756,6 +770,7 @@ double DMRG::sweep(const bool moving_right, const bool change, const int instruc
   if (moving_right) {
     for (int index = 0; index < L - 2; index++) {
       Energy = solve_site(index, rtol, noise_level, D, true, change);
+      step_energies_.push_back(Energy);
       TotalMinEnergy = std::min(TotalMinEnergy, Energy);
       LastMinEnergy = std::min(LastMinEnergy, Energy);
       update_moving_right(index);
@@ -763,6 +778,7 @@ double DMRG::sweep(const bool moving_right, const bool change, const int instruc
   } else {
     for (int index = L - 2; index > 0; index--) {
       Energy = solve_site(index, rtol, noise_level, D, false, change);
+      step_energies_.push_back(Energy);
       TotalMinEnergy = std::min(TotalMinEnergy, Energy);
       LastMinEnergy = std::min(LastMinEnergy, Energy);
       update_moving_left(index);
@@ -1186,6 +1202,21 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   return steps > 0 ? total_ms / steps : 0.0;
 }
 
+long long DMRG::mps_size(const int site) const {
+  if (site < 0 || site >= L) throw std::out_of_range("mps_size: site");
+  return mps_lay[site]->size();
+}
+
+void DMRG::get_mps(const int site, double* out, const long long n) const {
+  if (site < 0 || site >= L) throw std::out_of_range("get_mps: site");
+  if (n != mps_lay[site]->size()) throw std::invalid_argument("get_mps: length differs from the tensor size");
+  if (n > 0) {
+    if (!out) throw std::invalid_argument("get_mps: null buffer");
+    C2G_CUDA(cudaMemcpyAsync(out, mps_dev[site], sizeof(double) * n, cudaMemcpyDeviceToHost, rt->stream()));
+  }
+  rt->sync();
+}
+
 long long DMRG::sobject_size(const int index) const {
   if (index < 0 || index > L - 2) throw std::out_of_range("sobject_size: index");
   TwoSiteLayout S;
@@ -1250,16 +1281,31 @@ void DMRG::heff_apply_device(const int index, const double* x_dev, double* y_dev
 void DMRG::heff_apply_noalloc(const int index, const double* x, double* y, const long long n) {
   if (!x || !y) throw std::invalid_argument("heff_apply_noalloc: null buffer");
   if (index < 0 || index > L - 2) throw std::out_of_range("heff_apply_noalloc: index");
+  // the size limit is checked first, from the sector dimensions alone
+  const int64_t veclen = sobject_size(index);
+  if (n != veclen) throw std::invalid_argument("heff_apply_noalloc: vector length differs from the two-site object size");
+  if (veclen > c2g::kStaticScratchMaxVector)
+    throw std::invalid_argument("heff_apply_noalloc: two-site object of " + std::to_string(veclen) +
+                                " doubles is too large for the static scratch (at most " +
+                                std::to_string(c2g::kStaticScratchMaxVector) + ")");
+  const int64_t ystart = (veclen + 31) / 32 * 32;  // y starts on a 256-byte boundary
   HeffCache& c = *heff_cache_;
   if (!(c.index == index && c.version == version_ && c.program))
     throw std::invalid_argument("heff_apply_noalloc: no Heff program for this index and state (call heff_apply first)");
-  const int64_t veclen = c.S->size();
-  if (n != veclen) throw std::invalid_argument("heff_apply_noalloc: vector length differs from the two-site object size");
-  const int64_t ystart = (veclen + 31) / 32 * 32;  // y starts on a 256-byte boundary
-  if (ystart + veclen > c2g::kStaticScratchDoubles)
-    throw std::invalid_argument("heff_apply_noalloc: two-site object too large for the static scratch");
+  // the runtime's stream, memory and scratch belong to its device, whichever device the
+  // calling thread has current; that device is made current for this call and restored
+  int caller_dev = 0;
+  C2G_CUDA(cudaGetDevice(&caller_dev));
+  const int dev = rt->device();
+  if (caller_dev != dev) C2G_CUDA(cudaSetDevice(dev));
+  struct Restore {
+    int from, to;
+    ~Restore() {
+      if (from != to) cudaSetDevice(to);
+    }
+  } restore{dev, caller_dev};
   double* base = nullptr;
-  C2G_CUDA(c2g::static_scratch(&base));
+  C2G_CUDA(c2g::static_scratch(dev, &base));
   double* dx = base;
   double* dy = base + ystart;
   cudaStream_t s = rt->stream();

@@ -63,6 +63,7 @@ Runtime::Runtime(int L, int device) : L_(L) {
   if (count <= 0) throw std::runtime_error("no CUDA device available: the DMRG hot path runs only on the GPU");
   if (device < 0) C2G_CUDA(cudaGetDevice(&device));
   C2G_CUDA(cudaSetDevice(device));
+  device_ = device;
   C2G_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   // Keep freed blocks in the stream-ordered pool instead of returning them to the driver.
   cudaMemPool_t pool;

@@ -93,6 +93,8 @@ class Runtime {
   void wait_for(cudaStream_t other);
   void signal_to(cudaStream_t other);
   int L() const { return L_; }
+  // the CUDA device this runtime's stream and memory belong to
+  int device() const { return device_; }
 
   // Device memory, stream ordered on this runtime's stream.
   double* alloc(int64_t n_doubles);
@@ -141,6 +143,7 @@ class Runtime {
   unsigned int* transient_counters(int kind, int64_t n);
 
   int L_;
+  int device_ = 0;
   cudaStream_t stream_ = nullptr;
   cudaStream_t aux_ = nullptr;
   cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;

@@ -23,15 +23,21 @@ double* g_addr[kMaxDevices] = {};
 
 }  // namespace
 
-cudaError_t static_scratch(double** ptr) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
+cudaError_t static_scratch(int dev, double** ptr) {
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_mutex);
   if (!g_addr[dev]) {
+    // the symbol's address is per device: look it up with `dev` current
+    int cur = 0;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) return e;
+    if (cur != dev && (e = cudaSetDevice(dev)) != cudaSuccess) return e;
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (cur != dev) {
+      const cudaError_t r = cudaSetDevice(cur);
+      if (e == cudaSuccess) e = r;
+    }
     if (e != cudaSuccess) return e;
     g_addr[dev] = static_cast<double*>(p);
   }

@@ -74,6 +74,14 @@ class DMRG {
   double get_TotalMinEnergy() const { return TotalMinEnergy; }
   const SyBookkeeper* get_bookkeeper() const { return denBK.get(); }
   const DMRGStats& stats() const { return stats_; }
+  // Extension: the energy of every two-site step Solve() has run, in order (the reference
+  // prints them, CheMPS2/DMRG.cpp:335-402; here they are kept for comparison).
+  const std::vector<double>& step_energies() const { return step_energies_; }
+  // Extension for checking: the current MPS tensor of `site` as TensorT::gStorage holds it
+  // (CheMPS2/include/chemps2/TensorT.h:50; blocks in TensorT's order, column-major),
+  // copied to host memory, and its length.
+  long long mps_size(const int site) const;
+  void get_mps(const int site, double* out, const long long n) const;
   void reset_stats() { stats_ = DMRGStats(); }
   void set_verbose(bool v) { verbose = v; }
   // 0: FP64 Heff matvecs (the reference's arithmetic). 1: mixed, the Davidson solver
@@ -208,6 +216,7 @@ class DMRG {
   double LastMinEnergy = 1e8;
   double MaxDiscWeightLastSweep = 0.0;
   DMRGStats stats_;
+  std::vector<double> step_energies_;
 };
 
 }  // namespace CheMPS2

@@ -8,8 +8,7 @@
  * (CheMPS2/include/chemps2/DMRG.h, private-member comments).
  *
  * Each function names the reference interface it replaces (path:line inside the CheMPS2
- * project). The bindings a caller of the reference would switch to are shown in
- * INTEGRATION.md.
+ * project), or says that it has no counterpart there.
  */
 #ifndef CHEMPS2_GB300_H
 #define CHEMPS2_GB300_H
@@ -164,13 +163,34 @@ int c2g_dmrg_2dm_trace_energy(const c2g_dmrg* d, double* trace, double* energy);
  * pointer may be NULL. */
 int c2g_dmrg_get_correlations(const c2g_dmrg* d, int ham_order, double* cspin, double* cdens, double* cspinflip,
                               double* cdirad, double* mutinfo, double* entropy);
-/* No counterpart in the reference. As c2g_dmrg_heff_apply (FP64, no join, no diagonal)
- * without any device allocation: x and y are staged through a static device array of
- * 2 M doubles shared by the whole process (n up to about 1 M). The Heff program at `index`
- * must already exist for the current state (a c2g_dmrg_heff_apply call there), otherwise
- * C2G_ERR_INVALID; n too large for the array: C2G_ERR_INVALID. Not safe for concurrent
- * calls from several threads or DMRG objects: the array is shared; each call
- * synchronises before returning, so sequential calls are safe. */
+/* The DMRG object's own SyBookkeeper (current virtual dimensions after the sweeps so far,
+ * SyBookkeeper::gCurrentDim, CheMPS2/SyBookkeeper.cpp:165,271-280) at boundary b, in the
+ * row format of c2g_bookkeeper_sectors. */
+int c2g_dmrg_sectors(const c2g_dmrg* d, int boundary, int* out, int cap, int* count);
+/* TensorT::gStorage of the current MPS tensor of `site` (CheMPS2/include/chemps2/TensorT.h:50,
+ * block order of CheMPS2/TensorT.cpp:38-110, each block column-major), copied to `out`;
+ * *n receives its length (query with cap = 0). */
+int c2g_dmrg_get_mps(const c2g_dmrg* d, int site, double* out, int64_t cap, int64_t* n);
+/* The energy of every two-site step the sweeps of c2g_dmrg_solve have run, in order (the
+ * reference prints them in DMRG::sweepleft / sweepright, CheMPS2/DMRG.cpp:335-402, and
+ * keeps only their minimum). *count receives the number of steps; up to cap of them are
+ * written to out (which may be NULL). */
+int c2g_dmrg_step_energies(const c2g_dmrg* d, double* out, int cap, int* count);
+/* No counterpart in the reference. For callers that cannot allocate device memory while
+ * they run: a host program whose device memory is all handed out by its own allocator
+ * (a fixed budget reserved at start-up), or one that must not call cudaMalloc / cudaFree
+ * because those calls can synchronise the device and stall the work of other streams.
+ * As c2g_dmrg_heff_apply (FP64, no join, no diagonal) with no allocation at all: x and y
+ * are staged through one file-scope device array of 2 M doubles (16 MiB, held by every
+ * GPU that loads the library until the process exits), so n may be at most 1 048 544.
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. y's half of
+ * the array is cleared on every call. The Heff program at `index` must already exist for
+ * the current state (a c2g_dmrg_heff_apply call there); otherwise, or when n differs from
+ * the two-site object's size or exceeds the limit, C2G_ERR_INVALID. Every call shares
+ * the array: calls that overlap on the GPU (several threads or DMRG objects at once)
+ * race; each call synchronises before it returns, so calls made one after another are
+ * safe. */
 int c2g_dmrg_heff_apply_noalloc(c2g_dmrg* d, int index, const double* x, double* y, int64_t n);
 /* No counterpart in the reference (its Heff::makeHeff, CheMPS2/Heff.cpp:43-248, works on
  * host arrays): y_dev = Heff x_dev at sites (index, index + 1) on the caller's device
@@ -202,6 +222,11 @@ int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* sche
  * in ascending order (concatenated), evecs its eigenvectors in descending order of the
  * eigenvalue, each column signed so that its largest-magnitude entry is positive. */
 int c2g_truncation_eig(int count, const int* n, const double* mats, double* evals, double* evecs);
+/* No counterpart in the reference (a diagnostic): the free memory of `device` (< 0: the
+ * calling thread's current device; cudaMemGetInfo) and the bytes in use from that
+ * device's default stream-ordered pool (cudaMemPoolAttrUsedMemCurrent), where this
+ * library's stream-ordered allocations live. */
+int c2g_device_memory_info(int device, int64_t* free_bytes, int64_t* pool_used_bytes);
 /* The first n draws of the private random generator a batch member seeded with `seed`
  * uses (equal to srand(seed); rand() of the GNU C library). No GPU needed. */
 int c2g_host_rand_sample(unsigned int seed, int n, int* out);

@@ -696,6 +696,39 @@ int oracle_dmrg_stats(void* h, double* out) {
   });
 }
 
+// The MPS tensor of `site` (TensorT block order, column-major); *n receives its length.
+int oracle_dmrg_get_mps(void* h, int site, double* out, int64_t cap, int64_t* n) {
+  return guard([&] {
+    auto* d = static_cast<OracleHandle*>(h)->dmrg.get();
+    if (site < 0 || site >= d->L) throw std::out_of_range("site");
+    const int64_t len = d->mps_lay[site]->size();
+    *n = len;
+    if (cap <= 0) return;
+    if (cap < len) throw std::invalid_argument("buffer shorter than the tensor");
+    std::copy(d->mps[site].begin(), d->mps[site].begin() + len, out);
+  });
+}
+
+// Rows (N, 2S, I, FCI dim, current dim) of the oracle's bookkeeper at `boundary`.
+int oracle_dmrg_sectors(void* h, int boundary, int* out, int cap, int* count) {
+  return guard([&] {
+    auto* d = static_cast<OracleHandle*>(h)->dmrg.get();
+    const CheMPS2::SyBookkeeper& bk = *d->bk;
+    if (boundary < 0 || boundary > bk.gL()) throw std::out_of_range("boundary");
+    const int ns = bk.num_sectors(boundary);
+    *count = ns;
+    for (int id = 0; id < ns && id < cap; id++) {
+      int n, s2, i;
+      bk.sector_labels(boundary, id, &n, &s2, &i);
+      out[5 * id + 0] = n;
+      out[5 * id + 1] = s2;
+      out[5 * id + 2] = i;
+      out[5 * id + 3] = bk.fci_dim_by_id(boundary, id);
+      out[5 * id + 4] = bk.cur_dim_by_id(boundary, id);
+    }
+  });
+}
+
 int oracle_dmrg_num_mps_var(void* h, int* n) {
   return guard([&] {
     auto* d = static_cast<OracleHandle*>(h)->dmrg.get();

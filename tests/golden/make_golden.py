@@ -1,7 +1,8 @@
 """Regenerates the golden fixtures of this directory from the reference's own tests.
 
-Run in a checkout that has the reference at REFERENCE (default /root/reference); the
-outputs are committed so that the tests never read the reference at run time.
+Run as `python make_golden.py <path of the CheMPS2 checkout>` (or with REFERENCE set to
+that path); the outputs are committed so that the tests never read the reference at run
+time.
 
   * N2.STO3G.FCIDUMP    copied from tests/matrixelements/N2.STO3G.FCIDUMP (the input of
                         the reference's tests/test1.cpp.in and tests/test5.cpp.in)
@@ -62,4 +63,7 @@ def main(reference: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE", "/root/reference")))
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <path of the CheMPS2 checkout> (or set REFERENCE)")
+    main(Path(ref))

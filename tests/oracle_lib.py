@@ -149,6 +149,20 @@ class OracleDMRG:
     def update(self, index, moving_right):
         self._check(lib().oracle_dmrg_update(self.h, index, int(moving_right)))
 
+    def get_mps(self, site):
+        n = C.c_int64()
+        self._check(lib().oracle_dmrg_get_mps(self.h, int(site), None, C.c_int64(0), C.byref(n)))
+        out = np.zeros(n.value)
+        self._check(lib().oracle_dmrg_get_mps(self.h, int(site), _dp(out), C.c_int64(n.value), C.byref(n)))
+        return out
+
+    def sectors(self, boundary):
+        n = C.c_int()
+        self._check(lib().oracle_dmrg_sectors(self.h, int(boundary), None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 5), dtype=np.int32)
+        self._check(lib().oracle_dmrg_sectors(self.h, int(boundary), _ip(out), n.value, C.byref(n)))
+        return out[:n.value]
+
     def stats(self):
         out = np.zeros(3)
         self._check(lib().oracle_dmrg_stats(self.h, _dp(out)))

@@ -1,0 +1,90 @@
+"""GPU parity on the benchmark configurations themselves (not only on small chains).
+
+* Hubbard chain L=16, N=16, S=0, C1, t=1, U=4, D=200, four left+right sweeps, Davidson
+  rtol 1e-8, noise 0, srand(1) (the reference's CPU-runnable configuration, set up as
+  tests/test4.cpp.in:46-49 does): the GPU's Solve() against the oracle's CPU DMRG with the
+  same schedule and seed, the final energy and the energy of every one of the 112 two-site
+  steps to 1e-8 Ha.
+* Synthetic ab initio L=24, N=24, S=0, D2h, D=1000 (seed 1234): the first eight steps of
+  the first left sweep (sites (22,23) down to (15,16)), step by step against the oracle to
+  1e-8 Ha, with the two-site object sizes equal at every step.
+* Synthetic ab initio L=30, N=30, S=0, D2h, D=2000 (seed 1234): the first four steps of the
+  first left sweep, as above.
+
+Both solvers stop at a residual norm <= rtol, so their energies differ by O(rtol^2); 1e-8
+Ha is the bar north of which the reference's own tests fail (tests/test4.cpp.in:103).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import chemps2_gb300 as c2g
+import models
+import oracle_lib as ol
+from chemps2_gb300.models import synthetic_ab_initio
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_objects(model, two_s, n, irrep, schedule):
+    ham = c2g.Hamiltonian(model.L, model.group, model.irreps)
+    L = model.L
+    for i in range(L):
+        for j in range(i, L):
+            if model.tmat[i, j] != 0.0:
+                ham.setTmat(i, j, float(model.tmat[i, j]))
+    for i, j, k, l in np.argwhere(model.vmat != 0.0):
+        if i <= j and i <= k:
+            ham.setVmat(int(i), int(j), int(k), int(l), float(model.vmat[i, j, k, l]))
+    ham.setEconst(model.econst)
+    prob = c2g.Problem(ham, two_s, n, irrep)
+    scheme = c2g.ConvergenceScheme(len(schedule))
+    for i, s in enumerate(schedule):
+        scheme.set_instruction(i, *s)
+    return ham, prob, scheme
+
+
+def test_config1_hubbard_l16_d200_four_sweeps_against_oracle():
+    m = models.hubbard(16, 4.0)
+    # Econv far below any change between sweeps, so that all four sweeps run in both
+    sched = [(200, 1e-30, 4, 0.0, 1e-8)]
+    ham, prob, scheme = gpu_objects(m, 0, 16, 0, sched)
+    c2g.srand(1)
+    gpu = c2g.DMRG(prob, scheme)
+    try:
+        e_gpu = gpu.Solve()
+        steps_gpu = gpu.step_energies()
+    finally:
+        gpu.close()
+    ol.srand(1)
+    cpu = ol.OracleDMRG(m, 0, 16, 0, sched, check=False)
+    e_cpu = cpu.solve()
+    steps_cpu = cpu.step_energies()
+    assert len(steps_gpu) == len(steps_cpu) == 4 * 2 * 14
+    assert abs(e_gpu - e_cpu) < 1e-8, (e_gpu, e_cpu)
+    diff = np.abs(steps_gpu - steps_cpu)
+    assert float(np.max(diff)) < 1e-8, (int(np.argmax(diff)), float(np.max(diff)))
+    # converged: the last sweep moves the energy by far less than the tolerance
+    assert abs(steps_gpu[-1] - steps_gpu[-29]) < 1e-6
+
+
+@pytest.mark.parametrize("L,D,nsteps", [(24, 1000, 8), (30, 2000, 4)])
+def test_synthetic_ab_initio_first_left_steps_against_oracle(L, D, nsteps):
+    m = synthetic_ab_initio(L, 7, 1234)
+    sched = [(D, 1e-10, 1, 0.0, 1e-8)]
+    ham, prob, scheme = gpu_objects(m, 0, L, 0, sched)
+    c2g.srand(1234)
+    gpu = c2g.DMRG(prob, scheme)
+    ol.srand(1234)
+    cpu = ol.OracleDMRG(m, 0, L, 0, sched, check=False)
+    try:
+        for index in range(L - 2, L - 2 - nsteps, -1):
+            assert gpu.sobject_size(index) == cpu.sobject_size(index), index
+            eg = gpu.solve_site(index, 1e-8, 0.0, D, False, False)
+            ec = cpu.solve_site(index, 1e-8, 0.0, D, False, False)
+            assert abs(eg - ec) < 1e-8, (index, eg, ec)
+            gpu.update(index, False)
+            cpu.update(index, False)
+    finally:
+        gpu.close()

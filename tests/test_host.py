@@ -160,6 +160,47 @@ def test_sobject_layout_bit_exact(L, group, N, two_s, irrep, D, index):
     assert list(order) == exp_order
 
 
+# The benchmark configurations: Hubbard L=16 C1 D=200, synthetic ab initio L=24 D2h
+# D=1000, L=30 D2h D=2000 and L=40 C2v D=4000 (N = L, S = 0, irreps round robin, target
+# irrep 0). Every boundary's FCI and scaled dimensions are checked against the restatement
+# of CheMPS2/SyBookkeeper.cpp, and the middle two-site object's block list, kappa2index and
+# visiting order against the restatement of CheMPS2/Sobject.cpp:36-145. The pinned counts
+# (sectors at the middle boundary, blocks and amplitudes of the middle two-site object)
+# are those of an independent probe of the reference's bookkeeping.
+BENCH_CONFIGS = [
+    # L, group, D, middle-boundary sectors, nKappa, two-site vector length
+    (16, 0, 200, 45, 466, 38028),
+    (24, 7, 1000, 707, 8412, 97786),
+    (30, 7, 2000, 1066, 13452, 221852),
+    (40, 5, 4000, 915, 12220, 523676),
+]
+
+
+@pytest.mark.parametrize("L,group,D,nsec,nkappa,veclen", BENCH_CONFIGS)
+def test_bookkeeper_and_sobject_at_benchmark_configs(L, group, D, nsec, nkappa, veclen):
+    nirr = models.NIRREPS[group]
+    irreps = [i % nirr for i in range(L)]
+    ham = c2g.Hamiltonian(L, group, np.array(irreps, dtype=np.int32))
+    prob = c2g.Problem(ham, 0, L, 0)
+    fci, cur = ref_bookkeeper(L, irreps, nirr, L, 0, 0, D)
+    for b in range(L + 1):
+        got = prob.bookkeeper_sectors(D, b)
+        got_f = {(b, int(r[0]), int(r[1]), int(r[2])): int(r[3]) for r in got if r[3] > 0}
+        got_c = {(b, int(r[0]), int(r[1]), int(r[2])): int(r[4]) for r in got if r[3] > 0}
+        assert got_f == {k: v for k, v in fci.items() if k[0] == b}, b
+        assert got_c == {k: v for k, v in cur.items() if k[0] == b}, b
+    mid = L // 2
+    assert sum(1 for r in prob.bookkeeper_sectors(D, mid) if r[4] > 0) == nsec
+    index = L // 2 - 1
+    labels, k2i, order = prob.sobject_layout(D, index)
+    exp = ref_sobject_blocks(prob, D, index, L, irreps, nirr)
+    assert len(labels) == nkappa and int(k2i[-1]) == veclen
+    assert [tuple(int(v) for v in r) for r in labels] == [b[0] for b in exp]
+    sizes = [b[1] for b in exp]
+    assert list(k2i) == list(np.concatenate([[0], np.cumsum(sizes)]))
+    assert list(order) == sorted(range(len(sizes)), key=lambda k: -sizes[k])
+
+
 # ---------------------------------------------------------------- Wigner symbols
 def racah_6j(a, b, c, d, e, f):
     """Exact 6j symbol in rationals (arguments twice the spins), Racah's formula."""
@@ -197,6 +238,46 @@ def test_wigner6j_against_exact_racah():
     assert n > 1000
     # large arguments stay accurate (|err| <= 7e-12 at 2j <= 95 in the reference)
     assert abs(c2g.wigner6j(90, 90, 0, 90, 90, 0) - 1.0 / 91) < 1e-12
+
+
+def ninej_from_6j(a, b, c, d, e, f, g, h, i):
+    """9j symbol {a b c; d e f; g h i} (arguments twice the spins) as the sum over x of
+    (-1)^(2x) (2x + 1) {a b c; f i x} {d e f; b x h} {g h i; x a d} (Edmonds 6.4.3), from
+    the exact-rational 6j symbols above."""
+    tot = 0.0
+    for x in range(0, 2 * max(a, b, c, d, e, f, g, h, i) + 2):
+        w = racah_6j(a, b, c, f, i, x)
+        if w == 0.0:
+            continue
+        w *= racah_6j(d, e, f, b, x, h)
+        if w == 0.0:
+            continue
+        w *= racah_6j(g, h, i, x, a, d)
+        tot += (-1) ** x * (x + 1) * w
+    return tot
+
+
+def test_wigner9j_against_6j_sums():
+    rng = np.random.default_rng(5)
+    n = 0
+    for _ in range(4000):
+        a, b, d, e = (int(x) for x in rng.integers(0, 6, size=4))
+        for c in range(abs(a - b), a + b + 1, 2):
+            for f in range(abs(d - e), d + e + 1, 2):
+                g = int(rng.integers(0, 6))
+                for h in range(abs(b - e) + ((abs(b - e) + g) % 2 != (b + e + g) % 2), b + e + 1, 2):
+                    for i in range(abs(c - f), c + f + 1, 2):
+                        if not (abs(a - d) <= g <= a + d and (a + d + g) % 2 == 0):
+                            continue
+                        if not (abs(g - h) <= i <= g + h and (g + h + i) % 2 == 0):
+                            continue
+                        ref = ninej_from_6j(a, b, c, d, e, f, g, h, i)
+                        got = c2g.wigner9j(a, b, c, d, e, f, g, h, i)
+                        assert abs(got - ref) < 1e-12, (a, b, c, d, e, f, g, h, i, got, ref)
+                        n += 1
+        if n > 400:
+            break
+    assert n > 400
 
 
 def test_wigner_argument_errors_are_status_codes():
