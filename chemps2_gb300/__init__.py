@@ -386,6 +386,15 @@ class DMRG:
         _check(load().c2g_dmrg_heff_apply_fp32(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size)))
         return y
 
+    def heff_apply_precision(self, index, x, precision="tc"):
+        """y = Heff x with the matvec arithmetic 'fp64', 'fp32' or 'tc' (large blocks on the
+        tensor cores as split-BF16 products, the rest FP32)."""
+        xx = np.ascontiguousarray(x, dtype=np.float64).copy()
+        y = np.zeros_like(xx)
+        _check(load().c2g_dmrg_heff_apply_precision(self._d, int(index), _dp(xx), _dp(y), C.c_int64(xx.size),
+                                                    int(PRECISION_CODES[precision])))
+        return y
+
     def loadedMPS(self):
         """True when the MPS was loaded from a checkpoint file (makechkpt)."""
         v = C.c_int()
@@ -472,22 +481,28 @@ class DMRG:
     def heff_apply_device(self, index, x_ptr, y_ptr, n, precision="fp64", stream=0):
         """y = Heff x on device buffers given as integer addresses (e.g. torch's data_ptr())
         of n doubles; `stream` an integer cudaStream_t (0: synchronous)."""
-        p = {"fp64": 0, "fp32": 1}[precision] if isinstance(precision, str) else int(precision)
+        p = PRECISION_CODES[precision] if isinstance(precision, str) else int(precision)
         _check(load().c2g_dmrg_heff_apply_device(self._d, int(index), C.c_void_p(int(x_ptr)), C.c_void_p(int(y_ptr)),
                                                  C.c_int64(int(n)), int(p), C.c_void_p(int(stream) or None)))
 
     def set_precision(self, mode="fp64", mixed_tol=1e-5):
-        """'fp64' (the reference's arithmetic) or 'mixed' (FP32 Davidson expansion, FP64 finish)."""
-        m = {"fp64": 0, "mixed": 1}[mode] if isinstance(mode, str) else int(mode)
+        """'fp64' (the reference's arithmetic), 'mixed' (FP32 Davidson expansion, FP64
+        refinement) or 'mixed_tc' (as 'mixed', the large blocks of the reduced-precision
+        matvecs on the tensor cores as split-BF16 products)."""
+        m = {"fp64": 0, "mixed": 1, "mixed_tc": 2}[mode] if isinstance(mode, str) else int(mode)
         _check(load().c2g_dmrg_set_precision(self._d, m, C.c_double(mixed_tol)))
 
     def bench_heff(self, index, warmup, steps, flush_bytes=0, precision="fp64"):
         ms, fl, by = C.c_double(), C.c_double(), C.c_double()
         nl = C.c_longlong()
-        p = {"fp64": 0, "fp32": 1, "mixed": 1}[precision]
+        p = PRECISION_CODES[precision]
         _check(load().c2g_dmrg_bench_heff(self._d, int(index), int(warmup), int(steps), C.c_longlong(flush_bytes),
                                           int(p), C.byref(ms), C.byref(fl), C.byref(by), C.byref(nl)))
         return {"ms_per_matvec": ms.value, "flops": fl.value, "bytes": by.value, "launches": nl.value}
+
+
+# matvec arithmetic codes of the C-ABI
+PRECISION_CODES = {"fp64": 0, "fp32": 1, "mixed": 1, "tc": 2, "mixed_tc": 2}
 
 
 def solve_batch(problems, schemes, seeds, workers=8, raise_on_error=True):
@@ -515,6 +530,28 @@ def solve_batch(problems, schemes, seeds, workers=8, raise_on_error=True):
         _check(rc)
     return [{"energy": float(energies[i]), "matvecs": int(matvecs[i]), "seconds": float(seconds[i]),
              "status": int(statuses[i]), "stats": dict(zip(STAT_NAMES, stats[i].tolist()))} for i in range(n)]
+
+
+def rayleigh_ritz_eig(mat, prev_evecs=None, reps=1):
+    """The Davidson solver's device eigensolver on a symmetric matrix of order <= 32:
+    (eigenvalues ascending, eigenvectors as columns, microseconds per call). prev_evecs:
+    eigenvectors of the leading (n-1) x (n-1) block (warm start)."""
+    a = np.asfortranarray(mat, dtype=np.float64)
+    n = a.shape[0]
+    ev = np.zeros(n)
+    vec = np.zeros((n, n), order="F")
+    warm = prev_evecs is not None
+    if warm:
+        vec[: n - 1, : n - 1] = prev_evecs
+        buf = np.asfortranarray(np.asarray(prev_evecs, dtype=np.float64)).ravel(order="F").copy()
+        flat = np.zeros(n * n)
+        flat[: buf.size] = buf
+    else:
+        flat = np.zeros(n * n)
+    us = C.c_double()
+    _check(load().c2g_rayleigh_ritz_eig(int(n), _dp(a.ravel(order="F")), int(warm), _dp(ev), _dp(flat), int(reps),
+                                        C.byref(us)))
+    return ev, flat.reshape((n, n), order="F"), us.value
 
 
 def device_memory_info(device: int = -1):

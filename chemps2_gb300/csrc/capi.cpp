@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "device/kernels.cuh"
 #include "dmrg/runtime.hpp"
 #include "host/chemps2/Batch.h"
 #include "host/chemps2/ConvergenceScheme.h"
@@ -398,7 +399,8 @@ int c2g_dmrg_presolve(c2g_dmrg* d) {
 int c2g_dmrg_set_precision(c2g_dmrg* d, int mode, double mixed_tol) {
   return guarded([&] {
     NEED(d);
-    if (mode != 0 && mode != 1) throw std::invalid_argument("precision mode must be 0 (FP64) or 1 (mixed)");
+    if (mode < 0 || mode > 2)
+      throw std::invalid_argument("precision mode must be 0 (FP64), 1 (mixed, FP32) or 2 (mixed, tensor cores)");
     if (!(mixed_tol > 0.0)) throw std::invalid_argument("mixed tolerance must be positive");
     d->d->set_precision(mode, mixed_tol);
   });
@@ -479,6 +481,12 @@ int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64
   return guarded([&] {
     NEED(d);
     d->d->heff_apply_host(index, false, x, y, nullptr, n, 1);
+  });
+}
+int c2g_dmrg_heff_apply_precision(c2g_dmrg* d, int index, double* x, double* y, int64_t n, int precision) {
+  return guarded([&] {
+    NEED(d);
+    d->d->heff_apply_host(index, false, x, y, nullptr, n, precision);
   });
 }
 int c2g_dmrg_activate_excitations(c2g_dmrg* d, int max_exc) {
@@ -685,6 +693,58 @@ int c2g_truncation_eig(int count, const int* n, const double* mats, double* eval
     C2G_CUDA(cudaMemcpy(evecs, d + tot + totn, sizeof(double) * tot, cudaMemcpyDeviceToHost));
     cudaFree(dj);
     cudaFree(d);
+  });
+}
+
+int c2g_rayleigh_ritz_eig(int n, const double* mat, int warm, double* evals, double* evecs, int reps,
+                          double* us_per_call) {
+  return guarded([&] {
+    if (n < 1 || n > 32) throw std::invalid_argument("c2g_rayleigh_ritz_eig: order outside 1..32");
+    if (reps < 1) throw std::invalid_argument("c2g_rayleigh_ritz_eig: reps must be positive");
+    NEED(mat);
+    NEED(evals);
+    NEED(evecs);
+    constexpr int ld = 32;
+    std::vector<double> hm(static_cast<size_t>(ld) * ld, 0.0), he(static_cast<size_t>(ld) * ld, 0.0);
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) hm[i + ld * j] = mat[i + static_cast<size_t>(n) * j];
+    if (warm)
+      for (int j = 0; j < n - 1; j++)
+        for (int i = 0; i < n - 1; i++) he[i + ld * j] = evecs[i + static_cast<size_t>(n - 1) * j];
+    double* d = nullptr;
+    C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), sizeof(double) * (2 * ld * ld + ld)));
+    struct Free {
+      double* p;
+      ~Free() { cudaFree(p); }
+    } guard_free{d};
+    double* dm = d;
+    double* de = d + ld * ld;
+    double* dv = d + 2 * ld * ld;
+    C2G_CUDA(cudaMemcpy(dm, hm.data(), sizeof(double) * ld * ld, cudaMemcpyHostToDevice));
+    cudaEvent_t e0, e1;
+    C2G_CUDA(cudaEventCreate(&e0));
+    C2G_CUDA(cudaEventCreate(&e1));
+    float total_ms = 0.f;
+    for (int r = 0; r < reps; r++) {
+      // every repetition starts from the same inputs (the kernel overwrites evecs)
+      C2G_CUDA(cudaMemcpy(de, he.data(), sizeof(double) * ld * ld, cudaMemcpyHostToDevice));
+      C2G_CUDA(cudaEventRecord(e0));
+      C2G_CUDA(c2g::launch_small_eig(dm, n, ld, dv, de, nullptr, warm != 0));
+      C2G_CUDA(cudaEventRecord(e1));
+      C2G_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      total_ms += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::vector<double> hv(ld);
+    C2G_CUDA(cudaMemcpy(hv.data(), dv, sizeof(double) * ld, cudaMemcpyDeviceToHost));
+    C2G_CUDA(cudaMemcpy(he.data(), de, sizeof(double) * ld * ld, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) evals[i] = hv[i];
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) evecs[i + static_cast<size_t>(n) * j] = he[i + ld * j];
+    if (us_per_call) *us_per_call = 1e3 * total_ms / reps;
   });
 }
 

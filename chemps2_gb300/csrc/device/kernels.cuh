@@ -109,7 +109,11 @@ inline int sandwich_grid(int m, int n) {
 // Arithmetic of the block sandwich: FP64 throughout, or FP32 operands (the FP32 copies of
 // SlotPtrs), products and per-lane sums, with the lane reduction and the FP64 output
 // update in FP64. The FP32 variant issues no FP64 instruction in its item loop.
-enum class Precision : int { kFP64 = 0, kFP32 = 1 };
+// kTC: the two-pass groups on the tensor cores as split-BF16 three-term products with FP32
+// accumulation (sandwich_tc.cu), every other kernel as kFP32 (same FP32 operand copies).
+enum class Precision : int { kFP64 = 0, kFP32 = 1, kTC = 2 };
+// The arithmetic of the SIMT kernels of a run of precision p.
+inline Precision simt_precision(Precision p) { return p == Precision::kTC ? Precision::kFP32 : p; }
 
 cudaError_t launch_inter_gemm(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp,
                               cudaStream_t stream, Precision prec);
@@ -121,6 +125,13 @@ cudaError_t launch_sum_gemm(const SumGroup* groups, const SumItem* items, const 
                             double* partials, unsigned int* counters, const SlotPtrs& sp, cudaStream_t stream,
                             Precision prec);
 
+
+// Tensor-core variants of the two passes (sandwich_tc.cu), reading the FP32 operand copies.
+// `err` (device-visible, may be null) is or-ed with 1 when a kernel gave up a bounded wait.
+cudaError_t launch_inter_tc(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp, int* err,
+                            cudaStream_t stream);
+cudaError_t launch_sum_tc(const SumGroup* groups, const SumItem* items, const GemmTile* tiles, int ntiles,
+                          double* partials, unsigned int* counters, const SlotPtrs& sp, int* err, cudaStream_t stream);
 
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
                             int ntiles, const SlotPtrs& sp, cudaStream_t stream, Precision prec = Precision::kFP64);
@@ -232,7 +243,11 @@ cudaError_t launch_reverse_columns(double* dst, const double* src, int rows, int
 
 // Davidson device steps (CheMPS2/Davidson.cpp). `sc` is a small device scratch of
 // scalars; layout documented in kernels.cu.
-cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream);
+// Eigenvalues ascending in evals[0, n), eigenvectors in the columns of evecs (ld). warm:
+// evecs holds the eigenvectors of the leading (n - 1) x (n - 1) block of mat (the previous
+// call on the same matrix before it grew by one row and column).
+cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream,
+                             bool warm = false);
 // Batched Jacobi eigendecompositions of the Gram matrices of the truncation step, one CTA
 // per job (n <= kBatchedEigMax); offsets in doubles from `base` (jobs on the device).
 constexpr int kBatchedEigMax = 32;

@@ -1,0 +1,479 @@
+// Two-pass path of large groups on the 5th-generation tensor cores (tcgen05), for the
+// mixed-precision Heff: both passes of sandwich_gemm.cu with the products formed as
+// split-BF16 three-term products accumulated in FP32 in tensor memory.
+//
+// Each FP32 operand value v (the FP32 copies of X, of the operators and of the pass-1
+// intermediates, times the item's coefficient for the left operand) is split into
+// hi = bf16(v) and lo = bf16(v - hi); a product is hi_a hi_b + hi_a lo_b + lo_a hi_b, which
+// keeps about 16 significant bits of each factor (relative error ~1e-5 per product, the
+// missing lo_a lo_b term ~2^-16 of it). Sums over the inner dimension and over the items
+// accumulate in FP32 in tensor memory; the item sum of a tile is turned into FP64 in the
+// epilogue (split tiles are reduced in FP64 in split order, as in the SIMT path).
+//
+// One 128-thread CTA per output tile (the same 64 x 64 grid and tile list as the SIMT
+// kernels). The tile is the top-left 64 x 64 of a 128 x 64 MMA (M = 128, N = 64): rows
+// 64..127 of the A operand are never written and their accumulator rows never read. The
+// inner dimension is staged in chunks of 16 through two shared-memory stages: all threads
+// load a chunk (FP32, coalesced along whichever index is unit-stride), scale, split and
+// store it in the no-swizzle K-major layout of the MMA (8-row x 16-byte core matrices,
+// core matrices adjacent along K 128 bytes apart, 8-row groups 256 bytes apart); one
+// thread issues the three MMAs of the chunk and commits them to the stage's mbarrier,
+// which the threads wait on before they overwrite that stage two chunks later. Items with
+// an inner dimension shorter than 16 are padded with zeros. The accumulator (64 FP32
+// columns of tensor memory, allocated by warp 0) is read by warps 0 and 1 (lanes 0..63 =
+// tile rows) with tcgen05.ld.
+//
+// Every mbarrier wait is bounded: after kTcSpinLimit polls the kernel records an error in
+// the runtime's mapped error word, waits (bounded again) for its own MMAs, frees its tensor
+// memory and returns without writing its tile.
+#include <cuda_bf16.h>
+
+#include "kernels.cuh"
+#include "slots.cuh"
+
+namespace c2g {
+
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr int kTcM = 128, kTcN = 64, kTcK = 16;
+constexpr int kTcStages = 2;
+constexpr int kTcABytes = kTcM * kTcK * 2;  // 4096: one BF16 A operand of a chunk
+constexpr int kTcBBytes = kTcN * kTcK * 2;  // 2048: one BF16 B operand of a chunk
+constexpr int kTcStageBytes = 2 * kTcABytes + 2 * kTcBBytes;  // A hi, A lo, B hi, B lo
+constexpr uint32_t kTcTmemCols = 64;
+constexpr long long kTcSpinLimit = 1LL << 26;
+
+struct __align__(1024) TcSmem {
+  unsigned char stage[kTcStages][kTcStageBytes];
+  unsigned long long bar[kTcStages];
+  uint32_t tmem_base;
+};
+
+// Instruction descriptor of kind::f16 (tcgen05.mma): D F32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t(kTcN) >> 3) << 17) |
+                              ((uint32_t(kTcM) >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor, no swizzle: start address, leading-dimension byte
+// offset (between core matrices adjacent along K), stride-dimension byte offset (between
+// 8-row groups), the descriptor version bit 46.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return static_cast<uint64_t>((saddr >> 4) & 0x3FFFu) | (static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16) |
+         (static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// byte offset of element (row, k) of a chunk operand (k < 16) in the K-major layout
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k) {
+  return static_cast<uint32_t>((row >> 3) * 256 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait for phase `parity` of the barrier; false when the limit was reached
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+  for (long long i = 0; i < kTcSpinLimit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "setp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 accumulator columns of this thread's lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcOpnd {  // element (i, k) of op(M): t ? p[k + ld i] : p[i + ld k]
+  const float* p;
+  int64_t ld;
+  bool t;
+};
+
+__device__ __forceinline__ TcOpnd tc_opnd(const SlotPtrs& sp, const GemmOperand& g, int di, int dk) {
+  const float* p = resolve<float>(sp, g.ref);
+  const int64_t ld = g.ld;
+  const bool t = g.trans != 0;
+  return TcOpnd{t ? p + dk + ld * di : p + di + ld * dk, ld, t};
+}
+
+// One chunk of values held by a thread between its loads and its shared-memory stores:
+// 8 elements of op(L) (64 rows x 16) and 8 of op(R)^T (64 columns x 16).
+struct TcChunk {
+  float a[8], b[8];
+};
+
+// element e = tid + 128 s of a 64 x 16 operand chunk: (row, k), unit-stride index fastest
+__device__ __forceinline__ void chunk_pos(bool t, int e, int& row, int& k) {
+  if (t) {
+    k = e & 15;
+    row = e >> 4;
+  } else {
+    row = e & 63;
+    k = e >> 6;
+  }
+}
+
+__device__ __forceinline__ void tc_fetch(TcChunk& c, const TcOpnd& L, int M, const TcOpnd& R, int N, int K, int k0,
+                                         float alpha) {
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    int i, k;
+    chunk_pos(L.t, tid + kTcThreads * s, i, k);
+    const int kk = k0 + k;
+    c.a[s] = (i < M && kk < K) ? alpha * (L.t ? L.p[kk + L.ld * i] : L.p[i + L.ld * kk]) : 0.0f;
+  }
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    int j, k;
+    chunk_pos(!R.t, tid + kTcThreads * s, j, k);  // op(R)(k, j): unit stride along j unless transposed
+    const int kk = k0 + k;
+    c.b[s] = (j < N && kk < K) ? (R.t ? R.p[j + R.ld * kk] : R.p[kk + R.ld * j]) : 0.0f;
+  }
+}
+
+__device__ __forceinline__ void split_store(unsigned char* hi, unsigned char* lo, uint32_t off, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+  *reinterpret_cast<__nv_bfloat16*>(hi + off) = h;
+  *reinterpret_cast<__nv_bfloat16*>(lo + off) = l;
+}
+
+__device__ __forceinline__ void tc_store(const TcChunk& c, bool lt, bool rt, unsigned char* stage) {
+  unsigned char* ahi = stage;
+  unsigned char* alo = stage + kTcABytes;
+  unsigned char* bhi = stage + 2 * kTcABytes;
+  unsigned char* blo = stage + 2 * kTcABytes + kTcBBytes;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    int i, k;
+    chunk_pos(lt, tid + kTcThreads * s, i, k);
+    split_store(ahi, alo, kmajor_off(i, k), c.a[s]);
+  }
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    int j, k;
+    chunk_pos(!rt, tid + kTcThreads * s, j, k);
+    split_store(bhi, blo, kmajor_off(j, k), c.b[s]);
+  }
+}
+
+// The three MMAs of a staged chunk: D (+)= Ahi Bhi + Ahi Blo + Alo Bhi.
+__device__ __forceinline__ void tc_issue(uint32_t tmem_d, const unsigned char* stage, bool first) {
+  const uint32_t base = smem_u32(stage);
+  const uint64_t ahi = smem_desc(base, 128, 256);
+  const uint64_t alo = smem_desc(base + kTcABytes, 128, 256);
+  const uint64_t bhi = smem_desc(base + 2 * kTcABytes, 128, 256);
+  const uint64_t blo = smem_desc(base + 2 * kTcABytes + kTcBBytes, 128, 256);
+  tc_mma(tmem_d, alo, bhi, first ? 0u : 1u);
+  tc_mma(tmem_d, ahi, blo, 1u);
+  tc_mma(tmem_d, ahi, bhi, 1u);
+}
+
+// Item sources: the (L, R, alpha, K) products a tile sums, in order.
+struct InterSource {  // pass 1: one product
+  const InterJob* J;
+  int row0, col0;
+  __device__ int count() const { return 1; }
+  __device__ bool get(int, const SlotPtrs& sp, TcOpnd& L, TcOpnd& R, float& alpha, int& K) const {
+    L = tc_opnd(sp, J->l, row0, 0);
+    R = tc_opnd(sp, J->r, 0, col0);
+    alpha = 1.0f;
+    K = J->k;
+    return K > 0;
+  }
+};
+
+struct SumSource {  // pass 2: the GEMM items of [item0, item1) (items with k = 0 are skipped)
+  const SumItem* items;
+  int item0, item1, row0, col0;
+  __device__ int count() const { return item1 - item0; }
+  __device__ bool get(int q, const SlotPtrs& sp, TcOpnd& L, TcOpnd& R, float& alpha, int& K) const {
+    const SumItem& I = items[item0 + q];
+    K = I.k;
+    if (K <= 0) return false;
+    L = tc_opnd(sp, I.l, row0, 0);
+    R = tc_opnd(sp, I.r, 0, col0);
+    alpha = static_cast<float>(I.alpha);
+    return true;
+  }
+};
+
+// Sums the products of `src` into the tensor-memory accumulator. Returns the number of
+// chunks issued (0: the accumulator was never written), or -1 when a wait ran out (the
+// decision is the same in every thread of the CTA).
+template <class Src>
+__device__ int tc_accumulate(const Src& src, int M, int N, const SlotPtrs& sp, TcSmem& sm, uint32_t tmem_d,
+                             uint32_t (&phase)[kTcStages], bool (&pending)[kTcStages]) {
+  int chunk = 0;
+  const int n = src.count();
+  for (int q = 0; q < n; q++) {
+    TcOpnd L, R;
+    float alpha;
+    int K;
+    if (!src.get(q, sp, L, R, alpha, K)) continue;
+    for (int k0 = 0; k0 < K; k0 += kTcK) {
+      const int s = chunk & 1;
+      TcChunk c;
+      tc_fetch(c, L, M, R, N, K, k0, alpha);
+      bool ok = true;
+      if (pending[s]) {  // the MMAs that read this stage two chunks ago
+        ok = mbar_wait(&sm.bar[s], phase[s]);
+        phase[s] ^= 1u;
+        pending[s] = false;
+      }
+      tc_store(c, L.t, R.t, sm.stage[s]);
+      fence_async_smem();
+      if (__syncthreads_or(!ok)) return -1;
+      if (threadIdx.x == 0) {
+        tc_fence_after();
+        tc_issue(tmem_d, sm.stage[s], chunk == 0);
+        tc_commit(&sm.bar[s]);
+      }
+      pending[s] = true;
+      chunk++;
+    }
+  }
+  return chunk;
+}
+
+// Waits for every committed chunk; false (in every thread) when a wait ran out.
+__device__ bool tc_drain(TcSmem& sm, uint32_t (&phase)[kTcStages], bool (&pending)[kTcStages]) {
+  bool ok = true;
+  for (int s = 0; s < kTcStages; s++) {
+    if (!pending[s]) continue;
+    if (!mbar_wait(&sm.bar[s], phase[s])) ok = false;
+    phase[s] ^= 1u;
+    pending[s] = false;
+  }
+  return !__syncthreads_or(!ok);
+}
+
+__device__ void tc_setup(TcSmem& sm) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTcStages; s++) mbar_init(&sm.bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(kTcTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+}
+
+__device__ void tc_teardown(uint32_t tmem_d) {
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(kTcTmemCols) : "memory");
+  }
+}
+
+// Accumulator columns c0 .. c0 + 15 of this thread's tile row (warps 0 and 1: rows 0..63);
+// zeros when no chunk was issued.
+__device__ __forceinline__ void tc_read16(uint32_t tmem_d, int chunks, int c0, float (&v)[16]) {
+  if (chunks <= 0) {
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = 0.0f;
+    return;
+  }
+  const int warp = threadIdx.x >> 5;
+  tmem_ld16(tmem_d + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
+}
+
+__device__ __forceinline__ void record_failure(int* err) {
+  if (threadIdx.x == 0 && err) atomicOr(err, 1);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 4)
+    inter_tc_kernel(const InterJob* __restrict__ jobs, const GemmTile* __restrict__ tiles, SlotPtrs sp, int* err) {
+  __shared__ TcSmem sm;
+  tc_setup(sm);
+  const uint32_t tmem_d = sm.tmem_base;
+  const GemmTile T = tiles[blockIdx.x];
+  const InterJob J = jobs[T.idx];
+  const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
+  const int tm = min(64, J.m - row0), tn = min(64, J.n - col0);
+  uint32_t phase[kTcStages] = {0u, 0u};
+  bool pending[kTcStages] = {false, false};
+  const InterSource src{&J, row0, col0};
+  const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
+  const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
+  tc_fence_after();
+  if (!ok) {
+    record_failure(err);
+  } else if (threadIdx.x < 64) {
+    float* S = sp.inter32 + J.off;
+    const int r = threadIdx.x;
+#pragma unroll
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      float v[16];
+      tc_read16(tmem_d, chunks, c0, v);
+      if (r < tm) {
+#pragma unroll
+        for (int c = 0; c < 16; c++)
+          if (c0 + c < tn) S[(row0 + r) + static_cast<int64_t>(J.m) * (col0 + c0 + c)] = v[c];
+      }
+    }
+  }
+  tc_teardown(tmem_d);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 4)
+    sum_tc_kernel(const SumGroup* __restrict__ groups, const SumItem* __restrict__ items,
+                  const GemmTile* __restrict__ tiles, double* partials, unsigned int* counters, SlotPtrs sp, int* err) {
+  __shared__ TcSmem sm;
+  __shared__ int is_last;
+  tc_setup(sm);
+  const uint32_t tmem_d = sm.tmem_base;
+  const GemmTile T = tiles[blockIdx.x];
+  const SumGroup G = groups[T.idx];
+  const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
+  const int tm = min(64, G.m - row0), tn = min(64, G.n - col0);
+  uint32_t phase[kTcStages] = {0u, 0u};
+  bool pending[kTcStages] = {false, false};
+  const SumSource src{items, T.item0, T.item1, row0, col0};
+  const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
+  const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
+  tc_fence_after();
+  if (!ok) record_failure(err);
+  const int r = threadIdx.x;
+  double* O = const_cast<double*>(resolve<double>(sp, G.out));
+  const int64_t ldo = G.ldo;
+  const bool accum = (G.flags & kAccumulate) != 0;
+  // partial tiles of a split tile: TM x TN doubles per split (the tile's 16-granular
+  // extents, as planned on the host), element (row, col) at row + TM col
+  const int TM = 16 * ((T.shape & 3) + 1);
+  double* part = partials + T.part;
+  const int64_t part_elems = static_cast<int64_t>(TM) * 16 * (((T.shape >> 2) & 3) + 1);
+  if (ok && r < 64) {
+#pragma unroll
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      float v[16];
+      tc_read16(tmem_d, chunks, c0, v);
+      double acc[16];
+#pragma unroll
+      for (int c = 0; c < 16; c++) acc[c] = static_cast<double>(v[c]);
+      // items without an inner dimension: out += alpha op(R), straight from global memory
+      if (r < tm) {
+        for (int it = T.item0; it < T.item1; it++) {
+          const SumItem I = items[it];
+          if (I.k > 0) continue;
+          const TcOpnd R = tc_opnd(sp, I.r, row0, col0 + c0);
+#pragma unroll
+          for (int c = 0; c < 16; c++)
+            if (c0 + c < tn)
+              acc[c] = fma(I.alpha, static_cast<double>(R.t ? R.p[c + R.ld * r] : R.p[r + R.ld * c]), acc[c]);
+        }
+      }
+      if (T.nsplit > 1) {
+        if (r < tm) {
+#pragma unroll
+          for (int c = 0; c < 16; c++)
+            if (c0 + c < tn) __stcg(part + T.split * part_elems + r + TM * (c0 + c), acc[c]);
+        }
+      } else if (r < tm) {
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          if (c0 + c < tn) {
+            const int64_t idx = (row0 + r) + ldo * (col0 + c0 + c);
+            O[idx] = accum ? O[idx] + acc[c] : acc[c];
+          }
+        }
+      }
+    }
+  }
+  if (T.nsplit > 1) {
+    // the last split to arrive adds the partial tiles up in split order
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(counters + T.counter, 1u) == static_cast<unsigned>(T.nsplit - 1);
+    __syncthreads();
+    if (is_last) {
+      __threadfence();
+      if (threadIdx.x == 0) counters[T.counter] = 0u;  // ready for the next launch
+      if (ok && r < tm) {
+        for (int c = 0; c < tn; c++) {
+          double v = 0.0;
+          for (int s = 0; s < T.nsplit; s++) v += __ldcg(part + s * part_elems + r + TM * c);
+          const int64_t idx = (row0 + r) + ldo * (col0 + c);
+          O[idx] = accum ? O[idx] + v : v;
+        }
+      }
+    }
+  }
+  tc_teardown(tmem_d);
+}
+
+}  // namespace
+
+cudaError_t launch_inter_tc(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp, int* err,
+                            cudaStream_t stream) {
+  if (ntiles <= 0) return cudaSuccess;
+  inter_tc_kernel<<<ntiles, kTcThreads, 0, stream>>>(jobs, tiles, sp, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_tc(const SumGroup* groups, const SumItem* items, const GemmTile* tiles, int ntiles,
+                          double* partials, unsigned int* counters, const SlotPtrs& sp, int* err, cudaStream_t stream) {
+  if (ntiles <= 0) return cudaSuccess;
+  sum_tc_kernel<<<ntiles, kTcThreads, 0, stream>>>(groups, items, tiles, partials, counters, sp, err);
+  return cudaGetLastError();
+}
+
+}  // namespace c2g

@@ -315,16 +315,142 @@ __device__ void jacobi_eig(EigSmem& sm, const double* __restrict__ mat, int n, i
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) small_eig_kernel(const double* __restrict__ mat, int n, int ld,
-                                                        double* __restrict__ evals, double* __restrict__ evecs) {
-  __shared__ EigSmem sm;
-  jacobi_eig(sm, mat, n, ld);
+// The Rayleigh-Ritz eigenproblem of the Davidson solver (CheMPS2/Davidson.cpp:242-276,
+// where the reference calls dsyev on the <= 32 x 32 projected matrix): cyclic Jacobi with
+// the round-robin (Brent-Luk) ordering, n / 2 disjoint rotations per round, one thread per
+// matrix element. A round is two barriers: the pair leaders compute their rotations, then
+// every thread forms its element of J^T A J and of V J from the four (two) elements it
+// depends on, into the other buffer. The pairs of round r are fixed by position:
+// pos(0) = 0, pos(k) = 1 + (k - 1 - r mod m - 1), pairs (pos(t), pos(m - 1 - t)).
+// Warm start (Davidson expansion): the matrix grew by one row and column since the
+// previous call, whose eigenvectors E are still in evecs; the solver starts from
+// A = diag(E, 1)^T M diag(E, 1) (diagonal but for the last row and column) and V = diag(E, 1),
+// which takes two to three sweeps instead of six to ten.
+constexpr int kRrThreads = kEigMax * kEigMax;
+__global__ void __launch_bounds__(kRrThreads) rr_eig_kernel(const double* __restrict__ mat, int n, int ld,
+                                                            double* __restrict__ evals, double* __restrict__ evecs,
+                                                            int warm) {
+  __shared__ double A[2][kEigMax][kEigMax + 1];
+  __shared__ double V[2][kEigMax][kEigMax + 1];
+  __shared__ double alpha[kEigMax], beta[kEigMax];
+  __shared__ int partner[kEigMax];
+  __shared__ double red[2][kEigMax];
+  __shared__ int done;
+  __shared__ int rank[kEigMax];
   const int tid = threadIdx.x;
-  if (tid < n) evals[tid] = sm.A[sm.order[tid]][sm.order[tid]];
-  for (int e = tid; e < n * n; e += blockDim.x) {
-    const int i = e % n, j = e / n;
-    evecs[i + ld * j] = sm.Vm[i][sm.order[j]];
+  const int i = tid % kEigMax, j = tid / kEigMax;  // element (i, j), column-major
+  const bool in = i < n && j < n;
+  // ---- start
+  if (warm) {
+    // E (n - 1 columns of the previous call, ld) extended by the unit vector e_{n-1}
+    auto Ehat = [&](int a, int b) -> double {
+      if (a == n - 1 || b == n - 1) return (a == b) ? 1.0 : 0.0;
+      return evecs[a + ld * b];
+    };
+    double t = 0.0;  // T = M Ehat, element (i, j)
+    if (in)
+      for (int b = 0; b < n; b++) t = fma(mat[i + ld * b], Ehat(b, j), t);
+    A[1][i][j] = t;
+    V[0][i][j] = in ? Ehat(i, j) : 0.0;
+    __syncthreads();
+    double g = 0.0;  // Ehat^T T
+    if (in)
+      for (int a = 0; a < n; a++) g = fma(V[0][a][i], A[1][a][j], g);
+    A[0][i][j] = g;
+  } else {
+    A[0][i][j] = in ? mat[i + ld * j] : 0.0;
+    V[0][i][j] = (in && i == j) ? 1.0 : 0.0;
   }
+  __syncthreads();
+  {  // exact symmetry of the starting matrix
+    const double a = in ? 0.5 * (A[0][i][j] + A[0][j][i]) : 0.0;
+    __syncthreads();
+    if (in) A[0][i][j] = a;
+  }
+  __syncthreads();
+  const int m = (n % 2 == 0) ? n : n + 1;  // index n is a dummy when n is odd
+  const int npair = m / 2;
+  int cur = 0;
+  for (int sweep = 0; sweep < 30 && n > 1; sweep++) {
+    // convergence: off-diagonal against total squared norm (every thread takes one element)
+    {
+      const double v = in ? A[cur][i][j] * A[cur][i][j] : 0.0;
+      double off = (i != j) ? v : 0.0, tot = v;
+      for (int o = 16; o > 0; o >>= 1) {
+        off += __shfl_down_sync(0xffffffffu, off, o);
+        tot += __shfl_down_sync(0xffffffffu, tot, o);
+      }
+      if ((tid & 31) == 0) {
+        red[0][tid >> 5] = off;
+        red[1][tid >> 5] = tot;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double so = 0.0, st = 0.0;
+        for (int w = 0; w < kEigMax; w++) {
+          so += red[0][w];
+          st += red[1][w];
+        }
+        done = !(so > 1e-28 * st);
+      }
+      __syncthreads();
+      if (done) break;
+    }
+    for (int r = 0; r < m - 1; r++) {
+      if (tid < npair) {
+        const int k1 = tid, k2 = m - 1 - tid;
+        const int a = (k1 == 0) ? 0 : 1 + ((k1 - 1 - r) % (m - 1) + (m - 1)) % (m - 1);
+        const int b = 1 + ((k2 - 1 - r) % (m - 1) + (m - 1)) % (m - 1);
+        const int p = a < b ? a : b, q = a < b ? b : a;
+        double c = 1.0, s = 0.0;
+        if (q < n) {
+          const double apq = A[cur][p][q];
+          if (apq != 0.0) {
+            const double tau = (A[cur][q][q] - A[cur][p][p]) / (2.0 * apq);
+            const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+          partner[p] = q;
+          partner[q] = p;
+          alpha[p] = c;
+          beta[p] = -s;
+          alpha[q] = c;
+          beta[q] = s;
+        } else if (p < n) {  // paired with the dummy: untouched
+          partner[p] = p;
+          alpha[p] = 1.0;
+          beta[p] = 0.0;
+        }
+      }
+      __syncthreads();
+      const int nxt = cur ^ 1;
+      if (in) {
+        const int pi = partner[i], pj = partner[j];
+        const double ai = alpha[i], bi = beta[i], aj = alpha[j], bj = beta[j];
+        // B = J^T A rows i: ai A[i] + bi A[pi]; then columns j: aj B[.][j] + bj B[.][pj]
+        const double bij = ai * A[cur][i][j] + bi * A[cur][pi][j];
+        const double bipj = ai * A[cur][i][pj] + bi * A[cur][pi][pj];
+        A[nxt][i][j] = aj * bij + bj * bipj;
+        V[nxt][i][j] = aj * V[cur][i][j] + bj * V[cur][i][pj];
+      }
+      cur = nxt;
+      __syncthreads();
+    }
+  }
+  // ascending order: the rank of each eigenvalue (ties by index)
+  if (tid < n) {
+    const double lam = A[cur][tid][tid];
+    int rk = 0;
+    for (int k = 0; k < n; k++) {
+      const double o = A[cur][k][k];
+      rk += (o < lam || (o == lam && k < tid)) ? 1 : 0;
+    }
+    rank[tid] = rk;
+    evals[rk] = lam;
+  }
+  __syncthreads();
+  if (in) evecs[i + ld * rank[j]] = V[cur][i][j];
 }
 
 // One CTA per job: Jacobi eigendecomposition of the n x n Gram matrix at base + offG; the
@@ -464,9 +590,10 @@ cudaError_t launch_reverse_columns(double* dst, const double* src, int rows, int
   return cudaGetLastError();
 }
 
-cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream) {
+cudaError_t launch_small_eig(double* mat, int n, int ld, double* evals, double* evecs, cudaStream_t stream,
+                             bool warm) {
   if (n < 1 || n > kEigMax || ld < n) return cudaErrorInvalidValue;
-  small_eig_kernel<<<1, 256, 0, stream>>>(mat, n, ld, evals, evecs);
+  rr_eig_kernel<<<1, kRrThreads, 0, stream>>>(mat, n, ld, evals, evecs, warm && n > 1 ? 1 : 0);
   return cudaGetLastError();
 }
 

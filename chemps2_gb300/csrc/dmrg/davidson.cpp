@@ -81,9 +81,10 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
   auto mv = [&](const double* x, double* y) {
     matvec(x, y, prec);
     st.n_matvec++;
-    if (prec == Precision::kFP32) st.n_matvec_fp32++;
+    if (prec != Precision::kFP64) st.n_matvec_fp32++;
   };
   int nv = 0;
+  eig_n_ = -1;
   add_new_vec(t, nv);
   mv(V(nv), HV(nv));
   double best = 1e300;
@@ -93,7 +94,9 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
     multi_dot(HV_, nv + 1, V(nv), sm_ + kDots);
     C2G_CUDA(launch_mxm_row(sm_ + kMxM, kLd, nv, sm_ + kDots, nv + 1, s));
     nv++;
-    C2G_CUDA(launch_small_eig(sm_ + kMxM, nv, kLd, sm_ + kEvals, sm_ + kEvecs, s));
+    // warm start when the previous solve was of this matrix's leading block
+    C2G_CUDA(launch_small_eig(sm_ + kMxM, nv, kLd, sm_ + kEvals, sm_ + kEvecs, s, eig_n_ == nv - 1));
+    eig_n_ = nv;
     C2G_CUDA(launch_combine(t, 0.0, HV_, n_, sm_ + kEvecs, nv, n_, s));
     C2G_CUDA(launch_combine(u, 0.0, V_, n_, sm_ + kEvecs, nv, n_, s));
     C2G_CUDA(launch_residual(t, u, sm_ + kEvals, n_, s));
@@ -131,6 +134,7 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
       }
       for (int c = 0; c < keep_; c++) mv(V(c), HV(c));
       // MxMafterDeflation (CheMPS2/Davidson.cpp:510-536)
+      eig_n_ = -1;  // the projected matrix is rebuilt
       for (int j = 0; j < keep_; j++) {
         multi_dot(V_, j + 1, HV(j), sm_ + kDots);
         C2G_CUDA(launch_mxm_row(sm_ + kMxM, kLd, j, sm_ + kDots, j + 1, s));
@@ -150,6 +154,7 @@ bool DeviceDavidson::refine_cycle(const double* diag, const MatVec& matvec, doub
   double* u = W(1);
   double* w = W(2);
   int nv = 0;
+  eig_n_ = -1;
   add_new_vec(t, nv);
   matvec(V(0), HV(0), Precision::kFP64);
   st.n_matvec++;
@@ -158,7 +163,8 @@ bool DeviceDavidson::refine_cycle(const double* diag, const MatVec& matvec, doub
     multi_dot(HV_, nv + 1, V(nv), sm_ + kDots);
     C2G_CUDA(launch_mxm_row(sm_ + kMxM, kLd, nv, sm_ + kDots, nv + 1, s));
     nv++;
-    C2G_CUDA(launch_small_eig(sm_ + kMxM, nv, kLd, sm_ + kEvals, sm_ + kEvecs, s));
+    C2G_CUDA(launch_small_eig(sm_ + kMxM, nv, kLd, sm_ + kEvals, sm_ + kEvecs, s, eig_n_ == nv - 1));
+    eig_n_ = nv;
     C2G_CUDA(launch_combine(t, 0.0, HV_, n_, sm_ + kEvecs, nv, n_, s));
     C2G_CUDA(launch_combine(u, 0.0, V_, n_, sm_ + kEvecs, nv, n_, s));
     C2G_CUDA(launch_residual(t, u, sm_ + kEvals, n_, s));
@@ -179,14 +185,15 @@ bool DeviceDavidson::refine_cycle(const double* diag, const MatVec& matvec, doub
     C2G_CUDA(launch_precond_t(t, u, diag, sm_ + kEvals, sm_ + kDots2, cutoff_, n_, s));
     count_launches(2);
     add_new_vec(t, nv);
-    matvec(V(nv), HV(nv), Precision::kFP32);
+    matvec(V(nv), HV(nv), lo_);
     st.n_matvec++;
     st.n_matvec_fp32++;
   }
 }
 
 DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const MatVec& matvec, bool mixed,
-                                    double lo_tol) {
+                                    double lo_tol, Precision lo) {
+  lo_ = lo;
   cudaStream_t s = rt_.stream();
   DavidsonStats st;
   double* t = W(0);
@@ -203,7 +210,7 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
   }
   bool done = false;
   if (mixed) {
-    run(diag, matvec, Precision::kFP32, std::max(lo_tol, rtol_), true, st);
+    run(diag, matvec, lo_, std::max(lo_tol, rtol_), true, st);
     // refinement cycles from the FP32 Ritz vector; a cycle that cannot improve (for
     // example an FP32 floor above the target) leaves it to the FP64 Davidson below
     double last = 1e300;

@@ -45,12 +45,18 @@ class DeviceDavidson {
   // guess: device vector of length n (in: start vector; out: converged eigenvector).
   // diag: device vector, the diagonal of the operator. mixed: run the FP32 phase first,
   // down to residual lo_tol (never below rtol).
+  // `lo`: the arithmetic of the reduced-precision matvecs of the mixed mode (kFP32, or kTC
+  // for the tensor-core products of the large groups).
   DavidsonStats solve(double* guess, const double* diag, const MatVec& matvec, bool mixed = false,
-                      double lo_tol = 1e-5);
+                      double lo_tol = 1e-5, Precision lo = Precision::kFP32);
   // source of the random start that replaces a zero guess (the C library's rand() unless set)
   void set_rand(HostRand* r) { rand_ = r; }
 
  private:
+  Precision lo_ = Precision::kFP32;
+  // order of the projected matrix whose eigenvectors are in the evecs scratch (-1: none
+  // valid for the matrix now being built)
+  int eig_n_ = -1;
   double* V(int i) { return V_ + n_ * i; }
   double* HV(int i) { return HV_ + n_ * i; }
   double* W(int i) { return W_ + n_ * i; }

@@ -629,11 +629,23 @@ void DMRG::enable_f32_ops() {
   for (int b = 0; b < L - 1; b++) refresh_f32(b);
 }
 
+namespace {
+// matvec arithmetic codes of the C-ABI: 0 FP64, 1 FP32, 2 tensor cores (split BF16)
+c2g::Precision matvec_precision(const int code) {
+  switch (code) {
+    case 0: return c2g::Precision::kFP64;
+    case 1: return c2g::Precision::kFP32;
+    case 2: return c2g::Precision::kTC;
+    default: throw std::invalid_argument("matvec precision must be 0 (FP64), 1 (FP32) or 2 (tensor cores)");
+  }
+}
+}  // namespace
+
 void DMRG::set_precision(int mode, double mixed_tol) {
-  if (mode != 0 && mode != 1) throw std::invalid_argument("precision mode must be 0 or 1");
+  if (mode < 0 || mode > 2) throw std::invalid_argument("precision mode must be 0, 1 or 2");
   precision_ = mode;
   mixed_tol_ = mixed_tol;
-  if (mode == 1) enable_f32_ops();
+  if (mode != 0) enable_f32_ops();
 }
 
 int DMRG::get_num_mps_var() const {
@@ -891,7 +903,8 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     mv_ms += ms;
   };
-  const c2g::DavidsonStats ds = dav.solve(svec, diag, matvec, precision_ == 1, mixed_tol_);
+  const c2g::DavidsonStats ds =
+      dav.solve(svec, diag, matvec, precision_ != 0, mixed_tol_, matvec_precision(precision_ == 0 ? 1 : precision_));
   stats_.n_matvec_fp32 += ds.n_matvec_fp32;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1156,7 +1169,7 @@ DMRG::HeffCache& DMRG::heff_program(const int index, const bool with_diag) {
 
 double DMRG::bench_heff(const int index, const int warmup, const int steps, double* flops, double* bytes,
                         long long* launches, const long long flush_bytes, const int precision) {
-  const c2g::Precision prec = (precision == 1) ? c2g::Precision::kFP32 : c2g::Precision::kFP64;
+  const c2g::Precision prec = matvec_precision(precision);
   cudaStream_t s = rt->stream();
   HeffCache& c = heff_program(index, false);
   const int64_t veclen = c.S->size();
@@ -1172,7 +1185,7 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   double* flush = nullptr;
   const int64_t nflush = flush_bytes > 0 ? (flush_bytes + 7) / 8 : 0;
   if (nflush > 0) flush = rt->alloc(nflush);
-  if (prec == c2g::Precision::kFP32) enable_f32_ops();
+  if (prec != c2g::Precision::kFP64) enable_f32_ops();
   for (int i = 0; i < warmup; i++) rt->run(*c.program, x, y, prec, veclen);
   rt->sync();
   const long long l0 = c2g::kernel_launches();
@@ -1248,8 +1261,9 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
   } else {
     C2G_CUDA(cudaMemcpyAsync(c.xbuf, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
   }
-  if (precision == 1) enable_f32_ops();
-  rt->run(*c.program, c.xbuf, c.ybuf, precision == 1 ? c2g::Precision::kFP32 : c2g::Precision::kFP64, veclen);
+  const c2g::Precision prec = matvec_precision(precision);
+  if (prec != c2g::Precision::kFP64) enable_f32_ops();
+  rt->run(*c.program, c.xbuf, c.ybuf, prec, veclen);
   C2G_CUDA(cudaMemcpyAsync(y, c.ybuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   if (diag) {
     int maxdim = 1;
@@ -1271,9 +1285,9 @@ void DMRG::heff_apply_device(const int index, const double* x_dev, double* y_dev
   if (n != veclen) throw std::invalid_argument("heff_apply_device: vector length differs from the two-site object size");
   cudaStream_t u = static_cast<cudaStream_t>(stream);
   if (u) rt->wait_for(u);  // x is ready once the caller's stream gets here
-  if (precision == 1) enable_f32_ops();
-  rt->run(*c.program, const_cast<double*>(x_dev), y_dev,
-          precision == 1 ? c2g::Precision::kFP32 : c2g::Precision::kFP64, veclen);
+  const c2g::Precision prec = matvec_precision(precision);
+  if (prec != c2g::Precision::kFP64) enable_f32_ops();
+  rt->run(*c.program, const_cast<double*>(x_dev), y_dev, prec, veclen);
   if (u) rt->signal_to(u);  // the caller's stream waits for y
   else rt->sync();
 }

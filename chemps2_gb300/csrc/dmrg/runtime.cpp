@@ -1,5 +1,7 @@
 #include "runtime.hpp"
 
+#include <string>
+
 #include <algorithm>
 #include <climits>
 #include <cstdint>
@@ -76,6 +78,11 @@ Runtime::Runtime(int L, int device) : L_(L) {
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots32_), sizeof(float*) * kMaxSlots));
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&partial_), sizeof(double) * (kDotBlocks * 64 + 4096)));
   C2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&pinned_), sizeof(double) * 8));
+  // error word of the kernels with bounded waits, mapped so that the host reads it after
+  // any synchronisation without a copy
+  C2G_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&err_host_), sizeof(int), cudaHostAllocMapped));
+  *err_host_ = 0;
+  C2G_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&err_dev_), err_host_, 0));
 }
 
 Runtime::~Runtime() {
@@ -91,6 +98,7 @@ Runtime::~Runtime() {
     if (transient_[k]) cudaFreeAsync(transient_[k], stream_);
   if (stream_) cudaStreamSynchronize(stream_);
   if (pinned_) cudaFreeHost(pinned_);
+  if (err_host_) cudaFreeHost(err_host_);
   if (aux_) {
     cudaStreamSynchronize(aux_);
     cudaStreamDestroy(aux_);
@@ -898,7 +906,7 @@ void Runtime::prepare(DevProgram& p) {
 void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t xlen) {
   prepare(p);
   SlotPtrs sp = ptrs(x, y, p.combo);
-  if (prec == Precision::kFP32) {
+  if (prec != Precision::kFP64) {
     if (p.combo_size > 0 && !p.combo32_ready) {
       if (!p.combo32) p.combo32 = alloc_f32(p.combo_size);
       C2G_CUDA(launch_to_f32(p.combo32, p.combo, p.combo_size, stream_));
@@ -925,15 +933,23 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
 
 // One stage: the two passes of its large groups, then the one-pass variants (all write
 // disjoint output blocks).
-void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec) {
-  C2G_CUDA(launch_inter_gemm(ds.jobs, ds.jtiles, ds.njtiles, sp, stream_, prec));
+void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec_run) {
+  const Precision prec = simt_precision(prec_run);
+  if (prec_run == Precision::kTC)
+    C2G_CUDA(launch_inter_tc(ds.jobs, ds.jtiles, ds.njtiles, sp, err_dev_, stream_));
+  else
+    C2G_CUDA(launch_inter_gemm(ds.jobs, ds.jtiles, ds.njtiles, sp, stream_, prec));
   C2G_CUDA(launch_inter_small(ds.jobs, ds.jsmall, ds.njsmall, sp, stream_, prec));
   double* gemm_partials = transient_doubles(kTransientGemmPartials, p.gemm_part_size);
   unsigned* gemm_counters = transient_counters(kTransientGemmCounters, p.gemm_counter_count);
   double* partials = transient_doubles(kTransientPartials, p.part_size);
   unsigned* counters = transient_counters(kTransientCounters, p.counter_count);
-  C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp,
-                           stream_, prec));
+  if (prec_run == Precision::kTC)
+    C2G_CUDA(launch_sum_tc(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp, err_dev_,
+                           stream_));
+  else
+    C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp,
+                             stream_, prec));
   C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
   int nw = 0;
   const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, partials, counters};
@@ -945,6 +961,16 @@ void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPt
 void Runtime::sync() {
   C2G_CUDA(cudaStreamSynchronize(stream_));
   if (aux_) C2G_CUDA(cudaStreamSynchronize(aux_));
+  check_device_error();
+}
+
+void Runtime::check_device_error() {
+  if (err_host_ && *err_host_ != 0) {
+    const int e = *err_host_;
+    *err_host_ = 0;
+    throw std::runtime_error("a tensor-core kernel gave up a bounded wait (device error word " + std::to_string(e) +
+                             "); its output tiles were not written");
+  }
 }
 
 cudaStream_t Runtime::aux_stream() {

@@ -121,7 +121,10 @@ class Runtime {
   void run(DevProgram& p, double* x, double* y, Precision prec = Precision::kFP64, int64_t xlen = 0);
 
   const double* ones(int64_t n);
+  // Synchronises the runtime's streams, then throws if a kernel reported a failed bounded
+  // wait since the last check (the device error word is cleared).
   void sync();
+  void check_device_error();
 
   // Scratch for reductions and small Davidson quantities.
   double* partial() { return partial_; }
@@ -159,6 +162,8 @@ class Runtime {
   int64_t ones_cap_ = 0;
   double* partial_ = nullptr;
   double* pinned_ = nullptr;
+  int* err_host_ = nullptr;  // mapped pinned error word (host view)
+  int* err_dev_ = nullptr;   // its device address
   // pinned host buffer in which upload assembles a program before the copy to the device
   char* staging_ = nullptr;
   int64_t staging_cap_ = 0;

@@ -106,8 +106,11 @@ int c2g_dmrg_solve(c2g_dmrg* d, double* energy);            /* DMRG::Solve    */
 int c2g_dmrg_presolve(c2g_dmrg* d);                         /* DMRG::PreSolve */
 int c2g_dmrg_set_verbose(c2g_dmrg* d, int verbose);
 /* Arithmetic of the Heff matvecs: 0 FP64 (default, the reference's); 1 mixed (FP32
- * matvecs inside Davidson down to residual mixed_tol, then FP64 to the instruction's
- * tolerance). No counterpart in the reference. */
+ * matvecs inside Davidson down to residual mixed_tol, then FP64 refinement to the
+ * instruction's tolerance); 2 mixed as 1 with the reduced-precision matvecs' large blocks
+ * on the tensor cores (split-BF16 three-term products, FP32 accumulation). No counterpart
+ * in the reference. The `precision` argument of the matvec entry points below takes the
+ * matching codes for one matvec: 0 FP64, 1 FP32, 2 tensor cores. */
 int c2g_dmrg_set_precision(c2g_dmrg* d, int mode, double mixed_tol);
 int c2g_dmrg_num_mps_var(const c2g_dmrg* d, int* n);        /* DMRG::get_num_mps_var */
 int c2g_dmrg_max_discarded_weight(const c2g_dmrg* d, double* w);
@@ -141,6 +144,11 @@ int c2g_dmrg_heff_apply(c2g_dmrg* d, int index, int join_into_x, double* x, doub
 /* As c2g_dmrg_heff_apply with the matvec in FP32 arithmetic (operands converted on load,
  * lane sums in FP32, the output in FP64). No counterpart in the reference. */
 int c2g_dmrg_heff_apply_fp32(c2g_dmrg* d, int index, double* x, double* y, int64_t n);
+/* As c2g_dmrg_heff_apply (no join, no diagonal) with the matvec arithmetic chosen by
+ * `precision`: 0 FP64, 1 FP32, 2 the large blocks on the tensor cores (split-BF16
+ * three-term products, FP32 accumulation) and the rest in FP32. No counterpart in the
+ * reference. */
+int c2g_dmrg_heff_apply_precision(c2g_dmrg* d, int index, double* x, double* y, int64_t n, int precision);
 /* DMRG::activateExcitations (CheMPS2/DMRG.cpp:464-473): allow up to max_exc stored states. */
 int c2g_dmrg_activate_excitations(c2g_dmrg* d, int max_exc);
 /* DMRG::newExcitation (CheMPS2/DMRG.cpp:475-505): store the current state; the next
@@ -222,6 +230,14 @@ int c2g_batch_solve(int n, c2g_problem* const* problems, c2g_scheme* const* sche
  * in ascending order (concatenated), evecs its eigenvectors in descending order of the
  * eigenvalue, each column signed so that its largest-magnitude entry is positive. */
 int c2g_truncation_eig(int count, const int* n, const double* mats, double* evals, double* evecs);
+/* The Rayleigh-Ritz eigensolver of the Davidson solver (CheMPS2/Davidson.cpp:242-276,
+ * where the reference calls dsyev), exposed for testing: the symmetric n x n matrix `mat`
+ * (column-major, n <= 32) on the device, `reps` times, CUDA-event timed (*us_per_call,
+ * nullable). Eigenvalues ascending in evals, eigenvectors in the columns of evecs (n x n).
+ * warm != 0: on entry evecs holds ((n-1) x (n-1), column-major) the eigenvectors of the
+ * leading (n-1) x (n-1) block, as in a Davidson expansion step. */
+int c2g_rayleigh_ritz_eig(int n, const double* mat, int warm, double* evals, double* evecs, int reps,
+                          double* us_per_call);
 /* No counterpart in the reference (a diagnostic): the free memory of `device` (< 0: the
  * calling thread's current device; cudaMemGetInfo) and the bytes in use from that
  * device's default stream-ordered pool (cudaMemPoolAttrUsedMemCurrent), where this
