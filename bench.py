@@ -1,32 +1,43 @@
 #!/usr/bin/env python3
-"""Benchmark of the two-site DMRG hot path on GB300: Heff matvecs/s.
+"""Benchmark of the two-site DMRG hot path on GB300: Heff matvecs/s and s/sweep, mixed
+precision against FP64 on the GPU, with the CPU baseline alongside.
 
-Workload (the configuration the headline metric is quoted on): synthetic ab initio
-Hamiltonian, L = N = 24, S = 0, D2h with irreps round robin, target irrep 0, virtual
-dimension D = 1000 (seeded generator chemps2_gb300/models.py, seed 1234). The DMRG object
-is built as the reference builds it (random MPS, sector dimensions of
-SyBookkeeper::ScaleCURdim for D = 1000, all renormalized operators), the right-hand
-operators are renormalized down to the middle of the chain, and one step is one
-effective-Hamiltonian matvec at sites (11, 12) in FP64: the operation the Davidson
-solver repeats inside every sweep step.
+Workload (the configuration the headline metric is quoted on): seeded synthetic ab initio
+Hamiltonian, L = N = 30, S = 0, D2h with irreps round robin, target irrep 0, virtual
+dimension D = 2000 (generator chemps2_gb300/models.py, seed 1234; no molecule data ships
+with the reference's benchmarks, so seeded integrals of the configuration's distribution
+stand in). Two DMRG runs from the same random start (srand(1234)), each swept --sweeps
+times (left + right sweeps, Davidson rtol 1e-8, noise 0):
 
-  value   device matvecs/s (CUDA events on the DMRG stream, L2 overwritten between
-          steps outside the timed interval)
-  e2e     the same matvec through the C-ABI with host buffers (c2g_dmrg_heff_apply):
-          copy of x to the device, matvec, copy of y back, wall clock
-  sweep   seconds per left+right sweep of the Hubbard chain L = 16, D = 200 (the CPU
-          configuration of the reference's benchmark list), after one warm-up sweep
+  fp64      plain FP64 matvecs (the reference's arithmetic)
+  mixed_tc  the Davidson solver expands with reduced-precision matvecs whose large
+            blocks run on the tensor cores (tcgen05, split-BF16 three-term products,
+            FP32 accumulation; the rest FP32), then refines with FP64 products to rtol
 
-The reference arm (--impl reference) times the CPU oracle port of the same matvec on
-all the host cores (the reference itself needs external BLAS/LAPACK/HDF5 builds and is not
-compiled here). Multi-GPU runs are independent replicas (the path has no exchange step
-on one problem): each rank runs the full workload on its own GPU.
+Then, on the FP64 run's swept state with the right-hand operators renormalized down to
+the middle, one step = one Heff matvec at sites (14, 15):
+
+  value     mixed-form (tensor-core) matvecs/s, device time (CUDA events on the DMRG's
+            stream; a 258 MiB buffer is overwritten between steps, outside the timed
+            interval, so the operators come from HBM)
+  e2e       the same matvec through the C-ABI with host buffers
+            (c2g_dmrg_heff_apply_precision): x copied in, matvec, y copied out, wall clock
+  fp64 / fp32  the same state's FP64 and all-FP32 matvec rates
+  sweeps    seconds per sweep of both runs, their energy difference and the time split
+            (matvecs, task compilation, upload, truncation, operator updates)
+
+The reference arm (--impl reference) and `cpu_baseline` time the CPU oracle's port of the
+same matvec on all host cores, on a state with the swept state's sector dimensions (the
+reference itself needs external BLAS/LAPACK/HDF5 builds and is not compiled here).
+Multi-GPU runs are independent replicas (one problem has no exchange step on one GPU):
+each rank runs the full workload on its own GPU.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -39,11 +50,18 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-L_SITES, N_ELEC, TWO_S, IRREP, GROUP, D_VIRT, SEED = 24, 24, 0, 0, 7, 1000, 1234
+L_SITES, N_ELEC, TWO_S, IRREP, GROUP, D_VIRT, SEED = 30, 30, 0, 0, 7, 2000, 1234
 MID = L_SITES // 2 - 1
 L2_FLUSH_BYTES = 2 * 129 * 1024 * 1024
 METRIC = "Heff matvecs/s & s/sweep: mixed vs FP64 GPU at ≤1e-6 Ha; CPU ref"
 UNIT = "matvec/s"
+WORKLOAD = (f"synthetic ab initio L={L_SITES} N={N_ELEC} S=0 D2h D={D_VIRT}: Heff matvec at sites ({MID},{MID + 1}) "
+            f"of the state after the FP64 sweeps, mixed (tensor-core) form; FP64 and mixed sweeps")
+# Sector dimensions of every boundary of the L = 30 D = 2000 state after the two FP64
+# sweeps of the GPU run (written by `bench.py --dump-dims`): the CPU baseline builds a
+# state with exactly these dimensions, so that its matvec has the same shape and ledger
+# work as the GPU's.
+DIMS_FIXTURE = ROOT / "oracle" / "bench_l30_d2000_swept_dims.json"
 
 
 def dist_env():
@@ -70,13 +88,15 @@ def replica_throughput(world, steps, seconds):
     return world * steps / seconds
 
 
-def make_model():
+def make_model(L=L_SITES):
     from chemps2_gb300.models import synthetic_ab_initio
 
-    return synthetic_ab_initio(L_SITES, GROUP, SEED)
+    return synthetic_ab_initio(L, GROUP, SEED)
 
 
-def build_gpu_dmrg(model, D=D_VIRT, sweeps=1, right_ops=True):
+def build_gpu_dmrg(model, D=D_VIRT, sweeps=1, seed=SEED):
+    """The DMRG objects of `model` (N = L, S = 0, target irrep 0) with one instruction of
+    `sweeps` sweeps at D, after srand(seed)."""
     import chemps2_gb300 as c2g
 
     L = model.L
@@ -88,15 +108,24 @@ def build_gpu_dmrg(model, D=D_VIRT, sweeps=1, right_ops=True):
     for i, j, k, l in np.argwhere(model.vmat != 0.0):
         if i <= j and i <= k:  # one representative of each 8-fold orbit
             ham.setVmat(int(i), int(j), int(k), int(l), float(model.vmat[i, j, k, l]))
-    prob = c2g.Problem(ham, TWO_S, N_ELEC, IRREP)
+    prob = c2g.Problem(ham, TWO_S, L, IRREP)
     scheme = c2g.ConvergenceScheme(1)
     scheme.set_instruction(0, D, 1e-10, sweeps, 0.0, 1e-8)
-    c2g.srand(SEED)
+    c2g.srand(seed)
     dmrg = c2g.DMRG(prob, scheme)
-    if right_ops:
-        for index in range(L - 2, MID, -1):  # right-hand operators down to the middle
-            dmrg.update(index, False)
     return ham, prob, scheme, dmrg
+
+
+def host_cpu():
+    model = platform.processor() or platform.machine()
+    try:
+        for line in subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return model
 
 
 class ClockSampler:
@@ -162,105 +191,82 @@ def measured_peaks():
 
 
 def profiled_traffic():
-    """DRAM bytes per Heff launch from the committed ncu summary (scaled to this workload)."""
+    """DRAM bytes per mixed-form matvec from the committed ncu summary (None when absent)."""
     try:
-        prof = json.loads((ROOT / "profiles" / "heff_team_kernel_l24_d1000.json").read_text())
+        prof = json.loads((ROOT / "profiles" / "heff_mixed_tc_l30_d2000.json").read_text())
         return prof.get("dram_bytes_per_matvec")
     except (OSError, ValueError):
         return None
 
 
-def cpu_baseline_sample(model, n_matvec=1):
-    """The CPU oracle port of the same matvec on all host cores (the executor runs the
-    independent output blocks of a stage on parallel threads), bounded to n_matvec
-    applications after its own setup."""
+def swept_dims():
+    try:
+        return json.loads(DIMS_FIXTURE.read_text())["rows"]
+    except (OSError, ValueError, KeyError):
+        return None
+
+
+def state_dims(dmrg, L=L_SITES):
+    return [[b, int(r[0]), int(r[1]), int(r[2]), int(r[4])] for b in range(L + 1) for r in dmrg.sectors(b)
+            if r[4] > 0]
+
+
+def cpu_baseline_sample(n_matvec=3):
+    """The CPU oracle's port of the same matvec on all host cores (its executor runs the
+    independent output blocks of a stage on parallel threads): a state of the L = 30
+    D = 2000 chain with the sector dimensions of the GPU run's swept state (random tensors:
+    the matvec's work depends on the dimensions only), left operators up to the middle,
+    right operators down to it, then n_matvec matvecs at sites (14, 15) after one untimed
+    one. Without the dimensions file, the initial (scaled) dimensions of D = 2000."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as ol
 
     threads = os.cpu_count() or 1
     ol.set_threads(threads)
     ol.srand(SEED)
-    cpu = ol.OracleDMRG(model, TWO_S, N_ELEC, IRREP, [(D_VIRT, 1e-10, 1, 0.0, 1e-8)], check=False)
+    model = make_model()
+    rows = swept_dims()
+    sched = [(D_VIRT, 1e-10, 1, 0.0, 1e-8)]
+    t0 = time.perf_counter()
+    if rows is not None:
+        cpu = ol.OracleDMRG(model, TWO_S, N_ELEC, IRREP, sched, check=False, dims=rows, left_upto=MID)
+        state = "the sector dimensions of the GPU run's swept state"
+    else:
+        cpu = ol.OracleDMRG(model, TWO_S, N_ELEC, IRREP, sched, check=False)
+        state = "the initial sector dimensions"
     for index in range(L_SITES - 2, MID, -1):
         cpu.update(index, False)
-    x, _, _ = cpu.heff_apply(MID)  # joins the two-site object, compiles (untimed)
+    x, _, _ = cpu.heff_apply(MID)  # joins the two-site object, compiles, first matvec (untimed)
+    setup = time.perf_counter() - t0
+    f0 = cpu.stats()["flops"]
     t0 = time.perf_counter()
     for _ in range(n_matvec):
         cpu.heff_apply(MID, x)
     dt = time.perf_counter() - t0
-    return {"value": n_matvec / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n_matvec} Heff matvec(s) at sites ({MID},{MID + 1}) of the same L=24 D=1000 state "
-                      f"(oracle CPU executor on {threads} threads, compile excluded, as for the GPU)"}
+    flops = (cpu.stats()["flops"] - f0) / n_matvec
+    return {"value": n_matvec / dt, "unit": UNIT, "cores": threads, "kind": "port", "cpu": host_cpu(),
+            "flops_per_matvec": flops, "two_site_vector_length": int(x.size), "setup_s": setup,
+            "sample": f"{n_matvec} FP64 Heff matvecs at sites ({MID},{MID + 1}) of L={L_SITES} D={D_VIRT} with "
+                      f"{state} (oracle CPU executor, {threads} threads; compile and setup excluded, as for the "
+                      f"GPU)"}
 
 
-def sweep_seconds():
-    """The Hubbard chain L = 16, U = 4, D = 200 with 4 left+right sweeps (the reference's
-    CPU-runnable configuration), plain FP64 and mixed precision: seconds per sweep over the
-    whole run (compilation and the first sweeps from the random start included) and the
-    energy difference between the two."""
-    import chemps2_gb300 as c2g
-    from chemps2_gb300.models import hubbard
-
-    L = 16
-    m = hubbard(L, 4.0)
-    out = {"config": "hubbard L=16 N=16 U=4 D=200, 4 sweeps, Davidson rtol 1e-8"}
-    for mode in ("fp64", "mixed"):
-        ham = c2g.Hamiltonian(L, 0, m.irreps)
-        for i in range(L - 1):
-            ham.setTmat(i, i + 1, -1.0)
-        for i in range(L):
-            ham.setVmat(i, i, i, i, 4.0)
-        prob = c2g.Problem(ham, 0, L, 0)
-        scheme = c2g.ConvergenceScheme(1)
-        scheme.set_instruction(0, 200, 1e-14, 4, 0.0, 1e-8)
-        c2g.srand(1)
-        d = c2g.DMRG(prob, scheme)
-        d.set_precision(mode)
+def run_sweeps(model, mode, sweeps, D=D_VIRT, seed=SEED):
+    """`sweeps` left+right sweeps from the seeded random start in `mode`; returns the DMRG
+    objects and the per-sweep record."""
+    objs = build_gpu_dmrg(model, D=D, sweeps=1, seed=seed)
+    d = objs[3]
+    d.set_precision(mode)
+    per, stats = [], []
+    e = None
+    for _ in range(sweeps):
+        d.reset_stats()
         t0 = time.perf_counter()
         e = d.Solve()
-        dt = time.perf_counter() - t0
-        st = d.stats()
-        d.close()
-        out[mode] = {"s_per_sweep": dt / 4, "energy": e, "matvecs": st["n_matvec"],
-                     "fp32_matvecs": st["n_matvec_fp32"]}
-    out["s_per_sweep"] = out["fp64"]["s_per_sweep"]
-    out["mixed_speedup"] = out["fp64"]["s_per_sweep"] / out["mixed"]["s_per_sweep"]
-    out["mixed_energy_error"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"])
-    return out
-
-
-def sweep_config2(model, sweeps=2, steps=20):
-    """The headline system (L = 24, D = 1000) swept `sweeps` times from the random start in
-    plain FP64 and in mixed precision: seconds per sweep (first and last sweep, host task
-    compilation included), the energy difference, and the matvec rate at sites (11, 12) on
-    the swept state (sector dimensions after truncation, larger blocks than the initial
-    state), FP64 and FP32."""
-    out = {"config": f"synthetic ab initio L=24 N=24 S=0 D2h D=1000, {sweeps} sweeps, Davidson rtol 1e-8"}
-    for mode in ("fp64", "mixed"):
-        ham, prob, scheme, d = build_gpu_dmrg(model, sweeps=1, right_ops=False)  # one sweep per Solve()
-        d.set_precision(mode)
-        per = []
-        for _ in range(sweeps):
-            d.reset_stats()
-            t0 = time.perf_counter()
-            e = d.Solve()
-            per.append(time.perf_counter() - t0)
-        st = d.stats()
-        res = {"s_per_sweep": per, "energy": e, "last_sweep": {k: v for k, v in st.items() if k.startswith(("t_", "n_"))}}
-        if mode == "fp64":
-            for index in range(L_SITES - 2, MID, -1):
-                d.update(index, False)
-            r64 = d.bench_heff(MID, 3, steps, L2_FLUSH_BYTES)
-            r32 = d.bench_heff(MID, 3, steps, L2_FLUSH_BYTES, precision="fp32")
-            res["swept_state_matvec"] = {
-                "fp64_matvec_per_s": 1e3 / r64["ms_per_matvec"], "fp64_gflops": r64["flops"] / r64["ms_per_matvec"] / 1e6,
-                "fp32_matvec_per_s": 1e3 / r32["ms_per_matvec"], "fp32_gflops": r32["flops"] / r32["ms_per_matvec"] / 1e6,
-                "ledger_flops_per_matvec": r64["flops"], "two_site_vector_length": d.sobject_size(MID)}
-        d.close()
-        out[mode] = res
-    out["mixed_speedup_last_sweep"] = out["fp64"]["s_per_sweep"][-1] / out["mixed"]["s_per_sweep"][-1]
-    out["mixed_energy_error"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"])
-    return out
+        per.append(time.perf_counter() - t0)
+        stats.append({k: (round(v, 4) if isinstance(v, float) else v) for k, v in d.stats().items()
+                      if k.startswith(("t_", "n_"))})
+    return objs, {"s_per_sweep": per, "energy": e, "stats": stats}
 
 
 def run_ours(args):
@@ -277,17 +283,38 @@ def run_ours(args):
 
     model = make_model()
     t_setup = time.perf_counter()
-    ham, prob, scheme, dmrg = build_gpu_dmrg(model)
+    sweeps = {}
+    keep = None
+    for mode in ("mixed_tc", "fp64"):
+        objs, rec = run_sweeps(model, mode, args.sweeps)
+        sweeps[mode] = rec
+        if mode == "fp64":
+            keep = objs
+        else:
+            objs[3].close()
+    dmrg = keep[3]
+    dims = state_dims(dmrg)
+    if args.dump_dims:
+        Path(args.dump_dims).write_text(json.dumps({
+            "about": f"sector dimensions (boundary, N, 2S, I, dim) of the synthetic ab initio L={L_SITES} D2h "
+                     f"D={D_VIRT} state after {args.sweeps} FP64 sweeps from srand({SEED}); written by "
+                     f"bench.py --dump-dims",
+            "rows": dims}) + "\n")
+    fixture = swept_dims()
+    dims_match = (fixture == dims) if fixture is not None else None
+    for index in range(L_SITES - 2, MID, -1):  # right-hand operators down to the middle
+        dmrg.update(index, False)
     setup_s = time.perf_counter() - t_setup
     n = dmrg.sobject_size(MID)
-    # warm-up (untimed): compile + W applications
-    dmrg.bench_heff(MID, args.warmup, 0, 0)
+    for p in ("tc", "fp64", "fp32"):  # compile + warm-up (untimed)
+        dmrg.bench_heff(MID, args.warmup, 0, 0, precision=p)
     if args.profile:
-        # profiling mode: one launch sequence of one matvec between cudaProfilerStart/Stop
+        # profiling mode: --profile matvecs of each precision between cudaProfilerStart/Stop
         # (for ncu --profile-from-start off); prints nothing.
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
-        dmrg.bench_heff(MID, 0, args.profile, 0)
+        for p in ("tc", "fp64", "fp32"):
+            dmrg.bench_heff(MID, 0, args.profile, 0, precision=p)
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
         dmrg.close()
@@ -296,158 +323,100 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        res = dmrg.bench_heff(MID, 0, args.steps, L2_FLUSH_BYTES)
+        res = dmrg.bench_heff(MID, 0, args.steps, L2_FLUSH_BYTES, precision="tc")
     torch.cuda.synchronize()
     ms = res["ms_per_matvec"]
-    total_s = ms * args.steps / 1e3
-    # the FP32-arithmetic matvec of the mixed-precision Davidson, same flush discipline
-    dmrg.bench_heff(MID, args.warmup, 0, 0, precision="fp32")
-    res32 = dmrg.bench_heff(MID, 0, args.steps, L2_FLUSH_BYTES, precision="fp32")
-    mixed = {"matvec_per_s": 1e3 / res32["ms_per_matvec"], "ms_per_matvec": res32["ms_per_matvec"],
-             "speedup_vs_fp64": ms / res32["ms_per_matvec"],
-             "arithmetic": "FP32 operand copies, products and per-slot sums; FP64 slot reduction and output"}
-    total_s = max_over_ranks(total_s, world)
+    total_s = max_over_ranks(ms * args.steps / 1e3, world)
     if world > 1:
         torch.distributed.barrier()
     value = replica_throughput(world, args.steps, total_s)
-    # end to end through the C-ABI with host buffers
+    r64 = dmrg.bench_heff(MID, 0, args.steps, L2_FLUSH_BYTES, precision="fp64")
+    r32 = dmrg.bench_heff(MID, 0, args.steps, L2_FLUSH_BYTES, precision="fp32")
+    # end to end through the C-ABI with host buffers, same arithmetic as `value`
     rng = np.random.default_rng(0)
     x = rng.standard_normal(n)
-    dmrg.heff_apply(MID, x)  # warm
+    dmrg.heff_apply_precision(MID, x, "tc")  # warm
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        dmrg.heff_apply(MID, x)
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, world)
-    e2e = {"value": replica_throughput(world, args.steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
-    peaks = measured_peaks()
-    hbm = peaks.get("hbm_gbs")
-    achieved = res["bytes"] / (ms * 1e-3) / 1e9
-    # The kernel is bound by the FP64 pipe, not by HBM: the compute roofline sits beside the
-    # HBM one. FP64 peak = ncu's device peak of 608 FP64 flops per cycle (2 DFMA lanes per SM
-    # and cycle) at the maximum SM clock; FP32 peak likewise 38912 flops per cycle.
-    sm_hz = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
-    fp64_peak = 608 * sm_hz / 1e9
-    fp32_peak = 38912 * sm_hz / 1e9
-    gflops = res["flops"] / (ms * 1e-3) / 1e9
-    gflops32 = res32["flops"] / (res32["ms_per_matvec"] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm if hbm else 6800.0,
-                "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "traffic": profiled_traffic(),
-                "peak_source": "measured" if hbm else "fallback",
-                "kernel": "sandwich_warp_kernel<double, R> (team block sandwich, one launch per row class)",
-                "ledger_bytes_per_matvec": res["bytes"], "ledger_flops_per_matvec": res["flops"],
-                "compute": {"pipe": "fp64", "achieved_gflops": gflops, "peak_gflops": fp64_peak,
-                            "frac": gflops / fp64_peak,
-                            "peak_source": "ncu device peak 608 FP64 flop/cycle x max SM clock"},
-                "compute_fp32_variant": {"pipe": "fp32", "achieved_gflops": gflops32, "peak_gflops": fp32_peak,
-                                         "frac": gflops32 / fp32_peak}}
+        dmrg.heff_apply_precision(MID, x, "tc")
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": replica_throughput(world, args.steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 8 * n,
+           "d2h_bytes_per_step": 8 * n}
+    y64 = dmrg.heff_apply_precision(MID, x, "fp64")
+    ytc = dmrg.heff_apply_precision(MID, x, "tc")
+    tc_rel_err = float(np.linalg.norm(ytc - y64) / np.linalg.norm(y64))
     dmrg.close()
-    sweep = sweep24 = None
-    if rank == 0 and not args.no_sweep:
-        sweep = sweep_seconds()
-        sweep24 = sweep_config2(model)
+
+    peaks = measured_peaks()
+    sm_hz = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    bf16_peak = peaks.get("bf16_tflops")
+    fp64_peak = 608 * sm_hz / 1e12  # ncu device attribute: 608 FP64 flop/cycle on this GPU
+    fp32_peak = 38912 * sm_hz / 1e12
+    tflops = res["flops"] / (ms * 1e-3) / 1e12
+    t64 = r64["flops"] / (r64["ms_per_matvec"] * 1e-3) / 1e12
+    t32 = r32["flops"] / (r32["ms_per_matvec"] * 1e-3) / 1e12
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    peak = bf16_peak or 1900.0
+    roofline = {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                "traffic": profiled_traffic(),
+                "peak_source": "measured bf16 dense (burst)" if bf16_peak else "fallback bf16 dense (1.9 PFLOP/s)",
+                "kernel": "mixed-form Heff matvec (tcgen05 sum_tc/inter_tc kernels for the large groups, FP32 team "
+                          "kernel for the rest); achieved = ledger flops of one matvec / its CUDA-event time",
+                "ledger_flops_per_matvec": res["flops"], "ledger_bytes_per_matvec": res["bytes"],
+                "hbm": {"achieved_gbs": res["bytes"] / (ms * 1e-3) / 1e9, "peak_gbs": hbm},
+                "fp64_form": {"pipe": "fp64", "achieved_tflops": t64, "peak_tflops": fp64_peak,
+                              "frac": t64 / fp64_peak, "peak_source": "608 FP64 flop/cycle x max SM clock"},
+                "fp32_form": {"pipe": "fp32", "achieved_tflops": t32, "peak_tflops": fp32_peak,
+                              "frac": t32 / fp32_peak}}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline_sample(model, n_matvec=1)
+        cpu = cpu_baseline_sample(n_matvec=3)
     if rank == 0:
+        f64, mx = sweeps["fp64"], sweeps["mixed_tc"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ab initio generator, seed 1234)",
-            "config": {"workload": "synthetic ab initio L=24 N=24 S=0 D2h D=1000, Heff matvec at sites (11,12), "
-                                   "initial SyBookkeeper dimensions", "L": L_SITES, "N": N_ELEC, "two_s": TWO_S,
-                       "group": "D2h", "D": D_VIRT, "two_site_vector_length": n, "l2": "flushed between steps",
+            "vs_baseline": None, "dtype": "bf16x3",
+            "arithmetic": "split-BF16 three-term tensor-core products with FP32 accumulation for the large groups, "
+                          "FP32 elsewhere, FP64 output; FP64 refinement inside the solver",
+            "data": "synthetic (seeded ab initio generator, seed 1234)",
+            "config": {"workload": WORKLOAD, "L": L_SITES, "N": N_ELEC, "two_s": TWO_S, "group": "D2h",
+                       "D": D_VIRT, "sweeps": args.sweeps, "two_site_vector_length": n,
+                       "state_dims_equal_cpu_baseline_state": dims_match,
+                       "l2": "flushed between steps (258 MiB overwrite outside the timed interval)",
                        "parallelism": f"replicas x{world}", "setup_s": setup_s},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
-            "gpu_launches": res["launches"], "sweep": sweep, "sweep_l24_d1000": sweep24, "mixed": mixed,
+            "gpu_launches": res["launches"],
+            "fp64": {"matvec_per_s": 1e3 / r64["ms_per_matvec"], "ms_per_matvec": r64["ms_per_matvec"]},
+            "fp32": {"matvec_per_s": 1e3 / r32["ms_per_matvec"], "ms_per_matvec": r32["ms_per_matvec"]},
+            "mixed_matvec_speedup_vs_fp64": r64["ms_per_matvec"] / ms,
+            "mixed_matvec_rel_error": tc_rel_err,
+            "sweeps": {"fp64": f64, "mixed_tc": mx,
+                       "mixed_speedup_last_sweep": f64["s_per_sweep"][-1] / mx["s_per_sweep"][-1],
+                       "mixed_speedup_total": sum(f64["s_per_sweep"]) / sum(mx["s_per_sweep"]),
+                       "mixed_energy_error": abs(mx["energy"] - f64["energy"])},
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def extra_config3(args):
-    """Precision form: synthetic ab initio L = N = 30, S = 0, D2h, D = 2000, swept in plain
-    FP64 and in mixed precision (FP32 Davidson expansion with FP64 refinement, FP64
-    truncation): seconds per sweep and the energy difference. --sweeps sets the number of
-    sweeps (8 in the reference configuration)."""
-    import chemps2_gb300 as c2g
-    from chemps2_gb300.models import synthetic_ab_initio
-
-    L = 30
-    model = synthetic_ab_initio(L, GROUP, SEED)
-    out = {"config": f"synthetic ab initio L=30 N=30 S=0 D2h D=2000, {args.sweeps} sweeps, Davidson rtol 1e-8"}
-    if args.profile:
-        # profiling mode: --sweeps FP64 sweeps, right-hand operators down to the middle, then
-        # --profile matvecs at sites (14, 15) in each precision between cudaProfilerStart/Stop
-        import torch
-
-        ham = c2g.Hamiltonian(L, model.group, model.irreps)
-        for i in range(L):
-            for j in range(i, L):
-                if model.tmat[i, j] != 0.0:
-                    ham.setTmat(i, j, float(model.tmat[i, j]))
-        for i, j, k, l in np.argwhere(model.vmat != 0.0):
-            if i <= j and i <= k:
-                ham.setVmat(int(i), int(j), int(k), int(l), float(model.vmat[i, j, k, l]))
-        prob = c2g.Problem(ham, 0, L, 0)
-        scheme = c2g.ConvergenceScheme(1)
-        scheme.set_instruction(0, 2000, 1e-10, args.sweeps, 0.0, 1e-8)
-        c2g.srand(SEED)
-        d = c2g.DMRG(prob, scheme)
-        d.Solve()
-        mid = L // 2 - 1
-        for index in range(L - 2, mid, -1):
-            d.update(index, False)
-        precs = ["fp64", "fp32"]
-        for p in precs:
-            d.bench_heff(mid, args.warmup, 0, 0, precision=p)
-        torch.cuda.synchronize()
-        torch.cuda.profiler.start()
-        for p in precs:
-            d.bench_heff(mid, 0, args.profile, 0, precision=p)
-        torch.cuda.synchronize()
-        torch.cuda.profiler.stop()
-        for p in precs:
-            r = d.bench_heff(mid, 0, 5, L2_FLUSH_BYTES, precision=p)
-            print(json.dumps({"precision": p, "ms_per_matvec": r["ms_per_matvec"], "ledger_flops": r["flops"],
-                              "ledger_bytes": r["bytes"], "n": d.sobject_size(mid)}), flush=True)
-        d.close()
-        return
-    for mode in ("fp64", "mixed"):
-        ham = c2g.Hamiltonian(L, model.group, model.irreps)
-        for i in range(L):
-            for j in range(i, L):
-                if model.tmat[i, j] != 0.0:
-                    ham.setTmat(i, j, float(model.tmat[i, j]))
-        for i, j, k, l in np.argwhere(model.vmat != 0.0):
-            if i <= j and i <= k:
-                ham.setVmat(int(i), int(j), int(k), int(l), float(model.vmat[i, j, k, l]))
-        prob = c2g.Problem(ham, 0, L, 0)
-        scheme = c2g.ConvergenceScheme(1)
-        scheme.set_instruction(0, 2000, 1e-10, 1, 0.0, 1e-8)
-        c2g.srand(SEED)
-        d = c2g.DMRG(prob, scheme)
-        d.set_precision(mode)
-        per, stats = [], []
-        for _ in range(args.sweeps):
-            d.reset_stats()
-            t0 = time.perf_counter()
-            e = d.Solve()
-            per.append(time.perf_counter() - t0)
-            stats.append({k: v for k, v in d.stats().items() if k.startswith(("t_", "n_"))})
-        d.close()
-        out[mode] = {"s_per_sweep": per, "energy": e, "stats": stats}
-    out["mixed_speedup_last_sweep"] = out["fp64"]["s_per_sweep"][-1] / out["mixed"]["s_per_sweep"][-1]
-    out["mixed_speedup_total"] = sum(out["fp64"]["s_per_sweep"]) / sum(out["mixed"]["s_per_sweep"])
-    out["mixed_energy_error"] = abs(out["mixed"]["energy"] - out["fp64"]["energy"])
-    print(json.dumps({"extra": "precision_l30_d2000", **out}), flush=True)
+def extra_sweeps(args, label, model, D, seed=SEED):
+    """Sweeps of another configuration in FP64 and in the mixed tensor-core form."""
+    out = {"config": f"{label}, {args.sweeps} sweeps, Davidson rtol 1e-8"}
+    for mode in ("fp64", "mixed_tc"):
+        objs, rec = run_sweeps(model, mode, args.sweeps, D=D, seed=seed)
+        objs[3].close()
+        out[mode] = rec
+    out["mixed_speedup_last_sweep"] = out["fp64"]["s_per_sweep"][-1] / out["mixed_tc"]["s_per_sweep"][-1]
+    out["mixed_energy_error"] = abs(out["mixed_tc"]["energy"] - out["fp64"]["energy"])
+    print(json.dumps({"extra": label, **out}), flush=True)
 
 
 def extra_hubbard(args):
     """Large sector blocks: the Hubbard chain L = N = 20, U = 4, C1, D = 512 swept --sweeps
-    times, right-hand operators renormalized down to the middle, then --steps FP64 and FP32
-    matvecs at sites (9, 10) (the two-pass path of large groups carries most of the work).
+    times, right-hand operators renormalized down to the middle, then --steps FP64, FP32 and
+    tensor-core matvecs at sites (9, 10) (the two-pass path of large groups carries most of the work).
     With --profile n: n matvecs (--profile-precision) between cudaProfilerStart/Stop,
     nothing printed."""
     import torch
@@ -485,12 +454,15 @@ def extra_hubbard(args):
     r64 = d.bench_heff(mid, 0, args.steps, L2_FLUSH_BYTES)
     d.bench_heff(mid, args.warmup, 0, 0, precision="fp32")
     r32 = d.bench_heff(mid, 0, args.steps, L2_FLUSH_BYTES, precision="fp32")
+    d.bench_heff(mid, args.warmup, 0, 0, precision="tc")
+    rtc = d.bench_heff(mid, 0, args.steps, L2_FLUSH_BYTES, precision="tc")
     d.close()
     out = {"config": f"hubbard L=20 N=20 U=4 C1 D=512, {args.sweeps} sweep(s), matvec at sites (9,10)",
            "solve_s": solve_s, "energy": e,
            "fp64": {"ms_per_matvec": r64["ms_per_matvec"], "gflops": r64["flops"] / r64["ms_per_matvec"] / 1e6,
                     "launches_per_matvec": r64["launches"] / max(args.steps, 1)},
            "fp32": {"ms_per_matvec": r32["ms_per_matvec"], "gflops": r32["flops"] / r32["ms_per_matvec"] / 1e6},
+           "tc": {"ms_per_matvec": rtc["ms_per_matvec"], "gflops": rtc["flops"] / rtc["ms_per_matvec"] / 1e6},
            "ledger_flops_per_matvec": r64["flops"]}
     print(json.dumps({"extra": "hubbard_l20_d512", **out}), flush=True)
 
@@ -549,17 +521,15 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    model = make_model()
     steps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
-    cb = cpu_baseline_sample(model, n_matvec=steps)
+    cb = cpu_baseline_sample(n_matvec=steps)
     wall = time.perf_counter() - t0
     line = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ab initio generator, seed 1234)",
-        "config": {"workload": "synthetic ab initio L=24 N=24 S=0 D2h D=1000, Heff matvec at sites (11,12), "
-                               "initial SyBookkeeper dimensions", "setup_and_sample_s": wall},
+        "config": {"workload": WORKLOAD, "sample": cb["sample"], "setup_and_sample_s": wall},
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU oracle port of the reference's Heff (the reference needs BLAS/LAPACK/HDF5 builds absent here)",
@@ -568,27 +538,32 @@ def run_reference(args):
 
 
 def main():
-    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[1])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--no-sweep", action="store_true", help="skip the sweep timing")
-    ap.add_argument("--extra", choices=["config3", "batch", "hubbard"], default=None,
+    ap.add_argument("--extra", choices=["config1", "config2", "batch", "hubbard"], default=None,
                     help="run one of the further configurations instead (prints its own JSON line)")
-    ap.add_argument("--sweeps", type=int, default=2, help="sweeps per problem for --extra")
+    ap.add_argument("--sweeps", type=int, default=2, help="sweeps of each run")
     ap.add_argument("--batch-count", type=int, default=64, help="problems for --extra batch")
     ap.add_argument("--workers", type=int, default=16, help="concurrent problems for --extra batch")
-    ap.add_argument("--profile-precision", choices=["fp64", "fp32"], default="fp64",
+    ap.add_argument("--profile-precision", choices=["fp64", "fp32", "tc"], default="fp64",
                     help="arithmetic of the profiled matvecs of --extra hubbard --profile")
+    ap.add_argument("--dump-dims", default=None,
+                    help="write the sector dimensions of the swept FP64 state to this JSON file")
     ap.add_argument("--profile", type=int, default=0,
                     help="profiling mode: set up, then run this many matvecs between cudaProfilerStart/Stop")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.extra == "config3":
-        extra_config3(args)
+    if args.extra == "config1":
+        from chemps2_gb300.models import hubbard
+
+        extra_sweeps(args, "hubbard L=16 N=16 U=4 C1 D=200", hubbard(16, 4.0), 200, seed=1)
+    elif args.extra == "config2":
+        extra_sweeps(args, "synthetic ab initio L=24 N=24 S=0 D2h D=1000", make_model(24), 1000)
     elif args.extra == "batch":
         extra_batch(args)
     elif args.extra == "hubbard":

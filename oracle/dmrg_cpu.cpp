@@ -14,6 +14,7 @@
 // Exposed through a C API (oracle_*), loaded by the tests and the benchmark's CPU
 // baseline with ctypes.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -220,12 +221,32 @@ struct OracleDMRG {
   double t_matvec = 0.0;
   bool check = true;
   std::vector<double> ones;
+  int left_upto_ = -1;
 
-  OracleDMRG(CheMPS2::Problem* p, CheMPS2::ConvergenceScheme* o, bool check_programs)
+  // dims (optional): rows (boundary, N, 2S, I, dim) that replace the bookkeeper's scaled
+  // dimensions (every sector not listed gets 0), for a state with given sector dimensions;
+  // left_upto: the left operators are built for the first left_upto boundaries only (all
+  // when negative).
+  OracleDMRG(CheMPS2::Problem* p, CheMPS2::ConvergenceScheme* o, bool check_programs,
+             const std::vector<std::array<int, 5>>* dims = nullptr, int left_upto = -1)
       : Prob(p), Opt(o), L(p->gL()), ex(c2g::num_slots(p->gL()) + 8), check(check_programs) {
     Prob->construct_mxelem();
     bk = std::make_unique<SyBookkeeper>(Prob, Opt->get_D(0));
     if (!bk->IsPossible()) throw std::invalid_argument("impossible symmetry sector");
+    if (dims) {
+      for (int b = 0; b <= L; b++)
+        for (int id = 0; id < bk->num_sectors(b); id++) {
+          int n, s2, i;
+          bk->sector_labels(b, id, &n, &s2, &i);
+          bk->SetDim(b, n, s2, i, 0);
+        }
+      for (const auto& r : *dims) {
+        if (r[0] < 0 || r[0] > L) throw std::invalid_argument("dims: boundary out of range");
+        if (r[4] > bk->gFCIdim(r[0], r[1], r[2], r[3])) throw std::invalid_argument("dims: above the FCI dimension");
+        bk->SetDim(r[0], r[1], r[2], r[3], r[4]);
+      }
+    }
+    left_upto_ = left_upto;
     mps_lay.resize(L);
     mps.resize(L);
     ops.resize(L - 1);
@@ -357,7 +378,8 @@ struct OracleDMRG {
       ex.bind(slot_ops(L, b), nullptr, 0);
       isAllocated[b] = 0;
     }
-    for (int c = 0; c < L - 2; c++) update(c, true);
+    const int upto = (left_upto_ >= 0) ? std::min(left_upto_, L - 2) : L - 2;
+    for (int c = 0; c < upto; c++) update(c, true);
     TotalMinEnergy = 1e8;
     MaxDisc = 0.0;
   }
@@ -615,6 +637,36 @@ int oracle_dmrg_create(const char* fcidump, int L, int group, const int* irreps,
     h->opt = std::make_unique<CheMPS2::ConvergenceScheme>(ninstr);
     for (int i = 0; i < ninstr; i++) h->opt->set_instruction(i, D[i], econv[i], maxsweeps[i], noise[i], rtol[i]);
     h->dmrg = std::make_unique<oracle::OracleDMRG>(h->prob.get(), h->opt.get(), check_programs != 0);
+    *out = h.release();
+  });
+}
+
+// As oracle_dmrg_create (no FCIDUMP) with the sector dimensions given: ndims rows of
+// (boundary, N, 2S, I, dim) in `dims`; left operators for the first left_upto boundaries.
+int oracle_dmrg_create_dims(int L, int group, const int* irreps, const double* tmat, const double* vmat,
+                            double econst, int two_s, int n, int irrep, int D, int ndims, const int* dims,
+                            int left_upto, void** out) {
+  return guard([&] {
+    auto h = std::make_unique<OracleHandle>();
+    h->ham = std::make_unique<CheMPS2::Hamiltonian>(L, group, irreps);
+    for (int i = 0; i < L; i++)
+      for (int j = 0; j < L; j++)
+        if (tmat[i + L * j] != 0.0) h->ham->setTmat(i, j, tmat[i + L * j]);
+    for (int i = 0; i < L; i++)
+      for (int j = 0; j < L; j++)
+        for (int k = 0; k < L; k++)
+          for (int l = 0; l < L; l++) {
+            const double v = vmat[i + size_t(L) * (j + size_t(L) * (k + size_t(L) * l))];
+            if (v != 0.0) h->ham->setVmat(i, j, k, l, v);
+          }
+    h->ham->setEconst(econst);
+    h->prob = std::make_unique<CheMPS2::Problem>(h->ham.get(), two_s, n, irrep);
+    h->opt = std::make_unique<CheMPS2::ConvergenceScheme>(1);
+    h->opt->set_instruction(0, D, 1e-10, 1, 0.0, 1e-8);
+    std::vector<std::array<int, 5>> rows(ndims);
+    for (int r = 0; r < ndims; r++)
+      for (int c = 0; c < 5; c++) rows[r][c] = dims[5 * r + c];
+    h->dmrg = std::make_unique<oracle::OracleDMRG>(h->prob.get(), h->opt.get(), false, &rows, left_upto);
     *out = h.release();
   });
 }

@@ -80,8 +80,23 @@ class OracleDMRG:
     """CPU DMRG of the oracle. schedule: list of (D, econv, max_sweeps, noise, rtol)."""
 
     def __init__(self, model: Model | None, two_s, n, irrep, schedule, reorder=0, fcidump=None, group=None,
-                 check=True):
+                 check=True, dims=None, left_upto=-1):
+        """dims: rows (boundary, N, 2S, I, dim) replacing the scaled sector dimensions (the
+        state then has those dimensions, random tensors); left_upto: build the left operators
+        of the first left_upto boundaries only (-1: all)."""
         L = lib()
+        if dims is not None:
+            rows = np.ascontiguousarray(np.asarray(dims, dtype=np.int32).reshape(-1, 5))
+            tf, vf = model.tflat(), model.vflat()
+            self._keep = (rows, tf, vf)
+            h = C.c_void_p()
+            rc = L.oracle_dmrg_create_dims(model.L, model.group, _ip(model.irreps), _dp(tf), _dp(vf),
+                                           C.c_double(model.econst), two_s, n, irrep, int(schedule[0][0]),
+                                           len(rows), _ip(rows), int(left_upto), C.byref(h))
+            if rc != 0:
+                raise RuntimeError(L.oracle_last_error().decode())
+            self.h = h
+            return
         D = np.array([s[0] for s in schedule], dtype=np.int32)
         ec = np.array([s[1] for s in schedule], dtype=np.float64)
         ms = np.array([s[2] for s in schedule], dtype=np.int32)

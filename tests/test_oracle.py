@@ -197,3 +197,22 @@ def test_threaded_executor_gives_identical_results():
         ol.set_threads(1)
     assert np.array_equal(results[1][0], results[4][0])
     assert results[1][1] == results[4][1]
+
+
+def test_oracle_state_with_given_dimensions():
+    """The oracle built from explicit sector dimensions (the CPU baseline's way to reproduce
+    the shape of the GPU's swept state) equals the default construction when given the
+    default dimensions, with only the left operators it needs."""
+    m = models.hubbard(8, 4.0)
+    sched = [(20, 1e-10, 1, 0.0, 1e-9)]
+    ol.srand(3)
+    a = ol.OracleDMRG(m, 0, 8, 0, sched)
+    rows = [(b, *map(int, r[:3]), int(r[4])) for b in range(9) for r in a.sectors(b) if r[4] > 0]
+    ol.srand(3)
+    c = ol.OracleDMRG(m, 0, 8, 0, sched, dims=rows, left_upto=3)
+    for d in (a, c):
+        for i in range(6, 3, -1):
+            d.update(i, False)
+    xa, ya, _ = a.heff_apply(3)
+    xc, yc, _ = c.heff_apply(3)
+    assert np.array_equal(xa, xc) and np.array_equal(ya, yc)
