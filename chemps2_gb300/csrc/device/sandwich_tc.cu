@@ -10,18 +10,20 @@
 // accumulate in FP32 in tensor memory; the item sum of a tile is turned into FP64 in the
 // epilogue (split tiles are reduced in FP64 in split order, as in the SIMT path).
 //
-// One 128-thread CTA per output tile (the same 64 x 64 grid and tile list as the SIMT
+// One 256-thread CTA per output tile (the same 64 x 64 grid and tile list as the SIMT
 // kernels). The tile is the top-left 64 x 64 of a 128 x 64 MMA (M = 128, N = 64): rows
 // 64..127 of the A operand are never written and their accumulator rows never read. The
-// inner dimension is staged in chunks of 16 through two shared-memory stages: all threads
-// load a chunk (FP32, coalesced along whichever index is unit-stride), scale, split and
-// store it in the no-swizzle K-major layout of the MMA (8-row x 16-byte core matrices,
-// core matrices adjacent along K 128 bytes apart, 8-row groups 256 bytes apart); one
-// thread issues the three MMAs of the chunk and commits them to the stage's mbarrier,
-// which the threads wait on before they overwrite that stage two chunks later. Items with
-// an inner dimension shorter than 16 are padded with zeros. The accumulator (64 FP32
-// columns of tensor memory, allocated by warp 0) is read by warps 0 and 1 (lanes 0..63 =
-// tile rows) with tcgen05.ld.
+// inner dimension is staged in chunks of 16 through three shared-memory stages: all threads
+// load a chunk (FP32, pairs of k per thread, 32-byte segments whichever index is
+// unit-stride), scale, split and store it in the no-swizzle K-major layout of the MMA
+// (8-row x 16-byte core matrices, core matrices adjacent along K 128 bytes apart, 8-row
+// groups 256 bytes apart; the 4-byte stores of a warp hit 32 distinct banks); one thread
+// issues the three MMAs of the chunk and commits them to the stage's mbarrier, which the
+// threads wait on before they overwrite that stage three chunks later. A chunk's global
+// loads are issued three chunks ahead of its shared-memory stores, so they are in flight
+// while the chunks before it are stored and their MMAs issued. Items with an inner
+// dimension shorter than 16 are padded with zeros. The accumulator (64 FP32 columns of tensor memory, allocated by warp 0) is read
+// with tcgen05.ld by warps 0, 1, 4 and 5 (lanes 0..63 = tile rows, two column halves).
 //
 // Every mbarrier wait is bounded: after kTcSpinLimit polls the kernel records an error in
 // the runtime's mapped error word, waits (bounded again) for its own MMAs, frees its tensor
@@ -35,9 +37,9 @@ namespace c2g {
 
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;
 constexpr int kTcM = 128, kTcN = 64, kTcK = 16;
-constexpr int kTcStages = 2;
+constexpr int kTcStages = 3;
 constexpr int kTcABytes = kTcM * kTcK * 2;  // 4096: one BF16 A operand of a chunk
 constexpr int kTcBBytes = kTcN * kTcK * 2;  // 2048: one BF16 B operand of a chunk
 constexpr int kTcStageBytes = 2 * kTcABytes + 2 * kTcBBytes;  // A hi, A lo, B hi, B lo
@@ -145,66 +147,63 @@ __device__ __forceinline__ TcOpnd tc_opnd(const SlotPtrs& sp, const GemmOperand&
   return TcOpnd{t ? p + dk + ld * di : p + di + ld * dk, ld, t};
 }
 
-// One chunk of values held by a thread between its loads and its shared-memory stores:
-// 8 elements of op(L) (64 rows x 16) and 8 of op(R)^T (64 columns x 16).
-struct TcChunk {
-  float a[8], b[8];
+// Staging map of a 64 x 16 chunk operand (op(L) rows, or op(R)^T columns): 512 k-pairs,
+// two per thread. Slot g = warp + 8 s (s = 0, 1) is the row group g & 7 and the k-pair
+// half g >> 3; lane = (row & 7) + 8 (k-pair & 3). A warp thus reads eight rows at eight
+// consecutive k (32-byte segments whichever index is unit-stride) and its 4-byte
+// shared-memory stores of a BF16 pair fall in 32 distinct banks.
+struct TcRegs {
+  float a[2][2], b[2][2];  // [slot][k of the pair]
 };
 
-// element e = tid + 128 s of a 64 x 16 operand chunk: (row, k), unit-stride index fastest
-__device__ __forceinline__ void chunk_pos(bool t, int e, int& row, int& k) {
-  if (t) {
-    k = e & 15;
-    row = e >> 4;
-  } else {
-    row = e & 63;
-    k = e >> 6;
-  }
+__device__ __forceinline__ void stage_pos(int s, int& row, int& k) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = warp + 8 * s;
+  row = (g & 7) * 8 + (lane & 7);
+  k = 2 * ((g >> 3) * 4 + (lane >> 3));
 }
 
-__device__ __forceinline__ void tc_fetch(TcChunk& c, const TcOpnd& L, int M, const TcOpnd& R, int N, int K, int k0,
+__device__ __forceinline__ void tc_fetch(TcRegs& c, const TcOpnd& L, int M, const TcOpnd& R, int N, int K, int k0,
                                          float alpha) {
-  const int tid = threadIdx.x;
 #pragma unroll
-  for (int s = 0; s < 8; s++) {
+  for (int s = 0; s < 2; s++) {
     int i, k;
-    chunk_pos(L.t, tid + kTcThreads * s, i, k);
-    const int kk = k0 + k;
-    c.a[s] = (i < M && kk < K) ? alpha * (L.t ? L.p[kk + L.ld * i] : L.p[i + L.ld * kk]) : 0.0f;
-  }
+    stage_pos(s, i, k);
 #pragma unroll
-  for (int s = 0; s < 8; s++) {
-    int j, k;
-    chunk_pos(!R.t, tid + kTcThreads * s, j, k);  // op(R)(k, j): unit stride along j unless transposed
-    const int kk = k0 + k;
-    c.b[s] = (j < N && kk < K) ? (R.t ? R.p[j + R.ld * kk] : R.p[kk + R.ld * j]) : 0.0f;
+    for (int h = 0; h < 2; h++) {
+      const int kk = k0 + k + h;
+      c.a[s][h] = (i < M && kk < K) ? alpha * (L.t ? L.p[kk + L.ld * i] : L.p[i + L.ld * kk]) : 0.0f;
+      c.b[s][h] = (i < N && kk < K) ? (R.t ? R.p[i + R.ld * kk] : R.p[kk + R.ld * i]) : 0.0f;
+    }
   }
 }
 
-__device__ __forceinline__ void split_store(unsigned char* hi, unsigned char* lo, uint32_t off, float v) {
-  const __nv_bfloat16 h = __float2bfloat16_rn(v);
-  const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-  *reinterpret_cast<__nv_bfloat16*>(hi + off) = h;
-  *reinterpret_cast<__nv_bfloat16*>(lo + off) = l;
+// hi = bf16(v), lo = bf16(v - hi) of a pair, packed low k first
+__device__ __forceinline__ void split_pair(float v0, float v1, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-__device__ __forceinline__ void tc_store(const TcChunk& c, bool lt, bool rt, unsigned char* stage) {
+__device__ __forceinline__ void tc_store(const TcRegs& c, unsigned char* stage) {
   unsigned char* ahi = stage;
   unsigned char* alo = stage + kTcABytes;
   unsigned char* bhi = stage + 2 * kTcABytes;
   unsigned char* blo = stage + 2 * kTcABytes + kTcBBytes;
-  const int tid = threadIdx.x;
 #pragma unroll
-  for (int s = 0; s < 8; s++) {
+  for (int s = 0; s < 2; s++) {
     int i, k;
-    chunk_pos(lt, tid + kTcThreads * s, i, k);
-    split_store(ahi, alo, kmajor_off(i, k), c.a[s]);
-  }
-#pragma unroll
-  for (int s = 0; s < 8; s++) {
-    int j, k;
-    chunk_pos(!rt, tid + kTcThreads * s, j, k);
-    split_store(bhi, blo, kmajor_off(j, k), c.b[s]);
+    stage_pos(s, i, k);
+    const uint32_t off = kmajor_off(i, k);
+    uint32_t hi, lo;
+    split_pair(c.a[s][0], c.a[s][1], hi, lo);
+    *reinterpret_cast<uint32_t*>(ahi + off) = hi;
+    *reinterpret_cast<uint32_t*>(alo + off) = lo;
+    split_pair(c.b[s][0], c.b[s][1], hi, lo);
+    *reinterpret_cast<uint32_t*>(bhi + off) = hi;
+    *reinterpret_cast<uint32_t*>(blo + off) = lo;
   }
 }
 
@@ -249,52 +248,112 @@ struct SumSource {  // pass 2: the GEMM items of [item0, item1) (items with k = 
   }
 };
 
+// Position in the chunk sequence of a tile: item q of the source, inner offset k0.
+struct TcCursor {
+  int q, k0, K;
+  float alpha;
+  TcOpnd L, R;
+};
+
+// Moves `c` to the first chunk at or after item q (k0 = 0); false when none is left.
+template <class Src>
+__device__ __forceinline__ bool tc_seek(const Src& src, const SlotPtrs& sp, TcCursor& c, int q) {
+  const int n = src.count();
+  for (; q < n; q++)
+    if (src.get(q, sp, c.L, c.R, c.alpha, c.K)) {
+      c.q = q;
+      c.k0 = 0;
+      return true;
+    }
+  return false;
+}
+
+// The chunk loop of tc_accumulate: kTcAhead chunks of operand loads are in flight in
+// registers (one TcRegs each, held in unrolled code so that no register is moved while its
+// load is pending); each step stores the oldest, issues the loads of the chunk kTcAhead
+// further on, and hands the stored chunk to the MMA issuer.
+constexpr int kTcAhead = 3;
+
+struct TcPipe {
+  TcCursor cur;   // the next chunk to fetch
+  bool more;      // cur is valid
+  int fetched, stored;
+};
+
+template <class Src>
+__device__ __forceinline__ void tc_fetch_next(const Src& src, const SlotPtrs& sp, TcPipe& pp, TcRegs& r, int M,
+                                              int N) {
+  if (!pp.more) return;
+  tc_fetch(r, pp.cur.L, M, pp.cur.R, N, pp.cur.K, pp.cur.k0, pp.cur.alpha);
+  pp.fetched++;
+  pp.cur.k0 += kTcK;
+  if (pp.cur.k0 >= pp.cur.K) pp.more = tc_seek(src, sp, pp.cur, pp.cur.q + 1);
+}
+
+// One step: store `r` (chunk pp.stored) into its stage, refill `r` with the chunk kTcAhead
+// further on, then issue the stored chunk's MMAs. False (in every thread) when a wait ran
+// out.
+template <class Src>
+__device__ __forceinline__ bool tc_step(const Src& src, const SlotPtrs& sp, TcPipe& pp, TcRegs& r, int M, int N,
+                                        TcSmem& sm, uint32_t tmem_d, uint32_t& phase, uint32_t& pending) {
+  const int chunk = pp.stored;
+  const int s = chunk % kTcStages;
+  const uint32_t bit = 1u << s;
+  bool ok = true;
+  if (pending & bit) {  // the MMAs that read this stage kTcStages chunks ago
+    ok = mbar_wait(&sm.bar[s], (phase >> s) & 1u);
+    phase ^= bit;
+    pending &= ~bit;
+  }
+  tc_store(r, sm.stage[s]);
+  pp.stored++;
+  tc_fetch_next(src, sp, pp, r, M, N);
+  fence_async_smem();
+  if (__syncthreads_or(!ok)) return false;
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    tc_issue(tmem_d, sm.stage[s], chunk == 0);
+    tc_commit(&sm.bar[s]);
+  }
+  pending |= bit;
+  return true;
+}
+
 // Sums the products of `src` into the tensor-memory accumulator. Returns the number of
 // chunks issued (0: the accumulator was never written), or -1 when a wait ran out (the
 // decision is the same in every thread of the CTA).
 template <class Src>
 __device__ int tc_accumulate(const Src& src, int M, int N, const SlotPtrs& sp, TcSmem& sm, uint32_t tmem_d,
-                             uint32_t (&phase)[kTcStages], bool (&pending)[kTcStages]) {
-  int chunk = 0;
-  const int n = src.count();
-  for (int q = 0; q < n; q++) {
-    TcOpnd L, R;
-    float alpha;
-    int K;
-    if (!src.get(q, sp, L, R, alpha, K)) continue;
-    for (int k0 = 0; k0 < K; k0 += kTcK) {
-      const int s = chunk & 1;
-      TcChunk c;
-      tc_fetch(c, L, M, R, N, K, k0, alpha);
-      bool ok = true;
-      if (pending[s]) {  // the MMAs that read this stage two chunks ago
-        ok = mbar_wait(&sm.bar[s], phase[s]);
-        phase[s] ^= 1u;
-        pending[s] = false;
-      }
-      tc_store(c, L.t, R.t, sm.stage[s]);
-      fence_async_smem();
-      if (__syncthreads_or(!ok)) return -1;
-      if (threadIdx.x == 0) {
-        tc_fence_after();
-        tc_issue(tmem_d, sm.stage[s], chunk == 0);
-        tc_commit(&sm.bar[s]);
-      }
-      pending[s] = true;
-      chunk++;
-    }
+                             uint32_t& phase, uint32_t& pending) {
+  TcPipe pp;
+  pp.fetched = pp.stored = 0;
+  pp.more = tc_seek(src, sp, pp.cur, 0);
+  if (!pp.more) return 0;
+  static_assert(kTcAhead == 3, "the step loop below holds three register sets");
+  TcRegs r0, r1, r2;
+  tc_fetch_next(src, sp, pp, r0, M, N);
+  tc_fetch_next(src, sp, pp, r1, M, N);
+  tc_fetch_next(src, sp, pp, r2, M, N);
+  for (;;) {
+    if (pp.stored == pp.fetched) break;
+    if (!tc_step(src, sp, pp, r0, M, N, sm, tmem_d, phase, pending)) return -1;
+    if (pp.stored == pp.fetched) break;
+    if (!tc_step(src, sp, pp, r1, M, N, sm, tmem_d, phase, pending)) return -1;
+    if (pp.stored == pp.fetched) break;
+    if (!tc_step(src, sp, pp, r2, M, N, sm, tmem_d, phase, pending)) return -1;
   }
-  return chunk;
+  return pp.stored;
 }
 
 // Waits for every committed chunk; false (in every thread) when a wait ran out.
-__device__ bool tc_drain(TcSmem& sm, uint32_t (&phase)[kTcStages], bool (&pending)[kTcStages]) {
+__device__ bool tc_drain(TcSmem& sm, uint32_t& phase, uint32_t& pending) {
   bool ok = true;
   for (int s = 0; s < kTcStages; s++) {
-    if (!pending[s]) continue;
-    if (!mbar_wait(&sm.bar[s], phase[s])) ok = false;
-    phase[s] ^= 1u;
-    pending[s] = false;
+    const uint32_t bit = 1u << s;
+    if (!(pending & bit)) continue;
+    if (!mbar_wait(&sm.bar[s], (phase >> s) & 1u)) ok = false;
+    phase ^= bit;
+    pending &= ~bit;
   }
   return !__syncthreads_or(!ok);
 }
@@ -324,8 +383,18 @@ __device__ void tc_teardown(uint32_t tmem_d) {
   }
 }
 
-// Accumulator columns c0 .. c0 + 15 of this thread's tile row (warps 0 and 1: rows 0..63);
-// zeros when no chunk was issued.
+// The epilogue readers: warps 0, 1, 4 and 5 (warp w may read accumulator lanes
+// 32 (w % 4) .. 32 (w % 4) + 31), tile row (w % 4) * 32 + lane, columns 32 (w / 4) ..
+// 32 (w / 4) + 31.
+__device__ __forceinline__ bool tc_reader(int& row, int& col_base) {
+  const int warp = threadIdx.x >> 5;
+  row = (warp & 3) * 32 + (threadIdx.x & 31);
+  col_base = (warp >> 2) * 32;
+  return (warp & 3) < 2;
+}
+
+// Accumulator columns c0 .. c0 + 15 of this reader's tile row; zeros when no chunk was
+// issued.
 __device__ __forceinline__ void tc_read16(uint32_t tmem_d, int chunks, int c0, float (&v)[16]) {
   if (chunks <= 0) {
 #pragma unroll
@@ -333,14 +402,14 @@ __device__ __forceinline__ void tc_read16(uint32_t tmem_d, int chunks, int c0, f
     return;
   }
   const int warp = threadIdx.x >> 5;
-  tmem_ld16(tmem_d + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
+  tmem_ld16(tmem_d + (static_cast<uint32_t>((warp & 3) * 32) << 16) + static_cast<uint32_t>(c0), v);
 }
 
 __device__ __forceinline__ void record_failure(int* err) {
   if (threadIdx.x == 0 && err) atomicOr(err, 1);
 }
 
-__global__ void __launch_bounds__(kTcThreads, 4)
+__global__ void __launch_bounds__(kTcThreads, 3)
     inter_tc_kernel(const InterJob* __restrict__ jobs, const GemmTile* __restrict__ tiles, SlotPtrs sp, int* err) {
   __shared__ TcSmem sm;
   tc_setup(sm);
@@ -349,19 +418,19 @@ __global__ void __launch_bounds__(kTcThreads, 4)
   const InterJob J = jobs[T.idx];
   const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
   const int tm = min(64, J.m - row0), tn = min(64, J.n - col0);
-  uint32_t phase[kTcStages] = {0u, 0u};
-  bool pending[kTcStages] = {false, false};
+  uint32_t phase = 0u, pending = 0u;  // per stage: mbarrier phase and outstanding commit
   const InterSource src{&J, row0, col0};
   const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
   const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
   tc_fence_after();
+  int r, cb;
+  const bool reader = tc_reader(r, cb);
   if (!ok) {
     record_failure(err);
-  } else if (threadIdx.x < 64) {
+  } else if (reader) {
     float* S = sp.inter32 + J.off;
-    const int r = threadIdx.x;
 #pragma unroll
-    for (int c0 = 0; c0 < 64; c0 += 16) {
+    for (int c0 = cb; c0 < cb + 32; c0 += 16) {
       float v[16];
       tc_read16(tmem_d, chunks, c0, v);
       if (r < tm) {
@@ -374,7 +443,7 @@ __global__ void __launch_bounds__(kTcThreads, 4)
   tc_teardown(tmem_d);
 }
 
-__global__ void __launch_bounds__(kTcThreads, 4)
+__global__ void __launch_bounds__(kTcThreads, 3)
     sum_tc_kernel(const SumGroup* __restrict__ groups, const SumItem* __restrict__ items,
                   const GemmTile* __restrict__ tiles, double* partials, unsigned int* counters, SlotPtrs sp, int* err) {
   __shared__ TcSmem sm;
@@ -385,14 +454,14 @@ __global__ void __launch_bounds__(kTcThreads, 4)
   const SumGroup G = groups[T.idx];
   const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
   const int tm = min(64, G.m - row0), tn = min(64, G.n - col0);
-  uint32_t phase[kTcStages] = {0u, 0u};
-  bool pending[kTcStages] = {false, false};
+  uint32_t phase = 0u, pending = 0u;  // per stage: mbarrier phase and outstanding commit
   const SumSource src{items, T.item0, T.item1, row0, col0};
   const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
   const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
   tc_fence_after();
   if (!ok) record_failure(err);
-  const int r = threadIdx.x;
+  int r, cb;
+  const bool reader = tc_reader(r, cb);
   double* O = const_cast<double*>(resolve<double>(sp, G.out));
   const int64_t ldo = G.ldo;
   const bool accum = (G.flags & kAccumulate) != 0;
@@ -401,9 +470,9 @@ __global__ void __launch_bounds__(kTcThreads, 4)
   const int TM = 16 * ((T.shape & 3) + 1);
   double* part = partials + T.part;
   const int64_t part_elems = static_cast<int64_t>(TM) * 16 * (((T.shape >> 2) & 3) + 1);
-  if (ok && r < 64) {
+  if (ok && reader) {
 #pragma unroll
-    for (int c0 = 0; c0 < 64; c0 += 16) {
+    for (int c0 = cb; c0 < cb + 32; c0 += 16) {
       float v[16];
       tc_read16(tmem_d, chunks, c0, v);
       double acc[16];
@@ -447,11 +516,13 @@ __global__ void __launch_bounds__(kTcThreads, 4)
     if (is_last) {
       __threadfence();
       if (threadIdx.x == 0) counters[T.counter] = 0u;  // ready for the next launch
-      if (ok && r < tm) {
-        for (int c = 0; c < tn; c++) {
+      // every thread: row tid % 64, columns 16 (tid / 64) .. 16 (tid / 64) + 15
+      const int rr = threadIdx.x & 63, c1 = 16 * (threadIdx.x >> 6);
+      if (ok && rr < tm) {
+        for (int c = c1; c < min(tn, c1 + 16); c++) {
           double v = 0.0;
-          for (int s = 0; s < T.nsplit; s++) v += __ldcg(part + s * part_elems + r + TM * c);
-          const int64_t idx = (row0 + r) + ldo * (col0 + c);
+          for (int s = 0; s < T.nsplit; s++) v += __ldcg(part + s * part_elems + rr + TM * c);
+          const int64_t idx = (row0 + rr) + ldo * (col0 + c);
           O[idx] = accum ? O[idx] + v : v;
         }
       }
