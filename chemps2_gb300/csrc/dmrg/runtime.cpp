@@ -67,6 +67,8 @@ Runtime::Runtime(int L, int device) : L_(L) {
   C2G_CUDA(cudaSetDevice(device));
   device_ = device;
   C2G_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  C2G_CUDA(cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking));
+  for (int b = 0; b < 2; b++) C2G_CUDA(cudaEventCreateWithFlags(&stg_ev_[b], cudaEventDisableTiming));
   // Keep freed blocks in the stream-ordered pool instead of returning them to the driver.
   cudaMemPool_t pool;
   C2G_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
@@ -93,7 +95,12 @@ Runtime::~Runtime() {
   cudaFree(dev_slots_);
   cudaFree(dev_slots32_);
   cudaFree(partial_);
-  if (staging_) cudaFreeHost(staging_);
+  if (copy_) cudaStreamSynchronize(copy_);
+  for (int b = 0; b < 2; b++) {
+    if (stg_buf_[b]) cudaFreeHost(stg_buf_[b]);
+    if (stg_ev_[b]) cudaEventDestroy(stg_ev_[b]);
+  }
+  if (copy_) cudaStreamDestroy(copy_);
   for (int k = 0; k < kTransientKinds; k++)
     if (transient_[k]) cudaFreeAsync(transient_[k], stream_);
   if (stream_) cudaStreamSynchronize(stream_);
@@ -251,6 +258,20 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
   }
   if (eb > INT32_MAX) throw std::length_error("upload: batch table too large");
   dp->combo_size = cb;
+  // the staging buffer of this upload: the one whose previous copy is oldest
+  const int sb = stg_next_;
+  stg_next_ ^= 1;
+  if (stg_used_[sb]) C2G_CUDA(cudaEventSynchronize(stg_ev_[sb]));
+  staging_ = stg_buf_[sb];
+  staging_cap_ = stg_cap_[sb];
+  struct KeepStaging {  // the buffer (possibly grown) goes back to its ring slot
+    Runtime* rt;
+    int b;
+    ~KeepStaging() {
+      rt->stg_buf_[b] = rt->staging_;
+      rt->stg_cap_[b] = rt->staging_cap_;
+    }
+  } keep_staging{this, sb};
   auto reloc = [&](Ref r, size_t i) -> Ref {
     if (r != 0 && ref_slot(r) == kSlotCombo) return make_ref(kSlotCombo, ref_off(r) + combo_base[i]);
     return r;
@@ -836,7 +857,7 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
   }
   const int64_t bytes = head + tile_bytes;
   reserve_staging(bytes, head);  // keeps the part already assembled
-  C2G_CUDA(cudaMallocAsync(&dp->blob, std::max<int64_t>(bytes, 256), stream_));
+  C2G_CUDA(cudaMallocAsync(&dp->blob, std::max<int64_t>(bytes, 256), copy_));
   char* dbase = static_cast<char*>(dp->blob);
   int64_t off = head;
   auto put = [&](const void* src, size_t n) -> const void* {
@@ -882,8 +903,10 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     dp->stages.push_back(ds);
   }
   dp->bytes = bytes;
-  C2G_CUDA(cudaMemcpyAsync(dp->blob, staging_, bytes, cudaMemcpyHostToDevice, stream_));
-  C2G_CUDA(cudaStreamSynchronize(stream_));  // the staging buffer is reused by the next upload
+  C2G_CUDA(cudaMemcpyAsync(dp->blob, staging_, bytes, cudaMemcpyHostToDevice, copy_));
+  C2G_CUDA(cudaEventRecord(stg_ev_[sb], copy_));
+  stg_used_[sb] = true;
+  C2G_CUDA(cudaStreamWaitEvent(stream_, stg_ev_[sb], 0));  // every use of the program follows the copy
   if (dp->combo_size > 0) dp->combo = alloc(dp->combo_size);
   // transient buffers come from the runtime's shared ones at run time (sizes only here)
   dp->part_size = part_doubles;

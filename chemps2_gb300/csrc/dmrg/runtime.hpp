@@ -165,8 +165,18 @@ class Runtime {
   int* err_host_ = nullptr;  // mapped pinned error word (host view)
   int* err_dev_ = nullptr;   // its device address
   // pinned host buffer in which upload assembles a program before the copy to the device
+  // (the current one of a ring of two: a program is assembled in one while the copy of the
+  // previous program from the other may still be in flight)
   char* staging_ = nullptr;
   int64_t staging_cap_ = 0;
+  char* stg_buf_[2] = {nullptr, nullptr};
+  int64_t stg_cap_[2] = {0, 0};
+  cudaEvent_t stg_ev_[2] = {nullptr, nullptr};  // the copy out of each buffer
+  bool stg_used_[2] = {false, false};
+  int stg_next_ = 0;
+  // program copies run here, so that an upload does not wait for the compute work queued
+  // before it; the compute stream waits for each copy
+  cudaStream_t copy_ = nullptr;
   // grows the staging buffer to at least `bytes`, keeping its first `keep` bytes
   void reserve_staging(int64_t bytes, int64_t keep);
   std::unique_ptr<DevProgram> upload_parts(const Program* parts, size_t np);
