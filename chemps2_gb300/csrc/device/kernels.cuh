@@ -127,11 +127,14 @@ cudaError_t launch_sum_gemm(const SumGroup* groups, const SumItem* items, const 
 
 
 // Tensor-core variants of the two passes (sandwich_tc.cu), reading the FP32 operand copies.
-// `err` (device-visible, may be null) is or-ed with 1 when a kernel gave up a bounded wait.
-cudaError_t launch_inter_tc(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp, int* err,
-                            cudaStream_t stream);
+// `sched`: two device counters, zero between launches (the kernels' tile scheduler resets
+// them). `err` (device-visible, may be null) is or-ed with 1 when a kernel gave up a
+// bounded wait.
+cudaError_t launch_inter_tc(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp,
+                            unsigned int* sched, int* err, cudaStream_t stream);
 cudaError_t launch_sum_tc(const SumGroup* groups, const SumItem* items, const GemmTile* tiles, int ntiles,
-                          double* partials, unsigned int* counters, const SlotPtrs& sp, int* err, cudaStream_t stream);
+                          double* partials, unsigned int* counters, const SlotPtrs& sp, unsigned int* sched, int* err,
+                          cudaStream_t stream);
 
 cudaError_t launch_sandwich(const Group* groups, const Term* terms, const BatchEntry* entries, const TileDesc* tiles,
                             int ntiles, const SlotPtrs& sp, cudaStream_t stream, Precision prec = Precision::kFP64);

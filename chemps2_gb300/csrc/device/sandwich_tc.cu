@@ -10,8 +10,8 @@
 // accumulate in FP32 in tensor memory; the item sum of a tile is turned into FP64 in the
 // epilogue (split tiles are reduced in FP64 in split order, as in the SIMT path).
 //
-// One 256-thread CTA per output tile (the same 64 x 64 grid and tile list as the SIMT
-// kernels). The tile is the top-left 64 x 64 of a 128 x 64 MMA (M = 128, N = 64): rows
+// Persistent 256-thread CTAs (three per SM) take the output tiles of the SIMT kernels'
+// tile lists (64 x 64 grid) one after another from an atomic counter. The tile is the top-left 64 x 64 of a 128 x 64 MMA (M = 128, N = 64): rows
 // 64..127 of the A operand are never written and their accumulator rows never read. The
 // inner dimension is staged in chunks of 16 through three shared-memory stages: all threads
 // load a chunk (FP32, pairs of k per thread, 32-byte segments whichever index is
@@ -29,6 +29,8 @@
 // the runtime's mapped error word, waits (bounded again) for its own MMAs, frees its tensor
 // memory and returns without writing its tile.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "kernels.cuh"
 #include "slots.cuh"
@@ -233,12 +235,34 @@ struct InterSource {  // pass 1: one product
   }
 };
 
-struct SumSource {  // pass 2: the GEMM items of [item0, item1) (items with k = 0 are skipped)
+// pass 2: the GEMM items of [item0, item1) (items with k = 0 are skipped). The item
+// records are read through shared memory, kTcItemBatch at a time, loaded by the whole CTA
+// with 16-byte loads (the calls of get() are the same in every thread, so the refill's
+// barriers are uniform): an item's operand loads do not wait behind a global load of its
+// record.
+constexpr int kTcItemBatch = 32;
+static_assert(sizeof(SumItem) % 16 == 0, "item records are copied in 16-byte words");
+struct SumSource {
   const SumItem* items;
   int item0, item1, row0, col0;
+  SumItem* buf;  // shared memory, kTcItemBatch records
+  int* base;     // shared: first item held in buf (-1: none)
   __device__ int count() const { return item1 - item0; }
+  __device__ void refill(int q) const {
+    __syncthreads();  // every thread is done with the records held so far
+    const int first = item0 + q;
+    const int n = min(kTcItemBatch, item1 - first);
+    constexpr int kWords = static_cast<int>(sizeof(SumItem) / 16);
+    const int4* src = reinterpret_cast<const int4*>(items + first);
+    int4* dst = reinterpret_cast<int4*>(buf);
+    for (int w = threadIdx.x; w < n * kWords; w += kTcThreads) dst[w] = src[w];
+    if (threadIdx.x == 0) *base = q;
+    __syncthreads();
+  }
   __device__ bool get(int q, const SlotPtrs& sp, TcOpnd& L, TcOpnd& R, float& alpha, int& K) const {
-    const SumItem& I = items[item0 + q];
+    const int b = *base;
+    if (b < 0 || q < b || q >= b + kTcItemBatch) refill(q);
+    const SumItem& I = buf[q - *base];
     K = I.k;
     if (K <= 0) return false;
     L = tc_opnd(sp, I.l, row0, 0);
@@ -409,141 +433,196 @@ __device__ __forceinline__ void record_failure(int* err) {
   if (threadIdx.x == 0 && err) atomicOr(err, 1);
 }
 
+// Persistent CTAs: each takes the next tile of the list from sched[0] until the list is
+// exhausted (tiles are ordered by descending work, so the longest start first); the last
+// CTA to finish resets sched[0] and sched[1] for the next launch. Tensor memory and the
+// mbarriers are set up once per CTA.
+__device__ __forceinline__ int tc_next_tile(unsigned int* sched, int* slot) {
+  __syncthreads();  // the previous tile's epilogue is done in every thread
+  if (threadIdx.x == 0) *slot = static_cast<int>(atomicAdd(sched, 1u));
+  __syncthreads();
+  return *slot;
+}
+
+__device__ __forceinline__ void tc_finish(unsigned int* sched) {
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(sched + 1, 1u) == gridDim.x - 1) {
+    sched[0] = 0u;
+    sched[1] = 0u;
+  }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 3)
-    inter_tc_kernel(const InterJob* __restrict__ jobs, const GemmTile* __restrict__ tiles, SlotPtrs sp, int* err) {
+    inter_tc_kernel(const InterJob* __restrict__ jobs, const GemmTile* __restrict__ tiles, int ntiles, SlotPtrs sp,
+                    unsigned int* sched, int* err) {
   __shared__ TcSmem sm;
+  __shared__ int slot;
   tc_setup(sm);
   const uint32_t tmem_d = sm.tmem_base;
-  const GemmTile T = tiles[blockIdx.x];
-  const InterJob J = jobs[T.idx];
-  const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
-  const int tm = min(64, J.m - row0), tn = min(64, J.n - col0);
   uint32_t phase = 0u, pending = 0u;  // per stage: mbarrier phase and outstanding commit
-  const InterSource src{&J, row0, col0};
-  const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
-  const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
-  tc_fence_after();
-  int r, cb;
-  const bool reader = tc_reader(r, cb);
-  if (!ok) {
-    record_failure(err);
-  } else if (reader) {
-    float* S = sp.inter32 + J.off;
+  for (;;) {
+    const int t = tc_next_tile(sched, &slot);
+    if (t >= ntiles) break;
+    const GemmTile T = tiles[t];
+    const InterJob J = jobs[T.idx];
+    const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
+    const int tm = min(64, J.m - row0), tn = min(64, J.n - col0);
+    const InterSource src{&J, row0, col0};
+    const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
+    const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
+    tc_fence_after();
+    if (!ok) {
+      record_failure(err);
+      break;
+    }
+    int r, cb;
+    if (tc_reader(r, cb)) {
+      float* S = sp.inter32 + J.off;
 #pragma unroll
-    for (int c0 = cb; c0 < cb + 32; c0 += 16) {
-      float v[16];
-      tc_read16(tmem_d, chunks, c0, v);
-      if (r < tm) {
+      for (int c0 = cb; c0 < cb + 32; c0 += 16) {
+        float v[16];
+        tc_read16(tmem_d, chunks, c0, v);
+        if (r < tm) {
 #pragma unroll
-        for (int c = 0; c < 16; c++)
-          if (c0 + c < tn) S[(row0 + r) + static_cast<int64_t>(J.m) * (col0 + c0 + c)] = v[c];
+          for (int c = 0; c < 16; c++)
+            if (c0 + c < tn) S[(row0 + r) + static_cast<int64_t>(J.m) * (col0 + c0 + c)] = v[c];
+        }
       }
     }
+    tc_fence_before();  // the accumulator reads precede the next tile's MMAs
   }
+  tc_finish(sched);
   tc_teardown(tmem_d);
 }
 
 __global__ void __launch_bounds__(kTcThreads, 3)
     sum_tc_kernel(const SumGroup* __restrict__ groups, const SumItem* __restrict__ items,
-                  const GemmTile* __restrict__ tiles, double* partials, unsigned int* counters, SlotPtrs sp, int* err) {
+                  const GemmTile* __restrict__ tiles, int ntiles, double* partials, unsigned int* counters,
+                  SlotPtrs sp, unsigned int* sched, int* err) {
   __shared__ TcSmem sm;
-  __shared__ int is_last;
+  __shared__ int slot, is_last, item_base;
+  __shared__ __align__(16) SumItem item_buf[kTcItemBatch];
   tc_setup(sm);
   const uint32_t tmem_d = sm.tmem_base;
-  const GemmTile T = tiles[blockIdx.x];
-  const SumGroup G = groups[T.idx];
-  const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
-  const int tm = min(64, G.m - row0), tn = min(64, G.n - col0);
   uint32_t phase = 0u, pending = 0u;  // per stage: mbarrier phase and outstanding commit
-  const SumSource src{items, T.item0, T.item1, row0, col0};
-  const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
-  const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
-  tc_fence_after();
-  if (!ok) record_failure(err);
-  int r, cb;
-  const bool reader = tc_reader(r, cb);
-  double* O = const_cast<double*>(resolve<double>(sp, G.out));
-  const int64_t ldo = G.ldo;
-  const bool accum = (G.flags & kAccumulate) != 0;
-  // partial tiles of a split tile: TM x TN doubles per split (the tile's 16-granular
-  // extents, as planned on the host), element (row, col) at row + TM col
-  const int TM = 16 * ((T.shape & 3) + 1);
-  double* part = partials + T.part;
-  const int64_t part_elems = static_cast<int64_t>(TM) * 16 * (((T.shape >> 2) & 3) + 1);
-  if (ok && reader) {
+  for (;;) {
+    const int t = tc_next_tile(sched, &slot);
+    if (t >= ntiles) break;
+    const GemmTile T = tiles[t];
+    const SumGroup G = groups[T.idx];
+    const int row0 = (T.pos >> 16) * 64, col0 = (T.pos & 0xffff) * 64;
+    const int tm = min(64, G.m - row0), tn = min(64, G.n - col0);
+    if (threadIdx.x == 0) item_base = -1;
+    __syncthreads();
+    const SumSource src{items, T.item0, T.item1, row0, col0, item_buf, &item_base};
+    const int chunks = tc_accumulate(src, tm, tn, sp, sm, tmem_d, phase, pending);
+    const bool ok = tc_drain(sm, phase, pending) && chunks >= 0;
+    tc_fence_after();
+    if (!ok) {
+      record_failure(err);
+      break;
+    }
+    int r, cb;
+    const bool reader = tc_reader(r, cb);
+    double* O = const_cast<double*>(resolve<double>(sp, G.out));
+    const int64_t ldo = G.ldo;
+    const bool accum = (G.flags & kAccumulate) != 0;
+    // partial tiles of a split tile: TM x TN doubles per split (the tile's 16-granular
+    // extents, as planned on the host), element (row, col) at row + TM col
+    const int TM = 16 * ((T.shape & 3) + 1);
+    double* part = partials + T.part;
+    const int64_t part_elems = static_cast<int64_t>(TM) * 16 * (((T.shape >> 2) & 3) + 1);
+    if (reader) {
 #pragma unroll
-    for (int c0 = cb; c0 < cb + 32; c0 += 16) {
-      float v[16];
-      tc_read16(tmem_d, chunks, c0, v);
-      double acc[16];
+      for (int c0 = cb; c0 < cb + 32; c0 += 16) {
+        float v[16];
+        tc_read16(tmem_d, chunks, c0, v);
+        double acc[16];
 #pragma unroll
-      for (int c = 0; c < 16; c++) acc[c] = static_cast<double>(v[c]);
-      // items without an inner dimension: out += alpha op(R), straight from global memory
-      if (r < tm) {
-        for (int it = T.item0; it < T.item1; it++) {
-          const SumItem I = items[it];
-          if (I.k > 0) continue;
-          const TcOpnd R = tc_opnd(sp, I.r, row0, col0 + c0);
+        for (int c = 0; c < 16; c++) acc[c] = static_cast<double>(v[c]);
+        // items without an inner dimension: out += alpha op(R), straight from global memory
+        if (r < tm) {
+          for (int it = T.item0; it < T.item1; it++) {
+            const SumItem I = items[it];
+            if (I.k > 0) continue;
+            const TcOpnd R = tc_opnd(sp, I.r, row0, col0 + c0);
 #pragma unroll
-          for (int c = 0; c < 16; c++)
-            if (c0 + c < tn)
-              acc[c] = fma(I.alpha, static_cast<double>(R.t ? R.p[c + R.ld * r] : R.p[r + R.ld * c]), acc[c]);
+            for (int c = 0; c < 16; c++)
+              if (c0 + c < tn)
+                acc[c] = fma(I.alpha, static_cast<double>(R.t ? R.p[c + R.ld * r] : R.p[r + R.ld * c]), acc[c]);
+          }
+        }
+        if (T.nsplit > 1) {
+          if (r < tm) {
+#pragma unroll
+            for (int c = 0; c < 16; c++)
+              if (c0 + c < tn) __stcg(part + T.split * part_elems + r + TM * (c0 + c), acc[c]);
+          }
+        } else if (r < tm) {
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            if (c0 + c < tn) {
+              const int64_t idx = (row0 + r) + ldo * (col0 + c0 + c);
+              O[idx] = accum ? O[idx] + acc[c] : acc[c];
+            }
+          }
         }
       }
-      if (T.nsplit > 1) {
-        if (r < tm) {
-#pragma unroll
-          for (int c = 0; c < 16; c++)
-            if (c0 + c < tn) __stcg(part + T.split * part_elems + r + TM * (c0 + c), acc[c]);
-        }
-      } else if (r < tm) {
-#pragma unroll
-        for (int c = 0; c < 16; c++) {
-          if (c0 + c < tn) {
-            const int64_t idx = (row0 + r) + ldo * (col0 + c0 + c);
-            O[idx] = accum ? O[idx] + acc[c] : acc[c];
+    }
+    tc_fence_before();  // the accumulator reads precede the next tile's MMAs
+    if (T.nsplit > 1) {
+      // the last split to arrive adds the partial tiles up in split order
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) is_last = atomicAdd(counters + T.counter, 1u) == static_cast<unsigned>(T.nsplit - 1);
+      __syncthreads();
+      if (is_last) {
+        __threadfence();
+        if (threadIdx.x == 0) counters[T.counter] = 0u;  // ready for the next launch
+        // every thread: row tid % 64, columns 16 (tid / 64) .. 16 (tid / 64) + 15
+        const int rr = threadIdx.x & 63, c1 = 16 * (threadIdx.x >> 6);
+        if (rr < tm) {
+          for (int c = c1; c < min(tn, c1 + 16); c++) {
+            double v = 0.0;
+            for (int s = 0; s < T.nsplit; s++) v += __ldcg(part + s * part_elems + rr + TM * c);
+            const int64_t idx = (row0 + rr) + ldo * (col0 + c);
+            O[idx] = accum ? O[idx] + v : v;
           }
         }
       }
     }
   }
-  if (T.nsplit > 1) {
-    // the last split to arrive adds the partial tiles up in split order
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) is_last = atomicAdd(counters + T.counter, 1u) == static_cast<unsigned>(T.nsplit - 1);
-    __syncthreads();
-    if (is_last) {
-      __threadfence();
-      if (threadIdx.x == 0) counters[T.counter] = 0u;  // ready for the next launch
-      // every thread: row tid % 64, columns 16 (tid / 64) .. 16 (tid / 64) + 15
-      const int rr = threadIdx.x & 63, c1 = 16 * (threadIdx.x >> 6);
-      if (ok && rr < tm) {
-        for (int c = c1; c < min(tn, c1 + 16); c++) {
-          double v = 0.0;
-          for (int s = 0; s < T.nsplit; s++) v += __ldcg(part + s * part_elems + rr + TM * c);
-          const int64_t idx = (row0 + rr) + ldo * (col0 + c);
-          O[idx] = accum ? O[idx] + v : v;
-        }
-      }
-    }
-  }
+  tc_finish(sched);
   tc_teardown(tmem_d);
+}
+
+// Persistent grid: three CTAs per SM (the kernels' occupancy), at most one per tile.
+int tc_grid(int ntiles) {
+  static const int sms = [] {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    return n;
+  }();
+  return std::min(ntiles, 3 * sms);
 }
 
 }  // namespace
 
-cudaError_t launch_inter_tc(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp, int* err,
-                            cudaStream_t stream) {
+cudaError_t launch_inter_tc(const InterJob* jobs, const GemmTile* tiles, int ntiles, const SlotPtrs& sp,
+                            unsigned int* sched, int* err, cudaStream_t stream) {
   if (ntiles <= 0) return cudaSuccess;
-  inter_tc_kernel<<<ntiles, kTcThreads, 0, stream>>>(jobs, tiles, sp, err);
+  inter_tc_kernel<<<tc_grid(ntiles), kTcThreads, 0, stream>>>(jobs, tiles, ntiles, sp, sched, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sum_tc(const SumGroup* groups, const SumItem* items, const GemmTile* tiles, int ntiles,
-                          double* partials, unsigned int* counters, const SlotPtrs& sp, int* err, cudaStream_t stream) {
+                          double* partials, unsigned int* counters, const SlotPtrs& sp, unsigned int* sched, int* err,
+                          cudaStream_t stream) {
   if (ntiles <= 0) return cudaSuccess;
-  sum_tc_kernel<<<ntiles, kTcThreads, 0, stream>>>(groups, items, tiles, partials, counters, sp, err);
+  sum_tc_kernel<<<tc_grid(ntiles), kTcThreads, 0, stream>>>(groups, items, tiles, ntiles, partials, counters, sp,
+                                                           sched, err);
   return cudaGetLastError();
 }
 

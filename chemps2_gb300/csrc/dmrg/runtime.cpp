@@ -79,6 +79,9 @@ Runtime::Runtime(int L, int device) : L_(L) {
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots_), sizeof(double*) * kMaxSlots));
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&dev_slots32_), sizeof(float*) * kMaxSlots));
   C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&partial_), sizeof(double) * (kDotBlocks * 64 + 4096)));
+  // tile-scheduler counters of the persistent tensor-core kernels (two per kernel)
+  C2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&sched_), sizeof(unsigned int) * 4));
+  C2G_CUDA(cudaMemset(sched_, 0, sizeof(unsigned int) * 4));
   C2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&pinned_), sizeof(double) * 8));
   // error word of the kernels with bounded waits, mapped so that the host reads it after
   // any synchronisation without a copy
@@ -95,6 +98,7 @@ Runtime::~Runtime() {
   cudaFree(dev_slots_);
   cudaFree(dev_slots32_);
   cudaFree(partial_);
+  cudaFree(sched_);
   if (copy_) cudaStreamSynchronize(copy_);
   for (int b = 0; b < 2; b++) {
     if (stg_buf_[b]) cudaFreeHost(stg_buf_[b]);
@@ -959,7 +963,7 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
 void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec_run) {
   const Precision prec = simt_precision(prec_run);
   if (prec_run == Precision::kTC)
-    C2G_CUDA(launch_inter_tc(ds.jobs, ds.jtiles, ds.njtiles, sp, err_dev_, stream_));
+    C2G_CUDA(launch_inter_tc(ds.jobs, ds.jtiles, ds.njtiles, sp, sched_, err_dev_, stream_));
   else
     C2G_CUDA(launch_inter_gemm(ds.jobs, ds.jtiles, ds.njtiles, sp, stream_, prec));
   C2G_CUDA(launch_inter_small(ds.jobs, ds.jsmall, ds.njsmall, sp, stream_, prec));
@@ -968,8 +972,8 @@ void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPt
   double* partials = transient_doubles(kTransientPartials, p.part_size);
   unsigned* counters = transient_counters(kTransientCounters, p.counter_count);
   if (prec_run == Precision::kTC)
-    C2G_CUDA(launch_sum_tc(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp, err_dev_,
-                           stream_));
+    C2G_CUDA(launch_sum_tc(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp,
+                           sched_ + 2, err_dev_, stream_));
   else
     C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp,
                              stream_, prec));

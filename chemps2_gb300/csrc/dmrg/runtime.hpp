@@ -162,6 +162,7 @@ class Runtime {
   int64_t ones_cap_ = 0;
   double* partial_ = nullptr;
   double* pinned_ = nullptr;
+  unsigned int* sched_ = nullptr;  // tile-scheduler counters of the tensor-core kernels
   int* err_host_ = nullptr;  // mapped pinned error word (host view)
   int* err_dev_ = nullptr;   // its device address
   // pinned host buffer in which upload assembles a program before the copy to the device
