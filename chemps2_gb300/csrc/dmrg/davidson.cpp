@@ -39,10 +39,10 @@ DeviceDavidson::DeviceDavidson(Runtime& rt, int64_t n, int max_vec, int keep, do
 }
 
 DeviceDavidson::~DeviceDavidson() {
-  rt_.release(V_);
-  rt_.release(HV_);
-  rt_.release(W_);
-  rt_.release(sm_);
+  rt_.release_quiet(V_);
+  rt_.release_quiet(HV_);
+  rt_.release_quiet(W_);
+  rt_.release_quiet(sm_);
 }
 
 void DeviceDavidson::multi_dot(const double* A, int ncol, const double* x, double* out) {

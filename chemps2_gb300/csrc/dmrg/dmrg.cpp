@@ -69,6 +69,7 @@ struct DMRG::ProgramCache {
   struct Entry {
     std::unique_ptr<DevProgram> dp;
     long long operand_bytes = 0;
+    long long bytes = 0;  // device bytes counted against the limit
     unsigned long long last_use = 0;
   };
   std::unordered_map<std::string, Entry> map;
@@ -116,7 +117,9 @@ DevProgram& DMRG::program(const std::string& key, const std::function<c2g::Compi
   stats_.t_upload += now() - tu;
   e.operand_bytes = c.operand_bytes;
   e.last_use = pc.clock;
-  const long long size = e.dp->bytes + 8 * e.dp->combo_size;
+  // records and the FP64 combination buffer, plus its FP32 copy when matvecs run in FP32
+  const long long size = e.dp->bytes + (precision_ != 0 ? 12 : 8) * e.dp->combo_size;
+  e.bytes = size;
   // Least recently used programs leave first; the programs of the current step (the last
   // few requests) stay, since callers hold references to them.
   while (pc.bytes + size > pc.limit && !pc.map.empty()) {
@@ -125,7 +128,7 @@ DevProgram& DMRG::program(const std::string& key, const std::function<c2g::Compi
       if (jt->second.last_use + 8 < pc.clock && (victim == pc.map.end() || jt->second.last_use < victim->second.last_use))
         victim = jt;
     if (victim == pc.map.end()) break;
-    pc.bytes -= victim->second.dp->bytes + 8 * victim->second.dp->combo_size;
+    pc.bytes -= victim->second.bytes;
     pc.map.erase(victim);
   }
   pc.bytes += size;
@@ -201,15 +204,16 @@ DMRG::~DMRG() {
     if (heff_cache_) {
       heff_cache_->program.reset();
       heff_cache_->diag.reset();
-      rt->release(heff_cache_->xbuf);
-      rt->release(heff_cache_->ybuf);
+      rt->release_quiet(heff_cache_->xbuf);
+      rt->release_quiet(heff_cache_->ybuf);
     }
-    for (double* p : mps_dev) rt->release(p);
-    release_overlaps();
-    for (auto& st : exc_)
-      for (double* p : st->mps) rt->release(p);
-    for (double* p : ops_dev) rt->release(p);
-    for (float* p : ops_dev32) rt->release(p);
+    for (double* p : mps_dev) rt->release_quiet(p);
+    for (auto& st : exc_) {
+      for (double* p : st->odev) rt->release_quiet(p);
+      for (double* p : st->mps) rt->release_quiet(p);
+    }
+    for (double* p : ops_dev) rt->release_quiet(p);
+    for (float* p : ops_dev32) rt->release_quiet(p);
     try {
       rt->sync();
     } catch (...) {
@@ -448,6 +452,7 @@ void DMRG::update_overlaps(const int index, const bool moving_right) {
     auto lay = std::make_unique<c2g::OverlapLayout>();
     lay->build(*denBK, *st.bk, index + 1);
     if (st.odev[index]) rt->release(st.odev[index]);
+    st.odev[index] = nullptr;
     st.odev[index] = rt->alloc(std::max<int64_t>(lay->size(), 1));
     rt->zero(st.odev[index], lay->size());
     const int slot = exc_slot(static_cast<int>(k), true, index);
@@ -508,7 +513,13 @@ void DMRG::fill_2dm_site(int site) {
   const std::vector<c2g::TwoDMInstance> inst = c2g::twodm_instances(ctx);
   const int nvalues = inst.back().value0 + c2g::twodm_num_values(inst.back().kind);
   std::vector<double> values(nvalues, 0.0);
-  constexpr int64_t kWorkBudget = int64_t(1) << 25;  // doubles (256 MB) of products per program
+  // doubles (256 MB) of products per program; C2G_TWODM_BUDGET overrides it (tests force
+  // several programs per site with a small budget)
+  static const int64_t kWorkBudget = [] {
+    const char* e = std::getenv("C2G_TWODM_BUDGET");
+    const long long v = e ? std::atoll(e) : 0;
+    return v > 0 ? static_cast<int64_t>(v) : int64_t(1) << 25;
+  }();
   size_t first = 0;
   while (first < inst.size()) {
     size_t last = first;
@@ -607,6 +618,7 @@ void DMRG::calc2DMandCorrelations() {
 
 void DMRG::upload_mps(int site, const std::vector<double>& data) {
   if (mps_dev[site]) rt->release(mps_dev[site]);
+  mps_dev[site] = nullptr;
   mps_dev[site] = rt->alloc(static_cast<int64_t>(data.size()));
   C2G_CUDA(cudaMemcpyAsync(mps_dev[site], data.data(), sizeof(double) * data.size(), cudaMemcpyHostToDevice,
                            rt->stream()));
@@ -614,19 +626,30 @@ void DMRG::upload_mps(int site, const std::vector<double>& data) {
   rt->set_slot(c2g::kSlotMpsBase + site, mps_dev[site]);
 }
 
-void DMRG::refresh_f32(const int b) {
-  if (!ops[b] || !ops_dev[b]) return;
+void DMRG::drop_f32(const int b) {
   if (ops_dev32[b]) rt->release(ops_dev32[b]);
-  ops_dev32[b] = rt->alloc_f32(ops[b]->size);
-  C2G_CUDA(c2g::launch_to_f32(ops_dev32[b], ops_dev[b], ops[b]->size, rt->stream()));
-  c2g::count_launches(1);
-  rt->set_slot32(c2g::slot_ops(L, b), ops_dev32[b]);
+  ops_dev32[b] = nullptr;
+  rt->set_slot32(c2g::slot_ops(L, b), nullptr);
 }
 
-void DMRG::enable_f32_ops() {
-  if (f32_ops_) return;
-  f32_ops_ = true;
-  for (int b = 0; b < L - 1; b++) refresh_f32(b);
+// FP32 copies exist only for the operators that the Heff of sites (index, index + 1)
+// reads (boundaries index - 1 and index + 1); a conversion streams one boundary's
+// operators once (FP64 read, FP32 write), small beside the matvecs of a step, and the
+// copies of all other boundaries are released (at L = 40, D = 4000 they would hold half
+// as many bytes again as the FP64 operators).
+void DMRG::ensure_f32(const int index) {
+  for (int b = 0; b < L - 1; b++) {
+    const bool needed = (b == index - 1 || b == index + 1) && ops[b] && ops_dev[b];
+    if (!needed) {
+      if (ops_dev32[b]) drop_f32(b);
+      continue;
+    }
+    if (ops_dev32[b]) continue;
+    ops_dev32[b] = rt->alloc_f32(ops[b]->size);
+    C2G_CUDA(c2g::launch_to_f32(ops_dev32[b], ops_dev[b], ops[b]->size, rt->stream()));
+    c2g::count_launches(1);
+    rt->set_slot32(c2g::slot_ops(L, b), ops_dev32[b]);
+  }
 }
 
 namespace {
@@ -645,7 +668,6 @@ void DMRG::set_precision(int mode, double mixed_tol) {
   if (mode < 0 || mode > 2) throw std::invalid_argument("precision mode must be 0, 1 or 2");
   precision_ = mode;
   mixed_tol_ = mixed_tol;
-  if (mode != 0) enable_f32_ops();
 }
 
 int DMRG::get_num_mps_var() const {
@@ -659,9 +681,7 @@ void DMRG::delete_all_ops() {
   for (int b = 0; b < L - 1; b++) {
     if (ops_dev[b]) rt->release(ops_dev[b]);
     ops_dev[b] = nullptr;
-    if (ops_dev32[b]) rt->release(ops_dev32[b]);
-    ops_dev32[b] = nullptr;
-    rt->set_slot32(c2g::slot_ops(L, b), nullptr);
+    drop_f32(b);
     ops[b].reset();
     rt->set_slot(c2g::slot_ops(L, b), nullptr);
     isAllocated[b] = 0;
@@ -691,6 +711,7 @@ void DMRG::PreSolve() {
 void DMRG::update_moving_right(const int index) {
   const double t0 = now();
   if (ops_dev[index]) rt->release(ops_dev[index]);
+  ops_dev[index] = nullptr;
   ops[index] = std::make_unique<BoundaryOps>();
   c2g::allocate_ops(*ops[index], *denBK, L, index, true, c2g::slot_ops(L, index));
   ops_dev[index] = rt->alloc(ops[index]->size);
@@ -711,7 +732,7 @@ void DMRG::update_moving_right(const int index) {
                            [&] { return c2g::compile_update_program(ctx, false); });
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
-  if (f32_ops_) refresh_f32(index);
+  drop_f32(index);
   // no synchronisation: the host goes on compiling the next site's programs while the
   // update runs; everything that reads its results is ordered after it on the stream
   if (!exc_.empty()) update_overlaps(index, true);
@@ -722,6 +743,7 @@ void DMRG::update_moving_right(const int index) {
 void DMRG::update_moving_left(const int index) {
   const double t0 = now();
   if (ops_dev[index]) rt->release(ops_dev[index]);
+  ops_dev[index] = nullptr;
   ops[index] = std::make_unique<BoundaryOps>();
   c2g::allocate_ops(*ops[index], *denBK, L, index, false, c2g::slot_ops(L, index));
   ops_dev[index] = rt->alloc(ops[index]->size);
@@ -743,7 +765,7 @@ void DMRG::update_moving_left(const int index) {
                            [&] { return c2g::compile_update_program(ctx, false); });
   rt->zero(ops_dev[index], ops[index]->size);
   rt->run(dp, nullptr, nullptr);
-  if (f32_ops_) refresh_f32(index);
+  drop_f32(index);
   // no synchronisation (as in update_moving_right)
   if (!exc_.empty()) update_overlaps(index, false);
   stats_.t_update += now() - t0;
@@ -903,6 +925,7 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     C2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     mv_ms += ms;
   };
+  if (precision_ != 0) ensure_f32(index);
   const c2g::DavidsonStats ds =
       dav.solve(svec, diag, matvec, precision_ != 0, mixed_tol_, matvec_precision(precision_ == 0 ? 1 : precision_));
   stats_.n_matvec_fp32 += ds.n_matvec_fp32;
@@ -1185,7 +1208,7 @@ double DMRG::bench_heff(const int index, const int warmup, const int steps, doub
   double* flush = nullptr;
   const int64_t nflush = flush_bytes > 0 ? (flush_bytes + 7) / 8 : 0;
   if (nflush > 0) flush = rt->alloc(nflush);
-  if (prec != c2g::Precision::kFP64) enable_f32_ops();
+  if (prec != c2g::Precision::kFP64) ensure_f32(index);
   for (int i = 0; i < warmup; i++) rt->run(*c.program, x, y, prec, veclen);
   rt->sync();
   const long long l0 = c2g::kernel_launches();
@@ -1262,7 +1285,7 @@ void DMRG::heff_apply_host(const int index, const bool join_into_x, double* x, d
     C2G_CUDA(cudaMemcpyAsync(c.xbuf, x, sizeof(double) * veclen, cudaMemcpyHostToDevice, s));
   }
   const c2g::Precision prec = matvec_precision(precision);
-  if (prec != c2g::Precision::kFP64) enable_f32_ops();
+  if (prec != c2g::Precision::kFP64) ensure_f32(index);
   rt->run(*c.program, c.xbuf, c.ybuf, prec, veclen);
   C2G_CUDA(cudaMemcpyAsync(y, c.ybuf, sizeof(double) * veclen, cudaMemcpyDeviceToHost, s));
   if (diag) {
@@ -1286,7 +1309,7 @@ void DMRG::heff_apply_device(const int index, const double* x_dev, double* y_dev
   cudaStream_t u = static_cast<cudaStream_t>(stream);
   if (u) rt->wait_for(u);  // x is ready once the caller's stream gets here
   const c2g::Precision prec = matvec_precision(precision);
-  if (prec != c2g::Precision::kFP64) enable_f32_ops();
+  if (prec != c2g::Precision::kFP64) ensure_f32(index);
   rt->run(*c.program, const_cast<double*>(x_dev), y_dev, prec, veclen);
   if (u) rt->signal_to(u);  // the caller's stream waits for y
   else rt->sync();

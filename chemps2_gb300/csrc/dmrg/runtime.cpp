@@ -52,9 +52,9 @@ void cuda_check(cudaError_t e, const char* expr, const char* file, int line) {
 
 DevProgram::~DevProgram() {
   if (rt) {
-    if (blob) rt->release(blob);
-    if (combo) rt->release(combo);
-    if (combo32) rt->release(combo32);
+    rt->release_quiet(blob);
+    rt->release_quiet(combo);
+    rt->release_quiet(combo32);
   }
 }
 
@@ -132,6 +132,10 @@ void Runtime::release(void* p) {
   if (p) C2G_CUDA(cudaFreeAsync(p, stream_));
 }
 
+void Runtime::release_quiet(void* p) noexcept {
+  if (p && cudaFreeAsync(p, stream_) != cudaSuccess) cudaGetLastError();
+}
+
 void Runtime::zero(double* p, int64_t n) {
   if (n > 0) C2G_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, stream_));
 }
@@ -172,8 +176,11 @@ void Runtime::flush_slots() {
 const double* Runtime::ones(int64_t n) {
   if (n > ones_cap_) {
     if (ones_) release(ones_);
-    ones_cap_ = std::max<int64_t>(n, 1024);
-    ones_ = alloc(ones_cap_);
+    ones_ = nullptr;
+    ones_cap_ = 0;
+    const int64_t cap = std::max<int64_t>(n, 1024);
+    ones_ = alloc(cap);
+    ones_cap_ = cap;
     C2G_CUDA(launch_fill(ones_, 1.0, ones_cap_, stream_));
     count_launches(1);
   }
@@ -945,8 +952,10 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
       if (xlen <= 0) throw std::invalid_argument("Runtime::run: an FP32 run needs the length of X");
       if (xlen > x32_cap_) {
         if (x32_) release(x32_);
+        x32_ = nullptr;
+        x32_cap_ = 0;
+        x32_ = alloc_f32(xlen);
         x32_cap_ = xlen;
-        x32_ = alloc_f32(x32_cap_);
       }
       C2G_CUDA(launch_to_f32(x32_, x, xlen, stream_));
       count_launches(1);

@@ -99,6 +99,8 @@ class Runtime {
   // Device memory, stream ordered on this runtime's stream.
   double* alloc(int64_t n_doubles);
   void release(void* p);
+  // release for destructors and error paths: reports nothing
+  void release_quiet(void* p) noexcept;
   void zero(double* p, int64_t n);
 
   // Slot table (slots other than X, Y, Combo and Ones).

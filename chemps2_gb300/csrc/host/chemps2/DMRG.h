@@ -207,10 +207,9 @@ class DMRG {
   std::vector<double*> mps_dev;
   std::vector<std::unique_ptr<c2g::BoundaryOps>> ops;
   std::vector<double*> ops_dev;
-  std::vector<float*> ops_dev32;  // FP32 copies of the operators, for FP32 matvecs
-  bool f32_ops_ = false;          // keep ops_dev32 current
-  void refresh_f32(const int boundary);
-  void enable_f32_ops();
+  std::vector<float*> ops_dev32;  // FP32 copies of the operators the current FP32 matvec reads
+  void drop_f32(const int boundary);
+  void ensure_f32(const int index);
   std::vector<int> isAllocated;  // 0 none, 1 moving right, 2 moving left
   double TotalMinEnergy = 1e8;
   double LastMinEnergy = 1e8;

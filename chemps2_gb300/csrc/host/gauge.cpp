@@ -70,7 +70,18 @@ void left_normalize(const CheMPS2::SyBookkeeper& bk, int site, const MpsLayout& 
             blocks.push_back(k);
             m += lay.rows[k];
           }
-        if (m == 0) continue;
+        if (m == 0) {
+          // A right sector that no block of this site feeds holds states without a left
+          // history (a virtual dimension kept fixed through a sweep can leave such
+          // states): they are zero vectors, and R is zero there, so the next site's
+          // blocks of that left sector vanish. (The reference leaves this R block
+          // uninitialised, CheMPS2/TensorT.cpp:209 with CheMPS2/TensorOperator.cpp:100.)
+          if (next)
+            for (int k = 0; k < next_lay->nkappa; k++)
+              if (next_lay->NL[k] == NR && next_lay->TwoSL[k] == TwoSR && next_lay->IL[k] == IR)
+                std::fill_n(next->data() + next_lay->k2i[k], static_cast<size_t>(n) * next_lay->cols[k], 0.0);
+          continue;
+        }
         std::vector<double> a(static_cast<size_t>(m) * n), q, r;
         int r0 = 0;
         for (int k : blocks) {
@@ -116,7 +127,16 @@ void right_normalize(const CheMPS2::SyBookkeeper& bk, int site, const MpsLayout&
             blocks.push_back(k);
             ntot += lay.cols[k];
           }
-        if (ntot == 0) continue;
+        if (ntot == 0) {
+          // A left sector without any block to its right holds states without a right
+          // completion: L is zero there, so the previous site's blocks of that right
+          // sector vanish (left uninitialised by the reference, CheMPS2/TensorT.cpp:312).
+          if (prev)
+            for (int k = 0; k < prev_lay->nkappa; k++)
+              if (prev_lay->NR[k] == NL && prev_lay->TwoSR[k] == TwoSL && prev_lay->IR[k] == IL)
+                std::fill_n(prev->data() + prev_lay->k2i[k], static_cast<size_t>(prev_lay->rows[k]) * dimL, 0.0);
+          continue;
+        }
         // M^T (ntot x dimL), blocks scaled by sqrt((2 S_R + 1) / (2 S_L + 1))
         std::vector<double> mt(static_cast<size_t>(ntot) * dimL), q, r;
         int c0 = 0;

@@ -372,3 +372,22 @@ def joined_state(ts: TwoSite, x):
     """The many-electron state of a two-site vector in the stored normalisation."""
     s = np.where(ts.physical, 1.0 / np.sqrt(np.where(ts.norm2 > 0, ts.norm2, 1.0)), 0.0)
     return ts.embed(s * x)
+
+
+def two_rdm_a(H: FockHamiltonian, psi):
+    """The spin-summed 2-RDM A_ijkl = sum_{sigma,tau} <a+_i,s a+_j,t a_l,t a_k,s> of the
+    state psi (normalised here), from the E operators of H: <E_ik E_jl> - delta_jk <E_il>."""
+    L = H.L
+    psi = psi / np.sqrt(psi @ psi)
+    Ev = {(p, q): H.E[(p, q)] @ psi for p in range(L) for q in range(L)}
+    A = np.zeros((L, L, L, L))
+    one = np.array([[psi @ Ev[(i, l)] for l in range(L)] for i in range(L)])
+    for i in range(L):
+        for k in range(L):
+            left = Ev[(k, i)]  # (E_ki psi) = (E_ik^T psi)
+            for j in range(L):
+                for l in range(L):
+                    A[i, j, k, l] = left @ Ev[(j, l)]
+    for j in range(L):
+        A[:, j, j, :] -= one
+    return A

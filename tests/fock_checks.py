@@ -37,6 +37,23 @@ def chain_of(d, model, total):
     return fock.FockChain(L, model.irreps, secs, [d.get_mps(k) for k in range(L)], total)
 
 
+def dead_sectors(d, model):
+    """[(site, side, (N, 2S, I))] of sectors that hold states without a left history
+    ("right": a right sector of the site no block feeds) or without a right completion
+    ("left": a left sector with no block to its right). A virtual dimension kept fixed
+    through a sweep (the first sweep of a solve) can leave them."""
+    L = model.L
+    secs = [fock.sector_dims(d.sectors(b)) for b in range(L + 1)]
+    out = []
+    for s in range(L):
+        T = fock.mps_blocks(secs[s], secs[s + 1], model.irreps[s], np.asarray(d.get_mps(s)))
+        lefts = {k[:3] for k in T}
+        rights = {k[3:] for k in T}
+        out += [(s, "left", k) for k in secs[s] if k not in lefts]
+        out += [(s, "right", k) for k in secs[s + 1] if k not in rights]
+    return out
+
+
 def rel(a, b):
     return float(np.max(np.abs(a - b))) / max(1.0, float(np.max(np.abs(b))))
 
