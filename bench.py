@@ -413,6 +413,62 @@ def extra_sweeps(args, label, model, D, seed=SEED):
     print(json.dumps({"extra": label, **out}), flush=True)
 
 
+def extra_config5(args):
+    """The large configuration: synthetic ab initio L = N = 40, S = 0, C2v (irreps round
+    robin), mixed tensor-core form with every operator resident in HBM.
+
+    First the same-D comparison at the reduced D = --reduced-d: an FP64 and a mixed run of
+    --sweeps sweeps each from the same seeded start, each followed by the 2-RDM
+    (calc2DMandCorrelations): energies, the 2-RDM identities (trace = N(N-1), energy of the
+    2-RDM = energy of the MPS) and the Frobenius norm of the difference of the two 2-RDMs.
+    Then D = 4000 in the mixed form for --large-sweeps sweeps: seconds per sweep with the
+    step timers, the energy, device memory in use (the 2-RDM at D = 4000 only with
+    --large-2rdm)."""
+    import chemps2_gb300 as c2g
+    from chemps2_gb300.models import synthetic_ab_initio
+
+    L = 40
+    model = synthetic_ab_initio(L, 5, SEED)
+    out = {"config": f"synthetic ab initio L=40 N=40 S=0 C2v; FP64 and mixed at D={args.reduced_d}, "
+                     f"{args.sweeps} sweep(s) each, then the 2-RDM; mixed at D=4000, {args.large_sweeps} sweep(s)"}
+    rdm = {}
+    for mode in (("fp64", "mixed_tc") if args.reduced_d > 0 else ()):
+        objs, rec = run_sweeps(model, mode, args.sweeps, D=args.reduced_d)
+        d = objs[3]
+        t0 = time.perf_counter()
+        d.calc2DMandCorrelations()
+        t2 = time.perf_counter() - t0
+        tdm = d.get2DM()
+        rdm[mode] = (np.array(tdm.A), np.array(tdm.B))
+        out[f"reduced_d_{mode}"] = {"s_per_sweep": rec["s_per_sweep"], "energy": rec["energy"], "stats": rec["stats"],
+                                    "two_rdm_s": t2, "two_rdm_trace": tdm.trace(),
+                                    "two_rdm_trace_expected": L * (L - 1), "two_rdm_energy": tdm.energy()}
+        d.close()
+    if args.reduced_d > 0:
+        out["reduced_d_two_rdm_frobenius_diff"] = {
+            "A": float(np.linalg.norm(rdm["mixed_tc"][0] - rdm["fp64"][0])),
+            "B": float(np.linalg.norm(rdm["mixed_tc"][1] - rdm["fp64"][1])),
+            "A_norm": float(np.linalg.norm(rdm["fp64"][0])), "B_norm": float(np.linalg.norm(rdm["fp64"][1]))}
+        out["reduced_d_energy_diff"] = abs(out["reduced_d_mixed_tc"]["energy"] - out["reduced_d_fp64"]["energy"])
+        print(json.dumps({"extra": "config5_reduced", **out}), flush=True)
+    if args.large_sweeps <= 0:
+        return
+    free0, _ = c2g.device_memory_info()
+    objs, rec = run_sweeps(model, "mixed_tc", args.large_sweeps, D=4000)
+    d = objs[3]
+    free1, used1 = c2g.device_memory_info()
+    big = {"D": 4000, "s_per_sweep": rec["s_per_sweep"], "energy": rec["energy"], "stats": rec["stats"],
+           "device_bytes_held_after_sweeps": free0 - free1, "pool_bytes_in_use": used1}
+    if args.large_2rdm:
+        t0 = time.perf_counter()
+        d.calc2DMandCorrelations()
+        tdm = d.get2DM()
+        big.update({"two_rdm_s": time.perf_counter() - t0, "two_rdm_trace": tdm.trace(),
+                    "two_rdm_trace_expected": L * (L - 1), "two_rdm_energy": tdm.energy()})
+    d.close()
+    print(json.dumps({"extra": "config5_large", **big}), flush=True)
+
+
 def extra_hubbard(args):
     """Large sector blocks: the Hubbard chain L = N = 20, U = 4, C1, D = 512 swept --sweeps
     times, right-hand operators renormalized down to the middle, then --steps FP64, FP32 and
@@ -544,13 +600,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--extra", choices=["config1", "config2", "batch", "hubbard"], default=None,
+    ap.add_argument("--extra", choices=["config1", "config2", "config5", "batch", "hubbard"], default=None,
                     help="run one of the further configurations instead (prints its own JSON line)")
     ap.add_argument("--sweeps", type=int, default=2, help="sweeps of each run")
     ap.add_argument("--batch-count", type=int, default=64, help="problems for --extra batch")
     ap.add_argument("--workers", type=int, default=16, help="concurrent problems for --extra batch")
     ap.add_argument("--profile-precision", choices=["fp64", "fp32", "tc"], default="fp64",
                     help="arithmetic of the profiled matvecs of --extra hubbard --profile")
+    ap.add_argument("--reduced-d", type=int, default=1000,
+                    help="D of the FP64 2-RDM check of --extra config5 (0: skip it)")
+    ap.add_argument("--large-sweeps", type=int, default=1, help="sweeps at D=4000 of --extra config5")
+    ap.add_argument("--large-2rdm", action="store_true", help="also the 2-RDM at D=4000 in --extra config5")
     ap.add_argument("--dump-dims", default=None,
                     help="write the sector dimensions of the swept FP64 state to this JSON file")
     ap.add_argument("--profile", type=int, default=0,
@@ -564,6 +624,8 @@ def main():
         extra_sweeps(args, "hubbard L=16 N=16 U=4 C1 D=200", hubbard(16, 4.0), 200, seed=1)
     elif args.extra == "config2":
         extra_sweeps(args, "synthetic ab initio L=24 N=24 S=0 D2h D=1000", make_model(24), 1000)
+    elif args.extra == "config5":
+        extra_config5(args)
     elif args.extra == "batch":
         extra_batch(args)
     elif args.extra == "hubbard":

@@ -348,9 +348,18 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     std::vector<SumGroup> groups;
     std::vector<SumItem> items;
     std::vector<GemmTile> stiles;
+    std::vector<int32_t> chunk_first;  // first group (index into groups) of each chunk
+    std::vector<int64_t> jtile_first, small_first;  // per group, and the totals at the end
   };
   std::vector<TwoPass> twopass(ns);
+  // Bytes of pass-1 intermediates one chunk may hold (C2G_INTER_BUDGET_KB overrides).
+  int64_t inter_budget = int64_t(8) << 30;
+  if (const char* e = std::getenv("C2G_INTER_BUDGET_KB")) {
+    const long long v = std::atoll(e);
+    if (v > 0) inter_budget = static_cast<int64_t>(v) << 10;
+  }
   int64_t inter_doubles = 0, gemm_part_doubles = 0, gemm_counters = 0;
+  std::vector<std::vector<DevStage::PassChunk>> chunk_ranges(ns);
   // Blob layout: the batch table, then per stage its groups and terms, then the tile lists
   // of every stage. It is assembled in the runtime's pinned staging buffer: the terms of
   // each group are copied there in shape order (flags, k1, k2), so that neighbouring items
@@ -692,10 +701,34 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
       tp.small.resize(static_cast<size_t>(tot.small));
       tp.jtiles.resize(static_cast<size_t>(tot.jtile));
       tp.groups.resize(nl);
-      inter_off = tot.inter;
+      tp.jtile_first.resize(nl + 1);
+      tp.small_first.resize(nl + 1);
+      for (size_t q = 0; q < nl; q++) {
+        tp.jtile_first[q] = at[q].jtile;
+        tp.small_first[q] = at[q].small;
+      }
+      tp.jtile_first[nl] = tot.jtile;
+      tp.small_first[nl] = tot.small;
+      // chunks of whole groups whose intermediates fit the budget; a chunk's
+      // intermediates start at offset 0 of the buffer
+      std::vector<int64_t> inter_base(nl, 0);
+      tp.chunk_first.assign(1, 0);
+      inter_off = 0;
+      {
+        int64_t base = 0;
+        for (size_t q = 0; q < nl; q++) {
+          if (q > 0 && at[q].inter + cnt[q].inter - base > inter_budget / 8) {
+            tp.chunk_first.push_back(static_cast<int32_t>(q));
+            base = at[q].inter;
+          }
+          inter_base[q] = base;
+          inter_off = std::max(inter_off, at[q].inter + cnt[q].inter - base);
+        }
+      }
       parallel_groups(nl, 4 * lterms, [&](size_t q0, size_t q1) {
         for (size_t q = q0; q < q1; q++) {
           Cursor c = at[q];
+          c.inter -= inter_base[q];
           plan_group(lg[q], c, true);
           const Group& G = st.groups[lg[q]];
           SumGroup sg{};
@@ -814,7 +847,9 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
       const int64_t gpiece = std::max<int64_t>(total / kGemmCtaTarget, 1);
       int64_t gpart = 0, gcount = 0;
       std::vector<int32_t> bnd;
+      std::vector<int64_t> stile_of(tp.groups.size() + 1, 0);
       for (size_t q = 0; q < tp.groups.size(); q++) {
+        stile_of[q] = static_cast<int64_t>(tp.stiles.size());
         const SumGroup& sg = tp.groups[q];
         const int gm = gm16(sg), gn = gn16(sg);
         int64_t work = 0;
@@ -851,9 +886,21 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
             }
           }
       }
+      stile_of[tp.groups.size()] = static_cast<int64_t>(tp.stiles.size());
       gemm_part_doubles = std::max(gemm_part_doubles, gpart);
       gemm_counters = std::max(gemm_counters, gcount);
       inter_doubles = std::max(inter_doubles, inter_off);
+      // chunk ranges: the job tiles, small jobs and pass-2 tiles of a chunk's groups are
+      // contiguous (all filled in group order)
+      const size_t nch = tp.chunk_first.size();
+      chunk_ranges[s].resize(nch);
+      for (size_t c = 0; c < nch; c++) {
+        const size_t q0 = tp.chunk_first[c], q1 = (c + 1 < nch) ? tp.chunk_first[c + 1] : tp.groups.size();
+        chunk_ranges[s][c] = DevStage::PassChunk{
+            static_cast<int>(tp.jtile_first[q0]), static_cast<int>(tp.jtile_first[q1] - tp.jtile_first[q0]),
+            static_cast<int>(tp.small_first[q0]), static_cast<int>(tp.small_first[q1] - tp.small_first[q0]),
+            static_cast<int>(stile_of[q0]), static_cast<int>(stile_of[q1] - stile_of[q0])};
+      }
       if (tp.items.size() > size_t(INT32_MAX) || tp.jobs.size() > size_t(INT32_MAX))
         throw std::length_error("upload: too many large-group items");
     }
@@ -908,6 +955,7 @@ std::unique_ptr<DevProgram> Runtime::upload_parts(const Program* parts, size_t n
     ds.sitems = static_cast<const SumItem*>(put(tp.items.data(), sizeof(SumItem) * tp.items.size()));
     ds.stiles = static_cast<const GemmTile*>(put(tp.stiles.data(), sizeof(GemmTile) * tp.stiles.size()));
     ds.nstiles = static_cast<int>(tp.stiles.size());
+    ds.chunks = chunk_ranges[s];
     dp->nterms += ds.nterms;
     if (static_cast<int>(s) < dp->first_repeat) dp->flops_once += ds.flops;
     else dp->flops_repeat += ds.flops;
@@ -971,27 +1019,33 @@ void Runtime::run(DevProgram& p, double* x, double* y, Precision prec, int64_t x
 // disjoint output blocks).
 void Runtime::launch_stage(const DevProgram& p, const DevStage& ds, const SlotPtrs& sp, Precision prec_run) {
   const Precision prec = simt_precision(prec_run);
-  if (prec_run == Precision::kTC)
-    C2G_CUDA(launch_inter_tc(ds.jobs, ds.jtiles, ds.njtiles, sp, sched_, err_dev_, stream_));
-  else
-    C2G_CUDA(launch_inter_gemm(ds.jobs, ds.jtiles, ds.njtiles, sp, stream_, prec));
-  C2G_CUDA(launch_inter_small(ds.jobs, ds.jsmall, ds.njsmall, sp, stream_, prec));
   double* gemm_partials = transient_doubles(kTransientGemmPartials, p.gemm_part_size);
   unsigned* gemm_counters = transient_counters(kTransientGemmCounters, p.gemm_counter_count);
   double* partials = transient_doubles(kTransientPartials, p.part_size);
   unsigned* counters = transient_counters(kTransientCounters, p.counter_count);
-  if (prec_run == Precision::kTC)
-    C2G_CUDA(launch_sum_tc(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp,
-                           sched_ + 2, err_dev_, stream_));
-  else
-    C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, ds.stiles, ds.nstiles, gemm_partials, gemm_counters, sp,
-                             stream_, prec));
+  int npass = 0;
+  for (const DevStage::PassChunk& ch : ds.chunks) {
+    const GemmTile* jt = ds.jtiles + ch.jtile0;
+    if (prec_run == Precision::kTC)
+      C2G_CUDA(launch_inter_tc(ds.jobs, jt, ch.njtiles, sp, sched_, err_dev_, stream_));
+    else
+      C2G_CUDA(launch_inter_gemm(ds.jobs, jt, ch.njtiles, sp, stream_, prec));
+    C2G_CUDA(launch_inter_small(ds.jobs, ds.jsmall + ch.small0, ch.nsmall, sp, stream_, prec));
+    const GemmTile* st = ds.stiles + ch.stile0;
+    if (prec_run == Precision::kTC)
+      C2G_CUDA(launch_sum_tc(ds.sgroups, ds.sitems, st, ch.nstiles, gemm_partials, gemm_counters, sp, sched_ + 2,
+                             err_dev_, stream_));
+    else
+      C2G_CUDA(launch_sum_gemm(ds.sgroups, ds.sitems, st, ch.nstiles, gemm_partials, gemm_counters, sp, stream_,
+                               prec));
+    npass += (ch.njtiles > 0) + (ch.nsmall > 0) + (ch.nstiles > 0);
+  }
   C2G_CUDA(launch_sandwich_tiles(ds.groups, ds.terms, p.entries, ds.tiles_large, ds.ntiles_large, sp, stream_, prec));
   int nw = 0;
   const WarpLaunch wl{ds.groups, ds.terms, p.entries, ds.tiles_warp, partials, counters};
   C2G_CUDA(launch_sandwich_warp(wl, ds.nwarp, sp, stream_, prec, &nw));
   C2G_CUDA(launch_sandwich(ds.groups, ds.terms, p.entries, ds.tiles, ds.ntiles, sp, stream_, prec));
-  count_launches((ds.njtiles > 0) + (ds.njsmall > 0) + (ds.nstiles > 0) + (ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
+  count_launches(npass + (ds.ntiles > 0) + (ds.ntiles_large > 0) + nw);
 }
 
 void Runtime::sync() {

@@ -46,6 +46,13 @@ struct DevStage {
   const GemmTile* stiles = nullptr;
   const int32_t* jsmall = nullptr;  // pass-1 jobs run one per warp
   int njtiles = 0, nstiles = 0, njsmall = 0;
+  // The large groups in chunks of whole groups, each run as pass 1 then pass 2, so that
+  // the intermediates of one chunk at a time share the intermediate buffer: ranges of
+  // jtiles, jsmall and stiles.
+  struct PassChunk {
+    int jtile0, njtiles, small0, nsmall, stile0, nstiles;
+  };
+  std::vector<PassChunk> chunks;
   int64_t flops = 0, items = 0;
   std::string name;
 };

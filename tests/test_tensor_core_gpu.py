@@ -80,3 +80,38 @@ def test_mixed_tensor_core_solve_matches_fp64():
             assert st["n_matvec_fp32"] > 0
         d.close()
     assert abs(energies["mixed_tc"] - energies["fp64"]) < 1e-8
+
+
+def test_two_pass_chunks_give_identical_products(monkeypatch):
+    """The large groups run in chunks of whole groups whose pass-1 intermediates fit a
+    byte budget (default 8 GB; C2G_INTER_BUDGET_KB, read at each program upload). With a
+    64 KB budget the groups of this state run chunk by chunk (more launches per matvec),
+    and every product is bit-identical to the one-chunk run in all three arithmetics: a
+    group's items keep their order and their intermediates."""
+    L, D = 12, 256
+    ys, launches = {}, {}
+    for budget in (None, "64"):
+        if budget:
+            monkeypatch.setenv("C2G_INTER_BUDGET_KB", budget)
+        else:
+            monkeypatch.delenv("C2G_INTER_BUDGET_KB", raising=False)
+        ham, prob, scheme = hubbard_objects(L, D)
+        c2g.srand(9)
+        d = c2g.DMRG(prob, scheme)
+        try:
+            mid = L // 2 - 1
+            for index in range(L - 2, mid, -1):
+                d.update(index, False)
+            x = np.random.default_rng(4).standard_normal(d.sobject_size(mid))
+            out = {}
+            for prec in ("fp64", "fp32", "tc"):
+                out[prec] = d.heff_apply_precision(mid, x, prec)
+            n0 = c2g.kernel_launches()
+            d.heff_apply_precision(mid, x, "tc")
+            launches[budget] = c2g.kernel_launches() - n0
+            ys[budget] = out
+        finally:
+            d.close()
+    assert launches["64"] > launches[None], launches
+    for prec in ("fp64", "fp32", "tc"):
+        assert np.array_equal(ys["64"][prec], ys[None][prec]), prec

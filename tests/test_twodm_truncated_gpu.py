@@ -71,3 +71,47 @@ def test_2rdm_of_truncated_state_against_fock_space(name, make, two_s, n, irrep,
         assert np.max(np.abs(dm.A - A_fock)) < 1e-8, np.max(np.abs(dm.A - A_fock))
     finally:
         d.close()
+
+
+_CHUNK_SCRIPT = """
+import sys
+import numpy as np
+import chemps2_gb300 as c2g
+import models
+from test_twodm_truncated_gpu import _objects
+m = models.synthetic_ab_initio(8, 5, 41)
+ham, prob, scheme = _objects(m, 0, 8, 0, 16, 2)
+c2g.srand(3)
+d = c2g.DMRG(prob, scheme)
+d.Solve()
+d.calc2DMandCorrelations()
+dm = d.get2DM()
+np.savez(sys.argv[1], A=np.array(dm.A), B=np.array(dm.B))
+d.close()
+"""
+
+
+def test_2rdm_in_many_programs_per_site(tmp_path):
+    """The 2-RDM pass splits the products of a site into programs under a work budget
+    (C2G_TWODM_BUDGET doubles, read once per process). With a budget of 2048 doubles every
+    site runs many programs; the 2-RDM equals the one of the default budget to rounding
+    (the same seeded solve on both sides)."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, PYTHONPATH=os.pathsep.join([str(root), str(root / "tests")]))
+    out = {}
+    for name, budget in (("default", None), ("small", "2048")):
+        e = dict(env)
+        if budget:
+            e["C2G_TWODM_BUDGET"] = budget
+        else:
+            e.pop("C2G_TWODM_BUDGET", None)
+        path = tmp_path / f"{name}.npz"
+        subprocess.run([sys.executable, "-c", _CHUNK_SCRIPT, str(path)], cwd=root, env=e, check=True, timeout=600)
+        out[name] = np.load(path)
+    assert np.max(np.abs(out["small"]["A"] - out["default"]["A"])) < 1e-10
+    assert np.max(np.abs(out["small"]["B"] - out["default"]["B"])) < 1e-10
