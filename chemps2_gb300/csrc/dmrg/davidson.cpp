@@ -110,6 +110,7 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
         best = rnorm;
         since_best = 0;
       } else if (++since_best >= 6) {
+        st.lo_stalled = true;
         break;
       }
     }
@@ -211,13 +212,17 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
   bool done = false;
   if (mixed) {
     run(diag, matvec, lo_, std::max(lo_tol, rtol_), true, st);
+    st.n_lo = st.n_matvec;
+    st.lo_rnorm = st.rnorm;
     // refinement cycles from the FP32 Ritz vector; a cycle that cannot improve (for
     // example an FP32 floor above the target) leaves it to the FP64 Davidson below
     double last = 1e300;
     for (int cycle = 0; cycle < kRefineCycles && !done; cycle++) {
       C2G_CUDA(cudaMemcpyAsync(t, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
       double r = 0.0;
+      st.n_cycles++;
       done = refine_cycle(diag, matvec, rtol_, kRefineExpand, kRefineRel, st, &r);
+      if (cycle == 0) st.r_exact0 = r;
       if (!done && r > 0.5 * last) break;  // the exact residual no longer drops
       last = r;
     }

@@ -31,6 +31,13 @@ struct DavidsonStats {
   int n_matvec_fp32 = 0;  // of which in FP32
   int n_iter = 0;
   double rnorm = 0.0;
+  // mixed solves: matvecs of the reduced-precision phase, its last residual and whether it
+  // ended on a stall; refinement cycles run
+  int n_lo = 0;
+  double lo_rnorm = 0.0;
+  bool lo_stalled = false;
+  int n_cycles = 0;
+  double r_exact0 = 0.0;  // exact (FP64) residual at the start of the first cycle
 };
 
 class DeviceDavidson {

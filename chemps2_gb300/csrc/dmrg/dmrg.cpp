@@ -942,7 +942,15 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
   const double Energy = ds.energy + Prob->gEconst();
   stats_.last_energy = Energy;
   stats_.t_solve += now() - t0;
-  if (verbose) std::printf("Energy at sites (%d, %d) is %.15f  [%d matvecs]\n", index, index + 1, Energy, ds.n_matvec);
+  if (verbose) {
+    std::printf("Energy at sites (%d, %d) is %.15f  [%d matvecs]", index, index + 1, Energy, ds.n_matvec);
+    if (precision_ != 0)
+      std::printf("  reduced-precision phase %d matvecs to residual %.2e%s, exact residual %.2e, %d refinement cycles, "
+                  "%d reduced in all",
+                  ds.n_lo, ds.lo_rnorm, ds.lo_stalled ? " (stalled)" : "", ds.r_exact0, ds.n_cycles, ds.n_matvec_fp32);
+    std::printf("\n");
+    std::fflush(stdout);
+  }
 
   // ---- Split
   t0 = now();

@@ -4,7 +4,7 @@ oracle's FCI 2-RDM and FCI two-orbital mutual information, and its own identitie
 (CheMPS2/DMRGtechnics.cpp:105-110 prints the same checks): trace A = N(N-1) and
 Econst + 1/2 sum A h = E. The DMRG runs at a virtual dimension that holds the FCI space,
 so the density matrices agree with FCI up to the Davidson tolerance (1e-10 residual; the
-2-RDM error is O(residual), asserted at 1e-6)."""
+2-RDM error is O(residual), asserted at 1e-9)."""
 from __future__ import annotations
 
 import numpy as np
@@ -54,8 +54,8 @@ def test_2rdm_matches_fci(name, make, two_s, n, irrep):
         dm = d.get2DM()
         assert abs(dm.trace() - n * (n - 1)) < 1e-8
         assert abs(dm.energy() - E) < 1e-8, (dm.energy(), E)
-        assert np.max(np.abs(dm.A - A_fci)) < 1e-6, np.max(np.abs(dm.A - A_fci))
-        assert np.max(np.abs(dm.B - B_fci)) < 1e-6, np.max(np.abs(dm.B - B_fci))
+        assert np.max(np.abs(dm.A - A_fci)) < 1e-9, np.max(np.abs(dm.A - A_fci))
+        assert np.max(np.abs(dm.B - B_fci)) < 1e-9, np.max(np.abs(dm.B - B_fci))
         # correlation pass: mutual information and single-orbital entropies against FCI. The
         # reference's two-orbital density matrices are partial traces in the orbital
         # tensor-product basis without the Jordan-Wigner string of the orbitals between
@@ -63,8 +63,8 @@ def test_2rdm_matches_fci(name, make, two_s, n, irrep):
         # CheMPS2/TensorKM.cpp:27-30), which the oracle computes with jw=False.
         _, s1_fci, mi_fci = ol.fci_mutual_information(m, n_up, n_down, irrep, jw=False)
         corr = d.getCorrelations()
-        assert np.max(np.abs(corr["SingleOrbitalEntropy"] - s1_fci)) < 1e-6
-        assert np.max(np.abs(corr["MutInfo"] - mi_fci)) < 1e-6, np.max(np.abs(corr["MutInfo"] - mi_fci))
+        assert np.max(np.abs(corr["SingleOrbitalEntropy"] - s1_fci)) < 1e-9
+        assert np.max(np.abs(corr["MutInfo"] - mi_fci)) < 1e-9, np.max(np.abs(corr["MutInfo"] - mi_fci))
         # the state and the operators are left as after a right sweep: Solve continues
         E2 = d.Solve()
         assert abs(E2 - E) < 1e-8
