@@ -401,8 +401,27 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def extra_sweeps(args, label, model, D, seed=SEED):
-    """Sweeps of another configuration in FP64 and in the mixed tensor-core form."""
+def cpu_sweeps(model, sweeps, D, seed):
+    """The CPU oracle's sweeps (its port of the reference's Solve) from the same seeded
+    start, one Solve per sweep, on all host cores: seconds per sweep and the energy."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as ol
+
+    threads = os.cpu_count() or 1
+    ol.set_threads(threads)
+    ol.srand(seed)
+    cpu = ol.OracleDMRG(model, TWO_S, model.L, IRREP, [(D, 1e-10, 1, 0.0, 1e-8)], check=False)
+    per, e = [], None
+    for _ in range(sweeps):
+        t0 = time.perf_counter()
+        e = cpu.solve()
+        per.append(time.perf_counter() - t0)
+    return {"s_per_sweep": per, "energy": e, "threads": threads, "cpu": host_cpu(), "kind": "port"}
+
+
+def extra_sweeps(args, label, model, D, seed=SEED, cpu=False):
+    """Sweeps of another configuration in FP64 and in the mixed tensor-core form; with cpu,
+    also the CPU oracle's sweeps from the same start."""
     out = {"config": f"{label}, {args.sweeps} sweeps, Davidson rtol 1e-8"}
     for mode in ("fp64", "mixed_tc"):
         objs, rec = run_sweeps(model, mode, args.sweeps, D=D, seed=seed)
@@ -410,6 +429,10 @@ def extra_sweeps(args, label, model, D, seed=SEED):
         out[mode] = rec
     out["mixed_speedup_last_sweep"] = out["fp64"]["s_per_sweep"][-1] / out["mixed_tc"]["s_per_sweep"][-1]
     out["mixed_energy_error"] = abs(out["mixed_tc"]["energy"] - out["fp64"]["energy"])
+    if cpu:
+        out["cpu_oracle"] = cpu_sweeps(model, args.sweeps, D, seed)
+        out["fp64_speedup_vs_cpu_last_sweep"] = out["cpu_oracle"]["s_per_sweep"][-1] / out["fp64"]["s_per_sweep"][-1]
+        out["fp64_energy_minus_cpu"] = out["fp64"]["energy"] - out["cpu_oracle"]["energy"]
     print(json.dumps({"extra": label, **out}), flush=True)
 
 
@@ -621,7 +644,7 @@ def main():
     if args.extra == "config1":
         from chemps2_gb300.models import hubbard
 
-        extra_sweeps(args, "hubbard L=16 N=16 U=4 C1 D=200", hubbard(16, 4.0), 200, seed=1)
+        extra_sweeps(args, "hubbard L=16 N=16 U=4 C1 D=200", hubbard(16, 4.0), 200, seed=1, cpu=True)
     elif args.extra == "config2":
         extra_sweeps(args, "synthetic ab initio L=24 N=24 S=0 D2h D=1000", make_model(24), 1000)
     elif args.extra == "config5":

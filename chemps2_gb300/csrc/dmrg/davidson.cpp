@@ -24,6 +24,15 @@ constexpr int kLd = 32;
 constexpr int kRefineCycles = 8;
 constexpr int kRefineExpand = 12;
 constexpr double kRefineRel = 1e-3;
+// A stall of the reduced-precision phase (no 0.7x residual reduction in 6 iterations)
+// with a residual of at most kStallCeiling |theta| is its arithmetic's floor: the
+// refinement cycles take over. A stall above it marks a hard step: a residual plateau from
+// a poor guess (the first sweep from a random start), on which the FP64 solver may still
+// turn to a lower eigenpair after many more products while the reduced-precision one
+// settles on an excited state. Such a step, and one that needs more than kLoMaxMatvec
+// reduced-precision products, is solved by the FP64 solver from the guess.
+constexpr double kStallCeiling = 1e-3;
+constexpr int kLoMaxMatvec = 1000;
 }  // namespace
 
 DeviceDavidson::DeviceDavidson(Runtime& rt, int64_t n, int max_vec, int keep, double rtol, double cutoff)
@@ -50,10 +59,12 @@ void DeviceDavidson::multi_dot(const double* A, int ncol, const double* x, doubl
   count_launches(2);
 }
 
-double DeviceDavidson::norm2(const double* x) {
+double DeviceDavidson::norm2(const double* x, double* theta) {
   multi_dot(x, 1, x, sm_ + kSumSq);
   C2G_CUDA(cudaMemcpyAsync(host_, sm_ + kSumSq, sizeof(double), cudaMemcpyDeviceToHost, rt_.stream()));
+  if (theta) C2G_CUDA(cudaMemcpyAsync(host_ + 1, sm_ + kEvals, sizeof(double), cudaMemcpyDeviceToHost, rt_.stream()));
   rt_.sync();
+  if (theta) *theta = host_[1];
   return host_[0];
 }
 
@@ -72,7 +83,7 @@ void DeviceDavidson::add_new_vec(double* t, int nv) {
   C2G_CUDA(cudaMemcpyAsync(V(nv), t, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
 }
 
-void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision prec, double tol, bool stop_on_stall,
+bool DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision prec, double tol, bool stop_on_stall,
                          DavidsonStats& st) {
   cudaStream_t s = rt_.stream();
   double* t = W(0);
@@ -89,6 +100,7 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
   mv(V(nv), HV(nv));
   double best = 1e300;
   int since_best = 0;
+  const int matvec0 = st.n_matvec;
   for (;;) {
     // DiagonalizeSmallMatrixAndCalcResidual (CheMPS2/Davidson.cpp:238-289)
     multi_dot(HV_, nv + 1, V(nv), sm_ + kDots);
@@ -101,18 +113,21 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
     C2G_CUDA(launch_combine(u, 0.0, V_, n_, sm_ + kEvecs, nv, n_, s));
     C2G_CUDA(launch_residual(t, u, sm_ + kEvals, n_, s));
     count_launches(5);
-    const double rnorm = std::sqrt(norm2(t));
+    double theta = 0.0;
+    const double rnorm = std::sqrt(norm2(t, stop_on_stall ? &theta : nullptr));
     st.n_iter++;
     st.rnorm = rnorm;
     if (!(rnorm > tol)) break;
-    if (stop_on_stall) {  // FP32 phase: stop when the residual no longer improves
+    if (stop_on_stall) {  // reduced-precision phase: stop when the residual no longer improves
       if (rnorm < 0.7 * best) {
         best = rnorm;
         since_best = 0;
       } else if (++since_best >= 6) {
         st.lo_stalled = true;
+        if (rnorm > kStallCeiling * std::fabs(theta)) return false;
         break;
       }
+      if (st.n_matvec - matvec0 >= kLoMaxMatvec) return false;
     }
     // CalculateNewVec (CheMPS2/Davidson.cpp:291-317)
     C2G_CUDA(launch_precond_w(w, u, diag, sm_ + kEvals, cutoff_, n_, s));
@@ -146,6 +161,7 @@ void DeviceDavidson::run(const double* diag, const MatVec& matvec, Precision pre
     add_new_vec(t, nv);
     mv(V(nv), HV(nv));
   }
+  return true;
 }
 
 bool DeviceDavidson::refine_cycle(const double* diag, const MatVec& matvec, double tol, int max_expand, double rel,
@@ -207,13 +223,26 @@ DavidsonStats DeviceDavidson::solve(double* guess, const double* diag, const Mat
     HostRand& g = rand_ ? *rand_ : libc;
     for (int64_t i = 0; i < n_; i++) r[i] = g.unit();
     C2G_CUDA(cudaMemcpyAsync(t, r.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
+    // the start vector also stays in guess (overwritten by the result at the end), for a
+    // restart of the mixed solve
+    C2G_CUDA(cudaMemcpyAsync(guess, t, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
     rt_.sync();
   }
   bool done = false;
   if (mixed) {
-    run(diag, matvec, lo_, std::max(lo_tol, rtol_), true, st);
+    const bool lo_done = run(diag, matvec, lo_, std::max(lo_tol, rtol_), true, st);
     st.n_lo = st.n_matvec;
     st.lo_rnorm = st.rnorm;
+    if (!lo_done) {  // a hard step: the FP64 solver from the guess
+      st.fp64_fallback = true;
+      C2G_CUDA(cudaMemcpyAsync(t, guess, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+      run(diag, matvec, Precision::kFP64, rtol_, false, st);
+      C2G_CUDA(cudaMemcpyAsync(guess, u, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+      C2G_CUDA(cudaMemcpyAsync(host_, sm_ + kEvals, sizeof(double), cudaMemcpyDeviceToHost, s));
+      rt_.sync();
+      st.energy = host_[0];
+      return st;
+    }
     // refinement cycles from the FP32 Ritz vector; a cycle that cannot improve (for
     // example an FP32 floor above the target) leaves it to the FP64 Davidson below
     double last = 1e300;

@@ -36,6 +36,7 @@ struct DavidsonStats {
   int n_lo = 0;
   double lo_rnorm = 0.0;
   bool lo_stalled = false;
+  bool fp64_fallback = false;  // a hard step: solved by the FP64 solver from the guess
   int n_cycles = 0;
   double r_exact0 = 0.0;  // exact (FP64) residual at the start of the first cycle
 };
@@ -68,10 +69,13 @@ class DeviceDavidson {
   double* HV(int i) { return HV_ + n_ * i; }
   double* W(int i) { return W_ + n_ * i; }
   void add_new_vec(double* t, int nv);  // orthonormalise t against V[0..nv) into V[nv]
-  double norm2(const double* x);         // synchronising host read of x.x
+  // synchronising host read of x.x (and, with theta, of the lowest Ritz value)
+  double norm2(const double* x, double* theta = nullptr);
   void multi_dot(const double* A, int ncol, const double* x, double* out);
-  // One Davidson run from the vector in W(0); the Ritz vector ends in W(1).
-  void run(const double* diag, const MatVec& matvec, Precision prec, double tol, bool stop_on_stall,
+  // One Davidson run from the vector in W(0); the Ritz vector ends in W(1). False when a
+  // reduced-precision run (stop_on_stall) met a hard step (a stall far above its
+  // arithmetic's floor, or its product limit).
+  bool run(const double* diag, const MatVec& matvec, Precision prec, double tol, bool stop_on_stall,
            DavidsonStats& st);
   // One refinement cycle from the vector in W(0) (first product FP64, then FP32, at most
   // max_expand expansions, until the residual estimate falls below rel * the exact first

@@ -947,7 +947,8 @@ double DMRG::solve_site(const int index, const double dvdson_rtol, const double 
     if (precision_ != 0)
       std::printf("  reduced-precision phase %d matvecs to residual %.2e%s, exact residual %.2e, %d refinement cycles, "
                   "%d reduced in all",
-                  ds.n_lo, ds.lo_rnorm, ds.lo_stalled ? " (stalled)" : "", ds.r_exact0, ds.n_cycles, ds.n_matvec_fp32);
+                  ds.n_lo, ds.lo_rnorm, ds.lo_stalled ? (ds.fp64_fallback ? " (stalled: solved in FP64)" : " (stalled)") : "",
+                  ds.r_exact0, ds.n_cycles, ds.n_matvec_fp32);
     std::printf("\n");
     std::fflush(stdout);
   }

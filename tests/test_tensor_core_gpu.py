@@ -115,3 +115,40 @@ def test_two_pass_chunks_give_identical_products(monkeypatch):
     assert launches["64"] > launches[None], launches
     for prec in ("fp64", "fp32", "tc"):
         assert np.array_equal(ys["64"][prec], ys[None][prec]), prec
+
+
+def test_mixed_solve_of_a_hard_step_finds_the_ground_state():
+    """Synthetic ab initio L=40 C2v, D=1000, from the seeded random start: at the fifth step
+    of the first left half-sweep the FP64 solver needs 43 products, with plateaus of the
+    residual. The reduced-precision phase must not end on such a plateau: an unconverged
+    Ritz vector handed to the refinement cycles, whose single-vector restarts converge to
+    the nearest eigenpair, gave an excited state 5.6 Ha above the FP64 one. The first six
+    step energies of the mixed tensor-core solve equal the FP64 ones to 1e-8."""
+    from chemps2_gb300.models import synthetic_ab_initio
+
+    m = synthetic_ab_initio(40, 5, 1234)
+    energies = {}
+    for mode in ("fp64", "mixed_tc"):
+        ham = c2g.Hamiltonian(m.L, m.group, m.irreps)
+        for i in range(m.L):
+            for j in range(i, m.L):
+                if m.tmat[i, j] != 0.0:
+                    ham.setTmat(i, j, float(m.tmat[i, j]))
+        for i, j, k, l in np.argwhere(m.vmat != 0.0):
+            if i <= j and i <= k:
+                ham.setVmat(int(i), int(j), int(k), int(l), float(m.vmat[i, j, k, l]))
+        prob = c2g.Problem(ham, 0, m.L, 0)
+        scheme = c2g.ConvergenceScheme(1)
+        scheme.set_instruction(0, 1000, 1e-10, 1, 0.0, 1e-8)
+        c2g.srand(1234)
+        d = c2g.DMRG(prob, scheme)
+        try:
+            d.set_precision(mode)
+            es = []
+            for index in range(m.L - 2, m.L - 8, -1):
+                es.append(d.solve_site(index, 1e-8, 0.0, 1000, False, False))
+                d.update(index, False)
+            energies[mode] = np.array(es)
+        finally:
+            d.close()
+    assert np.max(np.abs(energies["mixed_tc"] - energies["fp64"])) < 1e-8, energies
