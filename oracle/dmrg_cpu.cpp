@@ -30,6 +30,7 @@
 #include "chemps2/SyBookkeeper.h"
 #include "compile.hpp"
 #include "exec_cpu.hpp"
+#include "gauge.hpp"
 #include "heff.hpp"
 #include "layout.hpp"
 #include "operators.hpp"
@@ -777,6 +778,30 @@ int oracle_dmrg_sectors(void* h, int boundary, int* out, int cap, int* count) {
       out[5 * id + 2] = i;
       out[5 * id + 3] = bk.fci_dim_by_id(boundary, id);
       out[5 * id + 4] = bk.cur_dim_by_id(boundary, id);
+    }
+  });
+}
+
+// The gauge changes of the 2-RDM pass (CheMPS2/DMRGtechnics.cpp:276-322) on the oracle's
+// MPS, with the product's host routines (chemps2_gb300/csrc/host/gauge.cpp): kind 0
+// left-normalises `site` and multiplies R into site + 1 (nothing at the last site), kind 1
+// right-normalises `site` and multiplies L into site - 1. The operators are not updated.
+int oracle_dmrg_gauge(void* h, int site, int kind) {
+  return guard([&] {
+    auto* d = static_cast<OracleHandle*>(h)->dmrg.get();
+    if (site < 0 || site >= d->L) throw std::out_of_range("site");
+    if (kind == 0) {
+      if (site + 1 < d->L)
+        c2g::left_normalize(*d->bk, site, *d->mps_lay[site], d->mps[site], d->mps_lay[site + 1].get(),
+                            &d->mps[site + 1]);
+      else
+        c2g::left_normalize(*d->bk, site, *d->mps_lay[site], d->mps[site]);
+    } else if (kind == 1) {
+      if (site < 1) throw std::out_of_range("right normalisation needs a previous site");
+      c2g::right_normalize(*d->bk, site, *d->mps_lay[site], d->mps[site], d->mps_lay[site - 1].get(),
+                           &d->mps[site - 1]);
+    } else {
+      throw std::invalid_argument("gauge kind must be 0 (left) or 1 (right)");
     }
   });
 }

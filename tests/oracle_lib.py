@@ -171,6 +171,11 @@ class OracleDMRG:
         self._check(lib().oracle_dmrg_get_mps(self.h, int(site), _dp(out), C.c_int64(n.value), C.byref(n)))
         return out
 
+    def gauge(self, site, right):
+        """Left-normalise `site` (R into site + 1) or, with right, right-normalise it (L into
+        site - 1), with the product's host gauge routines."""
+        self._check(lib().oracle_dmrg_gauge(self.h, int(site), 1 if right else 0))
+
     def sectors(self, boundary):
         n = C.c_int()
         self._check(lib().oracle_dmrg_sectors(self.h, int(boundary), None, 0, C.byref(n)))
