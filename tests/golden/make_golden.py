@@ -6,6 +6,10 @@ time.
 
   * N2.STO3G.FCIDUMP    copied from tests/matrixelements/N2.STO3G.FCIDUMP (the input of
                         the reference's tests/test1.cpp.in and tests/test5.cpp.in)
+  * CH4.STO3G.FCIDUMP   copied from tests/matrixelements/CH4.STO3G.FCIDUMP (the input of
+                        the reference's tests/test3.cpp.in, which compares DMRG with FCI;
+                        its schedule is recorded in golden.json, the FCI energy is computed
+                        by the oracle)
   * golden.json         energies the reference's tests assert, parsed from their sources:
                         tests/test5.cpp.in (N2 STO-3G ground and two excited states,
                         D = 1000) and
@@ -26,6 +30,8 @@ HERE = Path(__file__).resolve().parent
 def main(reference: Path) -> None:
     tests = reference / "tests"
     shutil.copyfile(tests / "matrixelements" / "N2.STO3G.FCIDUMP", HERE / "N2.STO3G.FCIDUMP")
+    shutil.copyfile(tests / "matrixelements" / "CH4.STO3G.FCIDUMP", HERE / "CH4.STO3G.FCIDUMP")
+    t3 = (tests / "test3.cpp.in").read_text()
     t5 = (tests / "test5.cpp.in").read_text()
     t12 = (tests / "test12.cpp.in").read_text()
     e5 = [float(x) for x in re.findall(r"fabs\(\s*Energy\d\s*\+\s*([0-9.]+)\s*\)", t5)]
@@ -58,6 +64,25 @@ def main(reference: Path) -> None:
             "energy": -e12[0],
             "tolerance": 1e-8,
         },
+    }
+    # tests/test3.cpp.in: group, particle numbers and the two instructions (D, Econv,
+    # sweeps, noise) of its ConvergenceScheme; the Davidson tolerance is the reference's
+    # default for DMRG (CheMPS2/include/chemps2/Options.h: DAVIDSON_DMRG_RTOL = 1e-5)
+    grp = int(re.search(r"psi4groupnumber\s*=\s*(\d+)", t3).group(1))
+    n3 = int(re.search(r"int\s+N\s*=\s*(\d+)", t3).group(1))
+    s3 = int(re.search(r"int\s+TwoS\s*=\s*(\d+)", t3).group(1))
+    i3 = int(re.search(r"int\s+Irrep\s*=\s*(\d+)", t3).group(1))
+    instr = re.findall(r"OptScheme->setInstruction\(\s*(\d+)\s*,\s*(\d+)\s*,\s*([0-9.e+-]+)\s*,\s*(\d+)\s*,"
+                       r"\s*([0-9.e+-]+)\s*\)", t3)
+    golden["ch4_sto3g"] = {
+        "source": "tests/test3.cpp.in",
+        "fcidump": "CH4.STO3G.FCIDUMP",
+        "group": grp,
+        "two_s": s3,
+        "n": n3,
+        "irrep": i3,
+        "schedule": [[int(d), float(e), int(sw), float(nz), 1e-5] for _, d, e, sw, nz in instr],
+        "tolerance": 1e-08,
     }
     (HERE / "golden.json").write_text(json.dumps(golden, indent=2) + "\n")
 

@@ -196,6 +196,24 @@ class OracleDMRG:
             pass
 
 
+def fcidump_model(path, group) -> Model:
+    """The Hamiltonian of an FCIDUMP file (read by the product's reader, whose conversions
+    the N2 golden pins) as a Model for the determinant FCI."""
+    import chemps2_gb300 as c2g
+
+    ham = c2g.Hamiltonian(0, int(group), [], filename=str(path))
+    L = ham.getL()
+    irreps = np.array([ham.getOrbitalIrrep(i) for i in range(L)], dtype=np.int32)
+    T = np.array([[ham.getTmat(i, j) for j in range(L)] for i in range(L)])
+    V = np.zeros((L, L, L, L))
+    for i in range(L):
+        for j in range(L):
+            for k in range(L):
+                for l in range(L):
+                    V[i, j, k, l] = ham.getVmat(i, j, k, l)
+    return Model(L, int(group), irreps, T, V, ham.getEconst())
+
+
 def set_threads(n: int):
     """Host threads of the oracle's task-program executor (results do not depend on it)."""
     lib().oracle_set_threads(int(n))

@@ -217,6 +217,28 @@ def test_n2_sto3g_golden_of_reference_test5():
     assert abs(e - g["energy"]) < g["tolerance"]
 
 
+def test_ch4_sto3g_against_fci_of_reference_test3():
+    """The reference's tests/test3.cpp.in: CH4 STO-3G (C2v, N = 10, singlet A1) with its
+    two-instruction schedule (D = 30 with noise, then D = 1000); the GPU energy equals the
+    oracle's determinant FCI energy to 1e-8."""
+    g = GOLDEN["ch4_sto3g"]
+    path = GOLDEN_DIR / g["fcidump"]
+    efci = ol.fci_energy(ol.fcidump_model(path, g["group"]), (g["n"] + g["two_s"]) // 2,
+                         (g["n"] - g["two_s"]) // 2, g["irrep"])
+    ham = c2g.Hamiltonian(0, g["group"], [], filename=str(path))
+    prob = c2g.Problem(ham, g["two_s"], g["n"], g["irrep"])
+    scheme = c2g.ConvergenceScheme(len(g["schedule"]))
+    for i, instr in enumerate(g["schedule"]):
+        scheme.set_instruction(i, *instr)
+    c2g.srand(1)
+    gpu = c2g.DMRG(prob, scheme)
+    try:
+        e = gpu.Solve()
+    finally:
+        gpu.close()
+    assert abs(e - efci) < g["tolerance"], (e, efci)
+
+
 def test_kernels_were_launched():
     before = c2g.kernel_launches()
     m = models.hubbard(6, 4.0)

@@ -126,6 +126,19 @@ def test_oracle_n2_sto3g_golden_of_reference_test5():
     assert abs(d.solve() - g["energy"]) < g["tolerance"]
 
 
+def test_oracle_ch4_sto3g_against_fci_of_reference_test3():
+    """The reference's tests/test3.cpp.in: CH4 STO-3G (C2v, N = 10, singlet A1) with its
+    two-instruction schedule; the DMRG energy equals the FCI energy to 1e-8."""
+    g = GOLDEN["ch4_sto3g"]
+    path = Path(__file__).parent / "golden" / g["fcidump"]
+    efci = ol.fci_energy(ol.fcidump_model(path, g["group"]), (g["n"] + g["two_s"]) // 2,
+                         (g["n"] - g["two_s"]) // 2, g["irrep"])
+    ol.srand(1)
+    d = ol.OracleDMRG(None, g["two_s"], g["n"], g["irrep"], [tuple(x) for x in g["schedule"]], fcidump=path,
+                      group=g["group"], check=False)
+    assert abs(d.solve() - efci) < g["tolerance"]
+
+
 def test_executor_rejects_out_of_bounds_programs():
     """The checker of the task programs: a program planted with a bad offset is refused on
     the CPU before it could ever reach a GPU (the mistake is planted in the oracle's input,
