@@ -10,7 +10,9 @@ time.
                         the reference's tests/test3.cpp.in, which compares DMRG with FCI;
                         its schedule is recorded in golden.json, the FCI energy is computed
                         by the oracle)
-  * golden.json         energies the reference's tests assert, parsed from their sources:
+  * golden.json         energies the reference's tests assert, parsed from their sources,
+                        and the settings of its DMRG-against-FCI tests (tests/test1.cpp.in:
+                        N2 STO-3G in six symmetry sectors; tests/test3.cpp.in: CH4 STO-3G):
                         tests/test5.cpp.in (N2 STO-3G ground and two excited states,
                         D = 1000) and
                         tests/test12.cpp.in (the BCS pairing model, L = 8)
@@ -32,6 +34,7 @@ def main(reference: Path) -> None:
     shutil.copyfile(tests / "matrixelements" / "N2.STO3G.FCIDUMP", HERE / "N2.STO3G.FCIDUMP")
     shutil.copyfile(tests / "matrixelements" / "CH4.STO3G.FCIDUMP", HERE / "CH4.STO3G.FCIDUMP")
     t3 = (tests / "test3.cpp.in").read_text()
+    t1 = (tests / "test1.cpp.in").read_text()
     t5 = (tests / "test5.cpp.in").read_text()
     t12 = (tests / "test12.cpp.in").read_text()
     e5 = [float(x) for x in re.findall(r"fabs\(\s*Energy\d\s*\+\s*([0-9.]+)\s*\)", t5)]
@@ -82,6 +85,21 @@ def main(reference: Path) -> None:
         "n": n3,
         "irrep": i3,
         "schedule": [[int(d), float(e), int(sw), float(nz), 1e-5] for _, d, e, sw, nz in instr],
+        "tolerance": 1e-08,
+    }
+    # tests/test1.cpp.in: N2 STO-3G in six (2S, irrep) sectors, each with its two
+    # set_instruction calls (D, Econv, sweeps, noise, Davidson rtol)
+    arr = lambda name: [int(x) for x in re.search(name + r"\[\]\s*=\s*\{([^}]*)\}", t1).group(1).split(",")]
+    instr1 = re.findall(r"opt_scheme\.set_instruction\(\s*\d+\s*,\s*(\d+)\s*,\s*([0-9.e+-]+)\s*,\s*(\d+)\s*,"
+                        r"\s*([0-9.e+-]+)\s*,\s*([0-9.e+-]+)\s*\)", t1)
+    golden["n2_sto3g_sectors"] = {
+        "source": "tests/test1.cpp.in",
+        "fcidump": "N2.STO3G.FCIDUMP",
+        "group": int(re.search(r"psi4groupnumber\s*=\s*(\d+)", t1).group(1)),
+        "n": int(re.search(r"Nelec\s*=\s*(\d+)", t1).group(1)),
+        "two_s": arr("TwoS"),
+        "irreps": arr("Irreps"),
+        "schedule": [[int(d), float(e), int(sw), float(nz), float(rt)] for d, e, sw, nz, rt in instr1],
         "tolerance": 1e-08,
     }
     (HERE / "golden.json").write_text(json.dumps(golden, indent=2) + "\n")

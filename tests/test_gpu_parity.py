@@ -239,6 +239,29 @@ def test_ch4_sto3g_against_fci_of_reference_test3():
     assert abs(e - efci) < g["tolerance"], (e, efci)
 
 
+def test_n2_sto3g_sectors_against_fci_of_reference_test1():
+    """The reference's tests/test1.cpp.in: N2 STO-3G (D2h, N = 14) in six (2S, irrep)
+    sectors, singlet to quintet, with its schedule (D = 500, then D = 1000 to a 1e-10
+    residual); every GPU energy equals the oracle's FCI energy of its sector to 1e-8."""
+    g = GOLDEN["n2_sto3g_sectors"]
+    path = GOLDEN_DIR / g["fcidump"]
+    m = ol.fcidump_model(path, g["group"])
+    for two_s, irrep in zip(g["two_s"], g["irreps"]):
+        efci = ol.fci_energy(m, (g["n"] + two_s) // 2, (g["n"] - two_s) // 2, irrep)
+        ham = c2g.Hamiltonian(0, g["group"], [], filename=str(path))
+        prob = c2g.Problem(ham, two_s, g["n"], irrep)
+        scheme = c2g.ConvergenceScheme(len(g["schedule"]))
+        for i, instr in enumerate(g["schedule"]):
+            scheme.set_instruction(i, *instr)
+        c2g.srand(1)
+        gpu = c2g.DMRG(prob, scheme)
+        try:
+            e = gpu.Solve()
+        finally:
+            gpu.close()
+        assert abs(e - efci) < g["tolerance"], (two_s, irrep, e, efci)
+
+
 def test_kernels_were_launched():
     before = c2g.kernel_launches()
     m = models.hubbard(6, 4.0)

@@ -139,6 +139,21 @@ def test_oracle_ch4_sto3g_against_fci_of_reference_test3():
     assert abs(d.solve() - efci) < g["tolerance"]
 
 
+def test_oracle_n2_sto3g_sectors_against_fci_of_reference_test1():
+    """The reference's tests/test1.cpp.in: N2 STO-3G (D2h, N = 14) in six (2S, irrep)
+    sectors with its schedule (D = 500, then D = 1000 to a 1e-10 residual); every DMRG
+    energy equals the FCI energy of its sector to 1e-8."""
+    g = GOLDEN["n2_sto3g_sectors"]
+    path = Path(__file__).parent / "golden" / g["fcidump"]
+    m = ol.fcidump_model(path, g["group"])
+    for two_s, irrep in zip(g["two_s"], g["irreps"]):
+        efci = ol.fci_energy(m, (g["n"] + two_s) // 2, (g["n"] - two_s) // 2, irrep)
+        ol.srand(1)
+        d = ol.OracleDMRG(None, two_s, g["n"], irrep, [tuple(x) for x in g["schedule"]], fcidump=path,
+                          group=g["group"], check=False)
+        assert abs(d.solve() - efci) < g["tolerance"], (two_s, irrep)
+
+
 def test_executor_rejects_out_of_bounds_programs():
     """The checker of the task programs: a program planted with a bad offset is refused on
     the CPU before it could ever reach a GPU (the mistake is planted in the oracle's input,
