@@ -262,6 +262,35 @@ def test_n2_sto3g_sectors_against_fci_of_reference_test1():
         assert abs(e - efci) < g["tolerance"], (two_s, irrep, e, efci)
 
 
+def test_hubbard_3x3_site_against_momentum_basis_of_reference_test9():
+    """The reference's tests/test9.cpp.in: the 3 x 3 periodic Hubbard model (U = 5, N = 9,
+    doublet) in the site basis and, through setMxElement + PreSolve on the same DMRG
+    object's problem, in the momentum basis (matrix elements with only fourfold
+    symmetry); the two GPU energies agree to 1e-8."""
+    site, mom = models.hubbard_3x3_site_and_momentum()
+    sched = [(500, 1e-10, 3, 0.05, 1e-5), (1000, 1e-10, 10, 0.0, 1e-5)]
+    ham, prob, scheme = gpu_objects(site, 1, 9, 0, sched)
+    c2g.srand(1)
+    gpu = c2g.DMRG(prob, scheme)
+    try:
+        e_site = gpu.Solve()
+    finally:
+        gpu.close()
+    c2g.srand(1)
+    gpu = c2g.DMRG(prob, scheme)
+    try:
+        for i in range(9):
+            for j in range(9):
+                for k in range(9):
+                    for l in range(9):
+                        prob.setMxElement(i, j, k, l, mom.get((i, j, k, l), 0.0))
+        gpu.PreSolve()
+        e_mom = gpu.Solve()
+    finally:
+        gpu.close()
+    assert abs(e_mom - e_site) < 1e-8, (e_site, e_mom)
+
+
 def test_kernels_were_launched():
     before = c2g.kernel_launches()
     m = models.hubbard(6, 4.0)

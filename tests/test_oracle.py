@@ -154,6 +154,26 @@ def test_oracle_n2_sto3g_sectors_against_fci_of_reference_test1():
         assert abs(d.solve() - efci) < g["tolerance"], (two_s, irrep)
 
 
+def test_oracle_hubbard_3x3_site_against_momentum_basis_of_reference_test9():
+    """The reference's tests/test9.cpp.in: the 3 x 3 periodic Hubbard model (U = 5, N = 9,
+    doublet) in the site basis and, through setMxElement + PreSolve, in the momentum
+    basis, whose matrix elements have only fourfold symmetry; the energies agree to
+    1e-8."""
+    site, mom = models.hubbard_3x3_site_and_momentum()
+    sched = [(500, 1e-10, 3, 0.05, 1e-5), (1000, 1e-10, 10, 0.0, 1e-5)]
+    ol.srand(1)
+    e_site = ol.OracleDMRG(site, 1, 9, 0, sched, check=False).solve()
+    ol.srand(1)
+    d = ol.OracleDMRG(site, 1, 9, 0, sched, check=False)
+    for i in range(9):
+        for j in range(9):
+            for k in range(9):
+                for l in range(9):
+                    d.set_mx_element(i, j, k, l, mom.get((i, j, k, l), 0.0))
+    d.presolve()
+    assert abs(d.solve() - e_site) < 1e-8
+
+
 def test_executor_rejects_out_of_bounds_programs():
     """The checker of the task programs: a program planted with a bad offset is refused on
     the CPU before it could ever reach a GPU (the mistake is planted in the oracle's input,
