@@ -174,6 +174,29 @@ def test_oracle_hubbard_3x3_site_against_momentum_basis_of_reference_test9():
     assert abs(d.solve() - e_site) < 1e-8
 
 
+@pytest.mark.parametrize("L,n,two_s", [(4, 4, 4), (4, 8, 0), (6, 0, 0), (5, 9, 1), (3, 2, 2), (3, 3, 1)])
+def test_oracle_edge_sectors_against_fci(L, n, two_s):
+    """Sectors at the edges of the Problem's consistency rules (CheMPS2/Problem.cpp:386-421):
+    the maximal spin TwoS = L - |N - L|, a full and an empty chain, N = 2L - 1, and the
+    shortest chain with two-site steps (L = 3; the triplet, since the determinant FCI of
+    M_S = 1 holds S >= 1 only). The DMRG at a D above the FCI space equals FCI to 1e-10."""
+    m = models.synthetic_ab_initio(L, 0, 4 + L + n)
+    efci = ol.fci_energy(m, (n + two_s) // 2, (n - two_s) // 2, 0)
+    ol.srand(1)
+    d = ol.OracleDMRG(m, two_s, n, 0, [(64, 1e-10, 4, 0.0, 1e-10)])
+    assert abs(d.solve() - efci) < 1e-10
+
+
+def test_oracle_two_orbitals_have_no_two_site_step():
+    """L = 2: the sweeps of CheMPS2/DMRG.cpp:357-402 run over index = L-2 .. 1 and
+    0 .. L-3, both empty, so Solve returns its initial minimum energy 1e8, as the
+    reference does."""
+    m = models.synthetic_ab_initio(2, 0, 3)
+    ol.srand(1)
+    d = ol.OracleDMRG(m, 0, 2, 0, [(16, 1e-10, 2, 0.0, 1e-10)])
+    assert d.solve() == 1e8
+
+
 def test_executor_rejects_out_of_bounds_programs():
     """The checker of the task programs: a program planted with a bad offset is refused on
     the CPU before it could ever reach a GPU (the mistake is planted in the oracle's input,
