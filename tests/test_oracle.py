@@ -187,6 +187,30 @@ def test_oracle_edge_sectors_against_fci(L, n, two_s):
     assert abs(d.solve() - efci) < 1e-10
 
 
+@pytest.mark.parametrize("group", range(8))
+def test_oracle_every_point_group_and_spin_against_fci(group):
+    """All eight point groups (C1 .. D2h), two target irreps each, N = 6 and N = 7: the
+    determinant FCI at M_S = S holds every spin S' >= S, so its energy equals the lowest
+    of the DMRG energies of the sectors S' = S .. S_max (empty sectors skipped) to 1e-10.
+    This covers the task compiler's irrep products and spin couplings up to the maximal
+    spin in every group's table."""
+    m = models.synthetic_ab_initio(7, group, 11 + group)
+    for irrep in sorted(set(m.irreps.tolist()))[:2]:
+        for n, two_s in ((6, 0), (7, 1)):
+            efci = ol.fci_energy(m, (n + two_s) // 2, (n - two_s) // 2, irrep)
+            energies = []
+            for sp in range(two_s, 7 - abs(n - 7) + 1, 2):
+                ol.srand(1)
+                try:
+                    d = ol.OracleDMRG(m, sp, n, irrep, [(200, 1e-10, 4, 0.0, 1e-10)])
+                except RuntimeError as e:
+                    if "empty" in str(e):
+                        continue
+                    raise
+                energies.append(d.solve())
+            assert abs(min(energies) - efci) < 1e-10, (group, irrep, n, two_s)
+
+
 def test_oracle_two_orbitals_have_no_two_site_step():
     """L = 2: the sweeps of CheMPS2/DMRG.cpp:357-402 run over index = L-2 .. 1 and
     0 .. L-3, both empty, so Solve returns its initial minimum energy 1e8, as the
