@@ -35,6 +35,7 @@
 #include "layout.hpp"
 #include "operators.hpp"
 #include "sobject.hpp"
+#include "twodm.hpp"
 #include "symm.hpp"
 
 namespace oracle {
@@ -383,6 +384,45 @@ struct OracleDMRG {
     for (int c = 0; c < upto; c++) update(c, true);
     TotalMinEnergy = 1e8;
     MaxDisc = 0.0;
+  }
+
+  // The 2-RDM pass of DMRG::calc2DMandCorrelations (CheMPS2/DMRGtechnics.cpp:40-120) with
+  // the product's host parts: gauge changes (host/gauge.cpp), operator updates and the
+  // 2-RDM programs (host/twodm.cpp), run on this executor. Leaves the state as the pass
+  // leaves it (site 0 the orthogonality centre, right operators of every boundary).
+  std::unique_ptr<CheMPS2::TwoDM> two_dm;
+  void calc_2dm() {
+    c2g::left_normalize(*bk, L - 2, *mps_lay[L - 2], mps[L - 2], mps_lay[L - 1].get(), &mps[L - 1]);
+    c2g::left_normalize(*bk, L - 1, *mps_lay[L - 1], mps[L - 1]);
+    update(L - 2, true);
+    two_dm = std::make_unique<CheMPS2::TwoDM>(Prob, L);
+    for (int site = L - 1; site >= 0; site--) {
+      c2g::TwoDMContext ctx;
+      ctx.bk = bk.get();
+      ctx.L = L;
+      ctx.site = site;
+      ctx.T = mpsT(site);
+      ctx.left = (site > 0) ? ops[site - 1].get() : nullptr;
+      ctx.right = (site < L - 1) ? ops[site].get() : nullptr;
+      if (site > 0 && isAllocated[site - 1] != 1) throw std::logic_error("2-RDM: left operators missing");
+      if (site < L - 1 && isAllocated[site] != 2) throw std::logic_error("2-RDM: right operators missing");
+      const std::vector<c2g::TwoDMInstance> inst = c2g::twodm_instances(ctx);
+      const int nv = inst.back().value0 + c2g::twodm_num_values(inst.back().kind);
+      int64_t work = 0;
+      for (const auto& in : inst) work += in.work;
+      std::vector<double> values(nv, 0.0), wmem(std::max<int64_t>(work, 1), 0.0);
+      TaskBuilder tb;
+      c2g::compile_twodm(tb, ctx, inst, 0, inst.size());
+      ex.bind(kSlotWork, wmem.data(), work);
+      exec(tb.finalize(), nullptr, 0, values.data(), nv);
+      ex.bind(kSlotWork, nullptr, 0);
+      c2g::twodm_assemble(*two_dm, site, inst, values);
+      if (site > 0) {
+        c2g::right_normalize(*bk, site, *mps_lay[site], mps[site], mps_lay[site - 1].get(), &mps[site - 1]);
+        update(site - 1, false);
+      }
+    }
+    two_dm->correct_higher_multiplicities();
   }
 
   HeffContext heff_ctx(const TwoSiteLayout& S, int index) {
@@ -804,6 +844,31 @@ int oracle_dmrg_gauge(void* h, int site, int kind) {
       throw std::invalid_argument("gauge kind must be 0 (left) or 1 (right)");
     }
   });
+}
+
+// The 2-RDM of the current state (OracleDMRG::calc_2dm); A and B (L^4 each, element
+// (a, b, c, d) at a + L (b + L (c + L d)), DMRG orbital order), its trace and energy.
+int oracle_dmrg_calc_2dm(void* h, double* A, double* B, double* trace, double* energy) {
+  return guard([&] {
+    auto* d = static_cast<OracleHandle*>(h)->dmrg.get();
+    d->calc_2dm();
+    const CheMPS2::TwoDM& dm = *d->two_dm;
+    const int L = d->L;
+    for (int a = 0; a < L; a++)
+      for (int b = 0; b < L; b++)
+        for (int c = 0; c < L; c++)
+          for (int e = 0; e < L; e++) {
+            const size_t at = a + size_t(L) * (b + size_t(L) * (c + size_t(L) * e));
+            if (A) A[at] = dm.getTwoDMA_DMRG(a, b, c, e);
+            if (B) B[at] = dm.getTwoDMB_DMRG(a, b, c, e);
+          }
+    *trace = dm.trace();
+    *energy = dm.energy();
+  });
+}
+
+int oracle_dmrg_num_orbitals(void* h, int* L) {
+  return guard([&] { *L = static_cast<OracleHandle*>(h)->dmrg->L; });
 }
 
 int oracle_dmrg_num_mps_var(void* h, int* n) {

@@ -171,6 +171,18 @@ class OracleDMRG:
         self._check(lib().oracle_dmrg_get_mps(self.h, int(site), _dp(out), C.c_int64(n.value), C.byref(n)))
         return out
 
+    def calc_2dm(self):
+        """The 2-RDM pass on the CPU executor: (A, B, trace, energy), A and B as L^4 arrays
+        indexed [a, b, c, d] in DMRG orbital order."""
+        nl = C.c_int()
+        self._check(lib().oracle_dmrg_num_orbitals(self.h, C.byref(nl)))
+        L = nl.value
+        A = np.zeros(L ** 4)
+        B = np.zeros(L ** 4)
+        tr, en = C.c_double(), C.c_double()
+        self._check(lib().oracle_dmrg_calc_2dm(self.h, _dp(A), _dp(B), C.byref(tr), C.byref(en)))
+        return A.reshape((L,) * 4, order="F"), B.reshape((L,) * 4, order="F"), tr.value, en.value
+
     def gauge(self, site, right):
         """Left-normalise `site` (R into site + 1) or, with right, right-normalise it (L into
         site - 1), with the product's host gauge routines."""

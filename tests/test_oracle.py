@@ -211,6 +211,47 @@ def test_oracle_every_point_group_and_spin_against_fci(group):
             assert abs(min(energies) - efci) < 1e-10, (group, irrep, n, two_s)
 
 
+@pytest.mark.parametrize("group", range(8))
+def test_oracle_2rdm_program_against_fci_in_every_point_group(group):
+    """The 2-RDM pass (the product's gauge changes, updates and 2-RDM programs of
+    host/twodm.cpp, run on the CPU executor) in all eight point groups, N = 6 and N = 7,
+    each in the spin sector of its ground state: A equals the FCI 2-RDM of that state (its
+    M_S = S component; A is a spin scalar) to 1e-8, the trace is N(N-1) and the 2-RDM
+    energy the DMRG energy to 1e-9. B carries the spin sign (-1)^(s-t), so it depends on
+    M_S for S >= 1; the DMRG's B is the average over the multiplet
+    (CheMPS2/TwoDM.cpp:630-640 divides the reduced elements by 2S + 1). The chosen
+    multiplet is the ground state of all spins, so each of its M components is the FCI
+    ground state of its M_S sector, and B equals the average of their FCI B to 1e-8."""
+    m = models.synthetic_ab_initio(7, group, 11 + group)
+    sched = [(200, 1e-11, 6, 0.0, 1e-10)]
+    for n, two_s in ((6, 0), (7, 1)):
+        best = None
+        for sp in range(two_s, 7 - abs(n - 7) + 1, 2):
+            ol.srand(1)
+            try:
+                d = ol.OracleDMRG(m, sp, n, 0, sched)
+            except RuntimeError as e:
+                if "empty" in str(e):
+                    continue
+                raise
+            e = d.solve()
+            if best is None or e < best[0] - 1e-9:
+                best = (e, sp, d)
+        e, sp, d = best
+        A, B, trace, energy = d.calc_2dm()
+        efci, A_fci, B_fci = ol.fci_2rdm(m, (n + sp) // 2, (n - sp) // 2, 0)
+        assert abs(e - efci) < 1e-9, (group, n, sp)
+        assert abs(trace - n * (n - 1)) < 1e-9
+        assert abs(energy - e) < 1e-9
+        assert np.max(np.abs(A - A_fci)) < 1e-8, (group, n, sp, np.max(np.abs(A - A_fci)))
+        B_avg = np.zeros_like(B)
+        for two_m in range(-sp, sp + 1, 2):
+            em, _, B_m = ol.fci_2rdm(m, (n + two_m) // 2, (n - two_m) // 2, 0)
+            assert abs(em - e) < 1e-9, (group, n, sp, two_m)
+            B_avg += B_m / (sp + 1)
+        assert np.max(np.abs(B - B_avg)) < 1e-8, (group, n, sp, np.max(np.abs(B - B_avg)))
+
+
 def test_oracle_two_orbitals_have_no_two_site_step():
     """L = 2: the sweeps of CheMPS2/DMRG.cpp:357-402 run over index = L-2 .. 1 and
     0 .. L-3, both empty, so Solve returns its initial minimum energy 1e8, as the
