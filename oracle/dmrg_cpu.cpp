@@ -34,6 +34,8 @@
 #include "heff.hpp"
 #include "layout.hpp"
 #include "operators.hpp"
+#include "chemps2/Correlations.h"
+#include "correlations.hpp"
 #include "sobject.hpp"
 #include "twodm.hpp"
 #include "symm.hpp"
@@ -423,6 +425,46 @@ struct OracleDMRG {
       }
     }
     two_dm->correct_higher_multiplicities();
+  }
+
+  // The correlation pass that follows the 2-RDM pass (CheMPS2/DMRGtechnics.cpp:157-176)
+  // with the product's host parts: left normalisation site by site, the G/Y/Z/K/M tensors
+  // (host/correlations.cpp programs) and Correlations::fill_pair.
+  std::unique_ptr<CheMPS2::Correlations> corr;
+  void calc_corr() {
+    if (!two_dm) throw std::logic_error("correlations: no 2-RDM");
+    corr = std::make_unique<CheMPS2::Correlations>(Prob, two_dm.get());
+    std::unique_ptr<c2g::CorrTensors> cprev;
+    std::vector<double> mprev;
+    for (int site = 0; site < L - 1; site++) {
+      c2g::left_normalize(*bk, site, *mps_lay[site], mps[site], mps_lay[site + 1].get(), &mps[site + 1]);
+      const int s = site + 1;
+      auto cnext = std::make_unique<c2g::CorrTensors>();
+      const int slot = (s % 2 == 0) ? kSlotCorr0 : kSlotCorr1;
+      c2g::allocate_corr(*cnext, *bk, s, slot);
+      std::vector<double> mnext(std::max<int64_t>(cnext->size, 1), 0.0);
+      ex.bind(slot, mnext.data(), cnext->size);
+      {
+        TaskBuilder tb;
+        c2g::compile_corr_update(tb, *bk, *Prob, L, s, cprev.get(), *cnext, mpsT(site));
+        exec(tb.finalize(), nullptr, 0, nullptr, 0);
+      }
+      {
+        TaskBuilder tb;
+        const int64_t work = c2g::compile_corr_fill(tb, *bk, s, mpsT(s), *cnext);
+        const int nv = s * c2g::kCorrValues;
+        std::vector<double> values(nv, 0.0), wmem(std::max<int64_t>(work, 1), 0.0);
+        ex.bind(kSlotWork, wmem.data(), work);
+        exec(tb.finalize(), nullptr, 0, values.data(), nv);
+        ex.bind(kSlotWork, nullptr, 0);
+        for (int q = 0; q < s; q++) corr->fill_pair(q, s, values.data() + q * c2g::kCorrValues);
+      }
+      if (cprev) ex.bind(cprev->slot, nullptr, 0);
+      cprev = std::move(cnext);
+      mprev = std::move(mnext);
+      if (site <= L - 3) update(site, true);
+    }
+    if (cprev) ex.bind(cprev->slot, nullptr, 0);
   }
 
   HeffContext heff_ctx(const TwoSiteLayout& S, int index) {
@@ -864,6 +906,20 @@ int oracle_dmrg_calc_2dm(void* h, double* A, double* B, double* trace, double* e
           }
     *trace = dm.trace();
     *energy = dm.energy();
+  });
+}
+
+// The correlation pass after oracle_dmrg_calc_2dm: mutual information (L x L, DMRG order,
+// element (r, c) at r + L c) and single-orbital entropies (L).
+int oracle_dmrg_calc_correlations(void* h, double* mutinfo, double* entropy) {
+  return guard([&] {
+    auto* d = static_cast<OracleHandle*>(h)->dmrg.get();
+    d->calc_corr();
+    const int L = d->L;
+    for (int r = 0; r < L; r++) {
+      entropy[r] = d->corr->SingleOrbitalEntropy_DMRG(r);
+      for (int c = 0; c < L; c++) mutinfo[r + size_t(L) * c] = d->corr->getMutualInformation_DMRG(r, c);
+    }
   });
 }
 

@@ -183,6 +183,17 @@ class OracleDMRG:
         self._check(lib().oracle_dmrg_calc_2dm(self.h, _dp(A), _dp(B), C.byref(tr), C.byref(en)))
         return A.reshape((L,) * 4, order="F"), B.reshape((L,) * 4, order="F"), tr.value, en.value
 
+    def calc_correlations(self):
+        """The correlation pass after calc_2dm: (mutual information L x L, single-orbital
+        entropies), DMRG orbital order."""
+        nl = C.c_int()
+        self._check(lib().oracle_dmrg_num_orbitals(self.h, C.byref(nl)))
+        L = nl.value
+        mi = np.zeros(L * L)
+        s1 = np.zeros(L)
+        self._check(lib().oracle_dmrg_calc_correlations(self.h, _dp(mi), _dp(s1)))
+        return mi.reshape((L, L), order="F"), s1
+
     def gauge(self, site, right):
         """Left-normalise `site` (R into site + 1) or, with right, right-normalise it (L into
         site - 1), with the product's host gauge routines."""

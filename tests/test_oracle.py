@@ -212,7 +212,7 @@ def test_oracle_every_point_group_and_spin_against_fci(group):
 
 
 @pytest.mark.parametrize("group", range(8))
-def test_oracle_2rdm_program_against_fci_in_every_point_group(group):
+def test_oracle_2rdm_and_correlation_programs_against_fci_in_every_point_group(group):
     """The 2-RDM pass (the product's gauge changes, updates and 2-RDM programs of
     host/twodm.cpp, run on the CPU executor) in all eight point groups, N = 6 and N = 7,
     each in the spin sector of its ground state: A equals the FCI 2-RDM of that state (its
@@ -221,7 +221,11 @@ def test_oracle_2rdm_program_against_fci_in_every_point_group(group):
     M_S for S >= 1; the DMRG's B is the average over the multiplet
     (CheMPS2/TwoDM.cpp:630-640 divides the reduced elements by 2S + 1). The chosen
     multiplet is the ground state of all spins, so each of its M components is the FCI
-    ground state of its M_S sector, and B equals the average of their FCI B to 1e-8."""
+    ground state of its M_S sector, and B equals the average of their FCI B to 1e-8.
+    The correlation pass that follows (host/correlations.cpp programs) gives the mutual
+    information and single-orbital entropies of FCI (two-orbital density matrices
+    without the Jordan-Wigner string, as the reference's) to 1e-8 for S <= 1/2, where a
+    global spin flip leaves every entropy unchanged."""
     m = models.synthetic_ab_initio(7, group, 11 + group)
     sched = [(200, 1e-11, 6, 0.0, 1e-10)]
     for n, two_s in ((6, 0), (7, 1)):
@@ -250,6 +254,11 @@ def test_oracle_2rdm_program_against_fci_in_every_point_group(group):
             assert abs(em - e) < 1e-9, (group, n, sp, two_m)
             B_avg += B_m / (sp + 1)
         assert np.max(np.abs(B - B_avg)) < 1e-8, (group, n, sp, np.max(np.abs(B - B_avg)))
+        if sp <= 1:
+            mi, s1 = d.calc_correlations()
+            _, s1_fci, mi_fci = ol.fci_mutual_information(m, (n + sp) // 2, (n - sp) // 2, 0, jw=False)
+            assert np.max(np.abs(mi - mi_fci)) < 1e-8, (group, n, sp)
+            assert np.max(np.abs(s1 - s1_fci)) < 1e-8, (group, n, sp)
 
 
 def test_oracle_two_orbitals_have_no_two_site_step():
