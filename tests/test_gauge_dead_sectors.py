@@ -67,3 +67,19 @@ def test_gauge_changes_drop_the_weight_on_dead_states():
     psi1 = fc.chain_of(d, m, (8, 0, 0)).state()
     err = min(np.max(np.abs(psi1 - psi0)), np.max(np.abs(psi1 + psi0)))
     assert err < 1e-12, err
+
+
+def test_2rdm_pass_of_the_state_with_dead_sectors():
+    """The whole 2-RDM pass on that state (gauge changes, updates and the 2-RDM programs on
+    the CPU executor): trace N(N-1) = 56, the 2-RDM energy equals <H> of the MPS, and A
+    equals the 2-RDM of the MPS in Fock space, all to 1e-10. Before the gauge changes
+    dropped the weight on dead states, the trace was 108."""
+    m, d = _state_with_dead_sectors()
+    psi = fc.chain_of(d, m, (8, 0, 0)).state()
+    H = fock.FockHamiltonian(m.tmat, m.vmat, m.econst)
+    e_mps = float(psi @ H.apply(psi)) / float(psi @ psi)
+    A_fock = fock.two_rdm_a(H, psi / np.sqrt(psi @ psi))
+    A, _, trace, energy = d.calc_2dm()
+    assert abs(trace - 56.0) < 1e-10, trace
+    assert abs(energy - e_mps) < 1e-10, (energy, e_mps)
+    assert np.max(np.abs(A - A_fock)) < 1e-10, np.max(np.abs(A - A_fock))
