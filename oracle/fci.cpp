@@ -16,7 +16,10 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
+
+#include "exec_cpu.hpp"
 
 namespace {
 
@@ -99,18 +102,31 @@ struct FCI {
   }
 
   // sigma = H c, with H = sum_ij k_ij E_ij + 1/2 sum_ijkl (ij|kl) E_ij E_kl,
-  // k_ij = T_ij - 1/2 sum_k (ik|kj), (ij|kl) = V_ikjl.
+  // k_ij = T_ij - 1/2 sum_k (ik|kj), (ij|kl) = V_ikjl. The E_kl c and the (i, j) terms
+  // run on the oracle's host threads (each thread sums its (i, j) terms into its own
+  // vector; the vectors are added in thread order, so the result does not depend on the
+  // scheduling).
   void sigma(const std::vector<double>& c, std::vector<double>& s) {
     const size_t n = dets.size();
     const size_t L2 = size_t(L) * L;
+    const int nt = std::max(1, std::min<int>(oracle::CpuExecutor::threads(), static_cast<int>(L2)));
+    auto parallel = [&](const std::function<void(int)>& f) {
+      std::vector<std::thread> pool;
+      for (int t = 1; t < nt; t++) pool.emplace_back(f, t);
+      f(0);
+      for (auto& th : pool) th.join();
+    };
     std::vector<std::vector<double>> D(L2, std::vector<double>(n));
-    for (int k = 0; k < L; k++)
-      for (int l = 0; l < L; l++) apply_E(k, l, c, D[k + size_t(L) * l]);
+    parallel([&](int t) {
+      for (size_t kl = t; kl < L2; kl += nt) apply_E(static_cast<int>(kl % L), static_cast<int>(kl / L), c, D[kl]);
+    });
     auto chem = [&](int i, int j, int k, int l) { return V[i + size_t(L) * (k + size_t(L) * (j + size_t(L) * l))]; };
-    std::fill(s.begin(), s.end(), 0.0);
-    std::vector<double> G(n), tmp(n);
-    for (int i = 0; i < L; i++)
-      for (int j = 0; j < L; j++) {
+    std::vector<std::vector<double>> part(nt, std::vector<double>(n, 0.0));
+    parallel([&](int t) {
+      std::vector<double> G(n), tmp(n);
+      std::vector<double>& acc = part[t];
+      for (size_t ij = t; ij < L2; ij += nt) {
+        const int i = static_cast<int>(ij % L), j = static_cast<int>(ij / L);
         double kij = T[i + size_t(L) * j];
         for (int k = 0; k < L; k++) kij -= 0.5 * chem(i, k, k, j);
         for (size_t d = 0; d < n; d++) G[d] = kij * c[d];
@@ -122,8 +138,12 @@ struct FCI {
             for (size_t d = 0; d < n; d++) G[d] += v * Dkl[d];
           }
         apply_E(i, j, G, tmp);
-        for (size_t d = 0; d < n; d++) s[d] += tmp[d];
+        for (size_t d = 0; d < n; d++) acc[d] += tmp[d];
       }
+    });
+    std::fill(s.begin(), s.end(), 0.0);
+    for (int t = 0; t < nt; t++)
+      for (size_t d = 0; d < n; d++) s[d] += part[t][d];
   }
 
   double diag_element(size_t d) {

@@ -6,6 +6,9 @@ time.
 
   * N2.STO3G.FCIDUMP    copied from tests/matrixelements/N2.STO3G.FCIDUMP (the input of
                         the reference's tests/test1.cpp.in and tests/test5.cpp.in)
+  * H2O.631G.FCIDUMP    copied from tests/matrixelements/H2O.631G.FCIDUMP (the input of
+                        the reference's tests/test2.cpp.in, DMRG against FCI; the FCI takes
+                        about 15 minutes on 8 threads, so its test runs on request only)
   * CH4.STO3G.FCIDUMP   copied from tests/matrixelements/CH4.STO3G.FCIDUMP (the input of
                         the reference's tests/test3.cpp.in, which compares DMRG with FCI;
                         its schedule is recorded in golden.json, the FCI energy is computed
@@ -33,6 +36,8 @@ def main(reference: Path) -> None:
     tests = reference / "tests"
     shutil.copyfile(tests / "matrixelements" / "N2.STO3G.FCIDUMP", HERE / "N2.STO3G.FCIDUMP")
     shutil.copyfile(tests / "matrixelements" / "CH4.STO3G.FCIDUMP", HERE / "CH4.STO3G.FCIDUMP")
+    shutil.copyfile(tests / "matrixelements" / "H2O.631G.FCIDUMP", HERE / "H2O.631G.FCIDUMP")
+    t2 = (tests / "test2.cpp.in").read_text()
     t3 = (tests / "test3.cpp.in").read_text()
     t1 = (tests / "test1.cpp.in").read_text()
     t5 = (tests / "test5.cpp.in").read_text()
@@ -100,6 +105,19 @@ def main(reference: Path) -> None:
         "two_s": arr("TwoS"),
         "irreps": arr("Irreps"),
         "schedule": [[int(d), float(e), int(sw), float(nz), float(rt)] for d, e, sw, nz, rt in instr1],
+        "tolerance": 1e-08,
+    }
+    # tests/test2.cpp.in: H2O 6-31G, same layout as test3
+    instr2 = re.findall(r"OptScheme->setInstruction\(\s*(\d+)\s*,\s*(\d+)\s*,\s*([0-9.e+-]+)\s*,\s*(\d+)\s*,"
+                        r"\s*([0-9.e+-]+)\s*\)", t2)
+    golden["h2o_631g"] = {
+        "source": "tests/test2.cpp.in",
+        "fcidump": "H2O.631G.FCIDUMP",
+        "group": int(re.search(r"psi4groupnumber\s*=\s*(\d+)", t2).group(1)),
+        "two_s": int(re.search(r"TwoS\s*=\s*(\d+)", t2).group(1)),
+        "n": int(re.search(r"\bN\s*=\s*(\d+)", t2).group(1)),
+        "irrep": int(re.search(r"Irrep\s*=\s*(\d+)", t2).group(1)),
+        "schedule": [[int(d), float(e), int(sw), float(nz), 1e-5] for _, d, e, sw, nz in instr2],
         "tolerance": 1e-08,
     }
     (HERE / "golden.json").write_text(json.dumps(golden, indent=2) + "\n")

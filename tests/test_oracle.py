@@ -4,6 +4,7 @@ from __future__ import annotations
 
 import itertools
 import json
+import os
 from pathlib import Path
 
 import numpy as np
@@ -131,6 +132,22 @@ def test_oracle_ch4_sto3g_against_fci_of_reference_test3():
     two-instruction schedule; the DMRG energy equals the FCI energy to 1e-8."""
     g = GOLDEN["ch4_sto3g"]
     path = Path(__file__).parent / "golden" / g["fcidump"]
+    efci = ol.fci_energy(ol.fcidump_model(path, g["group"]), (g["n"] + g["two_s"]) // 2,
+                         (g["n"] - g["two_s"]) // 2, g["irrep"])
+    ol.srand(1)
+    d = ol.OracleDMRG(None, g["two_s"], g["n"], g["irrep"], [tuple(x) for x in g["schedule"]], fcidump=path,
+                      group=g["group"], check=False)
+    assert abs(d.solve() - efci) < g["tolerance"]
+
+
+@pytest.mark.skipif(os.environ.get("C2G_SLOW_TESTS") != "1", reason="about 15 minutes of FCI; C2G_SLOW_TESTS=1")
+def test_oracle_h2o_631g_against_fci_of_reference_test2():
+    """The reference's tests/test2.cpp.in: H2O 6-31G (C2v, 13 orbitals, N = 10, singlet A1)
+    with its two-instruction schedule; the DMRG energy equals the FCI energy (1.66 M
+    determinants) to 1e-8. Runs only with C2G_SLOW_TESTS=1."""
+    g = GOLDEN["h2o_631g"]
+    path = Path(__file__).parent / "golden" / g["fcidump"]
+    ol.set_threads(os.cpu_count() or 1)
     efci = ol.fci_energy(ol.fcidump_model(path, g["group"]), (g["n"] + g["two_s"]) // 2,
                          (g["n"] - g["two_s"]) // 2, g["irrep"])
     ol.srand(1)
