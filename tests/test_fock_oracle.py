@@ -19,6 +19,12 @@ CASES = [
     ("abinit6_c2v", lambda: models.synthetic_ab_initio(6, 5, 21), 0, 6, 0, 64, True),
     ("abinit7_d2h_doublet", lambda: models.synthetic_ab_initio(7, 7, 22), 1, 7, 3, 128, True),
     ("abinit6_c2v_triplet", lambda: models.synthetic_ab_initio(6, 5, 23), 2, 6, 0, 64, True),
+    # the remaining point groups: Ci, C2, Cs, D2, C2h (psi4 numbering 1, 2, 3, 4, 6)
+    ("abinit6_ci", lambda: models.synthetic_ab_initio(6, 1, 24), 0, 6, 1, 64, True),
+    ("abinit7_c2_doublet", lambda: models.synthetic_ab_initio(7, 2, 25), 1, 7, 1, 128, True),
+    ("abinit6_cs_truncated", lambda: models.synthetic_ab_initio(6, 3, 26), 0, 6, 0, 10, False),
+    ("abinit7_d2_quartet", lambda: models.synthetic_ab_initio(7, 4, 27), 3, 7, 2, 128, True),
+    ("abinit6_c2h", lambda: models.synthetic_ab_initio(6, 6, 28), 0, 6, 3, 64, True),
 ]
 
 
