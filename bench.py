@@ -211,13 +211,14 @@ def state_dims(dmrg, L=L_SITES):
             if r[4] > 0]
 
 
-def cpu_baseline_sample(n_matvec=3):
+def cpu_baseline_sample(n_matvec=3, n_warmup=1):
     """The CPU oracle's port of the same matvec on all host cores (its executor runs the
     independent output blocks of a stage on parallel threads): a state of the L = 30
     D = 2000 chain with the sector dimensions of the GPU run's swept state (random tensors:
     the matvec's work depends on the dimensions only), left operators up to the middle,
-    right operators down to it, then n_matvec matvecs at sites (14, 15) after one untimed
-    one. Without the dimensions file, the initial (scaled) dimensions of D = 2000."""
+    right operators down to it, then n_matvec timed matvecs at sites (14, 15) after
+    n_warmup untimed ones (the first of which joins the two-site object and compiles the
+    program). Without the dimensions file, the initial (scaled) dimensions of D = 2000."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as ol
 
@@ -237,6 +238,8 @@ def cpu_baseline_sample(n_matvec=3):
     for index in range(L_SITES - 2, MID, -1):
         cpu.update(index, False)
     x, _, _ = cpu.heff_apply(MID)  # joins the two-site object, compiles, first matvec (untimed)
+    for _ in range(max(n_warmup, 1) - 1):
+        cpu.heff_apply(MID, x)
     setup = time.perf_counter() - t0
     f0 = cpu.stats()["flops"]
     t0 = time.perf_counter()
@@ -246,7 +249,8 @@ def cpu_baseline_sample(n_matvec=3):
     flops = (cpu.stats()["flops"] - f0) / n_matvec
     return {"value": n_matvec / dt, "unit": UNIT, "cores": threads, "kind": "port", "cpu": host_cpu(),
             "flops_per_matvec": flops, "two_site_vector_length": int(x.size), "setup_s": setup,
-            "sample": f"{n_matvec} FP64 Heff matvecs at sites ({MID},{MID + 1}) of L={L_SITES} D={D_VIRT} with "
+            "sample": f"{n_matvec} FP64 Heff matvecs ({max(n_warmup, 1)} untimed before them) at sites "
+                      f"({MID},{MID + 1}) of L={L_SITES} D={D_VIRT} with "
                       f"{state} (oracle CPU executor, {threads} threads; compile and setup excluded, as for the "
                       f"GPU)"}
 
@@ -600,9 +604,12 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    steps = max(1, min(args.steps, 3))
+    # the same K timed and W untimed steps as this script's own arm: on the 16 host cores
+    # of a GB300 machine one step is about 1.8 s, so the default K = 20, W = 3 take under a
+    # minute
+    steps = max(1, args.steps)
     t0 = time.perf_counter()
-    cb = cpu_baseline_sample(n_matvec=steps)
+    cb = cpu_baseline_sample(n_matvec=steps, n_warmup=max(1, args.warmup))
     wall = time.perf_counter() - t0
     line = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
