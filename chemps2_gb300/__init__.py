@@ -71,6 +71,10 @@ def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
 def srand(seed: int) -> None:
     """Seeds the generator of the random initial MPS, Davidson fallback guess and noise."""
     _check(load().c2g_srand(C.c_uint(seed)))
@@ -80,6 +84,13 @@ def kernel_launches() -> int:
     n = C.c_longlong()
     _check(load().c2g_kernel_launches(C.byref(n)))
     return n.value
+
+
+def wigner3j(ja, jb, jc, ma, mb, mc) -> float:
+    """3j symbol (ja jb jc; ma mb mc), arguments twice the spins and projections."""
+    v = C.c_double()
+    _check(load().c2g_wigner3j(ja, jb, jc, ma, mb, mc, C.byref(v)))
+    return v.value
 
 
 def wigner6j(a, b, c, d, e, f) -> float:
@@ -459,6 +470,26 @@ class DMRG:
         _check(load().c2g_dmrg_get_mps(self._d, int(site), _dp(out), C.c_int64(n.value), C.byref(n)))
         return out
 
+    def getFCIcoefficient(self, alpha, beta):
+        """The coefficient of the determinant with up occupations alpha[h] and down
+        occupations beta[h] (0 or 1) of the Hamiltonian orbitals (PyDMRG.getFCIcoefficient;
+        0 outside the targeted sector)."""
+        a = np.ascontiguousarray(alpha, dtype=np.int32)
+        b = np.ascontiguousarray(beta, dtype=np.int32)
+        if a.size != b.size:
+            raise ValueError("alpha and beta differ in length")
+        v = C.c_double()
+        _check(load().c2g_dmrg_fci_coefficient(self._d, _ip(a), _ip(b), C.byref(v)))
+        return v.value
+
+    def getSpecificCoefficient(self, coeff):
+        """The coefficient of the determinant with occupations coeff[h] in {0, 1, 2} (1: one
+        up electron), DMRG::getSpecificCoefficient."""
+        c = np.asarray(coeff, dtype=np.int32)
+        if np.any((c < 0) | (c > 2)):
+            raise ValueError("occupations must be 0, 1 or 2")
+        return self.getFCIcoefficient((c >= 1).astype(np.int32), (c == 2).astype(np.int32))
+
     def step_energies(self):
         """Energies of every two-site step Solve() has run, in order."""
         n = C.c_int()
@@ -575,5 +606,5 @@ PyConvergenceScheme = ConvergenceScheme
 PyDMRG = DMRG
 
 __all__ = ["Hamiltonian", "Problem", "ConvergenceScheme", "DMRG", "PyHamiltonian", "PyProblem",
-           "PyConvergenceScheme", "PyDMRG", "srand", "solve_batch", "host_rand_sample", "wigner6j", "wigner9j", "kernel_launches", "load",
+           "PyConvergenceScheme", "PyDMRG", "srand", "solve_batch", "host_rand_sample", "wigner3j", "wigner6j", "wigner9j", "kernel_launches", "load",
            "Chemps2Error", "NoDeviceError"]

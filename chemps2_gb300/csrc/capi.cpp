@@ -332,6 +332,13 @@ int c2g_sobject_layout(const c2g_problem* p, int D, int index, int* labels, int6
   });
 }
 
+int c2g_wigner3j(int ja, int jb, int jc, int ma, int mb, int mc, double* v) {
+  return guarded([&] {
+    NEED(v);
+    *v = c2g::wigner3j(ja, jb, jc, ma, mb, mc);
+  });
+}
+
 int c2g_wigner6j(int a, int b, int c, int d, int e, int f, double* v) {
   return guarded([&] {
     NEED(v);
@@ -588,6 +595,16 @@ int c2g_dmrg_get_mps(const c2g_dmrg* d, int site, double* out, int64_t cap, int6
     if (cap <= 0) return;
     if (cap < *n) throw std::invalid_argument("c2g_dmrg_get_mps: buffer shorter than the tensor");
     d->d->get_mps(site, out, *n);
+  });
+}
+
+int c2g_dmrg_fci_coefficient(const c2g_dmrg* d, const int* alpha, const int* beta, double* coeff) {
+  return guarded([&] {
+    NEED(d);
+    NEED(alpha);
+    NEED(beta);
+    NEED(coeff);
+    *coeff = d->d->getFCIcoefficient(const_cast<int*>(alpha), const_cast<int*>(beta));
   });
 }
 int c2g_dmrg_step_energies(const c2g_dmrg* d, double* out, int cap, int* count) {

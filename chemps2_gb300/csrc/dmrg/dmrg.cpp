@@ -18,6 +18,7 @@
 #include "davidson.hpp"
 #include "correlations.hpp"
 #include "excite.hpp"
+#include "fcicoef.hpp"
 #include "gauge.hpp"
 #include "twodm.hpp"
 #include "compile.hpp"
@@ -1260,6 +1261,34 @@ void DMRG::get_mps(const int site, double* out, const long long n) const {
     C2G_CUDA(cudaMemcpyAsync(out, mps_dev[site], sizeof(double) * n, cudaMemcpyDeviceToHost, rt->stream()));
   }
   rt->sync();
+}
+
+// CheMPS2/DMRGtechnics.cpp:341-470 on the host, from the downloaded MPS tensors
+double DMRG::getFCIcoefficient(int* alpha, int* beta) const {
+  if (!alpha || !beta) throw std::invalid_argument("getFCIcoefficient: null occupation array");
+  std::vector<std::vector<double>> data(L);
+  std::vector<const c2g::MpsLayout*> lay(L);
+  std::vector<const double*> T(L);
+  for (int k = 0; k < L; k++) {
+    const long long n = mps_size(k);
+    data[k].resize(static_cast<size_t>(std::max<long long>(n, 1)));
+    if (n > 0) get_mps(k, data[k].data(), n);
+    lay[k] = mps_lay[k].get();
+    T[k] = data[k].data();
+  }
+  return c2g::fci_coefficient(*denBK, *Prob, lay, T, alpha, beta);
+}
+
+// CheMPS2/DMRGtechnics.cpp:324-339
+double DMRG::getSpecificCoefficient(int* coeff) const {
+  if (!coeff) throw std::invalid_argument("getSpecificCoefficient: null occupation array");
+  std::vector<int> a(L), b(L);
+  for (int h = 0; h < L; h++) {
+    if (coeff[h] < 0 || coeff[h] > 2) throw std::invalid_argument("getSpecificCoefficient: occupations must be 0, 1 or 2");
+    a[h] = (coeff[h] >= 1) ? 1 : 0;
+    b[h] = (coeff[h] == 2) ? 1 : 0;
+  }
+  return getFCIcoefficient(a.data(), b.data());
 }
 
 long long DMRG::sobject_size(const int index) const {

@@ -82,6 +82,12 @@ class DMRG {
   // copied to host memory, and its length.
   long long mps_size(const int site) const;
   void get_mps(const int site, double* out, const long long n) const;
+  // The coefficient of the determinant with occupations alpha[h], beta[h] (0 or 1) of the
+  // Hamiltonian orbitals h in the current MPS (CheMPS2/DMRGtechnics.cpp:341-470), and of
+  // the one given by coeff[h] in {0 empty, 1 one up electron, 2 doubly occupied}
+  // (:324-339). Zero when the determinant lies outside the targeted sector.
+  double getFCIcoefficient(int* alpha, int* beta) const;
+  double getSpecificCoefficient(int* coeff) const;
   void reset_stats() { stats_ = DMRGStats(); }
   void set_verbose(bool v) { verbose = v; }
   // 0: FP64 Heff matvecs (the reference's arithmetic). 1: mixed, the Davidson solver

@@ -65,6 +65,34 @@ double wigner6j(int ja, int jb, int jc, int jd, int je, int jf) {
   return sum;
 }
 
+double wigner3j(int ja, int jb, int jc, int ma, int mb, int mc) {
+  if (ja < 0 || jb < 0 || jc < 0 || ja > kWignerMax2j || jb > kWignerMax2j || jc > kWignerMax2j)
+    throw std::logic_error("wigner3j: argument out of range (" + std::to_string(ja) + "," + std::to_string(jb) + "," +
+                           std::to_string(jc) + ")");
+  if (triangle_fails(ja, jb, jc) || ma + mb + mc != 0) return 0.0;
+  if (std::abs(ma) > ja || std::abs(mb) > jb || std::abs(mc) > jc) return 0.0;
+  if ((ja + ma) % 2 != 0 || (jb + mb) % 2 != 0 || (jc + mc) % 2 != 0) return 0.0;
+  // integer arguments of the factorials
+  const int c1 = (jc - jb + ma) / 2;       // k + c1 >= 0
+  const int c2 = (jc - ja - mb) / 2;       // k + c2 >= 0
+  const int d1 = (ja + jb - jc) / 2;       // d1 - k >= 0
+  const int d2 = (ja - ma) / 2;            // d2 - k >= 0
+  const int d3 = (jb + mb) / 2;            // d3 - k >= 0
+  const int kmin = std::max(0, std::max(-c1, -c2));
+  const int kmax = std::min(d1, std::min(d2, d3));
+  if (kmax < kmin) return 0.0;
+  const double pref = sqrt_delta(ja, jb, jc) * kSqrtFact[(ja + ma) / 2] * kSqrtFact[(ja - ma) / 2] *
+                      kSqrtFact[(jb + mb) / 2] * kSqrtFact[(jb - mb) / 2] * kSqrtFact[(jc + mc) / 2] *
+                      kSqrtFact[(jc - mc) / 2];
+  double sum = 0.0;
+  for (int k = kmin; k <= kmax; k++) {
+    const double den = kSqrtFact[k] * kSqrtFact[k + c1] * kSqrtFact[k + c2] * kSqrtFact[d1 - k] *
+                       kSqrtFact[d2 - k] * kSqrtFact[d3 - k];
+    sum += ((k % 2 == 0) ? 1.0 : -1.0) / (den * den);
+  }
+  return phase(ja - jb - mc) * pref * sum;
+}
+
 double wigner9j(int ja, int jb, int jc, int jd, int je, int jf, int jg, int jh, int ji) {
   if (triangle_fails(ja, jb, jc) || triangle_fails(jd, je, jf) ||
       triangle_fails(jg, jh, ji) || triangle_fails(ja, jd, jg) ||

@@ -40,6 +40,10 @@ inline void invert_triangle_two(int global, int* result) {
 constexpr int kWignerFactorialMax = 191;
 constexpr int kWignerMax2j = 95;
 
+// 3j symbol (ja jb jc; ma mb mc), arguments twice the (half-)integer values; zero unless
+// ma + mb + mc = 0, |m| <= j with j + m integer, and the triangle rule holds. Racah's
+// single sum over the same square-root-factorial table.
+double wigner3j(int two_ja, int two_jb, int two_jc, int two_ma, int two_mb, int two_mc);
 double wigner6j(int two_ja, int two_jb, int two_jc, int two_jd, int two_je, int two_jf);
 double wigner9j(int two_ja, int two_jb, int two_jc, int two_jd, int two_je, int two_jf,
                 int two_jg, int two_jh, int two_ji);

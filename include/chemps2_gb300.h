@@ -86,7 +86,9 @@ int c2g_bookkeeper_sectors(const c2g_problem* p, int D, int boundary, int* out, 
 int c2g_sobject_layout(const c2g_problem* p, int D, int index, int* labels, int64_t* kappa2index, int* reorder,
                        int cap, int* nkappa);
 
-/* Wigner symbols (CheMPS2/Wigner.cpp:294-370), arguments are twice the spins. */
+/* Wigner symbols (CheMPS2/Wigner.cpp:243-370), arguments are twice the spins (and, for
+ * the 3j symbol, twice the projections). */
+int c2g_wigner3j(int ja, int jb, int jc, int ma, int mb, int mc, double* value);
 int c2g_wigner6j(int a, int b, int c, int d, int e, int f, double* value);
 int c2g_wigner9j(int a, int b, int c, int d, int e, int f, int g, int h, int i, double* value);
 
@@ -179,6 +181,11 @@ int c2g_dmrg_sectors(const c2g_dmrg* d, int boundary, int* out, int cap, int* co
  * block order of CheMPS2/TensorT.cpp:38-110, each block column-major), copied to `out`;
  * *n receives its length (query with cap = 0). */
 int c2g_dmrg_get_mps(const c2g_dmrg* d, int site, double* out, int64_t cap, int64_t* n);
+/* The coefficient of one determinant in the current MPS (DMRG::getFCIcoefficient,
+ * CheMPS2/DMRGtechnics.cpp:341-470): alpha[h] and beta[h] in {0, 1} are the occupations
+ * of the L Hamiltonian orbitals; *coeff is 0 when the determinant lies outside the
+ * targeted (N, 2S, irrep) sector. */
+int c2g_dmrg_fci_coefficient(const c2g_dmrg* d, const int* alpha, const int* beta, double* coeff);
 /* The energy of every two-site step the sweeps of c2g_dmrg_solve have run, in order (the
  * reference prints them in DMRG::sweepleft / sweepright, CheMPS2/DMRG.cpp:335-402, and
  * keeps only their minimum). *count receives the number of steps; up to cap of them are

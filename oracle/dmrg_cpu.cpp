@@ -30,6 +30,7 @@
 #include "chemps2/SyBookkeeper.h"
 #include "compile.hpp"
 #include "exec_cpu.hpp"
+#include "fcicoef.hpp"
 #include "gauge.hpp"
 #include "heff.hpp"
 #include "layout.hpp"
@@ -920,6 +921,21 @@ int oracle_dmrg_calc_correlations(void* h, double* mutinfo, double* entropy) {
       entropy[r] = d->corr->SingleOrbitalEntropy_DMRG(r);
       for (int c = 0; c < L; c++) mutinfo[r + size_t(L) * c] = d->corr->getMutualInformation_DMRG(r, c);
     }
+  });
+}
+
+// DMRG::getFCIcoefficient on the oracle's MPS with the product's host routine
+// (chemps2_gb300/csrc/host/fcicoef.cpp).
+int oracle_dmrg_fci_coefficient(void* h, const int* alpha, const int* beta, double* coeff) {
+  return guard([&] {
+    auto* d = static_cast<OracleHandle*>(h)->dmrg.get();
+    std::vector<const c2g::MpsLayout*> lay(d->L);
+    std::vector<const double*> T(d->L);
+    for (int k = 0; k < d->L; k++) {
+      lay[k] = d->mps_lay[k].get();
+      T[k] = d->mps[k].data();
+    }
+    *coeff = c2g::fci_coefficient(*d->bk, *d->Prob, lay, T, alpha, beta);
   });
 }
 

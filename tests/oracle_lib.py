@@ -194,6 +194,14 @@ class OracleDMRG:
         self._check(lib().oracle_dmrg_calc_correlations(self.h, _dp(mi), _dp(s1)))
         return mi.reshape((L, L), order="F"), s1
 
+    def fci_coefficient(self, alpha, beta):
+        """DMRG::getFCIcoefficient of the oracle's MPS (the product's host routine)."""
+        a = np.ascontiguousarray(alpha, dtype=np.int32)
+        b = np.ascontiguousarray(beta, dtype=np.int32)
+        v = C.c_double()
+        self._check(lib().oracle_dmrg_fci_coefficient(self.h, _ip(a), _ip(b), C.byref(v)))
+        return v.value
+
     def gauge(self, site, right):
         """Left-normalise `site` (R into site + 1) or, with right, right-normalise it (L into
         site - 1), with the product's host gauge routines."""

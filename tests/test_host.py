@@ -240,6 +240,33 @@ def test_wigner6j_against_exact_racah():
     assert abs(c2g.wigner6j(90, 90, 0, 90, 90, 0) - 1.0 / 91) < 1e-12
 
 
+def test_wigner3j_against_sympy():
+    """The 3j symbol of getFCIcoefficient's Clebsch-Gordan couplings against sympy's exact
+    values, over all projections of random spins up to 11/2 and a large case."""
+    from sympy import Rational
+    from sympy.physics.wigner import wigner_3j
+
+    rng = np.random.default_rng(1)
+    n = 0
+    for _ in range(150):
+        a, b = (int(x) for x in rng.integers(0, 12, size=2))
+        for c in range(abs(a - b), a + b + 1, 2):
+            for ma in range(-a, a + 1, 2):
+                for mb in range(-b, b + 1, 2):
+                    mc = -ma - mb
+                    if abs(mc) > c:
+                        continue
+                    ref = float(wigner_3j(Rational(a, 2), Rational(b, 2), Rational(c, 2), Rational(ma, 2),
+                                          Rational(mb, 2), Rational(mc, 2)))
+                    assert abs(c2g.wigner3j(a, b, c, ma, mb, mc) - ref) < 1e-13, (a, b, c, ma, mb, mc)
+                    n += 1
+    assert n > 1000
+    assert c2g.wigner3j(2, 2, 2, 2, 2, -2) == 0.0  # projections that do not add to zero
+    assert c2g.wigner3j(2, 2, 6, 0, 0, 0) == 0.0  # triangle rule
+    ref = float(wigner_3j(40, 40, 0, 3, -3, 0))
+    assert abs(c2g.wigner3j(80, 80, 0, 6, -6, 0) - ref) < 1e-12
+
+
 def ninej_from_6j(a, b, c, d, e, f, g, h, i):
     """9j symbol {a b c; d e f; g h i} (arguments twice the spins) as the sum over x of
     (-1)^(2x) (2x + 1) {a b c; f i x} {d e f; b x h} {g h i; x a d} (Edmonds 6.4.3), from
