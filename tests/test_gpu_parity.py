@@ -291,6 +291,38 @@ def test_hubbard_3x3_site_against_momentum_basis_of_reference_test9():
     assert abs(e_mom - e_site) < 1e-8, (e_site, e_mom)
 
 
+def test_fci_coefficients_equal_fock_space_amplitudes():
+    """getFCIcoefficient / getSpecificCoefficient on the GPU's MPS (downloaded, then the
+    host routine) equal the Fock-space amplitudes of the same MPS (oracle/fock.py) for every
+    determinant of the sector, to 1e-12; C2v doublet."""
+    import itertools
+
+    import fock_checks as fc
+
+    m = models.synthetic_ab_initio(5, 5, 3)
+    ham, prob, scheme = gpu_objects(m, 1, 5, 2, [(64, 1e-10, 2, 0.0, 1e-10)])
+    c2g.srand(2)
+    gpu = c2g.DMRG(prob, scheme)
+    try:
+        gpu.Solve()
+        psi = fc.chain_of(gpu, m, (5, 1, 2)).state()
+        worst, count = 0.0, 0
+        for ups in itertools.combinations(range(5), 3):
+            for dns in itertools.combinations(range(5), 2):
+                a = np.zeros(5, dtype=np.int32)
+                b = np.zeros(5, dtype=np.int32)
+                a[list(ups)] = 1
+                b[list(dns)] = 1
+                conf = sum(int(a[k] + 2 * b[k]) * 4 ** (4 - k) for k in range(5))
+                worst = max(worst, abs(gpu.getFCIcoefficient(a, b) - psi[conf]))
+                count += 1
+        assert worst < 1e-12, worst
+        occ = np.array([2, 2, 1, 0, 0])
+        assert gpu.getSpecificCoefficient(occ) == gpu.getFCIcoefficient([1, 1, 1, 0, 0], [1, 1, 0, 0, 0])
+    finally:
+        gpu.close()
+
+
 def test_kernels_were_launched():
     before = c2g.kernel_launches()
     m = models.hubbard(6, 4.0)
