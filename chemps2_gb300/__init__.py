@@ -440,6 +440,58 @@ class DMRG:
         # element (a,b,c,d) at a + L*(b + L*(c + L*d)): Fortran order
         return TwoDM(A.reshape((L, L, L, L), order="F"), B.reshape((L, L, L, L), order="F"), tr.value, en.value)
 
+    # PyDMRG's element accessors (PyCheMPS2/PyCheMPS2.pyx:141-178), Hamiltonian orbital
+    # order as there; each reads the arrays of the last calc2DMandCorrelations.
+    def calc_rdms_and_correlations(self, do_3rdm=False):
+        """DMRG::calc_rdms_and_correlations: the 2-RDM and correlations; the 3-RDM is not
+        built here, so do_3rdm must be False."""
+        if do_3rdm:
+            raise NotImplementedError("the 3-RDM is not available in this implementation")
+        self.calc2DMandCorrelations()
+
+    def deleteStoredOperators(self):
+        """The renormalized operators live in device memory, never on disk: nothing to
+        delete (PyDMRG.deleteStoredOperators)."""
+
+    def get2DMA(self, i1, i2, i3, i4):
+        return self.get2DM(ham_order=True).getTwoDMA(i1, i2, i3, i4)
+
+    def get2DMB(self, i1, i2, i3, i4):
+        return self.get2DM(ham_order=True).getTwoDMB(i1, i2, i3, i4)
+
+    def get2DMenergy(self):
+        return self.get2DM().energy()
+
+    def getDoubleTrace2DMA(self):
+        return self.get2DM().trace()
+
+    def getCspin(self, row, col):
+        return float(self.getCorrelations(ham_order=True)["Cspin"][row, col])
+
+    def getCdens(self, row, col):
+        return float(self.getCorrelations(ham_order=True)["Cdens"][row, col])
+
+    def getCspinflip(self, row, col):
+        return float(self.getCorrelations(ham_order=True)["Cspinflip"][row, col])
+
+    def getCdirad(self, row, col):
+        return float(self.getCorrelations(ham_order=True)["Cdirad"][row, col])
+
+    def getMutInfo(self, row, col):
+        return float(self.getCorrelations(ham_order=True)["MutInfo"][row, col])
+
+    def getSingleOrbEntropy(self, index):
+        return float(self.getCorrelations(ham_order=True)["SingleOrbitalEntropy"][index])
+
+    def getMutInfoDistance(self, power):
+        """sum_{r != c} I(r, c) |r - c|^power over the DMRG chain order
+        (CheMPS2/Correlations.cpp:188-201)."""
+        mi = self.getCorrelations(ham_order=False)["MutInfo"]
+        L = mi.shape[0]
+        r, c = np.meshgrid(np.arange(L), np.arange(L), indexing="ij")
+        mask = r != c
+        return float(np.sum(mi[mask] * np.abs(r - c)[mask].astype(float) ** power))
+
     def getCorrelations(self, ham_order=False):
         """Correlation tables and mutual information (CheMPS2::Correlations) as a dict of
         L x L arrays [row, col] plus the single-orbital entropies."""

@@ -65,6 +65,17 @@ def test_2rdm_matches_fci(name, make, two_s, n, irrep):
         corr = d.getCorrelations()
         assert np.max(np.abs(corr["SingleOrbitalEntropy"] - s1_fci)) < 1e-9
         assert np.max(np.abs(corr["MutInfo"] - mi_fci)) < 1e-9, np.max(np.abs(corr["MutInfo"] - mi_fci))
+        # PyDMRG's element accessors, Hamiltonian order (no reordering here)
+        assert d.get2DMA(0, 1, 0, 1) == dm.A[0, 1, 0, 1] and d.get2DMB(1, 0, 0, 1) == dm.B[1, 0, 0, 1]
+        assert d.get2DMenergy() == dm.energy() and d.getDoubleTrace2DMA() == dm.trace()
+        assert d.getMutInfo(0, 2) == corr["MutInfo"][0, 2]
+        assert d.getSingleOrbEntropy(1) == corr["SingleOrbitalEntropy"][1]
+        assert d.getCspin(0, 1) == corr["Cspin"][0, 1] and d.getCdirad(1, 2) == corr["Cdirad"][1, 2]
+        L = m.L
+        ref = sum(corr["MutInfo"][r, c] * abs(r - c) ** 2 for r in range(L) for c in range(L) if r != c)
+        assert abs(d.getMutInfoDistance(2) - ref) < 1e-12
+        with pytest.raises(NotImplementedError):
+            d.calc_rdms_and_correlations(True)
         # the state and the operators are left as after a right sweep: Solve continues
         E2 = d.Solve()
         assert abs(E2 - E) < 1e-8
