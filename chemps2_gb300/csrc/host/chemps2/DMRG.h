@@ -10,6 +10,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <stdexcept>
 #include <vector>
 
 #include "ConvergenceScheme.h"
@@ -137,6 +138,16 @@ class DMRG {
   // (which also restores a left-canonical MPS and the operators of a finished right sweep,
   // so Solve() can continue). get2DM() / getCorrelations() return them (null before).
   void calc2DMandCorrelations();
+  // CheMPS2/include/chemps2/DMRG.h:111: the 2-RDM and correlations; the 3-RDM is not
+  // built in this implementation, so do_3rdm must be false.
+  void calc_rdms_and_correlations(const bool do_3rdm, const bool disk_3rdm = false) {
+    (void)disk_3rdm;
+    if (do_3rdm) throw std::invalid_argument("calc_rdms_and_correlations: the 3-RDM is not available");
+    calc2DMandCorrelations();
+  }
+  // CheMPS2/include/chemps2/DMRG.h:148: the renormalized operators live in device memory,
+  // never on disk, so there is nothing to delete.
+  void deleteStoredOperators() {}
   const TwoDM* get2DM() const { return two_dm_.get(); }
   const Correlations* getCorrelations() const { return corr_.get(); }
 
