@@ -165,6 +165,11 @@ class Hamiltonian:
         _check(load().c2g_hamiltonian_get_vmat(self._h, int(i), int(j), int(k), int(l), C.byref(v)))
         return v.value
 
+    def writeFCIDUMP(self, filename, Nelec, TwoS, TargetIrrep):
+        """Hamiltonian::writeFCIDUMP: this Hamiltonian as an FCIDUMP file."""
+        _check(load().c2g_hamiltonian_write_fcidump(self._h, str(filename).encode(), int(Nelec), int(TwoS),
+                                                    int(TargetIrrep)))
+
 
 class Problem:
     """CheMPS2::Problem (PyProblem)."""
@@ -222,6 +227,16 @@ class Problem:
     def checkConsistency(self):
         v = C.c_int()
         _check(load().c2g_problem_check_consistency(self._p, C.byref(v)))
+        return bool(v.value)
+
+    def check_rohf_occ(self, occupancies):
+        """Whether occupations 0, 1, 2 of the DMRG sites give the targeted sector
+        (Problem::check_rohf_occ)."""
+        occ = np.ascontiguousarray(occupancies, dtype=np.int32)
+        if occ.size != self.gL():
+            raise ValueError("one occupation per orbital")
+        v = C.c_int()
+        _check(load().c2g_problem_check_rohf_occ(self._p, occ.ctypes.data_as(C.POINTER(C.c_int)), C.byref(v)))
         return bool(v.value)
 
     def bookkeeper_sectors(self, D, boundary):

@@ -254,6 +254,23 @@ int c2g_problem_get_mx_element(const c2g_problem* p, int a, int b, int c, int d,
     *v = p->p->gMxElement(a, b, c, d);
   });
 }
+int c2g_problem_check_rohf_occ(const c2g_problem* p, const int* occupancies, int* ok) {
+  return guarded([&] {
+    NEED(p);
+    NEED(occupancies);
+    NEED(ok);
+    *ok = p->p->check_rohf_occ(occupancies) ? 1 : 0;
+  });
+}
+
+int c2g_hamiltonian_write_fcidump(const c2g_hamiltonian* h, const char* path, int nelec, int two_s, int irrep) {
+  return guarded([&] {
+    NEED(h);
+    NEED(path);
+    h->h->writeFCIDUMP(std::string(path), nelec, two_s, irrep);
+  });
+}
+
 int c2g_problem_check_consistency(const c2g_problem* p, int* ok) {
   return guarded([&] {
     NEED(p);

@@ -34,6 +34,11 @@ class Hamiltonian {
 
   void setVmat(const int i, const int j, const int k, const int l, const double val);
   void addToVmat(const int i, const int j, const int k, const int l, const double val);
+  // Writes the Hamiltonian as an FCIDUMP file (CheMPS2/Hamiltonian.cpp:539-582): the
+  // header with Molpro irrep numbers, every symmetry-allowed two-electron integral (pq|rs)
+  // with p >= q, r >= s and (p, q) >= (r, s), the one-electron integrals h_pq (p >= q,
+  // same irrep), then the constant.
+  void writeFCIDUMP(const std::string& fcidumpfile, const int Nelec, const int TwoS, const int TargetIrrep) const;
   double getVmat(const int i, const int j, const int k, const int l) const {
     return vmat[i + L * (j + L * (k + static_cast<size_t>(L) * l))];
   }

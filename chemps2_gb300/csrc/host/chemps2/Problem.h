@@ -38,6 +38,9 @@ class Problem {
   const double* mxelem_data() const { return mx_elem.data(); }
 
   bool checkConsistency() const;
+  // Whether occupations (0, 1, 2 per DMRG site) give the targeted (N, 2S, irrep) with the
+  // singly occupied sites high-spin coupled (CheMPS2/Problem.cpp:422-451).
+  bool check_rohf_occ(const int* occupancies) const;
 
   bool gReorder() const { return bReorder; }
   int gf1(const int HamOrb) const { return bReorder ? f1[HamOrb] : -1; }

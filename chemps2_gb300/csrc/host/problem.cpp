@@ -140,6 +140,32 @@ Hamiltonian::Hamiltonian(const std::string& fcidumpfile, const int psi4groupnumb
   }
 }
 
+void Hamiltonian::writeFCIDUMP(const std::string& fcidumpfile, const int Nelec, const int TwoS,
+                               const int TargetIrrep) const {
+  int map[8] = {0};
+  psi2molpro(group, map);
+  FILE* f = std::fopen(fcidumpfile.c_str(), "w");
+  if (!f) throw std::runtime_error("writeFCIDUMP: unable to open " + fcidumpfile);
+  std::fprintf(f, " &FCI NORB= %d,NELEC= %d,MS2= %d,\n  ORBSYM=", L, Nelec, TwoS);
+  for (int o = 0; o < L; o++) std::fprintf(f, "%d,", map[orb2irrep[o]]);
+  std::fprintf(f, "\n  ISYM=%d,\n /\n", map[TargetIrrep]);
+  auto line = [&](double v, int a, int b, int c, int d) { std::fprintf(f, " % 23.16E %3d %3d %3d %3d\n", v, a, b, c, d); };
+  // (pq|rs) = V_prqs in physics notation
+  for (int p = 0; p < L; p++)
+    for (int q = 0; q <= p; q++)
+      for (int r = 0; r <= p; r++)
+        for (int s = 0; s <= r; s++) {
+          if ((orb2irrep[p] ^ orb2irrep[q]) != (orb2irrep[r] ^ orb2irrep[s])) continue;
+          if (p == r && q < s) continue;
+          line(getVmat(p, r, q, s), p + 1, q + 1, r + 1, s + 1);
+        }
+  for (int p = 0; p < L; p++)
+    for (int q = 0; q <= p; q++)
+      if (orb2irrep[p] == orb2irrep[q]) line(getTmat(p, q), p + 1, q + 1, 0, 0);
+  std::fprintf(f, " % 23.16E %3d %3d %3d %3d", Econst, 0, 0, 0, 0);
+  std::fclose(f);
+}
+
 // ---------------------------------------------------------------- Problem --------
 
 Problem::Problem(const Hamiltonian* Hamin, const int TwoSin, const int Nin, const int Irrepin)
@@ -169,6 +195,20 @@ void Problem::construct_mxelem() {
       }
     }
   }
+}
+
+bool Problem::check_rohf_occ(const int* occupancies) const {
+  // CheMPS2/Problem.cpp:422-451
+  int n = 0, two_s = 0, irrep = 0;
+  for (int k = 0; k < L; k++) {
+    if (occupancies[k] < 0 || occupancies[k] > 2) return false;
+    n += occupancies[k];
+    if (occupancies[k] == 1) {
+      two_s += 1;
+      irrep ^= gIrrep(k);
+    }
+  }
+  return n == N && two_s == TwoS && irrep == Irrep;
 }
 
 bool Problem::checkConsistency() const {

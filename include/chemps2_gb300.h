@@ -66,6 +66,12 @@ int c2g_problem_construct_mxelem(c2g_problem* p);
 int c2g_problem_set_mx_element(c2g_problem* p, int a, int b, int c, int d, double value);
 int c2g_problem_get_mx_element(const c2g_problem* p, int a, int b, int c, int d, double* value);
 int c2g_problem_check_consistency(const c2g_problem* p, int* ok);
+/* Problem::check_rohf_occ (CheMPS2/Problem.cpp:422-451): whether occupations 0, 1, 2 of
+ * the L DMRG sites give the targeted (N, 2S, irrep) with the open shells high-spin. */
+int c2g_problem_check_rohf_occ(const c2g_problem* p, const int* occupancies, int* ok);
+/* Hamiltonian::writeFCIDUMP (CheMPS2/Hamiltonian.cpp:539-582): the Hamiltonian as an
+ * FCIDUMP file with NELEC, MS2 and ISYM as given. */
+int c2g_hamiltonian_write_fcidump(const c2g_hamiltonian* h, const char* path, int nelec, int two_s, int irrep);
 
 /* CheMPS2::ConvergenceScheme (CheMPS2/ConvergenceScheme.cpp:29-76) */
 int c2g_scheme_create(int n_instructions, c2g_scheme** out);

@@ -433,3 +433,51 @@ def test_truncation_eig_argument_errors_are_status_codes():
     with pytest.raises(c2g.Chemps2Error):
         c2g._check(lib.c2g_truncation_eig(-1, None, None, None, None))
     assert lib.c2g_truncation_eig(0, None, None, None, None) == 0
+
+
+def test_write_fcidump_round_trip(tmp_path):
+    """Hamiltonian::writeFCIDUMP (CheMPS2/Hamiltonian.cpp:539-582) then the FCIDUMP reader
+    give back every integral and the constant exactly (17 significant digits are
+    written), for a synthetic D2h Hamiltonian and for the reference's N2 STO-3G file;
+    the header carries NELEC, MS2 and the target irrep in Molpro numbering."""
+    from pathlib import Path
+
+    m = models.synthetic_ab_initio(6, 7, 5)
+    h = c2g.Hamiltonian(m.L, m.group, m.irreps)
+    for i in range(m.L):
+        for j in range(i, m.L):
+            if m.irreps[i] == m.irreps[j]:
+                h.setTmat(i, j, float(m.tmat[i, j]))
+    for i, j, k, l in np.argwhere(m.vmat != 0.0):
+        h.setVmat(int(i), int(j), int(k), int(l), float(m.vmat[i, j, k, l]))
+    h.setEconst(1.25)
+    golden = Path(__file__).parent / "golden" / "N2.STO3G.FCIDUMP"
+    for ham, group, name in ((h, 7, "synthetic"), (c2g.Hamiltonian(0, 7, [], filename=str(golden)), 7, "n2")):
+        path = tmp_path / f"{name}.FCIDUMP"
+        ham.writeFCIDUMP(str(path), 6, 0, 0)
+        back = c2g.Hamiltonian(0, group, [], filename=str(path))
+        L = ham.getL()
+        assert back.getL() == L and back.getEconst() == ham.getEconst()
+        assert all(back.getOrbitalIrrep(i) == ham.getOrbitalIrrep(i) for i in range(L))
+        for i in range(L):
+            for j in range(L):
+                assert back.getTmat(i, j) == ham.getTmat(i, j)
+                for k in range(L):
+                    for l in range(L):
+                        assert back.getVmat(i, j, k, l) == ham.getVmat(i, j, k, l), (name, i, j, k, l)
+        head = path.read_text().splitlines()[:3]
+        assert "NORB= %d" % L in head[0] and "NELEC= 6" in head[0] and "MS2= 0" in head[0]
+        assert head[2].strip() == "ISYM=1,"
+
+
+def test_check_rohf_occ():
+    """Problem::check_rohf_occ (CheMPS2/Problem.cpp:422-451): occupations must be 0, 1, 2
+    and give N, 2S (open shells high-spin) and the irrep of the targeted sector."""
+    h = c2g.Hamiltonian(4, 5, np.array([0, 1, 2, 3], dtype=np.int32))
+    p = c2g.Problem(h, 0, 4, 0)
+    assert p.check_rohf_occ([2, 2, 0, 0])
+    assert not p.check_rohf_occ([2, 1, 1, 0])  # 2S = 2
+    p3 = c2g.Problem(h, 2, 4, 3)
+    assert p3.check_rohf_occ([2, 1, 1, 0])  # irreps 1 x 2 = 3
+    assert not p3.check_rohf_occ([2, 1, 0, 1])  # irreps 1 x 3 = 2
+    assert not p.check_rohf_occ([3, 1, 0, 0])
